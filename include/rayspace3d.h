@@ -1,0 +1,192 @@
+/*
+ * rayspace3d.h -- C ABI of the GB300 engine for the RaySpace3D query path (librs.so).
+ *
+ * Conventions (all entry points):
+ *   - plain pointers and sizes; device pointers are prefixed d_, host pointers h_;
+ *   - the caller owns every input and output buffer; engine objects are opaque
+ *     handles released with the matching _destroy call;
+ *   - work is issued on `stream` (a cudaStream_t passed as void*, NULL = legacy
+ *     default stream) and the call returns after that stream has finished it,
+ *     like the reference launchers, which synchronise after every launch
+ *     (query/src/raytracing/RayLauncher.cpp:44-58, MeshOverlapEdgesLauncher.cpp:162-168);
+ *   - every call returns an rs_status and never exits the process.
+ *
+ * Section 2 keeps the reference's own extern "C" helper signatures so the
+ * reference host code links against this library unchanged.
+ */
+#ifndef RAYSPACE3D_H
+#define RAYSPACE3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rs_status {
+    RS_OK = 0,
+    RS_ERR_CUDA = 1,            /* a CUDA runtime call failed */
+    RS_ERR_INVALID = 2,         /* bad argument (null pointer, index out of range, size) */
+    RS_ERR_TABLE_FULL = 3,      /* pair table could not place a key (caller may grow and retry) */
+    RS_ERR_OUTPUT_OVERFLOW = 4, /* caller's output buffer is smaller than the result */
+    RS_ERR_ITER_LIMIT = 5,      /* an iteration budget ran out; result not valid */
+    RS_ERR_FORMAT = 6,          /* malformed input file */
+    RS_ERR_OOM = 7,             /* device allocation failed */
+    RS_ERR_TARGET_OVERFLOW = 8  /* containment ray crossed more distinct targets than supported */
+} rs_status;
+
+typedef struct rs_bvh rs_bvh;         /* triangle BVH of one geometry set, device resident */
+typedef struct rs_pairset rs_pairset; /* open-addressing table of (id1<<32 | id2) pair keys */
+
+/* ========================================================================== */
+/* 1. Engine entry points                                                      */
+/* ========================================================================== */
+
+/* Library version string and the size in bytes of the largest shared-memory
+ * configuration it was compiled for (diagnostics). */
+const char* rs_version(void);
+
+/* Build a BVH over all triangles of one set.
+ * Replaces OptixAccelerationStructure::buildInternal (query/src/optix/OptixAccelerationStructure.cpp:22-68),
+ * fed by GeometryUploader::upload (query/src/geometry/GeometryUploader.cpp:12-34).
+ * d_vertices: float32[nV*3]; d_indices: uint32[nF*3]; d_tri2obj: int32[nF].  The three
+ * arrays stay owned by the caller and must outlive the handle.  leaf_size in [1,8]
+ * (0 = default 4).  Fails with RS_ERR_INVALID if an index is >= nV. */
+int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                 const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream);
+int rs_bvh_destroy(rs_bvh* bvh);
+/* Number of triangles, nodes, engine-owned device bytes, and the bounds of all vertices. */
+int rs_bvh_info(const rs_bvh* bvh, uint64_t* n_tri, uint64_t* n_nodes, uint64_t* bytes,
+                float* h_min3, float* h_max3);
+
+/* Point-in-mesh parity (replaces __raygen__rg, query/src/cuda/raytracing.cu:9-78, launched by
+ * RayLauncher::launch, query/src/raytracing/RayLauncher.cpp:44-58).  One ray per point along
+ * (dx,dy,dz) (the reference uses +Z); hits are ordered by distance and counted with the
+ * reference's advance rule t_min = t + 1e-6.  d_obj[i] = object of the first counted hit
+ * when the count is odd, else -1 (RayResult.polygon_index); d_inside[i] = count & 1.
+ * Either output may be NULL.  d_points: float32[n*3]. */
+int rs_pim(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
+           int32_t* d_obj, uint8_t* d_inside, void* stream);
+
+/* Filter-refine (replaces FilterRefinePipeline::execute, query/src/raytracing/FilterRefine.cpp:81-122):
+ * parity against the 12-triangle box of all vertices (geometry/BoundingBox.cpp:12-50), then
+ * parity against the mesh for the points the box test keeps, in one fused launch. */
+int rs_pim_filtered(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
+                    int32_t* d_obj, uint8_t* d_inside, void* stream);
+
+/* Ordered compaction of point results (replaces ResultProcessor::compactAndDownload,
+ * query/src/raytracing/ResultProcessor.cpp:8-35): writes the ids of points with
+ * d_obj[i] != -1, ascending, to d_point_ids and their objects to d_point_obj; *h_count
+ * receives the number of hits.  RS_ERR_OUTPUT_OVERFLOW if it exceeds `capacity`. */
+int rs_compact_hits(const int32_t* d_obj, uint64_t n, int32_t* d_point_ids, int32_t* d_point_obj,
+                    uint64_t capacity, uint64_t* h_count, void* stream);
+
+/* Pair tables (the hash tables of query/src/cuda/mesh_overlap_edges.cu:62-104 and
+ * mesh_intersection.cu:108-132).  pow2 != 0: capacity is rounded up to a power of two and
+ * slots are hash & (capacity-1); pow2 == 0: slot = hash % capacity (the intersection
+ * variant).  A key that finds no slot raises RS_ERR_TABLE_FULL instead of being dropped. */
+int rs_pairset_create(uint64_t capacity, int pow2, rs_pairset** out, void* stream);
+int rs_pairset_clear(rs_pairset* ps, void* stream);
+int rs_pairset_destroy(rs_pairset* ps);
+/* Capacity in slots and number of distinct keys inserted so far. */
+int rs_pairset_info(const rs_pairset* ps, uint64_t* capacity, uint64_t* count, void* stream);
+
+/* Edge-ray overlap of one direction (replaces __raygen__mesh_overlap_edges,
+ * query/src/cuda/mesh_overlap_edges.cu:183-216, and __raygen__mesh_overlap,
+ * mesh_intersection.cu:288-334).  Each unique source edge is traced as the segment
+ * t in [1e-6, |e-s| + 1e-6] along normalize(e-s) against `target`; every crossed target
+ * object o and every source object k of the edge insert (k,o), or (o,k) when swap != 0.
+ * Edge arrays are the .pre v2 edge payload on the device (float32[nE*3] starts/ends,
+ * int32 offsets/counts[nE], int32 sources[]). */
+int rs_edge_join(const rs_bvh* target, const float* d_starts, const float* d_ends,
+                 const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources,
+                 uint64_t nE, int swap, rs_pairset* ps, void* stream);
+
+/* Containment fallback of one direction (replaces __raygen__mesh_containment_anyhit and
+ * __anyhit__ah_containment, query/src/cuda/mesh_intersection_anyhit.cu:46-240): for every
+ * source object, one +Z ray from the first vertex of its lowest-index triangle
+ * (raytracer_intersection_estimated_main.cpp:539-552), t in [1e-4, 1e10]; a target object
+ * crossed an odd number of times inserts (source,target), or (target,source) when swap. */
+int rs_containment(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
+                   const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj,
+                   int swap, rs_pairset* ps, void* stream);
+
+/* Sorted unique keys of a table (replaces compact_hash_table_pairs + the sort/unique of
+ * merge_and_deduplicate_pairs_gpu, query/src/cuda/mesh_query_deduplication.cu:56-144).
+ * order 0: ascending (id1,id2); order 1: ascending (id2,id1), the order of
+ * raytracer_mesh_overlap's output, whose dedup sorts MeshQueryResult{id1,id2} reinterpreted
+ * as a little-endian u64.  d_keys receives up to `capacity` keys (id1<<32 | id2) and
+ * *h_count the total; RS_ERR_OUTPUT_OVERFLOW if it exceeds capacity. */
+int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, uint64_t capacity,
+                        uint64_t* h_count, void* stream);
+
+/* Grid selectivity estimator (replaces estimateSelectivityKernel + thrust::reduce,
+ * query/src/cuda/estimated_overlap.cu:8-77 and estimated_intersection.cu:8-79, plus the host
+ * means calculateGlobalAvgSize / calculateGlobalAvgVolRatio,
+ * raytracer_overlap_estimated_main.cpp:129-158).  d_cells*: GridCell{u32 CenterCount,
+ * u32 TouchCount, f32 AvgSizeMean, f32 VolRatio}[ncells] on the device.  Writes the raw
+ * sum (per-cell float values summed in double, fixed order) and, when h_means is non-NULL,
+ * {avgSizeA, avgVolRatioA, avgSizeB, avgVolRatioB} as the reference host code computes them. */
+int rs_estimate_grid(const void* d_cellsA, const void* d_cellsB, uint64_t ncells, float cell_volume,
+                     float epsilon, float gamma, double* h_raw, float* h_means4, void* stream);
+
+/* Estimated pairs from the raw sum, as raytracer_overlap_estimated_main.cpp:275-291 does:
+ * alpha = max(1, ((sA*cbrt(rA)) + (sB*cbrt(rB)))^3 / cellVolume), est = (int64)((float)raw/alpha);
+ * alpha_correction == 0 uses alpha = 1 (raytracer_overlap_direct_estimation --no-alpha-correction). */
+int64_t rs_estimate_pairs_from_raw(double raw, const float* h_means4, float cell_volume, int alpha_correction);
+
+/* Hash table sizing rules of the reference:
+ *   pow2 variant (raytracer_overlap_estimated_main.cpp:316-325): nextPow2(clamp(est/0.5, 1024, 2^30)),
+ *     16777216 when est <= 0;
+ *   odd variant (raytracer_intersection_estimated_main.cpp:466-477): clamp(est/loadFactor, 1024, 2^30)
+ *     made odd, 16777216 when est <= 0. */
+uint64_t rs_hash_size_pow2(int64_t estimated_pairs);
+uint64_t rs_hash_size_odd(int64_t estimated_pairs, float load_factor);
+
+/* Full joins with automatic table growth on RS_ERR_TABLE_FULL.  The table `ps` is cleared
+ * first.  overlap: A-edges into B and B-edges into A (swapped).  intersection: overlap plus
+ * containment in both directions.  direction: 0 both, 1 mesh1->mesh2 only, 2 mesh2->mesh1 only
+ * (--query-direction). */
+int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_endsA, const int32_t* d_offsetsA,
+                    const int32_t* d_countsA, const int32_t* d_sourcesA, uint64_t nEA,
+                    const rs_bvh* B, const float* d_startsB, const float* d_endsB, const int32_t* d_offsetsB,
+                    const int32_t* d_countsB, const int32_t* d_sourcesB, uint64_t nEB,
+                    int direction, int with_containment, rs_pairset* ps, void* stream);
+
+/* Status text for a code. */
+const char* rs_status_string(int status);
+
+/* ========================================================================== */
+/* 2. Reference-compatible helpers (same names and signatures as the reference) */
+/* ========================================================================== */
+
+/* query/src/cuda/scan_utils.h:7-9 -- exclusive scan of int counts into int64 offsets; returns the total. */
+long long exclusive_scan_gpu(const int* d_input, long long* d_output, int num_elements);
+
+/* query/src/cuda/mesh_query_deduplication.h:6-18.  Pairs are MeshQueryResult{int,int} (8 bytes).
+ * merge: concatenates both inputs into d_merged_output, sorts them as little-endian u64 and
+ * removes duplicates; returns the unique count.  compact: copies occupied slots of a pair
+ * table, in slot order, to d_output; returns min(count, max_output_size). */
+long long merge_and_deduplicate_pairs_gpu(const void* d_results1, long long num_results1,
+                                          const void* d_results2, long long num_results2,
+                                          void* d_merged_output);
+int compact_hash_table_pairs(const unsigned long long* d_hash_table, unsigned long long table_size,
+                             void* d_output, int max_output_size);
+
+/* query/src/cuda/result_compaction.h:5-22.  RayResult{int ray_id; int polygon_index}. */
+int count_hits_gpu(const void* d_results, int num_results);
+void compact_hits_gpu(const void* d_input, void* d_output, int num_results, int* h_num_hits);
+
+/* query/src/cuda/estimated_overlap.h:6-13 and estimated_intersection.h: host GridCell arrays,
+ * returns the raw float estimate (-1.0f if device memory cannot be allocated). */
+float estimateOverlapSelectivity(const void* h_gridA, const void* h_gridB, int numCells, float cellVolume,
+                                 float epsilon, float gamma);
+float estimateIntersectionSelectivity(const void* h_gridA, const void* h_gridB, int numCells, float cellVolume,
+                                      float epsilon, float gamma);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAYSPACE3D_H */

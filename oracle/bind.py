@@ -1,0 +1,148 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE).
+
+Only tests/, ``__graft_entry__.smoke()`` and the cpu_baseline / reference leg of
+``bench.py`` may import this module.  It builds ``oracle/_build/liboracle.so`` from
+``oracle/oracle.cpp`` on first use if the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(LIB_DIR, "liboracle.so")
+
+_lib = None
+
+
+def build_cmd():
+    return ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
+            "-o", LIB_PATH, os.path.join(HERE, "oracle.cpp")]
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        os.makedirs(LIB_DIR, exist_ok=True)
+        subprocess.run(build_cmd(), check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        U64 = ctypes.c_uint64
+        F = ctypes.c_float
+        I = ctypes.c_int
+        L.orc_pim.argtypes = [P, U64, P, U64, P, P, U64, F, F, F, P, I, I]
+        L.orc_pim_filtered.argtypes = L.orc_pim.argtypes
+        L.orc_edge_join.argtypes = [P, P, P, P, P, U64, P, U64, P, U64, P, I,
+                                    ctypes.POINTER(ctypes.POINTER(U64)), ctypes.POINTER(U64), I, I]
+        L.orc_containment.argtypes = [P, U64, P, U64, P, P, U64, P, U64, P, I,
+                                      ctypes.POINTER(ctypes.POINTER(U64)), ctypes.POINTER(U64), I, I]
+        L.orc_estimate_raw.argtypes = [P, P, U64, F, F, F]
+        L.orc_estimate_raw.restype = ctypes.c_double
+        L.orc_estimate_pairs.argtypes = [P, P, U64, P, P, P, F, F, I, ctypes.POINTER(ctypes.c_double)]
+        L.orc_estimate_pairs.restype = ctypes.c_int64
+        L.orc_orient.argtypes = [P, P, P, P]
+        L.orc_perturbed_sign.argtypes = [P, P, P, P]
+        L.orc_free.argtypes = [P]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def pim(V, I, T, pts, direction=(0.0, 0.0, 1.0), threads=None, use_bvh=True, filtered=False):
+    """Object id of the first counted hit for points inside (odd parity), else -1."""
+    V, I, T, pts = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32), _c(pts, np.float32)
+    out = np.empty(len(pts), dtype=np.int32)
+    fn = lib().orc_pim_filtered if filtered else lib().orc_pim
+    fn(_p(V), len(V), _p(I), len(I), _p(T), _p(pts), len(pts), float(direction[0]),
+       float(direction[1]), float(direction[2]), _p(out), threads or os.cpu_count(), int(use_bvh))
+    return out
+
+
+def _take_keys(kp, nk):
+    n = int(nk.value)
+    out = np.ctypeslib.as_array(kp, shape=(max(n, 1),))[:n].copy() if n else np.zeros(0, np.uint64)
+    lib().orc_free(ctypes.cast(kp, ctypes.c_void_p))
+    return out
+
+
+def edge_join(edges, V, I, T, swap=False, threads=None, use_bvh=True):
+    """Sorted unique pair keys (id1<<32|id2) of one edge-ray direction."""
+    s, e = _c(edges.starts, np.float32), _c(edges.ends, np.float32)
+    off, cnt, src = _c(edges.offsets, np.int32), _c(edges.counts, np.int32), _c(edges.sources, np.int32)
+    V, I, T = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32)
+    kp = ctypes.POINTER(ctypes.c_uint64)()
+    nk = ctypes.c_uint64()
+    lib().orc_edge_join(_p(s), _p(e), _p(off), _p(cnt), _p(src), len(s), _p(V), len(V), _p(I), len(I), _p(T),
+                        int(swap), ctypes.byref(kp), ctypes.byref(nk), threads or os.cpu_count(), int(use_bvh))
+    return _take_keys(kp, nk)
+
+
+def containment(src_geom, V, I, T, swap=False, threads=None, use_bvh=True):
+    sV, sI, sT = _c(src_geom.vertices, np.float32), _c(src_geom.indices, np.uint32), _c(src_geom.tri2obj, np.int32)
+    V, I, T = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32)
+    kp = ctypes.POINTER(ctypes.c_uint64)()
+    nk = ctypes.c_uint64()
+    lib().orc_containment(_p(sV), len(sV), _p(sI), len(sI), _p(sT), _p(V), len(V), _p(I), len(I), _p(T),
+                          int(swap), ctypes.byref(kp), ctypes.byref(nk), threads or os.cpu_count(), int(use_bvh))
+    return _take_keys(kp, nk)
+
+
+def overlap_join(A, B, threads=None, use_bvh=True):
+    """Union of both edge directions: A-edges into B, B-edges into A (swapped)."""
+    k1 = edge_join(A.edges, B.vertices, B.indices, B.tri2obj, swap=False, threads=threads, use_bvh=use_bvh)
+    k2 = edge_join(B.edges, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh)
+    return np.union1d(k1, k2).astype(np.uint64)
+
+
+def intersection_join(A, B, threads=None, use_bvh=True):
+    """Overlap of both directions plus containment of both directions (sorted unique)."""
+    parts = [overlap_join(A, B, threads, use_bvh),
+             containment(A, B.vertices, B.indices, B.tri2obj, swap=False, threads=threads, use_bvh=use_bvh),
+             containment(B, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh)]
+    return np.unique(np.concatenate(parts)).astype(np.uint64)
+
+
+def estimate_raw(cellsA, cellsB, cell_volume, epsilon=0.001, gamma=0.8):
+    a = np.ascontiguousarray(cellsA)
+    b = np.ascontiguousarray(cellsB)
+    return lib().orc_estimate_raw(_p(a), _p(b), len(a), cell_volume, epsilon, gamma)
+
+
+def estimate_pairs(gridA, gridB, epsilon=0.001, gamma=0.8, alpha_correction=True):
+    a = np.ascontiguousarray(gridA.cells)
+    b = np.ascontiguousarray(gridB.cells)
+    mn = _c(gridA.min_bound, np.float32)
+    mx = _c(gridA.max_bound, np.float32)
+    rs = _c(gridA.resolution, np.uint32)
+    raw = ctypes.c_double()
+    est = lib().orc_estimate_pairs(_p(a), _p(b), len(a), _p(mn), _p(mx), _p(rs), epsilon, gamma,
+                                   int(alpha_correction), ctypes.byref(raw))
+    return int(est), float(raw.value)
+
+
+def orient(d, o, a, b):
+    arrs = [_c(x, np.float32) for x in (d, o, a, b)]
+    return lib().orc_orient(*[_p(x) for x in arrs])
+
+
+def perturbed_sign(d, o, a, b):
+    arrs = [_c(x, np.float32) for x in (d, o, a, b)]
+    return lib().orc_perturbed_sign(*[_p(x) for x in arrs])

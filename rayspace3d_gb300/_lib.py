@@ -1,0 +1,99 @@
+"""ctypes binding of librs.so (the C ABI declared in include/rayspace3d.h).
+
+There is no CPU fallback: importing the binding when the library has not been
+built raises, and every call that returns a non-zero rs_status raises RsError.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB_PATH
+
+RS_OK = 0
+RS_ERR_CUDA = 1
+RS_ERR_INVALID = 2
+RS_ERR_TABLE_FULL = 3
+RS_ERR_OUTPUT_OVERFLOW = 4
+RS_ERR_ITER_LIMIT = 5
+RS_ERR_FORMAT = 6
+RS_ERR_OOM = 7
+RS_ERR_TARGET_OVERFLOW = 8
+
+# Every entry point of include/rayspace3d.h: name -> (restype, argtypes).
+P = ctypes.c_void_p
+U64 = ctypes.c_uint64
+I64 = ctypes.c_int64
+F = ctypes.c_float
+I = ctypes.c_int
+PP = ctypes.POINTER(ctypes.c_void_p)
+PU64 = ctypes.POINTER(ctypes.c_uint64)
+
+SIGNATURES = {
+    "rs_version": (ctypes.c_char_p, []),
+    "rs_status_string": (ctypes.c_char_p, [I]),
+    "rs_bvh_build": (I, [P, U64, P, U64, P, I, PP, P]),
+    "rs_bvh_destroy": (I, [P]),
+    "rs_bvh_info": (I, [P, PU64, PU64, PU64, P, P]),
+    "rs_pim": (I, [P, P, U64, F, F, F, P, P, P]),
+    "rs_pim_filtered": (I, [P, P, U64, F, F, F, P, P, P]),
+    "rs_compact_hits": (I, [P, U64, P, P, U64, PU64, P]),
+    "rs_pairset_create": (I, [U64, I, PP, P]),
+    "rs_pairset_clear": (I, [P, P]),
+    "rs_pairset_destroy": (I, [P]),
+    "rs_pairset_info": (I, [P, PU64, PU64, P]),
+    "rs_edge_join": (I, [P, P, P, P, P, P, U64, I, P, P]),
+    "rs_containment": (I, [P, P, U64, P, U64, P, I, P, P]),
+    "rs_pairset_finalize": (I, [P, I, P, U64, PU64, P]),
+    "rs_estimate_grid": (I, [P, P, U64, F, F, F, ctypes.POINTER(ctypes.c_double), P, P]),
+    "rs_estimate_pairs_from_raw": (I64, [ctypes.c_double, P, F, I]),
+    "rs_hash_size_pow2": (U64, [I64]),
+    "rs_hash_size_odd": (U64, [I64, F]),
+    "rs_overlap_join": (I, [P, P, P, P, P, P, U64, P, P, P, P, P, P, U64, I, I, P, P]),
+    "exclusive_scan_gpu": (ctypes.c_longlong, [P, P, I]),
+    "merge_and_deduplicate_pairs_gpu": (ctypes.c_longlong, [P, ctypes.c_longlong, P, ctypes.c_longlong, P]),
+    "compact_hash_table_pairs": (I, [P, ctypes.c_ulonglong, P, I]),
+    "count_hits_gpu": (I, [P, I]),
+    "compact_hits_gpu": (None, [P, P, I, ctypes.POINTER(ctypes.c_int)]),
+    "estimateOverlapSelectivity": (F, [P, P, I, F, F, F]),
+    "estimateIntersectionSelectivity": (F, [P, P, I, F, F, F]),
+}
+
+_lib = None
+
+
+class RsError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: rs_status {status} ({status_string(status)})")
+
+
+def load(path: str = LIB_PATH):
+    """Load librs.so; raises if it is missing (build it with __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"librs.so not found at {path}: the CUDA engine is not built "
+                           "(run `python -c 'import __graft_entry__ as g; g.build()'`)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().rs_status_string(status).decode()
+    except Exception:  # pragma: no cover - only when the library is absent
+        return "?"
+
+
+def check(status: int, what: str) -> None:
+    if status != RS_OK:
+        raise RsError(status, what)

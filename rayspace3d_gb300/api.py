@@ -1,0 +1,241 @@
+"""Python host API over librs.so, shaped like the reference's host layer.
+
+Reference counterparts:
+  DeviceGeometry.upload      GeometryUploader::upload + PrecomputedEdgeData::uploadFromGeometry
+                             (query/src/geometry/GeometryUploader.cpp:12-34, PrecomputedEdgeData.cpp:5-35)
+  Bvh                        OptixAccelerationStructure (query/src/optix/OptixAccelerationStructure.cpp:22-68)
+  point_in_mesh              RayLauncher::launch + ResultProcessor (query/src/raytracing/RayLauncher.cpp:44-58)
+  filter_refine              FilterRefinePipeline::execute (query/src/raytracing/FilterRefine.cpp:81-122)
+  PairSet / overlap_join     executeHashQuery of the estimated mains
+                             (query/src/applications/raytracer_overlap_estimated_main.cpp:39-112,
+                              raytracer_intersection_estimated_main.cpp:77-176)
+  estimate_pairs             estimatePairs (raytracer_overlap_estimated_main.cpp:252-325)
+PyTorch supplies device memory and streams only; all compute is in librs.so.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from .formats import Geometry, Grid
+
+_check = _lib.check
+
+
+def _stream(stream: Optional[torch.cuda.Stream] = None) -> ctypes.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("device tensor expected")
+    if not t.is_contiguous():
+        raise ValueError("contiguous tensor expected")
+    return t.data_ptr()
+
+
+class DeviceGeometry:
+    """One .pre geometry set resident on the GPU (vertices, indices, tri2obj, edges, grid)."""
+
+    def __init__(self, g: Geometry, device: str = "cuda"):
+        self.host = g
+        dev = torch.device(device)
+        self.V = torch.from_numpy(np.ascontiguousarray(g.vertices, np.float32)).to(dev)
+        self.I = torch.from_numpy(np.ascontiguousarray(g.indices, np.uint32).view(np.int32)).to(dev)
+        self.T = torch.from_numpy(np.ascontiguousarray(g.tri2obj, np.int32)).to(dev)
+        self.nV = int(len(g.vertices))
+        self.nF = int(len(g.indices))
+        self.edges = None
+        if g.edges is not None and len(g.edges.starts):
+            e = g.edges
+            self.edges = (torch.from_numpy(np.ascontiguousarray(e.starts, np.float32)).to(dev),
+                          torch.from_numpy(np.ascontiguousarray(e.ends, np.float32)).to(dev),
+                          torch.from_numpy(np.ascontiguousarray(e.offsets, np.int32)).to(dev),
+                          torch.from_numpy(np.ascontiguousarray(e.counts, np.int32)).to(dev),
+                          torch.from_numpy(np.ascontiguousarray(e.sources, np.int32)).to(dev))
+            self.nE = int(len(e.starts))
+        else:
+            self.nE = 0
+        self.cells = None
+        if g.grid is not None:
+            raw = np.ascontiguousarray(g.grid.cells).view(np.uint8)
+            self.cells = torch.from_numpy(raw.copy()).to(dev)
+
+    def edge_ptrs(self):
+        if self.edges is None:
+            raise ValueError("geometry has no precomputed edge payload")
+        return [t.data_ptr() for t in self.edges]
+
+
+class Bvh:
+    """Engine-owned BVH over a DeviceGeometry (which must stay alive)."""
+
+    def __init__(self, geom: DeviceGeometry, leaf_size: int = 0, stream=None):
+        self.geom = geom
+        h = ctypes.c_void_p()
+        _check(_lib.load().rs_bvh_build(_ptr(geom.V), geom.nV, _ptr(geom.I), geom.nF, _ptr(geom.T), leaf_size,
+                                        ctypes.byref(h), _stream(stream)), "rs_bvh_build")
+        self.handle = h
+
+    def info(self):
+        nt, nn, nb = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        mn = (ctypes.c_float * 3)()
+        mx = (ctypes.c_float * 3)()
+        _check(_lib.load().rs_bvh_info(self.handle, ctypes.byref(nt), ctypes.byref(nn), ctypes.byref(nb), mn, mx),
+               "rs_bvh_info")
+        return {"triangles": nt.value, "nodes": nn.value, "bytes": nb.value, "min": list(mn), "max": list(mx)}
+
+    def close(self):
+        if self.handle:
+            _lib.load().rs_bvh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def point_in_mesh(bvh: Bvh, points: torch.Tensor, direction=(0.0, 0.0, 1.0), filtered: bool = False,
+                  out_obj: Optional[torch.Tensor] = None, out_inside: Optional[torch.Tensor] = None,
+                  stream=None) -> Tuple[torch.Tensor, torch.Tensor]:
+    """Object of the first counted hit (or -1) and the inside bit for each point (float32[n,3] on the GPU)."""
+    n = int(points.shape[0])
+    if out_obj is None:
+        out_obj = torch.empty(n, dtype=torch.int32, device=points.device)
+    if out_inside is None:
+        out_inside = torch.empty(n, dtype=torch.uint8, device=points.device)
+    fn = _lib.load().rs_pim_filtered if filtered else _lib.load().rs_pim
+    _check(fn(bvh.handle, _ptr(points), n, float(direction[0]), float(direction[1]), float(direction[2]),
+              _ptr(out_obj), _ptr(out_inside), _stream(stream)), "rs_pim")
+    return out_obj, out_inside
+
+
+def compact_hits(obj: torch.Tensor, stream=None) -> Tuple[torch.Tensor, torch.Tensor]:
+    """(point ids, objects) of the points with obj != -1, in ascending point order."""
+    n = int(obj.numel())
+    ids = torch.empty(max(n, 1), dtype=torch.int32, device=obj.device)
+    objs = torch.empty(max(n, 1), dtype=torch.int32, device=obj.device)
+    cnt = ctypes.c_uint64()
+    _check(_lib.load().rs_compact_hits(_ptr(obj), n, _ptr(ids), _ptr(objs), n, ctypes.byref(cnt), _stream(stream)),
+           "rs_compact_hits")
+    return ids[:cnt.value], objs[:cnt.value]
+
+
+class PairSet:
+    """Open-addressing table of pair keys (id1<<32 | id2)."""
+
+    def __init__(self, capacity: int, pow2: bool = True, stream=None):
+        h = ctypes.c_void_p()
+        _check(_lib.load().rs_pairset_create(int(capacity), int(pow2), ctypes.byref(h), _stream(stream)),
+               "rs_pairset_create")
+        self.handle = h
+
+    def clear(self, stream=None):
+        _check(_lib.load().rs_pairset_clear(self.handle, _stream(stream)), "rs_pairset_clear")
+
+    def info(self, stream=None):
+        cap, cnt = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(_lib.load().rs_pairset_info(self.handle, ctypes.byref(cap), ctypes.byref(cnt), _stream(stream)),
+               "rs_pairset_info")
+        return cap.value, cnt.value
+
+    def finalize(self, order: int = 0, stream=None) -> torch.Tensor:
+        """Sorted unique keys as an int64 tensor on the GPU (bit pattern of the u64 keys)."""
+        _, cnt = self.info(stream)
+        out = torch.empty(max(cnt, 1), dtype=torch.int64, device="cuda")
+        n = ctypes.c_uint64()
+        _check(_lib.load().rs_pairset_finalize(self.handle, int(order), _ptr(out), cnt, ctypes.byref(n),
+                                               _stream(stream)), "rs_pairset_finalize")
+        return out[:n.value]
+
+    def close(self):
+        if self.handle:
+            _lib.load().rs_pairset_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def edge_join(target: Bvh, source: DeviceGeometry, ps: PairSet, swap: bool = False, stream=None) -> None:
+    s, e, off, cnt, src = source.edge_ptrs()
+    _check(_lib.load().rs_edge_join(target.handle, s, e, off, cnt, src, source.nE, int(swap), ps.handle,
+                                    _stream(stream)), "rs_edge_join")
+
+
+def containment(target: Bvh, source: DeviceGeometry, ps: PairSet, swap: bool = False, stream=None) -> None:
+    _check(_lib.load().rs_containment(target.handle, _ptr(source.V), source.nV, _ptr(source.I), source.nF,
+                                      _ptr(source.T), int(swap), ps.handle, _stream(stream)), "rs_containment")
+
+
+def overlap_join(A: Bvh, B: Bvh, ps: PairSet, direction: int = 0, with_containment: bool = False,
+                 stream=None) -> None:
+    """Both edge directions (and containment when asked) into ps, growing it on overflow."""
+    ea = A.geom.edge_ptrs()
+    eb = B.geom.edge_ptrs()
+    _check(_lib.load().rs_overlap_join(A.handle, *ea, A.geom.nE, B.handle, *eb, B.geom.nE, int(direction),
+                                       int(with_containment), ps.handle, _stream(stream)), "rs_overlap_join")
+
+
+def keys_to_pairs(keys) -> np.ndarray:
+    """u64 keys (id1<<32 | id2) -> int32[n,2] (id1, id2)."""
+    k = np.asarray(keys.cpu().numpy() if isinstance(keys, torch.Tensor) else keys).astype(np.uint64)
+    return np.stack([(k >> np.uint64(32)).astype(np.int64), (k & np.uint64(0xffffffff)).astype(np.int64)],
+                    axis=1).astype(np.int32)
+
+
+def cell_volume(grid: Grid) -> float:
+    """Cell volume from mesh1's grid bounds as raytracer_overlap_estimated_main.cpp:256-262 computes it."""
+    f32 = np.float32
+    w = f32(grid.max_bound[0]) - f32(grid.min_bound[0])
+    h = f32(grid.max_bound[1]) - f32(grid.min_bound[1])
+    d = f32(grid.max_bound[2]) - f32(grid.min_bound[2])
+    cx = f32(w / f32(grid.resolution[0]))
+    cy = f32(h / f32(grid.resolution[1]))
+    cz = f32(d / f32(grid.resolution[2]))
+    return float(f32(f32(cx * cy) * cz))
+
+
+def estimate_grid(cellsA: torch.Tensor, cellsB: torch.Tensor, ncells: int, cell_vol: float, epsilon: float = 0.001,
+                  gamma: float = 0.8, stream=None):
+    raw = ctypes.c_double()
+    means = (ctypes.c_float * 4)()
+    _check(_lib.load().rs_estimate_grid(_ptr(cellsA), _ptr(cellsB), int(ncells), float(cell_vol), float(epsilon),
+                                        float(gamma), ctypes.byref(raw), means, _stream(stream)), "rs_estimate_grid")
+    return raw.value, list(means)
+
+
+def estimate_pairs(A: DeviceGeometry, B: DeviceGeometry, epsilon: float = 0.001, gamma: float = 0.8,
+                   alpha_correction: bool = True, stream=None) -> Tuple[int, float]:
+    """Estimated pair count (0 when either set has no grid or the grids differ in size)."""
+    ga, gb = A.host.grid, B.host.grid
+    if ga is None or gb is None or A.cells is None or B.cells is None:
+        return 0, 0.0
+    ncells = int(ga.resolution[0]) * int(ga.resolution[1]) * int(ga.resolution[2])
+    if len(ga.cells) != ncells or len(gb.cells) != ncells:
+        return 0, 0.0
+    cv = cell_volume(ga)
+    raw, means = estimate_grid(A.cells, B.cells, ncells, cv, epsilon, gamma, stream)
+    m = (ctypes.c_float * 4)(*means)
+    est = _lib.load().rs_estimate_pairs_from_raw(raw, m, cv, int(alpha_correction))
+    return int(est), raw
+
+
+def hash_size_pow2(est: int) -> int:
+    return int(_lib.load().rs_hash_size_pow2(int(est)))
+
+
+def hash_size_odd(est: int, load_factor: float = 0.5) -> int:
+    return int(_lib.load().rs_hash_size_odd(int(est), float(load_factor)))

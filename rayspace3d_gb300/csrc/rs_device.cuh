@@ -1,0 +1,378 @@
+// rs_device.cuh -- device-side geometry of the engine's hit contract.
+//
+// The reference traces rays with OptiX (query/src/cuda/raytracing.cu:34-46,
+// mesh_overlap_edges.cu:135-145, mesh_intersection_anyhit.cu:92-106), whose
+// ray/triangle test is closed.  The engine instead fixes an exact contract:
+//
+//  * a triangle is crossed when the ray origin, perturbed symbolically by
+//    delta*e_kx + delta^2*e_ky (kx, ky = the two axes other than the dominant
+//    axis of d), lies strictly inside the triangle's projection along d.  The
+//    three edge signs are exact: an FP32 evaluation with a static forward-error
+//    bound decides almost every case, and the rest are re-evaluated exactly as a
+//    sum of 36 FP64 triple products (each product of three floats is exactly a
+//    two-term FP64 expansion) accumulated into a non-overlapping expansion;
+//  * the hit distance is a fixed sequence of individually rounded float
+//    operations (no contraction), clamped to the slab interval of the
+//    triangle's own box, and accepted when it lies in [tmin, tmax];
+//  * box tests use the same slab formula, which is monotone in the box bounds,
+//    so BVH culling never changes the hit set.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rs {
+
+// ---------------------------------------------------------------------------
+// Status bits raised by kernels (OR-ed into a device word).
+// ---------------------------------------------------------------------------
+enum : uint32_t {
+    ST_TABLE_FULL = 1u << 0,     // a pair key found no free slot within the probe limit
+    ST_HIT_OVERFLOW = 1u << 1,   // a per-ray hit list overflowed (handled by a fallback pass)
+    ST_STACK_OVERFLOW = 1u << 2, // a traversal stack overflowed (result invalid)
+    ST_ITER_LIMIT = 1u << 3,     // an iteration budget ran out (result invalid)
+    ST_TARGET_OVERFLOW = 1u << 4 // containment: more distinct targets than the per-ray list holds
+};
+
+// ---------------------------------------------------------------------------
+// Exact FP64 building blocks (Knuth two-sum, FMA two-product, Shewchuk
+// grow-expansion).  Intrinsics keep the compiler from re-associating them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double two_sum(double a, double b, double& err) {
+    double s = __dadd_rn(a, b);
+    double bb = __dsub_rn(s, a);
+    double aa = __dsub_rn(s, bb);
+    err = __dadd_rn(__dsub_rn(a, aa), __dsub_rn(b, bb));
+    return s;
+}
+
+__device__ __forceinline__ double two_prod(double a, double b, double& err) {
+    double p = __dmul_rn(a, b);
+    err = __fma_rn(a, b, -p);
+    return p;
+}
+
+// Adds b into the non-overlapping expansion e[0..m) (increasing magnitude),
+// dropping zero components.  Returns the new length (<= m+1).
+__device__ __forceinline__ int grow_expansion(double* e, int m, double b) {
+    double q = b;
+    int k = 0;
+    for (int i = 0; i < m; ++i) {
+        double h;
+        q = two_sum(q, e[i], h);
+        if (h != 0.0) e[k++] = h;
+    }
+    if (q != 0.0) e[k++] = q;
+    return k;
+}
+
+__device__ __forceinline__ int expansion_sign(const double* e, int m) {
+    if (m == 0) return 0;
+    double top = e[m - 1];
+    return top > 0.0 ? 1 : (top < 0.0 ? -1 : 0);
+}
+
+// Exact sign of det[d, a-o, b-o] = d . (a x b + b x o + o x a).
+static __device__ __noinline__ int orient_exact(const float* d, const float* o, const float* a, const float* b) {
+    double e[40];
+    int m = 0;
+    const float* X[3] = {a, b, o};
+    const float* Y[3] = {b, o, a};
+#pragma unroll 1
+    for (int k = 0; k < 3; ++k) {
+        if (d[k] == 0.0f) continue;
+        const int i = (k + 1) % 3, j = (k + 2) % 3;
+        const double dk = (double)d[k];
+#pragma unroll 1
+        for (int s = 0; s < 3; ++s) {
+            double p = __dmul_rn((double)X[s][i], (double)Y[s][j]);  // exact: 48-bit product
+            double q = __dmul_rn((double)X[s][j], (double)Y[s][i]);
+            double lo;
+            double hi = two_prod(dk, p, lo);
+            m = grow_expansion(e, m, hi);
+            m = grow_expansion(e, m, lo);
+            hi = two_prod(dk, -q, lo);
+            m = grow_expansion(e, m, hi);
+            m = grow_expansion(e, m, lo);
+        }
+    }
+    return expansion_sign(e, m);
+}
+
+// Exact sign of det[d, e_k, b-a] = d_j (b_i - a_i) - d_i (b_j - a_j).
+__device__ __forceinline__ int axis_det_exact(const float* d, int k, const float* a, const float* b) {
+    const int i = (k + 1) % 3, j = (k + 2) % 3;
+    double e[5];
+    int m = 0;
+    m = grow_expansion(e, m, __dmul_rn((double)d[j], (double)b[i]));
+    m = grow_expansion(e, m, -__dmul_rn((double)d[j], (double)a[i]));
+    m = grow_expansion(e, m, -__dmul_rn((double)d[i], (double)b[j]));
+    m = grow_expansion(e, m, __dmul_rn((double)d[i], (double)a[j]));
+    return expansion_sign(e, m);
+}
+
+// FP32 filter for det[d, a-o, b-o].  Roundings on any elementary product are at
+// most 7 (two input differences, product, difference, scale by d, two sums), so
+// |computed - exact| <= 7.01u * M with u = 2^-24 and M the float magnitude sum;
+// 12u is used.  Tiny or non-finite magnitudes go to the exact path.
+template <int AXIS>
+__device__ __forceinline__ int orient_sign(const float* d, const float* o, const float* a, const float* b) {
+    float A[3], B[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        A[k] = __fsub_rn(a[k], o[k]);
+        B[k] = __fsub_rn(b[k], o[k]);
+    }
+    float det, mag;
+    if (AXIS >= 0) {
+        // d = +e_AXIS: det = A_i B_j - A_j B_i with i = AXIS+1, j = AXIS+2 (mod 3).
+        const int i = (AXIS + 1) % 3, j = (AXIS + 2) % 3;
+        float p = __fmul_rn(A[i], B[j]), q = __fmul_rn(A[j], B[i]);
+        det = __fsub_rn(p, q);
+        mag = __fadd_rn(fabsf(p), fabsf(q));
+    } else {
+        det = 0.0f;
+        mag = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int i = (k + 1) % 3, j = (k + 2) % 3;
+            float p = __fmul_rn(A[i], B[j]), q = __fmul_rn(A[j], B[i]);
+            float c = __fsub_rn(p, q);
+            det = __fadd_rn(det, __fmul_rn(d[k], c));
+            mag = __fadd_rn(mag, __fmul_rn(fabsf(d[k]), __fadd_rn(fabsf(p), fabsf(q))));
+        }
+    }
+    const float bound = __fmul_rn(mag, 12.0f * 5.9604644775390625e-08f);
+    if (mag > 7.888609052210118e-31f && mag < 3.0e38f) {  // 2^-100 < M < overflow
+        if (det > bound) return 1;
+        if (det < -bound) return -1;
+    }
+    return orient_exact(d, o, a, b);
+}
+
+// Edge sign of (a,b) for the perturbed origin (see file header).
+template <int AXIS>
+__device__ __forceinline__ int perturbed_sign(const float* d, const float* o, const float* a, const float* b,
+                                              int kx, int ky) {
+    int s = orient_sign<AXIS>(d, o, a, b);
+    if (s) return s;
+    if (AXIS >= 0) {
+        // d = +e_AXIS, kx = AXIS+1, ky = AXIS+2 (mod 3):
+        // det[d,e_kx,b-a] = b_ky - a_ky and det[d,e_ky,b-a] = -(b_kx - a_kx), so the
+        // perturbation terms are -(b_ky - a_ky) and then +(b_kx - a_kx).
+        const int kxa = (AXIS + 1) % 3, kya = (AXIS + 2) % 3;
+        if (b[kya] != a[kya]) return b[kya] > a[kya] ? -1 : 1;
+        if (b[kxa] != a[kxa]) return b[kxa] > a[kxa] ? 1 : -1;
+        return 0;
+    }
+    s = -axis_det_exact(d, kx, a, b);
+    if (s) return s;
+    return -axis_det_exact(d, ky, a, b);
+}
+
+// ---------------------------------------------------------------------------
+// Rays and the slab rule.
+// ---------------------------------------------------------------------------
+struct Ray {
+    float o[3], d[3], inv[3];
+    int zero[3];
+    int kx, ky;
+    float tmin, tmax;
+};
+
+__device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, float dy, float dz,
+                                        float tmin, float tmax) {
+    Ray r;
+    r.o[0] = ox; r.o[1] = oy; r.o[2] = oz;
+    r.d[0] = dx; r.d[1] = dy; r.d[2] = dz;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        r.zero[k] = 0;
+        r.inv[k] = 0.0f;
+        if (r.d[k] == 0.0f) {
+            r.zero[k] = 1;
+        } else {
+            r.inv[k] = __fdiv_rn(1.0f, r.d[k]);
+            if (isinf(r.inv[k])) r.zero[k] = 1;
+        }
+    }
+    int kz = 2;
+    if (fabsf(r.d[0]) > fabsf(r.d[kz])) kz = 0;
+    if (fabsf(r.d[1]) > fabsf(r.d[kz])) kz = 1;
+    r.kx = (kz + 1) % 3;
+    r.ky = (kz + 2) % 3;
+    r.tmin = tmin;
+    r.tmax = tmax;
+    return r;
+}
+
+// Slab interval of [lo,hi] intersected with [en,ex].  For AXIS >= 0 the ray is
+// +e_AXIS and the two other axes reduce to exact containment tests.
+template <int AXIS>
+__device__ __forceinline__ bool slab(const Ray& r, const float* lo, const float* hi, float en, float ex,
+                                     float& enter, float& exit) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const bool zero = (AXIS >= 0) ? (k != AXIS) : (r.zero[k] != 0);
+        if (zero) {
+            if (r.o[k] < lo[k] || r.o[k] > hi[k]) return false;
+            continue;
+        }
+        float inv = (AXIS >= 0) ? 1.0f : r.inv[k];
+        float t1 = (AXIS >= 0) ? __fsub_rn(lo[k], r.o[k]) : __fmul_rn(__fsub_rn(lo[k], r.o[k]), inv);
+        float t2 = (AXIS >= 0) ? __fsub_rn(hi[k], r.o[k]) : __fmul_rn(__fsub_rn(hi[k], r.o[k]), inv);
+        float tn = inv > 0.0f ? t1 : t2;
+        float tf = inv > 0.0f ? t2 : t1;
+        en = tn > en ? tn : en;
+        ex = tf < ex ? tf : ex;
+    }
+    enter = en;
+    exit = ex;
+    return en <= ex;
+}
+
+// The triangle hit contract.  Returns true and the hit distance t when the
+// triangle (a,b,c) is crossed with t in [tmin, tmax].
+template <int AXIS>
+__device__ __forceinline__ bool hit_triangle(const Ray& r, const float* a, const float* b, const float* c, float& t) {
+    float lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float mn = a[k] < b[k] ? a[k] : b[k];
+        mn = c[k] < mn ? c[k] : mn;
+        float mx = a[k] > b[k] ? a[k] : b[k];
+        mx = c[k] > mx ? c[k] : mx;
+        lo[k] = mn;
+        hi[k] = mx;
+    }
+    float en, ex;
+    if (!slab<AXIS>(r, lo, hi, -INFINITY, INFINITY, en, ex)) return false;
+    // Cheap reject before the sign tests: the clamped t lies in [en, ex].
+    if (ex < r.tmin || en > r.tmax) return false;
+    const int s0 = perturbed_sign<AXIS>(r.d, r.o, a, b, r.kx, r.ky);
+    if (s0 == 0) return false;
+    if (perturbed_sign<AXIS>(r.d, r.o, b, c, r.kx, r.ky) != s0) return false;
+    if (perturbed_sign<AXIS>(r.d, r.o, c, a, r.kx, r.ky) != s0) return false;
+    const float e1x = __fsub_rn(b[0], a[0]), e1y = __fsub_rn(b[1], a[1]), e1z = __fsub_rn(b[2], a[2]);
+    const float e2x = __fsub_rn(c[0], a[0]), e2y = __fsub_rn(c[1], a[1]), e2z = __fsub_rn(c[2], a[2]);
+    const float nx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
+    const float ny = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
+    const float nz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
+    const float wx = __fsub_rn(a[0], r.o[0]), wy = __fsub_rn(a[1], r.o[1]), wz = __fsub_rn(a[2], r.o[2]);
+    const float num = __fadd_rn(__fadd_rn(__fmul_rn(wx, nx), __fmul_rn(wy, ny)), __fmul_rn(wz, nz));
+    const float den = __fadd_rn(__fadd_rn(__fmul_rn(r.d[0], nx), __fmul_rn(r.d[1], ny)), __fmul_rn(r.d[2], nz));
+    const float traw = __fdiv_rn(num, den);
+    t = (traw >= en) ? ((traw <= ex) ? traw : ex) : en;
+    return t >= r.tmin && t <= r.tmax;
+}
+
+// ---------------------------------------------------------------------------
+// BVH layout in HBM.  One 64-byte node holds both child boxes; a child with
+// count > 0 is a leaf of `count` consecutive triangles starting at `idx`,
+// count == 0 is the internal node `idx`.  Triangles are three float4 each in
+// leaf order: (v0, original triangle id), (v1, object id), (v2, 0).
+// ---------------------------------------------------------------------------
+struct __align__(16) BNode {
+    float4 a;  // lo0.x lo0.y lo0.z hi0.x
+    float4 b;  // hi0.y hi0.z lo1.x lo1.y
+    float4 c;  // lo1.z hi1.x hi1.y hi1.z
+    int4 d;    // idx0 count0 idx1 count1
+};
+
+constexpr int kStack = 64;
+
+// Visits every leaf whose box passes the slab test and calls on_leaf(first, count)
+// for it.  A valid tree visits each node at most once, so `max_steps` (the node
+// count) bounds the loop even if the node array were corrupt.  Returns false on
+// stack overflow or an exhausted step budget.
+template <int AXIS, class F>
+__device__ __forceinline__ bool traverse(const BNode* __restrict__ nodes, uint32_t max_steps, const Ray& r,
+                                         F&& on_leaf) {
+    int stack[kStack];
+    int sp = 0;
+    int node = 0;
+    for (uint32_t step = 0;; ++step) {
+        if (step > max_steps) return false;
+        const float4 na = __ldg(&nodes[node].a);
+        const float4 nb = __ldg(&nodes[node].b);
+        const float4 nc = __ldg(&nodes[node].c);
+        const int4 nd = __ldg(&nodes[node].d);
+        const float lo0[3] = {na.x, na.y, na.z}, hi0[3] = {na.w, nb.x, nb.y};
+        const float lo1[3] = {nb.z, nb.w, nc.x}, hi1[3] = {nc.y, nc.z, nc.w};
+        float e, x;
+        bool h0 = slab<AXIS>(r, lo0, hi0, r.tmin, r.tmax, e, x);
+        bool h1 = slab<AXIS>(r, lo1, hi1, r.tmin, r.tmax, e, x);
+        if (h0 && nd.y > 0) { on_leaf(nd.x, nd.y); h0 = false; }
+        if (h1 && nd.w > 0) { on_leaf(nd.z, nd.w); h1 = false; }
+        if (h0 && h1) {
+            if (sp == kStack) return false;
+            stack[sp++] = nd.z;
+            node = nd.x;
+        } else if (h0) {
+            node = nd.x;
+        } else if (h1) {
+            node = nd.z;
+        } else {
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void load_tri(const float4* __restrict__ tris, int k, float* a, float* b, float* c,
+                                         uint32_t& tri_id, int32_t& obj) {
+    const float4 p = __ldg(&tris[3 * (size_t)k]);
+    const float4 q = __ldg(&tris[3 * (size_t)k + 1]);
+    const float4 s = __ldg(&tris[3 * (size_t)k + 2]);
+    a[0] = p.x; a[1] = p.y; a[2] = p.z;
+    b[0] = q.x; b[1] = q.y; b[2] = q.z;
+    c[0] = s.x; c[1] = s.y; c[2] = s.z;
+    tri_id = __float_as_uint(p.w);
+    obj = __float_as_int(q.w);
+}
+
+// ---------------------------------------------------------------------------
+// Pair hash table: open addressing, linear probing, MurmurHash3 fmix64 of the
+// key (id1<<32 | id2), empty slot = all ones (mesh_overlap_edges.cu:62-104).
+// ---------------------------------------------------------------------------
+constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+
+__device__ __forceinline__ unsigned long long fmix64(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+struct PairTable {
+    unsigned long long* slots;
+    unsigned long long capacity;  // power of two when pow2 != 0
+    int pow2;
+    unsigned int max_probes;
+    unsigned int* status;         // OR of ST_* bits
+    unsigned long long* count;    // number of distinct keys inserted
+};
+
+__device__ __forceinline__ void table_insert(const PairTable& t, unsigned long long key) {
+    const unsigned long long h = fmix64(key);
+    unsigned long long slot = t.pow2 ? (h & (t.capacity - 1)) : (h % t.capacity);
+    for (unsigned int i = 0; i < t.max_probes; ++i) {
+        unsigned long long cur = t.slots[slot];
+        if (cur == key) return;
+        if (cur == kEmptyKey) {
+            unsigned long long old = atomicCAS(&t.slots[slot], kEmptyKey, key);
+            if (old == kEmptyKey) {
+                atomicAdd(t.count, 1ull);
+                return;
+            }
+            if (old == key) return;
+        }
+        slot = slot + 1;
+        if (slot == t.capacity) slot = 0;
+    }
+    atomicOr(t.status, ST_TABLE_FULL);
+}
+
+}  // namespace rs

@@ -1,0 +1,43 @@
+// rs_engine.h -- engine-internal host structures behind the opaque C-ABI handles.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rayspace3d.h"
+#include "rs_device.cuh"
+
+struct rs_bvh {
+    // Caller-owned device inputs; they must outlive the handle.
+    const float* V = nullptr;
+    uint64_t nV = 0;
+    const uint32_t* I = nullptr;
+    uint64_t nF = 0;
+    const int32_t* t2o = nullptr;
+    // Engine-owned device arrays.
+    rs::BNode* nodes = nullptr;
+    uint64_t n_nodes = 0;
+    float4* tris = nullptr;
+    uint64_t n_tris = 0;
+    int leaf_size = 4;
+    // Bounds of all vertices (the reference's BoundingBox::computeFromGeometry).
+    float vmin[3] = {0, 0, 0};
+    float vmax[3] = {0, 0, 0};
+    int device = 0;
+};
+
+struct rs_pairset {
+    unsigned long long* slots = nullptr;
+    unsigned long long capacity = 0;
+    int pow2 = 1;
+    unsigned int max_probes = 4096;
+    // Device scratch: [0] status bits (u32 in the low word), [1] distinct-key count.
+    unsigned long long* meta = nullptr;
+    int device = 0;
+};
+
+namespace rs {
+// Upper bound on the node visits of one traversal of a valid tree.
+inline uint32_t max_steps(const rs_bvh* b) { return (uint32_t)(2 * b->n_nodes + 8); }
+int to_status(cudaError_t e);
+int status_from_bits(uint32_t bits);
+}  // namespace rs

@@ -1,0 +1,214 @@
+// rs_pairs.cu -- pair tables, deterministic finalisation and the join drivers.
+//
+// Replaces the hash-table lifecycle of executeHashQuery
+// (query/src/applications/raytracer_overlap_estimated_main.cpp:39-112,
+// raytracer_intersection_estimated_main.cpp:77-176), compact_hash_table_pairs and
+// merge_and_deduplicate_pairs_gpu (query/src/cuda/mesh_query_deduplication.cu:56-144).
+// Differences by design: a key that cannot be placed raises RS_ERR_TABLE_FULL
+// (the reference drops it after 5000 / 1000 probes) and the drivers grow the
+// table and rerun; the finalised output is sorted, so it does not depend on
+// slot order or atomic timing.
+#include <algorithm>
+#include <cstring>
+
+#include "rs_engine.h"
+#include "rs_prims.cuh"
+
+namespace rs {
+PairTable table_view(rs_pairset* ps);
+
+namespace {
+
+__global__ void k_swap_halves(uint64_t* __restrict__ k, uint64_t n) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) k[i] = (k[i] << 32) | (k[i] >> 32);
+}
+
+uint64_t next_pow2(uint64_t v) {
+    if (v == 0) return 1;
+    --v;
+    v |= v >> 1;
+    v |= v >> 2;
+    v |= v >> 4;
+    v |= v >> 8;
+    v |= v >> 16;
+    v |= v >> 32;
+    return v + 1;
+}
+
+cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s) {
+    if (ps->slots) cudaFreeAsync(ps->slots, s);
+    ps->slots = nullptr;
+    ps->capacity = capacity;
+    ps->max_probes = (unsigned)std::min<uint64_t>(capacity, 8192);
+    return cudaMallocAsync((void**)&ps->slots, capacity * sizeof(unsigned long long), s);
+}
+
+}  // namespace
+}  // namespace rs
+
+using namespace rs;
+
+extern "C" uint64_t rs_hash_size_pow2(int64_t est) {
+    uint64_t size = 16777216ull;
+    if (est > 0) {
+        uint64_t target = (uint64_t)(est / 0.5);
+        if (target < 1024) target = 1024;
+        if (target > 1073741824ull) target = 1073741824ull;
+        size = next_pow2(target);
+    }
+    return size;
+}
+
+extern "C" uint64_t rs_hash_size_odd(int64_t est, float load_factor) {
+    int64_t size = 16777216;
+    if (est > 0) {
+        uint64_t target = (uint64_t)(est / load_factor);
+        if (target < 1024) target = 1024;
+        if (target > 1073741824ull) target = 1073741824ull;
+        size = (int64_t)target;
+        if (size % 2 == 0) size += 1;
+    }
+    return (uint64_t)size;
+}
+
+extern "C" int rs_pairset_create(uint64_t capacity, int pow2, rs_pairset** out, void* stream) {
+    if (!out || capacity == 0 || capacity > (1ull << 36)) return RS_ERR_INVALID;
+    *out = nullptr;
+    cudaStream_t s = (cudaStream_t)stream;
+    rs_pairset* ps = new rs_pairset();
+    cudaGetDevice(&ps->device);
+    ps->pow2 = pow2 ? 1 : 0;
+    if (ps->pow2) capacity = next_pow2(capacity);
+    cudaError_t e = cudaMallocAsync((void**)&ps->meta, 2 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = alloc_slots(ps, capacity, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        if (ps->meta) cudaFree(ps->meta);
+        if (ps->slots) cudaFree(ps->slots);
+        delete ps;
+        return to_status(e);
+    }
+    *out = ps;
+    return rs_pairset_clear(ps, stream);
+}
+
+extern "C" int rs_pairset_clear(rs_pairset* ps, void* stream) {
+    if (!ps) return RS_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, 2 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return to_status(e);
+}
+
+extern "C" int rs_pairset_destroy(rs_pairset* ps) {
+    if (!ps) return RS_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(ps->device);
+    if (ps->slots) cudaFree(ps->slots);
+    if (ps->meta) cudaFree(ps->meta);
+    cudaSetDevice(prev);
+    delete ps;
+    return RS_OK;
+}
+
+extern "C" int rs_pairset_info(const rs_pairset* ps, uint64_t* capacity, uint64_t* count, void* stream) {
+    if (!ps) return RS_ERR_INVALID;
+    if (capacity) *capacity = ps->capacity;
+    if (count) {
+        cudaStream_t s = (cudaStream_t)stream;
+        unsigned long long c = 0;
+        cudaError_t e = cudaMemcpyAsync(&c, ps->meta + 1, sizeof(c), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return to_status(e);
+        *count = c;
+    }
+    return RS_OK;
+}
+
+extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, uint64_t capacity,
+                                   uint64_t* h_count, void* stream) {
+    if (!ps || !h_count || (capacity && !d_keys)) return RS_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    *h_count = 0;
+    unsigned long long meta[2] = {0, 0};
+    cudaError_t e = cudaMemcpyAsync(meta, ps->meta, sizeof(meta), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return to_status(e);
+    int st = status_from_bits((uint32_t)meta[0]);
+    if (st != RS_OK) return st;
+    const uint64_t n = meta[1];
+    if (n == 0) return RS_OK;
+    uint64_t* tmp = nullptr;
+    uint64_t* dcount = nullptr;
+    e = cudaMallocAsync((void**)&tmp, n * sizeof(uint64_t), s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dcount, sizeof(uint64_t), s);
+    if (e == cudaSuccess) e = compact_u64(reinterpret_cast<const uint64_t*>(ps->slots), ps->capacity, kEmptyKey, tmp,
+                                          dcount, s);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (e == cudaSuccess && order == 1) k_swap_halves<<<grid, 256, 0, s>>>(tmp, n);
+    if (e == cudaSuccess) e = radix_sort_u64(tmp, nullptr, n, 64, s);
+    if (e == cudaSuccess && order == 1) k_swap_halves<<<grid, 256, 0, s>>>(tmp, n);
+    const uint64_t ncopy = std::min<uint64_t>(n, capacity);
+    if (e == cudaSuccess && ncopy)
+        e = cudaMemcpyAsync(d_keys, tmp, ncopy * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
+    if (tmp) cudaFreeAsync(tmp, s);
+    if (dcount) cudaFreeAsync(dcount, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return to_status(e);
+    *h_count = n;
+    return n > capacity ? RS_ERR_OUTPUT_OVERFLOW : RS_OK;
+}
+
+extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
+                               const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
+                               uint64_t nEA, const rs_bvh* B, const float* d_startsB, const float* d_endsB,
+                               const int32_t* d_offsetsB, const int32_t* d_countsB, const int32_t* d_sourcesB,
+                               uint64_t nEB, int direction, int with_containment, rs_pairset* ps, void* stream) {
+    if (!A || !B || !ps || direction < 0 || direction > 2) return RS_ERR_INVALID;
+    const bool a2b = direction == 0 || direction == 1;
+    const bool b2a = direction == 0 || direction == 2;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        int st = rs_pairset_clear(ps, stream);
+        if (st != RS_OK) return st;
+        // Order of MeshIntersectionLauncher use in executeHashQuery: overlap A->B, overlap B->A,
+        // containment A->B, containment B->A (raytracer_intersection_estimated_main.cpp:107-158).
+        if (st == RS_OK && a2b)
+            st = rs_edge_join(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, stream);
+        if (st == RS_OK && b2a)
+            st = rs_edge_join(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, stream);
+        if (with_containment) {
+            if (st == RS_OK && a2b) st = rs_containment(B, A->V, A->nV, A->I, A->nF, A->t2o, 0, ps, stream);
+            if (st == RS_OK && b2a) st = rs_containment(A, B->V, B->nV, B->I, B->nF, B->t2o, 1, ps, stream);
+        }
+        if (st != RS_ERR_TABLE_FULL) return st;
+        // Grow and rerun: the table keeps the hashing variant, with four times the slots.
+        uint64_t cap = ps->capacity * 4;
+        if (!ps->pow2 && cap % 2 == 0) cap += 1;
+        if (cap > (1ull << 34)) return RS_ERR_TABLE_FULL;
+        cudaError_t e = alloc_slots(ps, cap, s);
+        if (e != cudaSuccess) return to_status(e);
+    }
+    return RS_ERR_TABLE_FULL;
+}
+
+extern "C" const char* rs_status_string(int status) {
+    switch (status) {
+        case RS_OK: return "ok";
+        case RS_ERR_CUDA: return "CUDA runtime error";
+        case RS_ERR_INVALID: return "invalid argument";
+        case RS_ERR_TABLE_FULL: return "pair table full";
+        case RS_ERR_OUTPUT_OVERFLOW: return "output buffer too small";
+        case RS_ERR_ITER_LIMIT: return "iteration or stack budget exhausted";
+        case RS_ERR_FORMAT: return "malformed input";
+        case RS_ERR_OOM: return "out of device memory";
+        case RS_ERR_TARGET_OVERFLOW: return "containment ray crossed too many distinct targets";
+        default: return "unknown status";
+    }
+}
+
+extern "C" const char* rs_version(void) { return "rayspace3d-gb300 0.1 (sm_103a)"; }

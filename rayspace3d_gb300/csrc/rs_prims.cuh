@@ -1,0 +1,30 @@
+// rs_prims.cuh -- host entry points of the engine's device primitives.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace rs {
+
+// Stable LSD radix sort of 64-bit keys (and optional 32-bit values) on bits
+// [0, end_bit), 8 bits per pass, in place.  Temporaries come from the stream's
+// memory pool.
+cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s);
+
+// Exclusive prefix sums.  `total` (device, nullable) receives the sum of all inputs.
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, cudaStream_t s);
+cudaError_t exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, size_t n, int64_t* total, cudaStream_t s);
+
+// Ordered stream compaction of a u64 array: copies every element != skip, in
+// index order, to out; *count (device) receives how many were written.
+cudaError_t compact_u64(const uint64_t* in, size_t n, uint64_t skip, uint64_t* out, uint64_t* count,
+                        cudaStream_t s);
+
+// Remove consecutive duplicates of a sorted u64 array in place; *count (device)
+// receives the new length.
+cudaError_t unique_sorted_u64(uint64_t* keys, size_t n, uint64_t* count, cudaStream_t s);
+
+// Number of thread blocks of a launch that keeps every SM busy.
+int sm_count();
+
+}  // namespace rs
