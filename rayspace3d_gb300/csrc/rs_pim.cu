@@ -52,14 +52,21 @@ struct Chain {
 };
 
 template <int AXIS>
-__device__ __forceinline__ bool box_filter(const BoxMesh& box, const Ray& r) {
+__device__ __forceinline__ bool box_filter(const float* __restrict__ box, const Ray& r) {
     float ht[12];
     uint32_t hid[12];
     int nh = 0;
 #pragma unroll 1
     for (int k = 0; k < 12; ++k) {
+        float a[3], b[3], c[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            a[q] = __ldg(&box[9 * k + q]);
+            b[q] = __ldg(&box[9 * k + 3 + q]);
+            c[q] = __ldg(&box[9 * k + 6 + q]);
+        }
         float t;
-        if (hit_triangle<AXIS>(r, &box.v[k][0], &box.v[k][3], &box.v[k][6], t)) {
+        if (hit_triangle<AXIS>(r, a, b, c, t)) {
             int j = nh++;
             while (j > 0 && hit_less(t, (uint32_t)k, ht[j - 1], hid[j - 1])) {
                 ht[j] = ht[j - 1];
@@ -79,7 +86,8 @@ template <int AXIS, bool FILTER>
 __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint64_t n, float dx, float dy, float dz,
                                             const BNode* __restrict__ nodes, uint32_t max_steps,
                                             const float4* __restrict__ tris,
-                                            BoxMesh box, int32_t* __restrict__ out_obj, uint8_t* __restrict__ out_in,
+                                            const float* __restrict__ box, int32_t* __restrict__ out_obj,
+                                            uint8_t* __restrict__ out_in,
                                             unsigned int* __restrict__ status, uint32_t* __restrict__ ovf_list,
                                             unsigned long long* __restrict__ ovf_count) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -198,7 +206,7 @@ __global__ void __launch_bounds__(kT) k_pim_fallback(const float* __restrict__ p
 
 template <int AXIS, bool FILTER>
 cudaError_t launch_pim(const rs_bvh* bvh, const float* pts, uint64_t n, float dx, float dy, float dz,
-                       const BoxMesh& box, int32_t* obj, uint8_t* in, unsigned int* status, uint32_t* ovf_list,
+                       const float* box, int32_t* obj, uint8_t* in, unsigned int* status, uint32_t* ovf_list,
                        unsigned long long* ovf_count, cudaStream_t s) {
     const unsigned grid = (unsigned)((n + kT - 1) / kT);
     k_pim<AXIS, FILTER><<<grid, kT, 0, s>>>(pts, n, dx, dy, dz, bvh->nodes, max_steps(bvh), bvh->tris, box, obj, in, status,
@@ -236,9 +244,9 @@ int pim_impl(const rs_bvh* bvh, const float* pts, uint64_t n, float dx, float dy
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         return to_status(e);
     }
-    unsigned long long* meta = nullptr;  // [0] status, [1] overflow count
+    unsigned long long* meta = nullptr;  // [0] status, [1] overflow count, then the 12 box triangles
     uint32_t* ovf = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&meta, 2 * sizeof(unsigned long long), s);
+    cudaError_t e = cudaMallocAsync((void**)&meta, 2 * sizeof(unsigned long long) + sizeof(BoxMesh), s);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&ovf, n * sizeof(uint32_t), s);
     if (e != cudaSuccess) {
         if (meta) cudaFreeAsync(meta, s);
@@ -247,7 +255,10 @@ int pim_impl(const rs_bvh* bvh, const float* pts, uint64_t n, float dx, float dy
     }
     cudaMemsetAsync(meta, 0, 2 * sizeof(unsigned long long), s);
     unsigned int* status = reinterpret_cast<unsigned int*>(meta);
-    const BoxMesh box = filter ? make_box(bvh) : BoxMesh{};
+    static_assert(sizeof(BoxMesh) == 108 * sizeof(float), "box mesh layout");
+    BoxMesh hbox = filter ? make_box(bvh) : BoxMesh{};
+    float* box = reinterpret_cast<float*>(meta + 2);
+    if (filter) cudaMemcpyAsync(box, &hbox, sizeof(BoxMesh), cudaMemcpyHostToDevice, s);
     const bool zx = dx == 0.0f, zy = dy == 0.0f, zz = dz == 0.0f;
     if (dz == 1.0f && zx && zy) {
         e = filter ? launch_pim<2, true>(bvh, pts, n, dx, dy, dz, box, obj, in, status, ovf, meta + 1, s)
