@@ -157,6 +157,15 @@ int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_ends
 /* Status text for a code. */
 const char* rs_status_string(int status);
 
+/* Diagnostics (no counterpart in the reference).  rs_launch_count: kernels launched by this
+ * library since load.  rs_profile_*: when enabled, device time of the main kernels is
+ * accumulated with CUDA events on the launching stream; ids 0 edge join, 1 containment,
+ * 2 point-in-mesh, 3 BVH build (whole), 4 pair finalisation, 5 estimator. */
+uint64_t rs_launch_count(void);
+int rs_profile_enable(int on);
+int rs_profile_reset(void);
+int rs_profile_read(int kernel, double* total_ms, uint64_t* launches);
+
 /* ========================================================================== */
 /* 2. Reference-compatible helpers (same names and signatures as the reference) */
 /* ========================================================================== */

@@ -52,6 +52,10 @@ SIGNATURES = {
     "rs_hash_size_pow2": (U64, [I64]),
     "rs_hash_size_odd": (U64, [I64, F]),
     "rs_overlap_join": (I, [P, P, P, P, P, P, U64, P, P, P, P, P, P, U64, I, I, P, P]),
+    "rs_launch_count": (U64, []),
+    "rs_profile_enable": (I, [I]),
+    "rs_profile_reset": (I, []),
+    "rs_profile_read": (I, [I, ctypes.POINTER(ctypes.c_double), PU64]),
     "exclusive_scan_gpu": (ctypes.c_longlong, [P, P, I]),
     "merge_and_deduplicate_pairs_gpu": (ctypes.c_longlong, [P, ctypes.c_longlong, P, ctypes.c_longlong, P]),
     "compact_hash_table_pairs": (I, [P, ctypes.c_ulonglong, P, I]),

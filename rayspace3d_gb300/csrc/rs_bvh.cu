@@ -4,14 +4,21 @@
 // (query/src/optix/OptixAccelerationStructure.cpp:22-68), which builds one
 // triangle GAS over every triangle of a .pre set.  Steps:
 //   1. per-triangle boxes, scene bounds of triangle centres and of all vertices;
-//   2. 63-bit Morton codes of the centres (21 bits per axis);
-//   3. stable radix sort of (code, triangle id);
-//   4. Karras' binary radix tree over the sorted codes (ties broken by index);
-//   5. bottom-up box refit with one atomic arrival counter per node;
-//   6. emission of 64-byte nodes (subtrees of <= leaf_size triangles become
-//      leaves) and of the triangles in leaf order (3 x float4 each).
+//   2. keys = 32-bit Morton code of the centre (11/11/10 bits) << 32 | triangle id,
+//      unique by construction;
+//   3. stable radix sort of the 32 Morton bits only (4 passes; ids stay ascending
+//      within equal codes);
+//   4. Karras' binary radix tree over the sorted keys;
+//   5. the triangles in leaf order (3 x float4 each);
+//   6. bottom-up box refit that starts from leaf groups (subtrees of <= leaf_size
+//      triangles, whose boxes are read straight from the leaf-ordered triangles),
+//      with one acquire-release arrival counter per node;
+//   7. emission of 64-byte nodes in which the leaf groups become leaves.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+
+#include <cuda/atomic>
 
 #include "rs_engine.h"
 #include "rs_prims.cuh"
@@ -63,9 +70,13 @@ __global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, int* b
     block_minmax_atomic(mn, mx, bounds + 6);
 }
 
-__device__ __forceinline__ void tri_box(const float* __restrict__ V, const uint32_t* __restrict__ I, uint64_t t,
-                                        float lo[3], float hi[3]) {
-    const uint32_t i0 = I[3 * t], i1 = I[3 * t + 1], i2 = I[3 * t + 2];
+// Indices are clamped so a malformed index buffer cannot read out of bounds; the
+// build reports RS_ERR_INVALID for such input after the fact.
+__device__ __forceinline__ void tri_box(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I,
+                                        uint64_t t, float lo[3], float hi[3]) {
+    const uint64_t last = nV - 1;
+    const uint64_t i0 = min((uint64_t)I[3 * t], last), i1 = min((uint64_t)I[3 * t + 1], last),
+                   i2 = min((uint64_t)I[3 * t + 2], last);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float a = V[3 * (uint64_t)i0 + k], b = V[3 * (uint64_t)i1 + k], c = V[3 * (uint64_t)i2 + k];
@@ -83,7 +94,7 @@ __global__ void k_centroid_bounds(const float* __restrict__ V, uint64_t nV, cons
             continue;
         }
         float lo[3], hi[3];
-        tri_box(V, I, t, lo, hi);
+        tri_box(V, nV, I, t, lo, hi);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const float c = 0.5f * lo[k] + 0.5f * hi[k];
@@ -94,23 +105,23 @@ __global__ void k_centroid_bounds(const float* __restrict__ V, uint64_t nV, cons
     block_minmax_atomic(mn, mx, bounds);
 }
 
-__device__ __forceinline__ uint64_t spread21(uint64_t x) {
-    x &= 0x1fffffull;
-    x = (x | (x << 32)) & 0x1f00000000ffffull;
-    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
-    x = (x | (x << 8)) & 0x100f00f00f00f00full;
-    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
-    x = (x | (x << 2)) & 0x1249249249249249ull;
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
     return x;
 }
 
-__global__ void k_morton(const float* __restrict__ V, const uint32_t* __restrict__ I, uint64_t nF,
-                         const int* __restrict__ bounds, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+__global__ void k_morton(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I, uint64_t nF,
+                         const int* __restrict__ bounds, uint64_t* __restrict__ keys) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t >= nF) return;
     float lo[3], hi[3];
-    tri_box(V, I, t, lo, hi);
-    uint64_t q[3];
+    tri_box(V, nV, I, t, lo, hi);
+    uint32_t q[3];
+    const float scale[3] = {2048.0f, 2048.0f, 1024.0f};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float cmin = ord_flt(bounds[k]), cmax = ord_flt(bounds[3 + k]);
@@ -118,10 +129,11 @@ __global__ void k_morton(const float* __restrict__ V, const uint32_t* __restrict
         const float c = 0.5f * lo[k] + 0.5f * hi[k];
         float u = ext > 0.0f ? (c - cmin) / ext : 0.0f;
         u = fminf(fmaxf(u, 0.0f), 1.0f);
-        q[k] = (uint64_t)fminf(u * 2097152.0f, 2097151.0f);
+        q[k] = (uint32_t)fminf(u * scale[k], scale[k] - 1.0f);
     }
-    keys[t] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
-    vals[t] = (uint32_t)t;
+    const uint32_t code = ((q[0] >> 10) << 31) | ((q[1] >> 10) << 30) | (spread10(q[0]) << 2) |
+                          (spread10(q[1]) << 1) | spread10(q[2]);
+    keys[t] = ((uint64_t)code << 32) | (uint32_t)t;
 }
 
 __device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, int n, int i, int j) {
@@ -163,29 +175,61 @@ __global__ void k_karras(const uint64_t* __restrict__ keys, int n, int* __restri
     range[i] = make_int2(lo, hi);
 }
 
-__global__ void k_refit(const float* __restrict__ V, const uint32_t* __restrict__ I, const uint32_t* __restrict__ order,
-                        int n, const int* __restrict__ left, const int* __restrict__ right,
-                        const int* __restrict__ parent, float4* __restrict__ blo, float4* __restrict__ bhi,
-                        int* __restrict__ flags) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    float lo[3], hi[3];
-    tri_box(V, I, order[k], lo, hi);
-    int node = n - 1 + k;
-    blo[node] = make_float4(lo[0], lo[1], lo[2], 0.0f);
-    bhi[node] = make_float4(hi[0], hi[1], hi[2], 0.0f);
-    int p = parent[node];
+// Bottom-up refit from the leaf groups.  One thread per internal node p whose range
+// is larger than leaf_size (and the root): each child of p that spans <= leaf_size
+// triangles is a leaf group whose box is the union of its triangles, contiguous in
+// leaf order.  The thread stores that box and arrives at p; the second arrival at a
+// node merges both children and moves up.  The arrival counter is an acquire-release
+// device-scope atomic, so the first arrival's box store is visible to the second.
+__device__ __forceinline__ void arrive(int node, float4 lo, float4 hi, int p, const int* __restrict__ left,
+                                       const int* __restrict__ right, const int* __restrict__ parent,
+                                       float4* __restrict__ blo, float4* __restrict__ bhi, int* __restrict__ flags) {
     while (p >= 0) {
-        __threadfence();
-        if (atomicAdd(&flags[p], 1) == 0) return;
-        __threadfence();
-        const int l = left[p], r = right[p];
-        const float4 al = __ldcg(&blo[l]), ah = __ldcg(&bhi[l]);
-        const float4 bl = __ldcg(&blo[r]), bh = __ldcg(&bhi[r]);
-        blo[p] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.0f);
-        bhi[p] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f);
+        cuda::atomic_ref<int, cuda::thread_scope_device> arrivals(flags[p]);
+        if (arrivals.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
+        const int other = (left[p] == node) ? right[p] : left[p];
+        const float4 ol = __ldcg(&blo[other]), oh = __ldcg(&bhi[other]);
+        lo = make_float4(fminf(lo.x, ol.x), fminf(lo.y, ol.y), fminf(lo.z, ol.z), 0.f);
+        hi = make_float4(fmaxf(hi.x, oh.x), fmaxf(hi.y, oh.y), fmaxf(hi.z, oh.z), 0.f);
+        __stcg(&blo[p], lo);
+        __stcg(&bhi[p], hi);
         node = p;
         p = parent[p];
+    }
+}
+
+__global__ void k_refit(const float4* __restrict__ tris, int n, int leaf_size, const int* __restrict__ left,
+                        const int* __restrict__ right, const int* __restrict__ parent, const int2* __restrict__ range,
+                        float4* __restrict__ blo, float4* __restrict__ bhi, int* __restrict__ flags) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n - 1) return;
+    const int2 rp = range[p];
+    if (p != 0 && rp.y - rp.x + 1 <= leaf_size) return;  // inside a leaf group
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const int c = side == 0 ? left[p] : right[p];
+        int first, size;
+        if (c >= n - 1) {
+            first = c - (n - 1);
+            size = 1;
+        } else {
+            const int2 rc = range[c];
+            first = rc.x;
+            size = rc.y - rc.x + 1;
+        }
+        if (size > leaf_size) continue;
+        float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+        for (int k = first; k < first + size; ++k) {
+#pragma unroll
+            for (int v = 0; v < 3; ++v) {
+                const float4 q = tris[3 * (size_t)k + v];
+                lo = make_float4(fminf(lo.x, q.x), fminf(lo.y, q.y), fminf(lo.z, q.z), 0.f);
+                hi = make_float4(fmaxf(hi.x, q.x), fmaxf(hi.y, q.y), fmaxf(hi.z, q.z), 0.f);
+            }
+        }
+        __stcg(&blo[c], lo);
+        __stcg(&bhi[c], hi);
+        arrive(c, lo, hi, p, left, right, parent, blo, bhi, flags);
     }
 }
 
@@ -225,13 +269,15 @@ __global__ void k_emit_nodes(int n, int leaf_size, const int* __restrict__ left,
     nodes[i] = nd;
 }
 
-__global__ void k_emit_tris(const float* __restrict__ V, const uint32_t* __restrict__ I,
-                            const int32_t* __restrict__ t2o, const uint32_t* __restrict__ order, int n,
+__global__ void k_emit_tris(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I,
+                            const int32_t* __restrict__ t2o, const uint64_t* __restrict__ order, int n,
                             float4* __restrict__ tris) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const uint32_t t = order[k];
-    const uint32_t i0 = I[3 * (uint64_t)t], i1 = I[3 * (uint64_t)t + 1], i2 = I[3 * (uint64_t)t + 2];
+    const uint32_t t = (uint32_t)(order[k] & 0xffffffffull);
+    const uint64_t last = nV - 1;
+    const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last), i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
+                   i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
     const float* a = V + 3 * (uint64_t)i0;
     const float* b = V + 3 * (uint64_t)i1;
     const float* c = V + 3 * (uint64_t)i2;
@@ -241,10 +287,11 @@ __global__ void k_emit_tris(const float* __restrict__ V, const uint32_t* __restr
 }
 
 // Root for n <= 1: child 0 is the single leaf (if any), child 1 an empty box.
-__global__ void k_small_root(const float* __restrict__ V, const uint32_t* __restrict__ I, int n, BNode* nodes) {
+__global__ void k_small_root(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I, int n,
+                             BNode* nodes) {
     const float inf = INFINITY;
     float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-    if (n == 1) tri_box(V, I, 0, lo, hi);
+    if (n == 1) tri_box(V, nV, I, 0, lo, hi);
     BNode nd;
     nd.a = make_float4(lo[0], lo[1], lo[2], hi[0]);
     nd.b = make_float4(hi[1], hi[2], inf, inf);
@@ -257,7 +304,7 @@ __global__ void k_small_root(const float* __restrict__ V, const uint32_t* __rest
 
 template <class T>
 cudaError_t alloc(T** p, size_t count, cudaStream_t s) {
-    return cudaMallocAsync((void**)p, (count ? count : 1) * sizeof(T), s);
+    return dmalloc((void**)p, (count ? count : 1) * sizeof(T), s);
 }
 
 }  // namespace
@@ -285,6 +332,7 @@ extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t
     if (!out) return RS_ERR_INVALID;
     *out = nullptr;
     if ((nF && (!d_indices || !d_tri2obj || !d_vertices)) || (nV && !d_vertices)) return RS_ERR_INVALID;
+    if (nF && nV == 0) return RS_ERR_INVALID;               // every index would be out of range
     if (nF >= (uint64_t)0x7fffffff) return RS_ERR_INVALID;  // node/leaf indices are int32
     if (leaf_size == 0) leaf_size = 4;
     if (leaf_size < 1 || leaf_size > 8) return RS_ERR_INVALID;
@@ -298,65 +346,38 @@ extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t
     h->leaf_size = leaf_size;
     cudaGetDevice(&h->device);
     const int n = (int)nF;
-    int* bounds = nullptr;
-    unsigned int* bad = nullptr;
+    int* bounds = nullptr;  // 12 ordered-int bounds, then the bad-index flag
     uint64_t* keys = nullptr;
-    uint32_t* vals = nullptr;
     int *left = nullptr, *right = nullptr, *parent = nullptr, *flags = nullptr;
     int2* range = nullptr;
     float4 *blo = nullptr, *bhi = nullptr;
     cudaError_t e = cudaSuccess;
-    int hb[12];
-    unsigned int hbad = 0;
+    int hb[13];
     const int grid = 4 * sm_count();
     h->n_nodes = n >= 2 ? (uint64_t)(n - 1) : 1;
     h->n_tris = (uint64_t)n;
+    prof_begin(P_BVH_BUILD, s);
     e = alloc(&h->nodes, h->n_nodes, s);
     if (e == cudaSuccess) e = alloc(&h->tris, 3 * (size_t)n, s);
-    if (e == cudaSuccess) e = alloc(&bounds, 12, s);
-    if (e == cudaSuccess) e = alloc(&bad, 1, s);
+    if (e == cudaSuccess) e = alloc(&bounds, 13, s);
     if (e != cudaSuccess) goto fail;
-    k_init_bounds<<<1, 32, 0, s>>>(bounds);
-    cudaMemsetAsync(bad, 0, sizeof(unsigned int), s);
-    if (nV) k_vertex_bounds<<<grid, kT, 0, s>>>(d_vertices, nV, bounds);
-    if (nF) k_centroid_bounds<<<grid, kT, 0, s>>>(d_vertices, nV, d_indices, nF, bounds, bad);
-    e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(hbad), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) goto fail;
-    for (int k = 0; k < 3; ++k) {
-        auto dec = [](int i) {
-            int b = i >= 0 ? i : i ^ 0x7fffffff;
-            float f;
-            memcpy(&f, &b, 4);
-            return f;
-        };
-        h->vmin[k] = dec(hb[6 + k]);
-        h->vmax[k] = dec(hb[9 + k]);
-    }
-    if (hbad) {
-        cudaFreeAsync(bounds, s);
-        cudaFreeAsync(bad, s);
-        cudaFreeAsync(h->nodes, s);
-        cudaFreeAsync(h->tris, s);
-        cudaStreamSynchronize(s);
-        delete h;
-        return RS_ERR_INVALID;
-    }
+    launch(k_init_bounds, 1, 32, 0, s, bounds);
+    cudaMemsetAsync(bounds + 12, 0, sizeof(int), s);
+    if (nV) launch(k_vertex_bounds, grid, kT, 0, s, d_vertices, nV, bounds);
+    if (nF) launch(k_centroid_bounds, grid, kT, 0, s, d_vertices, nV, d_indices, nF, bounds,
+                   reinterpret_cast<unsigned int*>(bounds + 12));
     if (n <= 1) {
-        k_small_root<<<1, 1, 0, s>>>(d_vertices, d_indices, n, h->nodes);
+        launch(k_small_root, 1, 1, 0, s, d_vertices, nV, d_indices, n, h->nodes);
         if (n == 1) {
-            uint32_t* order1 = nullptr;
-            e = alloc(&order1, 1, s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(order1, 0, sizeof(uint32_t), s);
-            if (e == cudaSuccess) k_emit_tris<<<1, 32, 0, s>>>(d_vertices, d_indices, d_tri2obj, order1, 1, h->tris);
-            if (order1) cudaFreeAsync(order1, s);
+            e = alloc(&keys, 1, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(keys, 0, sizeof(uint64_t), s);
+            if (e == cudaSuccess) launch(k_emit_tris, 1, 32, 0, s, d_vertices, nV, d_indices, d_tri2obj,
+                                         (const uint64_t*)keys, 1, h->tris);
         }
     } else {
         const int nb = (n + kT - 1) / kT;
         const int nbi = (n - 1 + kT - 1) / kT;
         e = alloc(&keys, n, s);
-        if (e == cudaSuccess) e = alloc(&vals, n, s);
         if (e == cudaSuccess) e = alloc(&left, n - 1, s);
         if (e == cudaSuccess) e = alloc(&right, n - 1, s);
         if (e == cudaSuccess) e = alloc(&parent, 2 * (size_t)n - 1, s);
@@ -365,23 +386,26 @@ extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t
         if (e == cudaSuccess) e = alloc(&blo, 2 * (size_t)n - 1, s);
         if (e == cudaSuccess) e = alloc(&bhi, 2 * (size_t)n - 1, s);
         if (e != cudaSuccess) goto fail;
-        k_morton<<<nb, kT, 0, s>>>(d_vertices, d_indices, nF, bounds, keys, vals);
-        e = radix_sort_u64(keys, vals, (size_t)n, 63, s);
+        launch(k_morton, nb, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys);
+        e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32);
         if (e != cudaSuccess) goto fail;
         cudaMemsetAsync(parent, 0xff, (2 * (size_t)n - 1) * sizeof(int), s);
         cudaMemsetAsync(flags, 0, (size_t)(n - 1) * sizeof(int), s);
-        k_karras<<<nbi, kT, 0, s>>>(keys, n, left, right, parent, range);
-        k_refit<<<nb, kT, 0, s>>>(d_vertices, d_indices, vals, n, left, right, parent, blo, bhi, flags);
-        k_emit_nodes<<<nbi, kT, 0, s>>>(n, leaf_size, left, right, range, blo, bhi, h->nodes);
-        k_emit_tris<<<nb, kT, 0, s>>>(d_vertices, d_indices, d_tri2obj, vals, n, h->tris);
+        launch(k_karras, nbi, kT, 0, s, keys, n, left, right, parent, range);
+        launch(k_emit_tris, nb, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys, n, h->tris);
+        launch(k_refit, nbi, kT, 0, s, (const float4*)h->tris, n, leaf_size, left, right, parent, range, blo, bhi,
+               flags);
+        launch(k_emit_nodes, nbi, kT, 0, s, n, leaf_size, left, right, range, blo, bhi, h->nodes);
     }
+    prof_end(P_BVH_BUILD, s);
     e = cudaGetLastError();
+    // One host round trip: vertex bounds for the filter box and the bad-index flag.
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    prof_collect();
 fail:
     if (bounds) cudaFreeAsync(bounds, s);
-    if (bad) cudaFreeAsync(bad, s);
     if (keys) cudaFreeAsync(keys, s);
-    if (vals) cudaFreeAsync(vals, s);
     if (left) cudaFreeAsync(left, s);
     if (right) cudaFreeAsync(right, s);
     if (parent) cudaFreeAsync(parent, s);
@@ -389,12 +413,23 @@ fail:
     if (range) cudaFreeAsync(range, s);
     if (blo) cudaFreeAsync(blo, s);
     if (bhi) cudaFreeAsync(bhi, s);
-    if (e != cudaSuccess) {
+    const bool bad = (e == cudaSuccess) && hb[12] != 0;
+    if (e != cudaSuccess || bad) {
         if (h->nodes) cudaFreeAsync(h->nodes, s);
         if (h->tris) cudaFreeAsync(h->tris, s);
         cudaStreamSynchronize(s);
         delete h;
-        return to_status(e);
+        return bad ? RS_ERR_INVALID : to_status(e);
+    }
+    for (int k = 0; k < 3; ++k) {
+        auto dec = [](int i) {
+            int b = i >= 0 ? i : i ^ 0x7fffffff;
+            float f;
+            std::memcpy(&f, &b, 4);
+            return f;
+        };
+        h->vmin[k] = dec(hb[6 + k]);
+        h->vmax[k] = dec(hb[9 + k]);
     }
     *out = h;
     return RS_OK;
@@ -407,6 +442,10 @@ extern "C" int rs_bvh_destroy(rs_bvh* bvh) {
     cudaSetDevice(bvh->device);
     if (bvh->nodes) cudaFree(bvh->nodes);
     if (bvh->tris) cudaFree(bvh->tris);
+    for (auto& g : bvh->cgrid) {
+        if (g.start) cudaFree(g.start);
+        if (g.list) cudaFree(g.list);
+    }
     cudaSetDevice(prev);
     delete bvh;
     return RS_OK;

@@ -39,7 +39,7 @@ using namespace rs;
 extern "C" long long exclusive_scan_gpu(const int* d_input, long long* d_output, int num_elements) {
     if (num_elements <= 0) return 0;
     int64_t* total = nullptr;
-    if (cudaMallocAsync((void**)&total, sizeof(int64_t), 0) != cudaSuccess) return 0;
+    if (dmalloc((void**)&total, sizeof(int64_t), 0) != cudaSuccess) return 0;
     int64_t h = 0;
     if (exclusive_scan_i32_to_i64(d_input, reinterpret_cast<int64_t*>(d_output), (size_t)num_elements, total, 0) ==
         cudaSuccess)
@@ -64,7 +64,7 @@ extern "C" long long merge_and_deduplicate_pairs_gpu(const void* d_results1, lon
     uint64_t* cnt = nullptr;
     uint64_t h = 0;
     if (radix_sort_u64(keys, nullptr, (size_t)total, 64, 0) != cudaSuccess) return 0;
-    if (cudaMallocAsync((void**)&cnt, sizeof(uint64_t), 0) != cudaSuccess) return 0;
+    if (dmalloc((void**)&cnt, sizeof(uint64_t), 0) != cudaSuccess) return 0;
     if (unique_sorted_u64(keys, (size_t)total, cnt, 0) == cudaSuccess)
         cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, 0);
     cudaFreeAsync(cnt, 0);
@@ -78,8 +78,8 @@ extern "C" int compact_hash_table_pairs(const unsigned long long* d_hash_table, 
     uint64_t* tmp = nullptr;
     uint64_t* cnt = nullptr;
     uint64_t h = 0;
-    if (cudaMallocAsync((void**)&tmp, table_size * sizeof(uint64_t), 0) != cudaSuccess) return 0;
-    if (cudaMallocAsync((void**)&cnt, sizeof(uint64_t), 0) == cudaSuccess &&
+    if (dmalloc((void**)&tmp, table_size * sizeof(uint64_t), 0) != cudaSuccess) return 0;
+    if (dmalloc((void**)&cnt, sizeof(uint64_t), 0) == cudaSuccess &&
         compact_u64(reinterpret_cast<const uint64_t*>(d_hash_table), table_size, kEmptyKey, tmp, cnt, 0) ==
             cudaSuccess) {
         cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, 0);
@@ -87,7 +87,7 @@ extern "C" int compact_hash_table_pairs(const unsigned long long* d_hash_table, 
         const uint64_t m = h < (uint64_t)max_output_size ? h : (uint64_t)max_output_size;
         // key = id1<<32 | id2 becomes MeshQueryResult{id1, id2}, i.e. the swapped u64.
         if (m) {
-            k_swap_halves_c<<<(unsigned)((m + 255) / 256), 256, 0, 0>>>(tmp, m);
+            launch(k_swap_halves_c, (unsigned)((m + 255) / 256), 256, 0, 0, tmp, m);
             cudaMemcpyAsync(d_output, tmp, m * sizeof(uint64_t), cudaMemcpyDeviceToDevice, 0);
         }
     }
@@ -103,9 +103,9 @@ extern "C" int count_hits_gpu(const void* d_results, int num_results) {
     uint32_t* tot = nullptr;
     uint32_t h = 0;
     const uint64_t n = (uint64_t)num_results;
-    if (cudaMallocAsync((void**)&f, n * sizeof(uint32_t), 0) != cudaSuccess) return 0;
-    if (cudaMallocAsync((void**)&tot, sizeof(uint32_t), 0) == cudaSuccess) {
-        k_ray_flags<<<(unsigned)((n + 255) / 256), 256, 0, 0>>>(reinterpret_cast<const int2*>(d_results), n, f);
+    if (dmalloc((void**)&f, n * sizeof(uint32_t), 0) != cudaSuccess) return 0;
+    if (dmalloc((void**)&tot, sizeof(uint32_t), 0) == cudaSuccess) {
+        launch(k_ray_flags, (unsigned)((n + 255) / 256), 256, 0, 0, reinterpret_cast<const int2*>(d_results), n, f);
         if (exclusive_scan_u32(f, f, n, tot, 0) == cudaSuccess)
             cudaMemcpyAsync(&h, tot, sizeof(h), cudaMemcpyDeviceToHost, 0);
         cudaFreeAsync(tot, 0);
@@ -122,12 +122,12 @@ extern "C" void compact_hits_gpu(const void* d_input, void* d_output, int num_re
     uint32_t* tot = nullptr;
     uint32_t h = 0;
     const uint64_t n = (uint64_t)num_results;
-    if (cudaMallocAsync((void**)&f, n * sizeof(uint32_t), 0) != cudaSuccess) return;
-    if (cudaMallocAsync((void**)&tot, sizeof(uint32_t), 0) == cudaSuccess) {
+    if (dmalloc((void**)&f, n * sizeof(uint32_t), 0) != cudaSuccess) return;
+    if (dmalloc((void**)&tot, sizeof(uint32_t), 0) == cudaSuccess) {
         const unsigned grid = (unsigned)((n + 255) / 256);
-        k_ray_flags<<<grid, 256, 0, 0>>>(reinterpret_cast<const int2*>(d_input), n, f);
+        launch(k_ray_flags, grid, 256, 0, 0, reinterpret_cast<const int2*>(d_input), n, f);
         if (exclusive_scan_u32(f, f, n, tot, 0) == cudaSuccess) {
-            k_ray_scatter<<<grid, 256, 0, 0>>>(reinterpret_cast<const int2*>(d_input), n, f,
+            launch(k_ray_scatter, grid, 256, 0, 0, reinterpret_cast<const int2*>(d_input), n, f,
                                                reinterpret_cast<int2*>(d_output));
             cudaMemcpyAsync(&h, tot, sizeof(h), cudaMemcpyDeviceToHost, 0);
         }

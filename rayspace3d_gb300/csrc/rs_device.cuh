@@ -71,8 +71,11 @@ __device__ __forceinline__ int expansion_sign(const double* e, int m) {
     return top > 0.0 ? 1 : (top < 0.0 ? -1 : 0);
 }
 
-// Exact sign of det[d, a-o, b-o] = d . (a x b + b x o + o x a).
-static __device__ __noinline__ int orient_exact(const float* d, const float* o, const float* a, const float* b) {
+// Exact sign of det[d, a-o, b-o] = d . (a x b + b x o + o x a).  Operands are passed
+// by value so callers never have to keep them addressable in local memory.
+static __device__ __noinline__ int orient_exact(float d0, float d1, float d2, float o0, float o1, float o2,
+                                                float a0, float a1, float a2, float b0, float b1, float b2) {
+    const float d[3] = {d0, d1, d2}, o[3] = {o0, o1, o2}, a[3] = {a0, a1, a2}, b[3] = {b0, b1, b2};
     double e[40];
     int m = 0;
     const float* X[3] = {a, b, o};
@@ -98,15 +101,19 @@ static __device__ __noinline__ int orient_exact(const float* d, const float* o, 
     return expansion_sign(e, m);
 }
 
-// Exact sign of det[d, e_k, b-a] = d_j (b_i - a_i) - d_i (b_j - a_j).
-__device__ __forceinline__ int axis_det_exact(const float* d, int k, const float* a, const float* b) {
-    const int i = (k + 1) % 3, j = (k + 2) % 3;
+// Exact sign of det[d, e_k, b-a] = d_j (b_i - a_i) - d_i (b_j - a_j), i = k+1, j = k+2 (mod 3).
+// Components are picked with selects so no operand array is indexed by a variable.
+static __device__ __noinline__ int axis_det_exact(int k, float d0, float d1, float d2, float a0, float a1, float a2,
+                                                  float b0, float b1, float b2) {
+    const float di = k == 0 ? d1 : (k == 1 ? d2 : d0), dj = k == 0 ? d2 : (k == 1 ? d0 : d1);
+    const float ai = k == 0 ? a1 : (k == 1 ? a2 : a0), aj = k == 0 ? a2 : (k == 1 ? a0 : a1);
+    const float bi = k == 0 ? b1 : (k == 1 ? b2 : b0), bj = k == 0 ? b2 : (k == 1 ? b0 : b1);
     double e[5];
     int m = 0;
-    m = grow_expansion(e, m, __dmul_rn((double)d[j], (double)b[i]));
-    m = grow_expansion(e, m, -__dmul_rn((double)d[j], (double)a[i]));
-    m = grow_expansion(e, m, -__dmul_rn((double)d[i], (double)b[j]));
-    m = grow_expansion(e, m, __dmul_rn((double)d[i], (double)a[j]));
+    m = grow_expansion(e, m, __dmul_rn((double)dj, (double)bi));
+    m = grow_expansion(e, m, -__dmul_rn((double)dj, (double)ai));
+    m = grow_expansion(e, m, -__dmul_rn((double)di, (double)bj));
+    m = grow_expansion(e, m, __dmul_rn((double)di, (double)aj));
     return expansion_sign(e, m);
 }
 
@@ -146,7 +153,7 @@ __device__ __forceinline__ int orient_sign(const float* d, const float* o, const
         if (det > bound) return 1;
         if (det < -bound) return -1;
     }
-    return orient_exact(d, o, a, b);
+    return orient_exact(d[0], d[1], d[2], o[0], o[1], o[2], a[0], a[1], a[2], b[0], b[1], b[2]);
 }
 
 // Edge sign of (a,b) for the perturbed origin (see file header).
@@ -164,9 +171,9 @@ __device__ __forceinline__ int perturbed_sign(const float* d, const float* o, co
         if (b[kxa] != a[kxa]) return b[kxa] > a[kxa] ? 1 : -1;
         return 0;
     }
-    s = -axis_det_exact(d, kx, a, b);
+    s = -axis_det_exact(kx, d[0], d[1], d[2], a[0], a[1], a[2], b[0], b[1], b[2]);
     if (s) return s;
-    return -axis_det_exact(d, ky, a, b);
+    return -axis_det_exact(ky, d[0], d[1], d[2], a[0], a[1], a[2], b[0], b[1], b[2]);
 }
 
 // ---------------------------------------------------------------------------
@@ -195,11 +202,14 @@ __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, 
             if (isinf(r.inv[k])) r.zero[k] = 1;
         }
     }
+    // Dominant axis (ties keep z, then x): written without indexing r.d by a variable.
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
     int kz = 2;
-    if (fabsf(r.d[0]) > fabsf(r.d[kz])) kz = 0;
-    if (fabsf(r.d[1]) > fabsf(r.d[kz])) kz = 1;
-    r.kx = (kz + 1) % 3;
-    r.ky = (kz + 2) % 3;
+    float best = az;
+    if (ax > best) { kz = 0; best = ax; }
+    if (ay > best) kz = 1;
+    r.kx = kz == 2 ? 0 : kz + 1;
+    r.ky = kz == 0 ? 2 : (kz == 1 ? 0 : 1);
     r.tmin = tmin;
     r.tmax = tmax;
     return r;

@@ -6,6 +6,18 @@
 #include "../../include/rayspace3d.h"
 #include "rs_device.cuh"
 
+// Column grid for rays along +e_axis: a uniform grid over the two other axes whose
+// cells list (in leaf order) every triangle whose projected box touches the cell.
+struct rs_column_grid {
+    int built = 0;
+    float u0 = 0, v0 = 0, su = 0, sv = 0;  // cell(x) = clamp(floor((x - u0) * su), 0, gu - 1)
+    float u1 = 0, v1 = 0;                  // projected bounds of all triangles
+    int gu = 1, gv = 1;
+    uint32_t* start = nullptr;             // gu*gv + 1 offsets into list
+    uint32_t* list = nullptr;              // leaf-order triangle indices
+    uint64_t nlist = 0;
+};
+
 struct rs_bvh {
     // Caller-owned device inputs; they must outlive the handle.
     const float* V = nullptr;
@@ -19,6 +31,7 @@ struct rs_bvh {
     float4* tris = nullptr;
     uint64_t n_tris = 0;
     int leaf_size = 4;
+    rs_column_grid cgrid[3];
     // Bounds of all vertices (the reference's BoundingBox::computeFromGeometry).
     float vmin[3] = {0, 0, 0};
     float vmax[3] = {0, 0, 0};

@@ -82,16 +82,19 @@ __global__ void k_estimate_final(const double* __restrict__ part, double* __rest
 int estimate_device(const void* d_a, const void* d_b, uint64_t n, float cell_volume, float eps, float gamma,
                     double out[kSums], cudaStream_t s) {
     double* part = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&part, (kBlocks * kSums + kSums) * sizeof(double), s);
+    cudaError_t e = dmalloc((void**)&part, (kBlocks * kSums + kSums) * sizeof(double), s);
     if (e != cudaSuccess) return to_status(e);
-    k_estimate<<<kBlocks, kT, 0, s>>>(reinterpret_cast<const uint4*>(d_a), reinterpret_cast<const uint4*>(d_b), n,
+    prof_begin(P_ESTIMATE, s);
+    launch(k_estimate, kBlocks, kT, 0, s, reinterpret_cast<const uint4*>(d_a), reinterpret_cast<const uint4*>(d_b), n,
                                       cell_volume, eps, gamma, part);
-    k_estimate_final<<<1, 32, 0, s>>>(part, part + kBlocks * kSums);
+    launch(k_estimate_final, 1, 32, 0, s, part, part + kBlocks * kSums);
+    prof_end(P_ESTIMATE, s);
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out, part + kBlocks * kSums, kSums * sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(part, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
+    prof_collect();
     if (e == cudaSuccess) e = e2;
     return to_status(e);
 }

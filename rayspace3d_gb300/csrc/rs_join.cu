@@ -155,23 +155,40 @@ PairTable table_view(rs_pairset* ps) {
 
 using namespace rs;
 
+namespace rs {
+// Launches one edge-ray direction without waiting for it (status lands in the table's meta word).
+cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const float* d_ends,
+                            const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
+                            int swap, rs_pairset* ps, cudaStream_t s) {
+    if (nE == 0 || target->n_tris == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((nE + kT - 1) / kT);
+    prof_begin(P_EDGE_JOIN, s);
+    launch(k_edge_join, grid, kT, 0, s, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, target->nodes,
+           max_steps(target), target->tris, swap, table_view(ps));
+    prof_end(P_EDGE_JOIN, s);
+    return cudaGetLastError();
+}
+
+// Waits for the stream and turns the table's status bits into an rs_status.
+int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e) {
+    unsigned long long st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ps->meta, sizeof(st), cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    prof_collect();
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return to_status(e);
+    return status_from_bits((uint32_t)st);
+}
+}  // namespace rs
+
 extern "C" int rs_edge_join(const rs_bvh* target, const float* d_starts, const float* d_ends,
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources,
                             uint64_t nE, int swap, rs_pairset* ps, void* stream) {
     if (!target || !ps || (nE && (!d_starts || !d_ends || !d_offsets || !d_counts || !d_sources)))
         return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
-    if (nE == 0 || target->n_tris == 0) return RS_OK;
-    const unsigned grid = (unsigned)((nE + kT - 1) / kT);
-    k_edge_join<<<grid, kT, 0, s>>>(d_starts, d_ends, d_offsets, d_counts, d_sources, nE, target->nodes,
-                                    max_steps(target), target->tris, swap, table_view(ps));
-    cudaError_t e = cudaGetLastError();
-    unsigned long long st = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ps->meta, sizeof(st), cudaMemcpyDeviceToHost, s);
-    cudaError_t e2 = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = e2;
-    if (e != cudaSuccess) return to_status(e);
-    return status_from_bits((uint32_t)st);
+    cudaError_t e = edge_join_async(target, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, swap, ps, s);
+    return table_status(ps, s, e);
 }
 
 extern "C" int rs_containment(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
@@ -183,10 +200,10 @@ extern "C" int rs_containment(const rs_bvh* target, const float* d_src_vertices,
     int* dmx = nullptr;
     int32_t* first = nullptr;
     int hmx = -1;
-    cudaError_t e = cudaMallocAsync((void**)&dmx, sizeof(int), s);
+    cudaError_t e = dmalloc((void**)&dmx, sizeof(int), s);
     if (e == cudaSuccess) {
         cudaMemsetAsync(dmx, 0xff, sizeof(int), s);
-        k_max_obj<<<2 * sm_count(), 256, 0, s>>>(d_src_tri2obj, src_nF, dmx);
+        launch(k_max_obj, 2 * sm_count(), 256, 0, s, d_src_tri2obj, src_nF, dmx);
         e = cudaMemcpyAsync(&hmx, dmx, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     }
@@ -194,13 +211,15 @@ extern "C" int rs_containment(const rs_bvh* target, const float* d_src_vertices,
     // which is the same for the contiguous ids preprocess_dataset writes).
     const uint64_t nObj = hmx >= 0 ? (uint64_t)hmx + 1 : 0;
     if (e == cudaSuccess && nObj) {
-        e = cudaMallocAsync((void**)&first, nObj * sizeof(int32_t), s);
+        e = dmalloc((void**)&first, nObj * sizeof(int32_t), s);
         if (e == cudaSuccess) {
-            k_first_tri_init<<<(unsigned)((nObj + 255) / 256), 256, 0, s>>>(first, nObj);
-            k_first_tri<<<(unsigned)((src_nF + 255) / 256), 256, 0, s>>>(d_src_tri2obj, src_nF, first, nObj);
-            k_containment<<<(unsigned)((nObj + kT - 1) / kT), kT, 0, s>>>(d_src_vertices, src_nV, d_src_indices, first,
+            launch(k_first_tri_init, (unsigned)((nObj + 255) / 256), 256, 0, s, first, nObj);
+            launch(k_first_tri, (unsigned)((src_nF + 255) / 256), 256, 0, s, d_src_tri2obj, src_nF, first, nObj);
+            prof_begin(P_CONTAINMENT, s);
+            launch(k_containment, (unsigned)((nObj + kT - 1) / kT), kT, 0, s, d_src_vertices, src_nV, d_src_indices, first,
                                                                         nObj, target->nodes, max_steps(target), target->tris, swap,
                                                                         table_view(ps));
+            prof_end(P_CONTAINMENT, s);
             e = cudaGetLastError();
         }
     }
@@ -209,6 +228,7 @@ extern "C" int rs_containment(const rs_bvh* target, const float* d_src_vertices,
     if (dmx) cudaFreeAsync(dmx, s);
     if (first) cudaFreeAsync(first, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
+    prof_collect();
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return to_status(e);
     return status_from_bits((uint32_t)st);

@@ -16,6 +16,10 @@
 
 namespace rs {
 PairTable table_view(rs_pairset* ps);
+cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const float* d_ends,
+                            const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
+                            int swap, rs_pairset* ps, cudaStream_t s);
+int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e);
 
 namespace {
 
@@ -41,7 +45,7 @@ cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s) {
     ps->slots = nullptr;
     ps->capacity = capacity;
     ps->max_probes = (unsigned)std::min<uint64_t>(capacity, 8192);
-    return cudaMallocAsync((void**)&ps->slots, capacity * sizeof(unsigned long long), s);
+    return dmalloc((void**)&ps->slots, capacity * sizeof(unsigned long long), s);
 }
 
 }  // namespace
@@ -80,7 +84,7 @@ extern "C" int rs_pairset_create(uint64_t capacity, int pow2, rs_pairset** out, 
     cudaGetDevice(&ps->device);
     ps->pow2 = pow2 ? 1 : 0;
     if (ps->pow2) capacity = next_pow2(capacity);
-    cudaError_t e = cudaMallocAsync((void**)&ps->meta, 2 * sizeof(unsigned long long), s);
+    cudaError_t e = dmalloc((void**)&ps->meta, 2 * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = alloc_slots(ps, capacity, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -143,20 +147,23 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
     if (n == 0) return RS_OK;
     uint64_t* tmp = nullptr;
     uint64_t* dcount = nullptr;
-    e = cudaMallocAsync((void**)&tmp, n * sizeof(uint64_t), s);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dcount, sizeof(uint64_t), s);
+    prof_begin(P_FINALIZE, s);
+    e = dmalloc((void**)&tmp, n * sizeof(uint64_t), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&dcount, sizeof(uint64_t), s);
     if (e == cudaSuccess) e = compact_u64(reinterpret_cast<const uint64_t*>(ps->slots), ps->capacity, kEmptyKey, tmp,
                                           dcount, s);
     const unsigned grid = (unsigned)((n + 255) / 256);
-    if (e == cudaSuccess && order == 1) k_swap_halves<<<grid, 256, 0, s>>>(tmp, n);
+    if (e == cudaSuccess && order == 1) launch(k_swap_halves, grid, 256, 0, s, tmp, n);
     if (e == cudaSuccess) e = radix_sort_u64(tmp, nullptr, n, 64, s);
-    if (e == cudaSuccess && order == 1) k_swap_halves<<<grid, 256, 0, s>>>(tmp, n);
+    if (e == cudaSuccess && order == 1) launch(k_swap_halves, grid, 256, 0, s, tmp, n);
     const uint64_t ncopy = std::min<uint64_t>(n, capacity);
     if (e == cudaSuccess && ncopy)
         e = cudaMemcpyAsync(d_keys, tmp, ncopy * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
+    prof_end(P_FINALIZE, s);
     if (tmp) cudaFreeAsync(tmp, s);
     if (dcount) cudaFreeAsync(dcount, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
+    prof_collect();
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return to_status(e);
     *h_count = n;
@@ -173,14 +180,16 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
     const bool b2a = direction == 0 || direction == 2;
     cudaStream_t s = (cudaStream_t)stream;
     for (int attempt = 0; attempt < 8; ++attempt) {
-        int st = rs_pairset_clear(ps, stream);
-        if (st != RS_OK) return st;
-        // Order of MeshIntersectionLauncher use in executeHashQuery: overlap A->B, overlap B->A,
-        // containment A->B, containment B->A (raytracer_intersection_estimated_main.cpp:107-158).
-        if (st == RS_OK && a2b)
-            st = rs_edge_join(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, stream);
-        if (st == RS_OK && b2a)
-            st = rs_edge_join(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, stream);
+        // Order of executeHashQuery (raytracer_intersection_estimated_main.cpp:107-158): overlap A->B,
+        // overlap B->A, containment A->B, containment B->A.  The two edge directions are queued
+        // back to back and checked with one status read.
+        cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, 2 * sizeof(unsigned long long), s);
+        if (e == cudaSuccess && a2b)
+            e = edge_join_async(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s);
+        if (e == cudaSuccess && b2a)
+            e = edge_join_async(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, s);
+        int st = table_status(ps, s, e);
         if (with_containment) {
             if (st == RS_OK && a2b) st = rs_containment(B, A->V, A->nV, A->I, A->nF, A->t2o, 0, ps, stream);
             if (st == RS_OK && b2a) st = rs_containment(A, B->V, B->nV, B->I, B->nF, B->t2o, 1, ps, stream);
@@ -190,7 +199,7 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
         uint64_t cap = ps->capacity * 4;
         if (!ps->pow2 && cap % 2 == 0) cap += 1;
         if (cap > (1ull << 34)) return RS_ERR_TABLE_FULL;
-        cudaError_t e = alloc_slots(ps, cap, s);
+        e = alloc_slots(ps, cap, s);
         if (e != cudaSuccess) return to_status(e);
     }
     return RS_ERR_TABLE_FULL;

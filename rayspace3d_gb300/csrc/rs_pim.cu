@@ -6,12 +6,23 @@
 // (query/src/raytracing/ResultProcessor.cpp:8-60).
 //
 // The reference re-traces a closest-hit query from t_min = t + 1e-6 until it misses
-// (crossings + 1 traversals per ray).  Here one traversal collects every crossing
-// with t in [1e-6, 1e16] into a per-thread list kept sorted by (t, triangle id);
-// the reference's advance rule is then applied to the sorted list.  A ray with more
-// crossings than the list holds is queued for an exact fallback that walks the hits
-// in the same order by re-traversal.
+// (crossings + 1 traversals per ray).  Here every crossing with t in [1e-6, 1e16] is
+// collected once into a per-thread register list, sorted by (t, triangle id), and the
+// reference's advance rule is applied to the sorted list.  A ray with more crossings
+// than the list holds is queued for an exact fallback that walks the hits in the same
+// order by re-traversal.
+//
+// Candidates come from one of two structures with the same hit set:
+//  * rays along +x, +y or +z use a column grid: a uniform 2D grid over the projection
+//    of the leaf-ordered triangles.  Triangle boxes and query points go through the
+//    same monotone cell formula, so every triangle whose projection can contain the
+//    (perturbed) point is in the point's cell;
+//  * any other direction traverses the BVH.
+#include <algorithm>
 #include <climits>
+#include <cmath>
+#include <cstring>
+#include <mutex>
 
 #include "rs_engine.h"
 #include "rs_prims.cuh"
@@ -51,11 +62,58 @@ struct Chain {
     }
 };
 
+// Up to kHits crossings in registers: predicated append, sorting network at the end.
+struct HitList {
+    float t[kHits];
+    uint32_t id[kHits];
+    int32_t obj[kHits];
+    int n = 0;
+    bool ovf = false;
+    __device__ __forceinline__ void add(float tt, uint32_t ii, int32_t oo) {
+        if (n >= kHits) {
+            ovf = true;
+            return;
+        }
+#pragma unroll
+        for (int j = 0; j < kHits; ++j)
+            if (j == n) {
+                t[j] = tt;
+                id[j] = ii;
+                obj[j] = oo;
+            }
+        ++n;
+    }
+    // Odd-even transposition sort of all kHits slots (empty slots sort last).
+    __device__ __forceinline__ Chain finish() {
+#pragma unroll
+        for (int j = 0; j < kHits; ++j)
+            if (j >= n) {
+                t[j] = INFINITY;
+                id[j] = 0xffffffffu;
+                obj[j] = -1;
+            }
+#pragma unroll
+        for (int r = 0; r < kHits; ++r) {
+#pragma unroll
+            for (int j = r & 1; j + 1 < kHits; j += 2) {
+                if (hit_less(t[j + 1], id[j + 1], t[j], id[j])) {
+                    const float tt = t[j]; t[j] = t[j + 1]; t[j + 1] = tt;
+                    const uint32_t ii = id[j]; id[j] = id[j + 1]; id[j + 1] = ii;
+                    const int32_t oo = obj[j]; obj[j] = obj[j + 1]; obj[j + 1] = oo;
+                }
+            }
+        }
+        Chain c;
+#pragma unroll
+        for (int j = 0; j < kHits; ++j)
+            if (j < n) c.step(t[j], obj[j]);
+        return c;
+    }
+};
+
 template <int AXIS>
 __device__ __forceinline__ bool box_filter(const float* __restrict__ box, const Ray& r) {
-    float ht[12];
-    uint32_t hid[12];
-    int nh = 0;
+    HitList hl;
 #pragma unroll 1
     for (int k = 0; k < 12; ++k) {
         float a[3], b[3], c[3];
@@ -66,44 +124,34 @@ __device__ __forceinline__ bool box_filter(const float* __restrict__ box, const 
             c[q] = __ldg(&box[9 * k + 6 + q]);
         }
         float t;
-        if (hit_triangle<AXIS>(r, a, b, c, t)) {
-            int j = nh++;
-            while (j > 0 && hit_less(t, (uint32_t)k, ht[j - 1], hid[j - 1])) {
-                ht[j] = ht[j - 1];
-                hid[j] = hid[j - 1];
-                --j;
-            }
-            ht[j] = t;
-            hid[j] = (uint32_t)k;
-        }
+        if (hit_triangle<AXIS>(r, a, b, c, t)) hl.add(t, (uint32_t)k, 0);
     }
-    Chain c;
-    for (int j = 0; j < nh; ++j) c.step(ht[j], 0);
-    return (c.count & 1) != 0;
+    // A ray crosses at most two of the 12 faces under the hit contract.
+    const Chain ch = hl.finish();
+    return (ch.count & 1) != 0;
+}
+
+__device__ __forceinline__ void write_result(const Chain& ch, uint64_t i, int32_t* out_obj, uint8_t* out_in) {
+    const bool inside = (ch.count & 1) != 0;
+    if (out_obj) out_obj[i] = inside ? ch.first_obj : -1;
+    if (out_in) out_in[i] = inside ? 1 : 0;
 }
 
 template <int AXIS, bool FILTER>
 __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint64_t n, float dx, float dy, float dz,
                                             const BNode* __restrict__ nodes, uint32_t max_steps,
-                                            const float4* __restrict__ tris,
-                                            const float* __restrict__ box, int32_t* __restrict__ out_obj,
-                                            uint8_t* __restrict__ out_in,
+                                            const float4* __restrict__ tris, const float* __restrict__ box,
+                                            int32_t* __restrict__ out_obj, uint8_t* __restrict__ out_in,
                                             unsigned int* __restrict__ status, uint32_t* __restrict__ ovf_list,
                                             unsigned long long* __restrict__ ovf_count) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
-    const Ray r = make_ray(px, py, pz, dx, dy, dz, kEps, kTmax);
+    const Ray r = make_ray(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], dx, dy, dz, kEps, kTmax);
     if (FILTER && !box_filter<AXIS>(box, r)) {
-        if (out_obj) out_obj[i] = -1;
-        if (out_in) out_in[i] = 0;
+        write_result(Chain{}, i, out_obj, out_in);
         return;
     }
-    float ht[kHits];
-    uint32_t hid[kHits];
-    int32_t hob[kHits];
-    int nh = 0;
-    bool ovf = false;
+    HitList hl;
     const bool ok = traverse<AXIS>(nodes, max_steps, r, [&](int first, int cnt) {
         for (int k = first; k < first + cnt; ++k) {
             float a[3], b[3], c[3];
@@ -111,41 +159,74 @@ __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint6
             int32_t obj;
             load_tri(tris, k, a, b, c, tid, obj);
             float t;
-            if (!hit_triangle<AXIS>(r, a, b, c, t)) continue;
-            if (nh == kHits) {
-                ovf = true;
-                continue;
-            }
-            int j = nh++;
-            while (j > 0 && hit_less(t, tid, ht[j - 1], hid[j - 1])) {
-                ht[j] = ht[j - 1];
-                hid[j] = hid[j - 1];
-                hob[j] = hob[j - 1];
-                --j;
-            }
-            ht[j] = t;
-            hid[j] = tid;
-            hob[j] = obj;
+            if (hit_triangle<AXIS>(r, a, b, c, t)) hl.add(t, tid, obj);
         }
     });
     if (!ok) {
         atomicOr(status, ST_STACK_OVERFLOW);
         return;
     }
-    if (ovf) {
-        const unsigned long long slot = atomicAdd(ovf_count, 1ull);
-        ovf_list[slot] = (uint32_t)i;
+    if (hl.ovf) {
+        ovf_list[atomicAdd(ovf_count, 1ull)] = (uint32_t)i;
         return;
     }
-    Chain ch;
-    for (int j = 0; j < nh; ++j) ch.step(ht[j], hob[j]);
-    const bool inside = (ch.count & 1) != 0;
-    if (out_obj) out_obj[i] = inside ? ch.first_obj : -1;
-    if (out_in) out_in[i] = inside ? 1 : 0;
+    write_result(hl.finish(), i, out_obj, out_in);
+}
+
+struct GridView {
+    float u0, v0, su, sv, u1, v1;
+    int gu, gv;
+    const uint32_t* start;
+    const uint32_t* list;
+};
+
+// Monotone cell index: identical for triangle boxes and query points.
+__device__ __forceinline__ int cell_of(float x, float x0, float s, int g) {
+    float f = floorf(__fmul_rn(__fsub_rn(x, x0), s));
+    f = fminf(fmaxf(f, 0.0f), (float)(g - 1));
+    return (int)f;
+}
+
+template <int AXIS, bool FILTER>
+__global__ void __launch_bounds__(kT) k_pim_grid(const float* __restrict__ pts, uint64_t n, GridView g,
+                                                 const float4* __restrict__ tris, const float* __restrict__ box,
+                                                 int32_t* __restrict__ out_obj, uint8_t* __restrict__ out_in,
+                                                 uint32_t* __restrict__ ovf_list,
+                                                 unsigned long long* __restrict__ ovf_count) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+    const Ray r = make_ray(p[0], p[1], p[2], AXIS == 0 ? 1.0f : 0.0f, AXIS == 1 ? 1.0f : 0.0f,
+                           AXIS == 2 ? 1.0f : 0.0f, kEps, kTmax);
+    if (FILTER && !box_filter<AXIS>(box, r)) {
+        write_result(Chain{}, i, out_obj, out_in);
+        return;
+    }
+    constexpr int U = (AXIS + 1) % 3, V = (AXIS + 2) % 3;
+    HitList hl;
+    // A crossed triangle's projected box contains the point, and all boxes lie in [u0,u1]x[v0,v1].
+    if (p[U] >= g.u0 && p[U] <= g.u1 && p[V] >= g.v0 && p[V] <= g.v1) {
+        const int c = cell_of(p[V], g.v0, g.sv, g.gv) * g.gu + cell_of(p[U], g.u0, g.su, g.gu);
+        const uint32_t b = __ldg(&g.start[c]), e = __ldg(&g.start[c + 1]);
+        for (uint32_t j = b; j < e; ++j) {
+            const int k = (int)__ldg(&g.list[j]);
+            float a[3], bb[3], cc[3];
+            uint32_t tid;
+            int32_t obj;
+            load_tri(tris, k, a, bb, cc, tid, obj);
+            float t;
+            if (hit_triangle<AXIS>(r, a, bb, cc, t)) hl.add(t, tid, obj);
+        }
+    }
+    if (hl.ovf) {
+        ovf_list[atomicAdd(ovf_count, 1ull)] = (uint32_t)i;
+        return;
+    }
+    write_result(hl.finish(), i, out_obj, out_in);
 }
 
 // Exact fallback for rays with more than kHits crossings: each round re-traverses
-// and takes the smallest (t, id) above the previous one.
+// the BVH and takes the smallest (t, id) above the previous one.
 template <int AXIS>
 __global__ void __launch_bounds__(kT) k_pim_fallback(const float* __restrict__ pts, float dx, float dy, float dz,
                                                      const BNode* __restrict__ nodes, uint32_t max_steps,
@@ -198,10 +279,143 @@ __global__ void __launch_bounds__(kT) k_pim_fallback(const float* __restrict__ p
             have_prev = true;
         }
         if (it == kFallbackIters) atomicOr(status, ST_ITER_LIMIT);
-        const bool inside = (ch.count & 1) != 0;
-        if (out_obj) out_obj[i] = inside ? ch.first_obj : -1;
-        if (out_in) out_in[i] = inside ? 1 : 0;
+        write_result(ch, i, out_obj, out_in);
     }
+}
+
+// --- column grid build ---------------------------------------------------------------
+
+template <int AXIS>
+__device__ __forceinline__ void tri_uv_box(const float4* __restrict__ tris, int k, float& ul, float& uh, float& vl,
+                                           float& vh) {
+    const float4 a = __ldg(&tris[3 * (size_t)k]), b = __ldg(&tris[3 * (size_t)k + 1]),
+                 c = __ldg(&tris[3 * (size_t)k + 2]);
+    const float au = AXIS == 0 ? a.y : (AXIS == 1 ? a.z : a.x), av = AXIS == 0 ? a.z : (AXIS == 1 ? a.x : a.y);
+    const float bu = AXIS == 0 ? b.y : (AXIS == 1 ? b.z : b.x), bv = AXIS == 0 ? b.z : (AXIS == 1 ? b.x : b.y);
+    const float cu = AXIS == 0 ? c.y : (AXIS == 1 ? c.z : c.x), cv = AXIS == 0 ? c.z : (AXIS == 1 ? c.x : c.y);
+    ul = fminf(fminf(au, bu), cu);
+    uh = fmaxf(fmaxf(au, bu), cu);
+    vl = fminf(fminf(av, bv), cv);
+    vh = fmaxf(fmaxf(av, bv), cv);
+}
+
+__device__ __forceinline__ int ford(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+
+template <int AXIS>
+__global__ void k_cg_bounds(const float4* __restrict__ tris, int n, int* __restrict__ b) {
+    float ul = INFINITY, uh = -INFINITY, vl = INFINITY, vh = -INFINITY;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        float a0, a1, a2, a3;
+        tri_uv_box<AXIS>(tris, k, a0, a1, a2, a3);
+        ul = fminf(ul, a0);
+        uh = fmaxf(uh, a1);
+        vl = fminf(vl, a2);
+        vh = fmaxf(vh, a3);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ul = fminf(ul, __shfl_xor_sync(0xffffffffu, ul, o));
+        uh = fmaxf(uh, __shfl_xor_sync(0xffffffffu, uh, o));
+        vl = fminf(vl, __shfl_xor_sync(0xffffffffu, vl, o));
+        vh = fmaxf(vh, __shfl_xor_sync(0xffffffffu, vh, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&b[0], ford(ul));
+        atomicMax(&b[1], ford(uh));
+        atomicMin(&b[2], ford(vl));
+        atomicMax(&b[3], ford(vh));
+    }
+}
+
+template <int AXIS, bool FILL>
+__global__ void k_cg_cells(const float4* __restrict__ tris, int n, GridView g, uint32_t* __restrict__ count,
+                           uint32_t* __restrict__ list) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float ul, uh, vl, vh;
+    tri_uv_box<AXIS>(tris, k, ul, uh, vl, vh);
+    const int cu0 = cell_of(ul, g.u0, g.su, g.gu), cu1 = cell_of(uh, g.u0, g.su, g.gu);
+    const int cv0 = cell_of(vl, g.v0, g.sv, g.gv), cv1 = cell_of(vh, g.v0, g.sv, g.gv);
+    for (int cv = cv0; cv <= cv1; ++cv)
+        for (int cu = cu0; cu <= cu1; ++cu) {
+            const int c = cv * g.gu + cu;
+            const uint32_t slot = atomicAdd(&count[c], 1u);
+            if (FILL) list[g.start[c] + slot] = (uint32_t)k;
+        }
+}
+
+std::mutex g_grid_mu;
+
+float dec_ord(int i) {
+    int x = i >= 0 ? i : i ^ 0x7fffffff;
+    float f;
+    std::memcpy(&f, &x, 4);
+    return f;
+}
+
+template <int AXIS>
+cudaError_t build_grid(rs_bvh* bvh, cudaStream_t s) {
+    rs_column_grid& cg = bvh->cgrid[AXIS];
+    const int n = (int)bvh->n_tris;
+    int* b = nullptr;
+    cudaError_t e = dmalloc((void**)&b, 4 * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    const int init[4] = {0x7fffffff, (int)0x80000000, 0x7fffffff, (int)0x80000000};
+    cudaMemcpyAsync(b, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    launch(k_cg_bounds<AXIS>, 2 * sm_count(), 256, 0, s, (const float4*)bvh->tris, n, b);
+    int hb[4];
+    e = cudaMemcpyAsync(hb, b, sizeof(hb), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(b, s);
+    if (e != cudaSuccess) return e;
+    cg.u0 = dec_ord(hb[0]);
+    cg.u1 = dec_ord(hb[1]);
+    cg.v0 = dec_ord(hb[2]);
+    cg.v1 = dec_ord(hb[3]);
+    // About four cells per triangle, shaped like the projected bounds.
+    const double target = std::min(std::max(4.0 * n, 1.0), (double)(1 << 24));
+    const double w = (double)cg.u1 - cg.u0, h = (double)cg.v1 - cg.v0;
+    int gu = 1, gv = 1;
+    if (w > 0 && h > 0) {
+        gu = (int)std::lround(std::sqrt(target * w / h));
+        gu = std::min(std::max(gu, 1), 8192);
+        gv = (int)std::min(std::max(std::lround(target / gu), 1L), 8192L);
+    } else if (w > 0) {
+        gu = (int)std::min(target, 8192.0);
+    } else if (h > 0) {
+        gv = (int)std::min(target, 8192.0);
+    }
+    cg.gu = gu;
+    cg.gv = gv;
+    cg.su = w > 0 ? (float)gu / (float)w : 0.0f;
+    cg.sv = h > 0 ? (float)gv / (float)h : 0.0f;
+    const size_t ncell = (size_t)gu * gv;
+    uint32_t* count = nullptr;
+    e = dmalloc((void**)&count, ncell * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&cg.start, (ncell + 1) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    GridView gvw{cg.u0, cg.v0, cg.su, cg.sv, cg.u1, cg.v1, gu, gv, cg.start, nullptr};
+    cudaMemsetAsync(count, 0, ncell * sizeof(uint32_t), s);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    launch(k_cg_cells<AXIS, false>, grid, 256, 0, s, (const float4*)bvh->tris, n, gvw, count, (uint32_t*)nullptr);
+    e = exclusive_scan_u32(count, cg.start, ncell, cg.start + ncell, s);
+    uint32_t total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, cg.start + ncell, sizeof(total), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = dmalloc((void**)&cg.list, (size_t)std::max<uint32_t>(total, 1) * 4, s);
+    if (e == cudaSuccess) {
+        cudaMemsetAsync(count, 0, ncell * sizeof(uint32_t), s);
+        launch(k_cg_cells<AXIS, true>, grid, 256, 0, s, (const float4*)bvh->tris, n, gvw, count, cg.list);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(count, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cg.nlist = total;
+    if (e == cudaSuccess) cg.built = 1;
+    return e;
 }
 
 template <int AXIS, bool FILTER>
@@ -209,10 +423,20 @@ cudaError_t launch_pim(const rs_bvh* bvh, const float* pts, uint64_t n, float dx
                        const float* box, int32_t* obj, uint8_t* in, unsigned int* status, uint32_t* ovf_list,
                        unsigned long long* ovf_count, cudaStream_t s) {
     const unsigned grid = (unsigned)((n + kT - 1) / kT);
-    k_pim<AXIS, FILTER><<<grid, kT, 0, s>>>(pts, n, dx, dy, dz, bvh->nodes, max_steps(bvh), bvh->tris, box, obj, in, status,
-                                            ovf_list, ovf_count);
-    k_pim_fallback<AXIS><<<2 * sm_count(), 128, 0, s>>>(pts, dx, dy, dz, bvh->nodes, max_steps(bvh), bvh->tris, obj, in, status,
-                                                        ovf_list, ovf_count);
+    constexpr int GA = AXIS < 0 ? 0 : AXIS;
+    prof_begin(P_PIM, s);
+    if (AXIS >= 0 && bvh->cgrid[GA].built) {
+        const rs_column_grid& cg = bvh->cgrid[GA];
+        GridView g{cg.u0, cg.v0, cg.su, cg.sv, cg.u1, cg.v1, cg.gu, cg.gv, cg.start, cg.list};
+        launch(k_pim_grid<GA, FILTER>, grid, kT, 0, s, pts, n, g, (const float4*)bvh->tris, box, obj, in, ovf_list,
+               ovf_count);
+    } else {
+        launch(k_pim<AXIS, FILTER>, grid, kT, 0, s, pts, n, dx, dy, dz, bvh->nodes, max_steps(bvh),
+               (const float4*)bvh->tris, box, obj, in, status, ovf_list, ovf_count);
+    }
+    prof_end(P_PIM, s);
+    launch(k_pim_fallback<AXIS>, 2 * sm_count(), 128, 0, s, pts, dx, dy, dz, bvh->nodes, max_steps(bvh),
+           (const float4*)bvh->tris, obj, in, status, ovf_list, ovf_count);
     return cudaGetLastError();
 }
 
@@ -232,11 +456,12 @@ BoxMesh make_box(const rs_bvh* bvh) {
     return b;
 }
 
-int pim_impl(const rs_bvh* bvh, const float* pts, uint64_t n, float dx, float dy, float dz, int32_t* obj,
+int pim_impl(const rs_bvh* cbvh, const float* pts, uint64_t n, float dx, float dy, float dz, int32_t* obj,
              uint8_t* in, bool filter, cudaStream_t s) {
-    if (!bvh || (n && !pts)) return RS_ERR_INVALID;
+    if (!cbvh || (n && !pts)) return RS_ERR_INVALID;
     if (n == 0) return RS_OK;
     if (n > 0xffffffffull) return RS_ERR_INVALID;
+    rs_bvh* bvh = const_cast<rs_bvh*>(cbvh);
     if (filter && bvh->nV == 0) {
         cudaError_t e = cudaSuccess;
         if (obj) e = cudaMemsetAsync(obj, 0xff, n * sizeof(int32_t), s);
@@ -244,10 +469,23 @@ int pim_impl(const rs_bvh* bvh, const float* pts, uint64_t n, float dx, float dy
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         return to_status(e);
     }
+    const bool zx = dx == 0.0f, zy = dy == 0.0f, zz = dz == 0.0f;
+    int axis = -1;
+    if (dz == 1.0f && zx && zy) axis = 2;
+    else if (dx == 1.0f && zy && zz) axis = 0;
+    else if (dy == 1.0f && zx && zz) axis = 1;
+    if (axis >= 0 && bvh->n_tris > 0 && !bvh->cgrid[axis].built) {
+        // The column grid is built once per handle and axis, like the index build of the reference.
+        std::lock_guard<std::mutex> g(g_grid_mu);
+        if (!bvh->cgrid[axis].built) {
+            cudaError_t e = axis == 0 ? build_grid<0>(bvh, s) : (axis == 1 ? build_grid<1>(bvh, s) : build_grid<2>(bvh, s));
+            if (e != cudaSuccess) return to_status(e);
+        }
+    }
     unsigned long long* meta = nullptr;  // [0] status, [1] overflow count, then the 12 box triangles
     uint32_t* ovf = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&meta, 2 * sizeof(unsigned long long) + sizeof(BoxMesh), s);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&ovf, n * sizeof(uint32_t), s);
+    cudaError_t e = dmalloc((void**)&meta, 2 * sizeof(unsigned long long) + sizeof(BoxMesh), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&ovf, n * sizeof(uint32_t), s);
     if (e != cudaSuccess) {
         if (meta) cudaFreeAsync(meta, s);
         cudaStreamSynchronize(s);
@@ -259,14 +497,13 @@ int pim_impl(const rs_bvh* bvh, const float* pts, uint64_t n, float dx, float dy
     BoxMesh hbox = filter ? make_box(bvh) : BoxMesh{};
     float* box = reinterpret_cast<float*>(meta + 2);
     if (filter) cudaMemcpyAsync(box, &hbox, sizeof(BoxMesh), cudaMemcpyHostToDevice, s);
-    const bool zx = dx == 0.0f, zy = dy == 0.0f, zz = dz == 0.0f;
-    if (dz == 1.0f && zx && zy) {
+    if (axis == 2) {
         e = filter ? launch_pim<2, true>(bvh, pts, n, dx, dy, dz, box, obj, in, status, ovf, meta + 1, s)
                    : launch_pim<2, false>(bvh, pts, n, dx, dy, dz, box, obj, in, status, ovf, meta + 1, s);
-    } else if (dx == 1.0f && zy && zz) {
+    } else if (axis == 0) {
         e = filter ? launch_pim<0, true>(bvh, pts, n, dx, dy, dz, box, obj, in, status, ovf, meta + 1, s)
                    : launch_pim<0, false>(bvh, pts, n, dx, dy, dz, box, obj, in, status, ovf, meta + 1, s);
-    } else if (dy == 1.0f && zx && zz) {
+    } else if (axis == 1) {
         e = filter ? launch_pim<1, true>(bvh, pts, n, dx, dy, dz, box, obj, in, status, ovf, meta + 1, s)
                    : launch_pim<1, false>(bvh, pts, n, dx, dy, dz, box, obj, in, status, ovf, meta + 1, s);
     } else {
@@ -278,6 +515,7 @@ int pim_impl(const rs_bvh* bvh, const float* pts, uint64_t n, float dx, float dy
     cudaFreeAsync(meta, s);
     cudaFreeAsync(ovf, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
+    prof_collect();
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return to_status(e);
     return status_from_bits((uint32_t)hmeta[0]);
@@ -322,13 +560,13 @@ extern "C" int rs_compact_hits(const int32_t* d_obj, uint64_t n, int32_t* d_poin
     if (n == 0) return RS_OK;
     uint32_t* flags = nullptr;
     uint32_t* total = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&flags, n * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&total, sizeof(uint32_t), s);
+    cudaError_t e = dmalloc((void**)&flags, n * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&total, sizeof(uint32_t), s);
     if (e == cudaSuccess) {
         const unsigned grid = (unsigned)((n + kT - 1) / kT);
-        k_hit_flags<<<grid, kT, 0, s>>>(d_obj, n, flags);
+        launch(k_hit_flags, grid, kT, 0, s, d_obj, n, flags);
         e = exclusive_scan_u32(flags, flags, n, total, s);
-        if (e == cudaSuccess) k_hit_scatter<<<grid, kT, 0, s>>>(d_obj, n, flags, d_point_ids, d_point_obj, capacity);
+        if (e == cudaSuccess) launch(k_hit_scatter, grid, kT, 0, s, d_obj, n, flags, d_point_ids, d_point_obj, capacity);
     }
     uint32_t ht = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&ht, total, sizeof(ht), cudaMemcpyDeviceToHost, s);

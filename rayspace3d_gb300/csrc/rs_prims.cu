@@ -208,11 +208,11 @@ cudaError_t scan_impl(const Tin* in, Tacc* out, size_t n, Tacc* total, cudaStrea
     }
     const size_t nb = (n + kTile - 1) / kTile;
     Tacc* part = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&part, nb * sizeof(Tacc), s);
+    cudaError_t e = dmalloc((void**)&part, nb * sizeof(Tacc), s);
     if (e != cudaSuccess) return e;
-    k_scan_reduce<Tin, Tacc><<<(unsigned)nb, kThreads, 0, s>>>(in, n, part);
-    k_scan_top<Tacc><<<1, 1024, 0, s>>>(part, nb, total);
-    k_scan_down<Tin, Tacc><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, part);
+    launch(k_scan_reduce<Tin, Tacc>, (unsigned)nb, kThreads, 0, s, in, n, part);
+    launch(k_scan_top<Tacc>, 1, 1024, 0, s, part, nb, total);
+    launch(k_scan_down<Tin, Tacc>, (unsigned)nb, kThreads, 0, s, in, out, n, part);
     e = cudaGetLastError();
     cudaFreeAsync(part, s);
     return e;
@@ -292,16 +292,16 @@ int sm_count() {
     return cached;
 }
 
-cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s) {
-    if (n <= 1 || end_bit <= 0) return cudaSuccess;
-    const int passes = (end_bit + 7) / 8;
+cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit) {
+    if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
+    const int passes = (end_bit - begin_bit + 7) / 8;
     const size_t tiles = (n + kTile - 1) / kTile;
     uint64_t* k2 = nullptr;
     uint32_t* v2 = nullptr;
     uint32_t* hist = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&k2, n * sizeof(uint64_t), s);
-    if (e == cudaSuccess && vals) e = cudaMallocAsync((void**)&v2, n * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&hist, 256 * tiles * sizeof(uint32_t), s);
+    cudaError_t e = dmalloc((void**)&k2, n * sizeof(uint64_t), s);
+    if (e == cudaSuccess && vals) e = dmalloc((void**)&v2, n * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&hist, 256 * tiles * sizeof(uint32_t), s);
     if (e != cudaSuccess) {
         if (k2) cudaFreeAsync(k2, s);
         if (v2) cudaFreeAsync(v2, s);
@@ -312,11 +312,11 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit
     uint32_t* va = vals;
     uint32_t* vb = v2;
     for (int p = 0; p < passes && e == cudaSuccess; ++p) {
-        const int shift = 8 * p;
-        k_radix_hist<<<(unsigned)tiles, kThreads, 0, s>>>(ka, n, shift, hist, (int)tiles);
+        const int shift = begin_bit + 8 * p;
+        launch(k_radix_hist, (unsigned)tiles, kThreads, 0, s, ka, n, shift, hist, (int)tiles);
         e = scan_impl<uint32_t, uint32_t>(hist, hist, 256 * tiles, nullptr, s);
         if (e != cudaSuccess) break;
-        k_radix_scatter<<<(unsigned)tiles, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, hist, (int)tiles);
+        launch(k_radix_scatter, (unsigned)tiles, kThreads, 0, s, ka, va, kb, vb, n, shift, hist, (int)tiles);
         e = cudaGetLastError();
         uint64_t* tk = ka; ka = kb; kb = tk;
         uint32_t* tv = va; va = vb; vb = tv;
@@ -345,12 +345,12 @@ static cudaError_t compact_impl(const uint64_t* in, size_t n, uint64_t skip, con
     if (n == 0) return count ? cudaMemsetAsync(count, 0, sizeof(uint64_t), s) : cudaSuccess;
     const size_t nb = (n + kTile - 1) / kTile;
     uint64_t* part = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&part, nb * sizeof(uint64_t), s);
+    cudaError_t e = dmalloc((void**)&part, nb * sizeof(uint64_t), s);
     if (e != cudaSuccess) return e;
-    k_compact_count<<<(unsigned)nb, kThreads, 0, s>>>(in, n, skip, prev_of, part);
-    k_scan_top<unsigned long long><<<1, 1024, 0, s>>>(reinterpret_cast<unsigned long long*>(part), nb,
+    launch(k_compact_count, (unsigned)nb, kThreads, 0, s, in, n, skip, prev_of, part);
+    launch(k_scan_top<unsigned long long>, 1, 1024, 0, s, reinterpret_cast<unsigned long long*>(part), nb,
                                                       reinterpret_cast<unsigned long long*>(count));
-    k_compact_write<<<(unsigned)nb, kThreads, 0, s>>>(in, n, skip, prev_of, part, out);
+    launch(k_compact_write, (unsigned)nb, kThreads, 0, s, in, n, skip, prev_of, part, out);
     e = cudaGetLastError();
     cudaFreeAsync(part, s);
     return e;
@@ -364,7 +364,7 @@ cudaError_t compact_u64(const uint64_t* in, size_t n, uint64_t skip, uint64_t* o
 cudaError_t unique_sorted_u64(uint64_t* keys, size_t n, uint64_t* count, cudaStream_t s) {
     if (n == 0) return count ? cudaMemsetAsync(count, 0, sizeof(uint64_t), s) : cudaSuccess;
     uint64_t* tmp = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&tmp, n * sizeof(uint64_t), s);
+    cudaError_t e = dmalloc((void**)&tmp, n * sizeof(uint64_t), s);
     if (e != cudaSuccess) return e;
     e = compact_impl(keys, n, 0, keys, tmp, count, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(keys, tmp, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);

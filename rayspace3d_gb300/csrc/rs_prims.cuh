@@ -4,12 +4,15 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "rs_launch.cuh"
+
 namespace rs {
 
 // Stable LSD radix sort of 64-bit keys (and optional 32-bit values) on bits
-// [0, end_bit), 8 bits per pass, in place.  Temporaries come from the stream's
-// memory pool.
-cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s);
+// [begin_bit, end_bit), 8 bits per pass, in place.  Temporaries come from the
+// library's memory pool.
+cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s,
+                           int begin_bit = 0);
 
 // Exclusive prefix sums.  `total` (device, nullable) receives the sum of all inputs.
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, cudaStream_t s);
