@@ -18,7 +18,6 @@
 #include <cstdlib>
 #include <cstring>
 
-#include <cuda/atomic>
 
 #include "rs_engine.h"
 #include "rs_prims.cuh"
@@ -179,22 +178,23 @@ __global__ void k_karras(const uint64_t* __restrict__ keys, int n, int* __restri
 // is larger than leaf_size (and the root): each child of p that spans <= leaf_size
 // triangles is a leaf group whose box is the union of its triangles, contiguous in
 // leaf order.  The thread stores that box and arrives at p; the second arrival at a
-// node merges both children and moves up.  The arrival counter is an acquire-release
-// device-scope atomic, so the first arrival's box store is visible to the second.
+// node merges both children and moves up.  Each arrival publishes its box with a
+// release fence before the counter increment; the second arrival's loads depend on
+// the increment's result and bypass L1.
 __device__ __forceinline__ void arrive(int node, float4 lo, float4 hi, int p, const int* __restrict__ left,
                                        const int* __restrict__ right, const int* __restrict__ parent,
                                        float4* __restrict__ blo, float4* __restrict__ bhi, int* __restrict__ flags) {
     while (p >= 0) {
-        cuda::atomic_ref<int, cuda::thread_scope_device> arrivals(flags[p]);
-        if (arrivals.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
-        const int other = (left[p] == node) ? right[p] : left[p];
+        __threadfence();
+        if (atomicAdd(&flags[p], 1) == 0) return;
+        const int other = (__ldcg(&left[p]) == node) ? __ldcg(&right[p]) : __ldcg(&left[p]);
         const float4 ol = __ldcg(&blo[other]), oh = __ldcg(&bhi[other]);
         lo = make_float4(fminf(lo.x, ol.x), fminf(lo.y, ol.y), fminf(lo.z, ol.z), 0.f);
         hi = make_float4(fmaxf(hi.x, oh.x), fmaxf(hi.y, oh.y), fmaxf(hi.z, oh.z), 0.f);
         __stcg(&blo[p], lo);
         __stcg(&bhi[p], hi);
         node = p;
-        p = parent[p];
+        p = __ldcg(&parent[p]);
     }
 }
 

@@ -63,7 +63,7 @@ extern "C" long long merge_and_deduplicate_pairs_gpu(const void* d_results1, lon
     uint64_t* keys = reinterpret_cast<uint64_t*>(d_merged_output);
     uint64_t* cnt = nullptr;
     uint64_t h = 0;
-    if (radix_sort_u64(keys, nullptr, (size_t)total, 64, 0) != cudaSuccess) return 0;
+    if (sort_u64_any(keys, (size_t)total, 0) != cudaSuccess) return 0;
     if (dmalloc((void**)&cnt, sizeof(uint64_t), 0) != cudaSuccess) return 0;
     if (unique_sorted_u64(keys, (size_t)total, cnt, 0) == cudaSuccess)
         cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, 0);

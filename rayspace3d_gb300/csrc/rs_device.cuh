@@ -291,13 +291,13 @@ struct __align__(16) BNode {
 constexpr int kStack = 64;
 
 // Visits every leaf whose box passes the slab test and calls on_leaf(first, count)
-// for it.  A valid tree visits each node at most once, so `max_steps` (the node
-// count) bounds the loop even if the node array were corrupt.  Returns false on
-// stack overflow or an exhausted step budget.
+// for it.  The stack lives at stack[sp * stride] (a thread-private array, or a column
+// of a shared-memory array).  A valid tree visits each node at most once, so
+// `max_steps` (the node count) bounds the loop even if the node array were corrupt.
+// Returns false on stack overflow or an exhausted step budget.
 template <int AXIS, class F>
-__device__ __forceinline__ bool traverse(const BNode* __restrict__ nodes, uint32_t max_steps, const Ray& r,
-                                         F&& on_leaf) {
-    int stack[kStack];
+__device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNode* __restrict__ nodes,
+                                              uint32_t max_steps, const Ray& r, F&& on_leaf) {
     int sp = 0;
     int node = 0;
     for (uint32_t step = 0;; ++step) {
@@ -315,7 +315,8 @@ __device__ __forceinline__ bool traverse(const BNode* __restrict__ nodes, uint32
         if (h1 && nd.w > 0) { on_leaf(nd.z, nd.w); h1 = false; }
         if (h0 && h1) {
             if (sp == kStack) return false;
-            stack[sp++] = nd.z;
+            stack[sp * stride] = nd.z;
+            ++sp;
             node = nd.x;
         } else if (h0) {
             node = nd.x;
@@ -323,10 +324,18 @@ __device__ __forceinline__ bool traverse(const BNode* __restrict__ nodes, uint32
             node = nd.z;
         } else {
             if (sp == 0) break;
-            node = stack[--sp];
+            --sp;
+            node = stack[sp * stride];
         }
     }
     return true;
+}
+
+template <int AXIS, class F>
+__device__ __forceinline__ bool traverse(const BNode* __restrict__ nodes, uint32_t max_steps, const Ray& r,
+                                         F&& on_leaf) {
+    int stack[kStack];
+    return traverse_with<AXIS>(stack, 1, nodes, max_steps, r, on_leaf);
 }
 
 __device__ __forceinline__ void load_tri(const float4* __restrict__ tris, int k, float* a, float* b, float* c,

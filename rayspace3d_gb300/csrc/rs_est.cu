@@ -16,7 +16,7 @@ namespace rs {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kBlocks = 592;  // fixed, so the summation order is the same on every GPU
+constexpr int kBlocks = 1216;  // fixed, so the summation order is the same on every GPU
 constexpr int kSums = 7;      // raw, sizeA*touch, ratioA*touch, touchA, sizeB*touch, ratioB*touch, touchB
 
 struct Cell {
@@ -69,11 +69,26 @@ __global__ void __launch_bounds__(kT) k_estimate(const uint4* __restrict__ A, co
     if (threadIdx.x < kSums) part[blockIdx.x * kSums + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void k_estimate_final(const double* __restrict__ part, double* __restrict__ out) {
-    if (threadIdx.x >= kSums) return;
-    double s = 0.0;
-    for (int b = 0; b < kBlocks; ++b) s += part[b * kSums + threadIdx.x];
-    out[threadIdx.x] = s;
+// Fixed-order reduction of the per-block partials: thread t sums blocks t, t+256, ...
+// in order, then a fixed shared-memory tree combines the 256 thread sums.
+__global__ void __launch_bounds__(256) k_estimate_final(const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double sh[kSums][256];
+    double acc[kSums] = {0, 0, 0, 0, 0, 0, 0};
+    for (int b = threadIdx.x; b < kBlocks; b += 256) {
+#pragma unroll
+        for (int k = 0; k < kSums; ++k) acc[k] += part[b * kSums + k];
+    }
+#pragma unroll
+    for (int k = 0; k < kSums; ++k) sh[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+#pragma unroll
+            for (int k = 0; k < kSums; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < kSums) out[threadIdx.x] = sh[threadIdx.x][0];
 }
 
 }  // namespace
@@ -87,7 +102,7 @@ int estimate_device(const void* d_a, const void* d_b, uint64_t n, float cell_vol
     prof_begin(P_ESTIMATE, s);
     launch(k_estimate, kBlocks, kT, 0, s, reinterpret_cast<const uint4*>(d_a), reinterpret_cast<const uint4*>(d_b), n,
                                       cell_volume, eps, gamma, part);
-    launch(k_estimate_final, 1, 32, 0, s, part, part + kBlocks * kSums);
+    launch(k_estimate_final, 1, 256, 0, s, part, part + kBlocks * kSums);
     prof_end(P_ESTIMATE, s);
     e = cudaGetLastError();
     if (e == cudaSuccess)

@@ -154,7 +154,7 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
                                           dcount, s);
     const unsigned grid = (unsigned)((n + 255) / 256);
     if (e == cudaSuccess && order == 1) launch(k_swap_halves, grid, 256, 0, s, tmp, n);
-    if (e == cudaSuccess) e = radix_sort_u64(tmp, nullptr, n, 64, s);
+    if (e == cudaSuccess) e = sort_u64_any(tmp, n, s);
     if (e == cudaSuccess && order == 1) launch(k_swap_halves, grid, 256, 0, s, tmp, n);
     const uint64_t ncopy = std::min<uint64_t>(n, capacity);
     if (e == cudaSuccess && ncopy)

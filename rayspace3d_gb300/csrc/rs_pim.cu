@@ -187,41 +187,102 @@ __device__ __forceinline__ int cell_of(float x, float x0, float s, int g) {
     return (int)f;
 }
 
+// Warp-cooperative column-grid query.  Each warp owns 32 points; their candidate
+// lists are flattened into one (point, triangle) work list with a warp scan, so every
+// lane tests one candidate per round however unevenly the candidates are spread over
+// the points (points outside the projected bounds contribute none).  Crossings go to
+// per-point slots in shared memory; each lane then sorts and counts its own point's.
+constexpr int kWarps = kT / 32;
+
 template <int AXIS, bool FILTER>
 __global__ void __launch_bounds__(kT) k_pim_grid(const float* __restrict__ pts, uint64_t n, GridView g,
                                                  const float4* __restrict__ tris, const float* __restrict__ box,
                                                  int32_t* __restrict__ out_obj, uint8_t* __restrict__ out_in,
                                                  uint32_t* __restrict__ ovf_list,
                                                  unsigned long long* __restrict__ ovf_count) {
+    __shared__ float s_t[kWarps][kHits][32];
+    __shared__ uint32_t s_id[kWarps][kHits][32];
+    __shared__ int32_t s_obj[kWarps][kHits][32];
+    __shared__ int s_n[kWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
-    const Ray r = make_ray(p[0], p[1], p[2], AXIS == 0 ? 1.0f : 0.0f, AXIS == 1 ? 1.0f : 0.0f,
-                           AXIS == 2 ? 1.0f : 0.0f, kEps, kTmax);
-    if (FILTER && !box_filter<AXIS>(box, r)) {
-        write_result(Chain{}, i, out_obj, out_in);
-        return;
-    }
+    const bool valid = i < n;
     constexpr int U = (AXIS + 1) % 3, V = (AXIS + 2) % 3;
-    HitList hl;
+    float p[3] = {0.0f, 0.0f, 0.0f};
+    if (valid) {
+        p[0] = pts[3 * i];
+        p[1] = pts[3 * i + 1];
+        p[2] = pts[3 * i + 2];
+    }
+    const float dx = AXIS == 0 ? 1.0f : 0.0f, dy = AXIS == 1 ? 1.0f : 0.0f, dz = AXIS == 2 ? 1.0f : 0.0f;
+    bool keep = valid;
+    if (FILTER && valid) keep = box_filter<AXIS>(box, make_ray(p[0], p[1], p[2], dx, dy, dz, kEps, kTmax));
+    uint32_t b = 0, cnt = 0;
     // A crossed triangle's projected box contains the point, and all boxes lie in [u0,u1]x[v0,v1].
-    if (p[U] >= g.u0 && p[U] <= g.u1 && p[V] >= g.v0 && p[V] <= g.v1) {
+    if (keep && p[U] >= g.u0 && p[U] <= g.u1 && p[V] >= g.v0 && p[V] <= g.v1) {
         const int c = cell_of(p[V], g.v0, g.sv, g.gv) * g.gu + cell_of(p[U], g.u0, g.su, g.gu);
-        const uint32_t b = __ldg(&g.start[c]), e = __ldg(&g.start[c + 1]);
-        for (uint32_t j = b; j < e; ++j) {
-            const int k = (int)__ldg(&g.list[j]);
+        b = __ldg(&g.start[c]);
+        cnt = __ldg(&g.start[c + 1]) - b;
+    }
+    s_n[w][lane] = 0;
+    // Warp exclusive scan of the candidate counts.
+    uint32_t inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    const uint32_t pre = inc - cnt;
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    __syncwarp();
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t j = base + lane;
+        // Owner of work item j: the last lane whose prefix is <= j.
+        int owner = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t pc = __shfl_sync(0xffffffffu, pre, owner + step);
+            if (pc <= j) owner += step;
+        }
+        const uint32_t ob = __shfl_sync(0xffffffffu, b, owner);
+        const uint32_t opre = __shfl_sync(0xffffffffu, pre, owner);
+        const float ox = __shfl_sync(0xffffffffu, p[0], owner);
+        const float oy = __shfl_sync(0xffffffffu, p[1], owner);
+        const float oz = __shfl_sync(0xffffffffu, p[2], owner);
+        if (j < total) {
+            const int k = (int)__ldg(&g.list[ob + (j - opre)]);
             float a[3], bb[3], cc[3];
             uint32_t tid;
             int32_t obj;
             load_tri(tris, k, a, bb, cc, tid, obj);
+            const Ray r = make_ray(ox, oy, oz, dx, dy, dz, kEps, kTmax);
             float t;
-            if (hit_triangle<AXIS>(r, a, bb, cc, t)) hl.add(t, tid, obj);
+            if (hit_triangle<AXIS>(r, a, bb, cc, t)) {
+                const int slot = atomicAdd(&s_n[w][owner], 1);
+                if (slot < kHits) {
+                    s_t[w][slot][owner] = t;
+                    s_id[w][slot][owner] = tid;
+                    s_obj[w][slot][owner] = obj;
+                }
+            }
         }
     }
-    if (hl.ovf) {
+    __syncwarp();
+    if (!valid) return;
+    const int nh = s_n[w][lane];
+    if (nh > kHits) {
         ovf_list[atomicAdd(ovf_count, 1ull)] = (uint32_t)i;
         return;
     }
+    HitList hl;
+#pragma unroll
+    for (int q = 0; q < kHits; ++q)
+        if (q < nh) {
+            hl.t[q] = s_t[w][q][lane];
+            hl.id[q] = s_id[w][q][lane];
+            hl.obj[q] = s_obj[w][q][lane];
+        }
+    hl.n = nh;
     write_result(hl.finish(), i, out_obj, out_in);
 }
 

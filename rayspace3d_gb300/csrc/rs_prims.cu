@@ -279,7 +279,44 @@ __global__ void __launch_bounds__(kThreads) k_compact_write(const uint64_t* __re
     }
 }
 
+// Single-block bitonic sort of up to kSmallSort keys in shared memory.
+constexpr int kSmallSort = 4096;
+
+__global__ void __launch_bounds__(1024) k_sort_small(uint64_t* __restrict__ keys, int n) {
+    __shared__ uint64_t sh[kSmallSort];
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) sh[i] = i < n ? keys[i] : ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const uint64_t a = sh[i], b = sh[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        sh[i] = b;
+                        sh[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = sh[i];
+}
+
 }  // namespace
+
+cudaError_t sort_u64_any(uint64_t* keys, size_t n, cudaStream_t s) {
+    if (n <= 1) return cudaSuccess;
+    if (n <= (size_t)kSmallSort) {
+        launch(k_sort_small, 1, 1024, 0, s, keys, (int)n);
+        return cudaGetLastError();
+    }
+    return radix_sort_u64(keys, nullptr, n, 64, s);
+}
 
 int sm_count() {
     static int cached = 0;

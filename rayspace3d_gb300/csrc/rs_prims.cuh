@@ -14,6 +14,10 @@ namespace rs {
 cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s,
                            int begin_bit = 0);
 
+// Full 64-bit ascending sort of keys: a single-block bitonic sort for small inputs,
+// the radix sort otherwise.
+cudaError_t sort_u64_any(uint64_t* keys, size_t n, cudaStream_t s);
+
 // Exclusive prefix sums.  `total` (device, nullable) receives the sum of all inputs.
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, cudaStream_t s);
 cudaError_t exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, size_t n, int64_t* total, cudaStream_t s);
