@@ -33,7 +33,8 @@ typedef enum rs_status {
     RS_ERR_ITER_LIMIT = 5,      /* an iteration budget ran out; result not valid */
     RS_ERR_FORMAT = 6,          /* malformed input file */
     RS_ERR_OOM = 7,             /* device allocation failed */
-    RS_ERR_TARGET_OVERFLOW = 8  /* containment ray crossed more distinct targets than supported */
+    RS_ERR_TARGET_OVERFLOW = 8, /* containment ray crossed more distinct targets than supported */
+    RS_ERR_TOO_LARGE = 9        /* input larger than a fixed-capacity entry point accepts */
 } rs_status;
 
 typedef struct rs_bvh rs_bvh;         /* triangle BVH of one geometry set, device resident */
@@ -74,6 +75,20 @@ int rs_pim(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float
  * parity against the mesh for the points the box test keeps, in one fused launch. */
 int rs_pim_filtered(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
                     int32_t* d_obj, uint8_t* d_inside, void* stream);
+
+/* Point-in-mesh without any device allocation (no counterpart in the reference).
+ * For callers that cannot allocate device memory while they query: code running while
+ * another framework captures the stream into a CUDA graph, services whose allocator has
+ * reserved the whole GPU, or loops that cannot afford an allocation's implicit
+ * synchronisation.  Same results as rs_pim / rs_pim_filtered (filtered != 0).  Per-call
+ * scratch comes from a fixed 4 MiB array inside the library that every GPU which loads
+ * it holds until the process exits; n above 1,048,576 points returns RS_ERR_TOO_LARGE.
+ * The first call on a device looks the array up (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the one array, so calls whose work
+ * overlaps on the GPU (other streams or threads) race: serialise them.  It uses an
+ * axis-aligned column grid only if an earlier rs_pim built it, never building one. */
+int rs_pim_noalloc(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
+                   int32_t* d_obj, uint8_t* d_inside, int filtered, void* stream);
 
 /* Ordered compaction of point results (replaces ResultProcessor::compactAndDownload,
  * query/src/raytracing/ResultProcessor.cpp:8-35): writes the ids of points with

@@ -21,6 +21,7 @@ RS_ERR_ITER_LIMIT = 5
 RS_ERR_FORMAT = 6
 RS_ERR_OOM = 7
 RS_ERR_TARGET_OVERFLOW = 8
+RS_ERR_TOO_LARGE = 9
 
 # Every entry point of include/rayspace3d.h: name -> (restype, argtypes).
 P = ctypes.c_void_p
@@ -39,6 +40,7 @@ SIGNATURES = {
     "rs_bvh_info": (I, [P, PU64, PU64, PU64, P, P]),
     "rs_pim": (I, [P, P, U64, F, F, F, P, P, P]),
     "rs_pim_filtered": (I, [P, P, U64, F, F, F, P, P, P]),
+    "rs_pim_noalloc": (I, [P, P, U64, F, F, F, P, P, I, P]),
     "rs_compact_hits": (I, [P, U64, P, P, U64, PU64, P]),
     "rs_pairset_create": (I, [U64, I, PP, P]),
     "rs_pairset_clear": (I, [P, P]),

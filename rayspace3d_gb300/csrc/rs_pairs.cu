@@ -216,6 +216,7 @@ extern "C" const char* rs_status_string(int status) {
         case RS_ERR_FORMAT: return "malformed input";
         case RS_ERR_OOM: return "out of device memory";
         case RS_ERR_TARGET_OVERFLOW: return "containment ray crossed too many distinct targets";
+        case RS_ERR_TOO_LARGE: return "input larger than the entry point's fixed capacity";
         default: return "unknown status";
     }
 }

@@ -601,7 +601,109 @@ __global__ void k_hit_scatter(const int32_t* __restrict__ obj, uint64_t n, const
 }  // namespace
 }  // namespace rs
 
+// ---------------------------------------------------------------------------
+// Point-in-mesh without device allocation.
+//
+// Callers that cannot allocate device memory on their query path -- code that runs
+// while another framework captures the stream into a CUDA graph, services with a
+// fixed device-memory budget whose allocator already owns the GPU, or real-time
+// loops where an allocation's implicit synchronisation is not acceptable -- use
+// rs_pim_noalloc.  Its per-call scratch (status word, overflow count, the twelve
+// filter-box triangles and the list of points with more than kHits crossings) lives
+// in the fixed array below instead of coming from an allocator.  Host code may not
+// use the array's name as a device address, so its address is looked up with
+// cudaGetSymbolAddress once per device (with that device current) and passed to
+// the kernels.
+// ---------------------------------------------------------------------------
+constexpr uint64_t kNoAllocMaxPoints = 1ull << 20;  // 1,048,576 points per call
+constexpr size_t kNoAllocMetaOffset = 0;            // u64 status, u64 overflow count
+constexpr size_t kNoAllocBoxOffset = 256;           // 108 floats
+constexpr size_t kNoAllocListOffset = 1024;         // u32 per point
+constexpr size_t kNoAllocBytes = kNoAllocListOffset + kNoAllocMaxPoints * sizeof(uint32_t);
+
+static __device__ __align__(256) unsigned char g_pim_scratch[kNoAllocBytes];
+
+namespace rs {
+namespace {
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[64] = {};
+
+// Device address of g_pim_scratch on the current device (looked up on first use).
+cudaError_t scratch_address(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_pim_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+}  // namespace rs
+
 using namespace rs;
+
+extern "C" int rs_pim_noalloc(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
+                              int32_t* d_obj, uint8_t* d_inside, int filtered, void* stream) {
+    if (!bvh || (n && !d_points)) return RS_ERR_INVALID;
+    if (n > kNoAllocMaxPoints) return RS_ERR_TOO_LARGE;
+    if (n == 0) return RS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (filtered && bvh->nV == 0) {
+        cudaError_t e = cudaSuccess;
+        if (d_obj) e = cudaMemsetAsync(d_obj, 0xff, n * sizeof(int32_t), s);
+        if (e == cudaSuccess && d_inside) e = cudaMemsetAsync(d_inside, 0, n, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        return to_status(e);
+    }
+    void* base = nullptr;
+    cudaError_t e = scratch_address(&base);
+    if (e != cudaSuccess) return to_status(e);
+    unsigned char* sc = static_cast<unsigned char*>(base);
+    unsigned long long* meta = reinterpret_cast<unsigned long long*>(sc + kNoAllocMetaOffset);
+    float* box = reinterpret_cast<float*>(sc + kNoAllocBoxOffset);
+    uint32_t* ovf = reinterpret_cast<uint32_t*>(sc + kNoAllocListOffset);
+    // The array keeps the previous call's contents: the status word and overflow count
+    // must start at zero (the list is written before it is read).
+    e = cudaMemsetAsync(meta, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return to_status(e);
+    if (filtered) {
+        const BoxMesh hbox = make_box(bvh);
+        e = cudaMemcpyAsync(box, &hbox, sizeof(BoxMesh), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return to_status(e);
+    }
+    unsigned int* status = reinterpret_cast<unsigned int*>(meta);
+    const bool zx = dx == 0.0f, zy = dy == 0.0f, zz = dz == 0.0f;
+    // The column grid is used when it already exists; it is never built here, because
+    // building it allocates.  Without it the BVH path gives the same results.
+    const bool f = filtered != 0;
+    if (dz == 1.0f && zx && zy) {
+        e = f ? launch_pim<2, true>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s)
+              : launch_pim<2, false>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s);
+    } else if (dx == 1.0f && zy && zz) {
+        e = f ? launch_pim<0, true>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s)
+              : launch_pim<0, false>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s);
+    } else if (dy == 1.0f && zx && zz) {
+        e = f ? launch_pim<1, true>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s)
+              : launch_pim<1, false>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s);
+    } else {
+        e = f ? launch_pim<-1, true>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s)
+              : launch_pim<-1, false>(bvh, d_points, n, dx, dy, dz, box, d_obj, d_inside, status, ovf, meta + 1, s);
+    }
+    unsigned long long hmeta[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hmeta, meta, sizeof(hmeta), cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    prof_collect();
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return to_status(e);
+    return status_from_bits((uint32_t)hmeta[0]);
+}
 
 extern "C" int rs_pim(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
                       int32_t* d_obj, uint8_t* d_inside, void* stream) {
