@@ -44,8 +44,7 @@ typedef struct rs_pairset rs_pairset; /* open-addressing table of (id1<<32 | id2
 /* 1. Engine entry points                                                      */
 /* ========================================================================== */
 
-/* Library version string and the size in bytes of the largest shared-memory
- * configuration it was compiled for (diagnostics). */
+/* Library version string (diagnostics). */
 const char* rs_version(void);
 
 /* Build a BVH over all triangles of one set.
@@ -126,6 +125,25 @@ int rs_edge_join(const rs_bvh* target, const float* d_starts, const float* d_end
 int rs_containment(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
                    const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj,
                    int swap, rs_pairset* ps, void* stream);
+
+/* Containment with the per-source diagnostics of raytracer_intersection_estimated
+ * (query/src/utilities/PairHitTracking.h:31-150, ContainmentTracking.h:22-120): for every
+ * source object o < capacity, d_candidate_counts[o] = number of distinct target objects the
+ * ray crossed, and d_target_ids/d_target_hits[o*max_targets + j] = the odd-parity targets
+ * (first-crossed order) and how many of their triangles the ray crossed; -1/0 where unused.
+ * RS_ERR_OUTPUT_OVERFLOW if the source set has more than `capacity` objects. */
+int rs_containment_tracked(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
+                           const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj,
+                           int swap, rs_pairset* ps, int max_targets, int32_t* d_target_ids,
+                           uint32_t* d_target_hits, uint32_t* d_candidate_counts, uint64_t capacity, void* stream);
+
+/* Query counters of a table (mesh_overlap_edges.cu:83-96 hash contention tracking and the
+ * profiling counters of mesh_intersection.h:7-22), collected while tracking is on:
+ * [0] slot accesses, [1] contended probes, [2] edge rays traced, [3] edge-ray crossings,
+ * [4] containment rays, [5] containment crossings, [6] distinct containment targets, [7] 0.
+ * Counters reset with rs_pairset_clear. */
+int rs_pairset_set_tracking(rs_pairset* ps, int on);
+int rs_pairset_counters(const rs_pairset* ps, uint64_t* h_out8, void* stream);
 
 /* Sorted unique keys of a table (replaces compact_hash_table_pairs + the sort/unique of
  * merge_and_deduplicate_pairs_gpu, query/src/cuda/mesh_query_deduplication.cu:56-144).

@@ -54,6 +54,7 @@ def lib():
         L.orc_orient.argtypes = [P, P, P, P]
         L.orc_perturbed_sign.argtypes = [P, P, P, P]
         L.orc_free.argtypes = [P]
+        L.orc_box_mesh.argtypes = [P, U64, P, P]
         _lib = L
     return _lib
 
@@ -146,3 +147,11 @@ def orient(d, o, a, b):
 def perturbed_sign(d, o, a, b):
     arrs = [_c(x, np.float32) for x in (d, o, a, b)]
     return lib().orc_perturbed_sign(*[_p(x) for x in arrs])
+
+
+def box_mesh(V):
+    V = _c(V, np.float32)
+    bv = np.empty((8, 3), np.float32)
+    bi = np.empty((12, 3), np.uint32)
+    lib().orc_box_mesh(_p(V), len(V), _p(bv), _p(bi))
+    return bv, bi

@@ -743,6 +743,16 @@ int orc_perturbed_sign(const float d[3], const float o[3], const float a[3], con
     return perturbed_sign(d, o, a, b, kx, ky);
 }
 
+void orc_box_mesh(const float* V, uint64_t nV, float* out_v, uint32_t* out_i) {
+    Mesh m{V, nV, nullptr, 0, nullptr};
+    std::vector<float> bv;
+    std::vector<uint32_t> bi;
+    std::vector<int32_t> bo;
+    box_mesh(m, bv, bi, bo);
+    std::memcpy(out_v, bv.data(), 24 * sizeof(float));
+    std::memcpy(out_i, bi.data(), 36 * sizeof(uint32_t));
+}
+
 void orc_free(void* p) { std::free(p); }
 
 }  // extern "C"

@@ -67,6 +67,10 @@ int64_t orc_estimate_pairs(const void* cellsA, const void* cellsB, uint64_t ncel
 int orc_orient(const float d[3], const float o[3], const float a[3], const float b[3]);
 int orc_perturbed_sign(const float d[3], const float o[3], const float a[3], const float b[3]);
 
+/* The 12-triangle bounding-box mesh of all vertices (BoundingBox.cpp:4-50):
+ * out_v float[24] (8 vertices), out_i uint32[36] (12 triangles). */
+void orc_box_mesh(const float* V, uint64_t nV, float* out_v, uint32_t* out_i);
+
 void orc_free(void* p);
 
 #ifdef __cplusplus

@@ -7,10 +7,13 @@
 //   points  <in.txt> <out.bin>   loadPointDataset (query/src/runtime/PointIO.cpp:32-92)
 //   box     <in.bin> <out.bin>   BoundingBox::computeFromGeometry + createBoxMesh (geometry/BoundingBox.cpp:4-50)
 //   timer   <out.json>           PerformanceTimer::writeResultsToFile (query/src/timer.cpp:124-192)
+//   grid    <in.bin> <out.bin> <resolution> <worldSize>
+//                                generateGridStats (preprocess/src/preprocess_dataset.cpp:37-181)
 // in.bin layout: u64 nV, u64 nF, float V[nV*3], u32 I[nF*3], i32 T[nF], u8 hasGrid,
 //   [grid: f32 min[3], f32 max[3], u32 res[3], cells 16 B each].
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <string>
@@ -21,6 +24,8 @@
 #include "EdgePreprocessor.h"
 #include "PointIO.h"
 #include "timer.h"
+
+void generateGridStats(GeometryData& geometry, GridData& grid, int resolution, float worldSize);
 
 static std::vector<char> slurp(const char* p) {
     std::ifstream f(p, std::ios::binary);
@@ -115,6 +120,18 @@ int main(int argc, char** argv) {
         put(o, m.vertices);
         put(o, m.indices);
         put(o, m.triangleToObject);
+        return 0;
+    }
+    if (mode == "grid" && argc == 6) {
+        GeometryData g = read_in(argv[2]);
+        generateGridStats(g, g.grid, std::atoi(argv[4]), (float)std::atof(argv[5]));
+        std::ofstream o(argv[3], std::ios::binary);
+        const float b[6] = {g.grid.minBound.x, g.grid.minBound.y, g.grid.minBound.z,
+                            g.grid.maxBound.x, g.grid.maxBound.y, g.grid.maxBound.z};
+        const uint32_t r[3] = {g.grid.resolution.x, g.grid.resolution.y, g.grid.resolution.z};
+        o.write((const char*)b, sizeof b);
+        o.write((const char*)r, sizeof r);
+        put(o, g.grid.cells);
         return 0;
     }
     if (mode == "timer" && argc == 3) {

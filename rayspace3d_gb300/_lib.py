@@ -49,6 +49,9 @@ SIGNATURES = {
     "rs_edge_join": (I, [P, P, P, P, P, P, U64, I, P, P]),
     "rs_containment": (I, [P, P, U64, P, U64, P, I, P, P]),
     "rs_pairset_finalize": (I, [P, I, P, U64, PU64, P]),
+    "rs_containment_tracked": (I, [P, P, U64, P, U64, P, I, P, I, P, P, P, U64, P]),
+    "rs_pairset_set_tracking": (I, [P, I]),
+    "rs_pairset_counters": (I, [P, PU64, P]),
     "rs_estimate_grid": (I, [P, P, U64, F, F, F, ctypes.POINTER(ctypes.c_double), P, P]),
     "rs_estimate_pairs_from_raw": (I64, [ctypes.c_double, P, F, I]),
     "rs_hash_size_pow2": (U64, [I64]),

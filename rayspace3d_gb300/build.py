@@ -80,14 +80,14 @@ def build_lib(jobs: int = 8) -> str:
 
 def build_cli(jobs: int = 8) -> List[str]:
     """Drop-in executables (C++ host code over librs.so)."""
-    srcs_common = sorted(glob.glob(os.path.join(HOST, "common", "*.cpp")))
     if not os.path.isdir(HOST):
         return []
+    srcs_common = sorted(glob.glob(os.path.join(HOST, "common", "*.cpp")))
     os.makedirs(BIN, exist_ok=True)
     os.makedirs(os.path.join(BUILD, "host"), exist_ok=True)
     inc = ["-I", os.path.join(cuda_home(), "include"), "-I", HOST]
     headers = sorted(glob.glob(os.path.join(HOST, "**", "*.h"), recursive=True)) + [
-        os.path.join(ROOT, "include", "rayspace3d.h")]
+        os.path.join(ROOT, "include", "rayspace3d.h"), os.path.join(HOST, "apps", "raytracer_overlap_estimated.cpp")]
     objs = []
     cmds = []
     for src in srcs_common:

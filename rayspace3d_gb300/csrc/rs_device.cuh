@@ -372,12 +372,14 @@ struct PairTable {
     unsigned int max_probes;
     unsigned int* status;         // OR of ST_* bits
     unsigned long long* count;    // number of distinct keys inserted
+    unsigned long long* stats;    // nullable: [0] slot accesses, [1] contended probes (--track-hash-contention)
 };
 
 __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long long key) {
     const unsigned long long h = fmix64(key);
     unsigned long long slot = t.pow2 ? (h & (t.capacity - 1)) : (h % t.capacity);
     for (unsigned int i = 0; i < t.max_probes; ++i) {
+        if (t.stats) atomicAdd(&t.stats[0], 1ull);
         unsigned long long cur = t.slots[slot];
         if (cur == key) return;
         if (cur == kEmptyKey) {
@@ -388,6 +390,7 @@ __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long l
             }
             if (old == key) return;
         }
+        if (t.stats) atomicAdd(&t.stats[1], 1ull);
         slot = slot + 1;
         if (slot == t.capacity) slot = 0;
     }

@@ -43,12 +43,15 @@ struct rs_pairset {
     unsigned long long capacity = 0;
     int pow2 = 1;
     unsigned int max_probes = 4096;
-    // Device scratch: [0] status bits (u32 in the low word), [1] distinct-key count.
+    // Device scratch: [0] status bits (u32 in the low word), [1] distinct-key count,
+    // [2] slot accesses, [3] contended probes, [4..8] query counters (see rs_pairset_counters).
     unsigned long long* meta = nullptr;
+    int track = 0;  // count slot accesses and contention
     int device = 0;
 };
 
 namespace rs {
+constexpr int kMetaWords = 16;
 // Upper bound on the node visits of one traversal of a valid tree.
 inline uint32_t max_steps(const rs_bvh* b) { return (uint32_t)(2 * b->n_nodes + 8); }
 int to_status(cudaError_t e);

@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
     const int32_t* src = sources + offsets[i];
     int32_t last[4] = {INT_MIN, INT_MIN, INT_MIN, INT_MIN};
     int lp = 0;
+    unsigned int crossings = 0;
     const bool ok = traverse<-1>(nodes, max_steps, r, [&](int first, int cnt) {
         for (int k = first; k < first + cnt; ++k) {
             float a[3], b[3], c[3];
@@ -48,6 +49,7 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
             load_tri(tris, k, a, b, c, tid, obj);
             float t;
             if (!hit_triangle<-1>(r, a, b, c, t)) continue;
+            ++crossings;
             if (obj == last[0] || obj == last[1] || obj == last[2] || obj == last[3]) continue;
             last[lp] = obj;
             lp = (lp + 1) & 3;
@@ -60,6 +62,10 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
         }
     });
     if (!ok) atomicOr(table.status, ST_STACK_OVERFLOW);
+    if (table.stats) {
+        atomicAdd(&table.stats[2], 1ull);
+        if (crossings) atomicAdd(&table.stats[3], (unsigned long long)crossings);
+    }
 }
 
 __global__ void k_first_tri_init(int32_t* __restrict__ first, uint64_t nObj) {
@@ -83,13 +89,33 @@ __global__ void k_max_obj(const int32_t* __restrict__ t2o, uint64_t nF, int* __r
     if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
 }
 
+// Optional per-source outputs of the containment pass (the reference's pair-hit and
+// containment-tracking buffers, query/src/utilities/PairHitTracking.h,
+// ContainmentTracking.h): distinct targets crossed, and the odd-parity targets with
+// their crossing counts in first-crossed order.
+struct Tracking {
+    int max_targets;
+    int32_t* target_ids;      // [nObj * max_targets], -1 where unused
+    uint32_t* target_hits;    // [nObj * max_targets]
+    uint32_t* candidates;     // [nObj]
+};
+
+template <bool TRACK>
 __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V, uint64_t nV,
                                                     const uint32_t* __restrict__ I,
                                                     const int32_t* __restrict__ first, uint64_t nObj,
                                                     const BNode* __restrict__ nodes, uint32_t max_steps,
-                                                    const float4* __restrict__ tris, int swap, PairTable table) {
+                                                    const float4* __restrict__ tris, int swap, PairTable table,
+                                                    Tracking trk) {
     const uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (o >= nObj) return;
+    if (TRACK) {
+        trk.candidates[o] = 0;
+        for (int q = 0; q < trk.max_targets; ++q) {
+            trk.target_ids[o * trk.max_targets + q] = -1;
+            trk.target_hits[o * trk.max_targets + q] = 0;
+        }
+    }
     const int32_t ft = first[o];
     if (ft == INT_MAX) return;
     const uint32_t vi = I[3 * (uint64_t)ft];
@@ -97,9 +123,11 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
     const Ray r = make_ray(V[3 * (uint64_t)vi], V[3 * (uint64_t)vi + 1], V[3 * (uint64_t)vi + 2], 0.0f, 0.0f, 1.0f,
                            1e-4f, 1e10f);
     int32_t tgt[kTargets];
+    uint32_t hits[TRACK ? kTargets : 1];
     uint32_t par = 0;  // parity bit per list entry
     int nt = 0;
     bool ovf = false;
+    unsigned int crossings = 0;
     const bool ok = traverse<2>(nodes, max_steps, r, [&](int f, int cnt) {
         for (int k = f; k < f + cnt; ++k) {
             float a[3], b[3], c[3];
@@ -108,13 +136,16 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
             load_tri(tris, k, a, b, c, tid, obj);
             float t;
             if (!hit_triangle<2>(r, a, b, c, t)) continue;
+            ++crossings;
             int j = 0;
             for (; j < nt; ++j)
                 if (tgt[j] == obj) break;
             if (j < nt) {
                 par ^= 1u << j;
+                if (TRACK) ++hits[j];
             } else if (nt < kTargets) {
                 tgt[nt] = obj;
+                if (TRACK) hits[nt] = 1;
                 par |= 1u << nt;
                 ++nt;
             } else {
@@ -130,12 +161,24 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
         atomicOr(table.status, ST_TARGET_OVERFLOW);
         return;
     }
+    if (table.stats) {
+        atomicAdd(&table.stats[4], 1ull);
+        if (crossings) atomicAdd(&table.stats[5], (unsigned long long)crossings);
+        if (nt) atomicAdd(&table.stats[6], (unsigned long long)nt);
+    }
+    int out = 0;
     for (int j = 0; j < nt; ++j) {
         if (!((par >> j) & 1u)) continue;
         const unsigned long long key = swap ? (((unsigned long long)(uint32_t)tgt[j] << 32) | (uint32_t)o)
                                             : (((unsigned long long)(uint32_t)o << 32) | (uint32_t)tgt[j]);
         table_insert(table, key);
+        if (TRACK && out < trk.max_targets) {
+            trk.target_ids[o * trk.max_targets + out] = tgt[j];
+            trk.target_hits[o * trk.max_targets + out] = hits[j];
+            ++out;
+        }
     }
+    if (TRACK) trk.candidates[o] = (uint32_t)nt;
 }
 
 }  // namespace
@@ -148,6 +191,7 @@ PairTable table_view(rs_pairset* ps) {
     t.max_probes = ps->max_probes;
     t.status = reinterpret_cast<unsigned int*>(ps->meta);
     t.count = ps->meta + 1;
+    t.stats = ps->track ? ps->meta + 2 : nullptr;
     return t;
 }
 
@@ -191,11 +235,10 @@ extern "C" int rs_edge_join(const rs_bvh* target, const float* d_starts, const f
     return table_status(ps, s, e);
 }
 
-extern "C" int rs_containment(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
-                              const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj,
-                              int swap, rs_pairset* ps, void* stream) {
+static int containment_impl(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
+                            const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj, int swap,
+                            rs_pairset* ps, const Tracking* trk, uint64_t trk_capacity, cudaStream_t s) {
     if (!target || !ps || (src_nF && (!d_src_vertices || !d_src_indices || !d_src_tri2obj))) return RS_ERR_INVALID;
-    cudaStream_t s = (cudaStream_t)stream;
     if (src_nF == 0 || target->n_tris == 0) return RS_OK;
     int* dmx = nullptr;
     int32_t* first = nullptr;
@@ -210,26 +253,49 @@ extern "C" int rs_containment(const rs_bvh* target, const float* d_src_vertices,
     // Objects 0..max id (the reference sizes its launch by the number of distinct ids,
     // which is the same for the contiguous ids preprocess_dataset writes).
     const uint64_t nObj = hmx >= 0 ? (uint64_t)hmx + 1 : 0;
+    if (trk && nObj > trk_capacity) {
+        if (dmx) cudaFreeAsync(dmx, s);
+        cudaStreamSynchronize(s);
+        return RS_ERR_OUTPUT_OVERFLOW;
+    }
     if (e == cudaSuccess && nObj) {
         e = dmalloc((void**)&first, nObj * sizeof(int32_t), s);
         if (e == cudaSuccess) {
             launch(k_first_tri_init, (unsigned)((nObj + 255) / 256), 256, 0, s, first, nObj);
             launch(k_first_tri, (unsigned)((src_nF + 255) / 256), 256, 0, s, d_src_tri2obj, src_nF, first, nObj);
+            const unsigned grid = (unsigned)((nObj + kT - 1) / kT);
             prof_begin(P_CONTAINMENT, s);
-            launch(k_containment, (unsigned)((nObj + kT - 1) / kT), kT, 0, s, d_src_vertices, src_nV, d_src_indices, first,
-                                                                        nObj, target->nodes, max_steps(target), target->tris, swap,
-                                                                        table_view(ps));
+            if (trk)
+                launch(k_containment<true>, grid, kT, 0, s, d_src_vertices, src_nV, d_src_indices, (const int32_t*)first,
+                       nObj, (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap,
+                       table_view(ps), *trk);
+            else
+                launch(k_containment<false>, grid, kT, 0, s, d_src_vertices, src_nV, d_src_indices, (const int32_t*)first,
+                       nObj, (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap,
+                       table_view(ps), Tracking{0, nullptr, nullptr, nullptr});
             prof_end(P_CONTAINMENT, s);
             e = cudaGetLastError();
         }
     }
-    unsigned long long st = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ps->meta, sizeof(st), cudaMemcpyDeviceToHost, s);
     if (dmx) cudaFreeAsync(dmx, s);
     if (first) cudaFreeAsync(first, s);
-    cudaError_t e2 = cudaStreamSynchronize(s);
-    prof_collect();
-    if (e == cudaSuccess) e = e2;
-    if (e != cudaSuccess) return to_status(e);
-    return status_from_bits((uint32_t)st);
+    return table_status(ps, s, e);
+}
+
+extern "C" int rs_containment(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
+                              const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj,
+                              int swap, rs_pairset* ps, void* stream) {
+    return containment_impl(target, d_src_vertices, src_nV, d_src_indices, src_nF, d_src_tri2obj, swap, ps, nullptr,
+                            0, (cudaStream_t)stream);
+}
+
+extern "C" int rs_containment_tracked(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
+                                      const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj,
+                                      int swap, rs_pairset* ps, int max_targets, int32_t* d_target_ids,
+                                      uint32_t* d_target_hits, uint32_t* d_candidate_counts, uint64_t capacity,
+                                      void* stream) {
+    if (max_targets <= 0 || !d_target_ids || !d_target_hits || !d_candidate_counts) return RS_ERR_INVALID;
+    const Tracking trk{max_targets, d_target_ids, d_target_hits, d_candidate_counts};
+    return containment_impl(target, d_src_vertices, src_nV, d_src_indices, src_nF, d_src_tri2obj, swap, ps, &trk,
+                            capacity, (cudaStream_t)stream);
 }

@@ -84,7 +84,7 @@ extern "C" int rs_pairset_create(uint64_t capacity, int pow2, rs_pairset** out, 
     cudaGetDevice(&ps->device);
     ps->pow2 = pow2 ? 1 : 0;
     if (ps->pow2) capacity = next_pow2(capacity);
-    cudaError_t e = dmalloc((void**)&ps->meta, 2 * sizeof(unsigned long long), s);
+    cudaError_t e = dmalloc((void**)&ps->meta, kMetaWords * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = alloc_slots(ps, capacity, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -101,7 +101,7 @@ extern "C" int rs_pairset_clear(rs_pairset* ps, void* stream) {
     if (!ps) return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, 2 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     return to_status(e);
 }
@@ -184,7 +184,7 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
         // overlap B->A, containment A->B, containment B->A.  The two edge directions are queued
         // back to back and checked with one status read.
         cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, 2 * sizeof(unsigned long long), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
         if (e == cudaSuccess && a2b)
             e = edge_join_async(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s);
         if (e == cudaSuccess && b2a)
@@ -203,6 +203,23 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
         if (e != cudaSuccess) return to_status(e);
     }
     return RS_ERR_TABLE_FULL;
+}
+
+extern "C" int rs_pairset_set_tracking(rs_pairset* ps, int on) {
+    if (!ps) return RS_ERR_INVALID;
+    ps->track = on != 0;
+    return RS_OK;
+}
+
+extern "C" int rs_pairset_counters(const rs_pairset* ps, uint64_t* h_out8, void* stream) {
+    if (!ps || !h_out8) return RS_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long m[kMetaWords];
+    cudaError_t e = cudaMemcpyAsync(m, ps->meta, sizeof(m), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return to_status(e);
+    for (int k = 0; k < 8; ++k) h_out8[k] = m[2 + k];
+    return RS_OK;
 }
 
 extern "C" const char* rs_status_string(int status) {

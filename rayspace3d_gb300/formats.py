@@ -6,7 +6,7 @@
 * WKT / bare ``x y z`` point files (``query/src/runtime/PointIO.cpp:32-92``).
 * The phase-timing JSON (``query/src/timer.cpp:124-192``).
 
-The C++ executables carry their own reader (``rayspace3d_gb300/host/pre_io.cpp``); this
+The C++ executables carry their own reader (``rayspace3d_gb300/host/common/cli_common.cpp``); this
 module is the Python-side equivalent used by the Python API, the synthetic generator,
 the tests and the benchmark.
 """

@@ -11,8 +11,10 @@ benchmark and the tests can build the same kinds of inputs on any machine:
   ``llround(x*1e5)``, key = ordered pair of quantised endpoints in ``std::map`` order,
   endpoints taken from the first occurrence, source objects in first-seen order;
 * grid statistics, restating ``generateGridStats``
-  (``preprocess/src/preprocess_dataset.cpp:37-179``) with objects visited in ascending
-  id order (the reference visits an ``unordered_map``, whose order is unspecified).
+  (``preprocess/src/preprocess_dataset.cpp:37-181``).  The reference visits its objects
+  in the iteration order of a ``std::unordered_map<int, ObjectStats>`` and sums floats
+  per cell in that order; ``unordered_map_order`` reproduces GCC libstdc++'s order, so
+  the per-cell means match the reference built with GCC bit for bit.
 """
 from __future__ import annotations
 
@@ -181,6 +183,60 @@ def extract_edges(V: np.ndarray, I: np.ndarray, T: np.ndarray) -> Edges:
                  counts, sources)
 
 
+# Bucket counts a libstdc++ std::unordered_map<int, V> passes through when keys are inserted
+# one at a time (max_load_factor 1): the table rehashes when the (count+1)-th key arrives.
+_UMAP_BUCKETS = (13, 29, 59, 127, 257, 541, 1109, 2357, 5087, 10273, 20753, 42043, 85229, 172933, 351061,
+                 712697, 1447153, 2938679, 5967347, 12117689, 24607243, 49969847)
+
+
+def unordered_map_order(keys) -> List[int]:
+    """Iteration order of a GCC ``std::unordered_map<int, V>`` after ``m[k]`` for each key
+    in turn (repeated keys ignored).  Model: one singly linked node list; a key whose
+    bucket is empty goes to the front of the list, otherwise to the front of its bucket's
+    run; a rehash walks the list front to back and re-inserts by the same rule, which
+    reverses the runs.  std::hash<int> is the identity (sign-extended to 64 bits)."""
+    BB = "head"
+    nxt = {BB: None}
+    buckets = {}          # bucket -> node before the bucket's first node
+    nb = 1
+    growth = iter(_UMAP_BUCKETS)
+    count = 0
+    for k in keys:
+        k = int(k)
+        if k in nxt:
+            continue
+        if count + 1 > (nb if count else 0):
+            try:
+                nb = next(growth)
+            except StopIteration:
+                raise ValueError("too many objects for the unordered_map order model") from None
+            p, nxt[BB], buckets, before = nxt[BB], None, {}, None
+            while p is not None:
+                after, b = nxt[p], (p & 0xFFFFFFFFFFFFFFFF) % nb
+                if b not in buckets:
+                    nxt[p], nxt[BB], buckets[b] = nxt[BB], p, BB
+                    if nxt[p] is not None:
+                        buckets[before] = p
+                    before = b
+                else:
+                    nxt[p], nxt[buckets[b]] = nxt[buckets[b]], p
+                p = after
+        b = (k & 0xFFFFFFFFFFFFFFFF) % nb
+        if b in buckets:
+            nxt[k], nxt[buckets[b]] = nxt[buckets[b]], k
+        else:
+            nxt[k], nxt[BB] = nxt[BB], k
+            if nxt[k] is not None:
+                buckets[(nxt[k] & 0xFFFFFFFFFFFFFFFF) % nb] = k
+            buckets[b] = BB
+        count += 1
+    out, p = [], nxt[BB]
+    while p is not None:
+        out.append(p)
+        p = nxt[p]
+    return out
+
+
 def grid_stats(V: np.ndarray, I: np.ndarray, T: np.ndarray, resolution: int = 128,
                world_size: float = -1.0) -> Grid:
     """Per-cell statistics as generateGridStats computes them (float32 arithmetic)."""
@@ -205,7 +261,7 @@ def grid_stats(V: np.ndarray, I: np.ndarray, T: np.ndarray, resolution: int = 12
     T = T[valid]
     if len(I) == 0:
         return Grid(mn, mx, np.array([R, R, R], np.uint32), cells)
-    objs, tinv = np.unique(T, return_inverse=True)
+    objs, first, tinv = np.unique(T, return_index=True, return_inverse=True)
     nobj = len(objs)
     v0, v1, v2 = V[I[:, 0]], V[I[:, 1]], V[I[:, 2]]
     tmin = np.minimum(np.minimum(v0, v1), v2)
@@ -241,7 +297,8 @@ def grid_stats(V: np.ndarray, I: np.ndarray, T: np.ndarray, resolution: int = 12
     touch = np.zeros(R * R * R, np.uint32)
     asum = np.zeros(R * R * R, np.float32)
     rsum = np.zeros(R * R * R, np.float32)
-    for o in range(nobj):   # ascending object id; float32 accumulation per cell
+    visit = np.searchsorted(objs, unordered_map_order(objs[np.argsort(first, kind="stable")]))
+    for o in visit:         # the reference's object order; float32 accumulation per cell
         x0, y0, z0 = lo[o]
         x1, y1, z1 = hi[o]
         if x1 < x0 or y1 < y0 or z1 < z0:

@@ -1,0 +1,353 @@
+"""CPU tests against the golden fixtures (no GPU).
+
+* Restatements of the reference's host code -- edge extraction, grid statistics, the
+  ``.pre`` writer/reader, the point parser, the timing JSON -- against outputs of the
+  reference's own code (tests/golden/make_golden.py, oracle/_ref/ref_driver).
+* The CPU oracle: its box mesh against the reference's, its answers against the
+  committed fixtures, brute force against its BVH, its exact predicates against
+  rational arithmetic, and watertightness on shared edges and vertices.
+* The drop-in executables' argument handling (no device work).
+"""
+import json
+import os
+import subprocess
+import textwrap
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from oracle import bind
+from rayspace3d_gb300 import build, formats, synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(os.path.join(GOLD, "golden.npz"))
+
+
+@pytest.fixture(scope="module")
+def meta():
+    with open(os.path.join(GOLD, "golden_meta.json")) as f:
+        return json.load(f)
+
+
+# ----------------------------------------------------------------- reference host code
+
+@pytest.mark.parametrize("case", ["cube_grid", "spheres", "soup"])
+def test_extract_edges_matches_reference(golden, case):
+    """EdgePreprocessor::extractEdges (preprocess/src/EdgePreprocessor.cpp:41-119)."""
+    p = f"edges_{case}_"
+    e = synth.extract_edges(golden[p + "V"], golden[p + "I"], golden[p + "T"])
+    np.testing.assert_array_equal(e.starts.view(np.uint32), golden[p + "starts"].view(np.uint32))
+    np.testing.assert_array_equal(e.ends.view(np.uint32), golden[p + "ends"].view(np.uint32))
+    np.testing.assert_array_equal(e.offsets, golden[p + "offsets"])
+    np.testing.assert_array_equal(e.counts, golden[p + "counts"])
+    np.testing.assert_array_equal(e.sources, golden[p + "sources"])
+
+
+@pytest.mark.parametrize("case", ["fixed", "auto", "outside"])
+def test_grid_stats_matches_reference(golden, case):
+    """generateGridStats (preprocess/src/preprocess_dataset.cpp:37-181), bit for bit,
+    including the per-cell float sums in the reference's object order."""
+    p = f"grid_{case}_"
+    res, world = golden[p + "params"]
+    g = synth.grid_stats(golden[p + "V"], golden[p + "I"], golden[p + "T"], int(res), float(world))
+    np.testing.assert_array_equal(np.concatenate([g.min_bound, g.max_bound]).view(np.uint32),
+                                  golden[p + "bounds"].view(np.uint32))
+    np.testing.assert_array_equal(g.resolution, golden[p + "res"])
+    assert g.cells.tobytes() == golden[p + "cells"].tobytes()
+
+
+_UMAP_PROBE = textwrap.dedent("""
+    #include <cstdio>
+    #include <unordered_map>
+    int main() {
+        std::unordered_map<int, int> m;
+        int k;
+        while (std::scanf("%d", &k) == 1) m[k];
+        for (auto& kv : m) std::printf("%d ", kv.first);
+        std::printf("\\n");
+    }
+""")
+
+
+def test_unordered_map_order_model(tmp_path):
+    """The object-order model against a real GCC std::unordered_map<int, V>."""
+    src = tmp_path / "probe.cpp"
+    exe = tmp_path / "probe"
+    src.write_text(_UMAP_PROBE)
+    try:
+        subprocess.run(["g++", "-O1", "-o", str(exe), str(src)], check=True, capture_output=True)
+    except (OSError, subprocess.CalledProcessError):
+        pytest.skip("g++ is not available")
+    rng = np.random.default_rng(7)
+    cases = [list(range(1)), list(range(14)), list(range(600)), list(rng.permutation(3000)),
+             list(rng.integers(-100000, 100000, size=800)), list(rng.integers(0, 50, size=400) * 29)]
+    for keys in cases:
+        keys = [int(k) for k in keys]
+        out = subprocess.run([str(exe)], input=" ".join(map(str, keys)), capture_output=True, text=True,
+                             check=True).stdout.split()
+        assert [int(x) for x in out] == synth.unordered_map_order(keys)
+
+
+def _small_geometry():
+    A, _ = synth.overlap_workload(n_objects=6, level=1, world=10.0, seed=4, grid_resolution=4)
+    return A
+
+
+def test_write_pre_matches_reference_writer(tmp_path):
+    """RaySpace::IO::writeBinaryFile (common/include/BinaryIO.h:35-102).  Bytes 58-63 are
+    struct padding that the reference leaves uninitialised; the writer here zeroes them."""
+    ours = tmp_path / "ours.pre"
+    formats.write_pre(str(ours), _small_geometry())
+    a = bytearray(ours.read_bytes())
+    b = bytearray(open(os.path.join(GOLD, "ref_small.pre"), "rb").read())
+    assert len(a) == len(b)
+    assert a[58:64] == b"\0" * 6
+    a[58:64] = b[58:64]
+    assert a == b
+
+
+def test_read_pre_of_reference_file():
+    g = formats.read_pre(os.path.join(GOLD, "ref_small.pre"))
+    A = _small_geometry()
+    np.testing.assert_array_equal(g.vertices, A.vertices)
+    np.testing.assert_array_equal(g.indices, A.indices)
+    np.testing.assert_array_equal(g.tri2obj, A.tri2obj)
+    assert g.total_triangles == len(A.indices)
+    for f in ("starts", "ends", "offsets", "counts", "sources"):
+        np.testing.assert_array_equal(getattr(g.edges, f), getattr(A.edges, f))
+    assert g.grid.cells.tobytes() == A.grid.cells.tobytes()
+    np.testing.assert_array_equal(g.grid.resolution, [4, 4, 4])
+
+
+def test_read_pre_version1_and_errors(tmp_path):
+    """Version-1 layout (48-byte header, no edges) and the error cases of the reader
+    (BinaryIO.h:104-180: bad magic, unknown version, truncated payload)."""
+    import struct
+    V = np.arange(12, dtype=np.float32).reshape(4, 3)
+    I = np.array([[0, 1, 2], [1, 2, 3]], np.uint32)
+    T = np.array([0, 0], np.int32)
+    p = tmp_path / "v1.pre"
+    p.write_bytes(struct.pack("<IIQQQQB7x", formats.PRE_MAGIC, 1, 4, 2, 2, 2, 0) + V.tobytes() + I.tobytes() +
+                  T.tobytes())
+    g = formats.read_pre(str(p))
+    np.testing.assert_array_equal(g.vertices, V)
+    np.testing.assert_array_equal(g.indices, I)
+    assert g.edges is None and g.grid is None
+    good = open(os.path.join(GOLD, "ref_small.pre"), "rb").read()
+    for name, data in [("magic", b"XXXX" + good[4:]), ("version", good[:4] + struct.pack("<I", 7) + good[8:]),
+                       ("truncated", good[:-100]), ("header", good[:20])]:
+        q = tmp_path / f"bad_{name}.pre"
+        q.write_bytes(data)
+        with pytest.raises(formats.PreFormatError):
+            formats.read_pre(str(q))
+
+
+def test_read_points_matches_reference_parser(golden):
+    """loadPointDataset (query/src/runtime/PointIO.cpp:32-92) on a file with comments, blank
+    lines, POINT and POINT Z forms, bare coordinates and a non-point line."""
+    pts = formats.read_points(os.path.join(GOLD, "points.wkt"))
+    np.testing.assert_array_equal(pts.view(np.uint32), golden["points"].view(np.uint32))
+
+
+def test_write_points_roundtrip(tmp_path):
+    rng = np.random.default_rng(2)
+    pts = (rng.standard_normal((500, 3)) * 10.0 ** rng.integers(-6, 6, size=(500, 1))).astype(np.float32)
+    p = tmp_path / "p.wkt"
+    formats.write_points_wkt(str(p), pts)
+    np.testing.assert_array_equal(formats.read_points(str(p)).view(np.uint32), pts.view(np.uint32))
+
+
+def test_timing_json_matches_reference_writer():
+    """PerformanceTimer::writeResultsToFile (query/src/timer.cpp:124-192): key naming,
+    occurrence suffixes, two-decimal milliseconds, counters, total."""
+    text = open(os.path.join(GOLD, "timer_reference.json")).read()
+    ref = json.loads(text)
+    ph = ref["phases"]
+    phases = [("Data Reading", ph["data reading_1"]["duration_us"]), ("Query", ph["query_1"]["duration_us"]),
+              ("Raytrace_Mesh1ToMesh2_Pass1", 1234), ("Raytrace_Mesh1ToMesh2_Pass1", 5),
+              ("compact_hash_table_pairs", 987654)]
+    counters = {"Profile_Actual_Intersection_Pairs": 42, "Profile_Overlap_Hits_Total": 2 ** 64 - 1}
+    assert formats.timing_json(phases, counters, ref["total"]["duration_us"]) == text
+
+
+# ----------------------------------------------------------------------------- oracle
+
+def test_oracle_box_mesh_matches_reference(golden):
+    """BoundingBox::computeFromGeometry + createBoxMesh (query/src/geometry/BoundingBox.cpp:4-50)."""
+    bv, bi = bind.box_mesh(golden["box_V_in"])
+    np.testing.assert_array_equal(bv.view(np.uint32), golden["box_vertices"].view(np.uint32))
+    np.testing.assert_array_equal(bi, golden["box_indices"])
+
+
+def test_oracle_reproduces_golden_answers(golden, meta):
+    g = golden
+    np.testing.assert_array_equal(bind.pim(g["pim_V"], g["pim_I"], g["pim_T"], g["pim_pts"]), g["pim_z"])
+    np.testing.assert_array_equal(bind.pim(g["pim_V"], g["pim_I"], g["pim_T"], g["pim_pts"], direction=(1, 0, 0)),
+                                  g["pim_x"])
+    np.testing.assert_array_equal(bind.pim(g["pim_V"], g["pim_I"], g["pim_T"], g["pim_pts"], filtered=True),
+                                  g["pim_filtered"])
+    np.testing.assert_array_equal(bind.pim(g["cubes_V"], g["cubes_I"], g["cubes_T"], g["cubes_pts"]), g["cubes_z"])
+    A = formats.read_pre(os.path.join(GOLD, "join_A.pre"))
+    B = formats.read_pre(os.path.join(GOLD, "join_B.pre"))
+    np.testing.assert_array_equal(bind.overlap_join(A, B), g["join_overlap"])
+    np.testing.assert_array_equal(bind.intersection_join(A, B), g["join_intersection"])
+    est, raw = bind.estimate_pairs(A.grid, B.grid)
+    assert est == meta["join_estimate"] and raw == meta["join_estimate_raw"]
+    # sanity of the fixture itself: a sphere level-3 inside fraction near 4/3 pi / 27
+    frac = float((g["pim_z"] >= 0).mean())
+    assert abs(frac - 4.18879 / 27.0) < 0.02
+    assert len(g["join_overlap"]) > 0 and len(g["join_intersection"]) >= len(g["join_overlap"])
+
+
+def test_oracle_bvh_equals_brute_force(golden):
+    g = golden
+    pts = g["cubes_pts"][:800]
+    for d in [(0, 0, 1), (0, 0, -1), (1, 0, 0), (0, -1, 0), (0.3, -0.2, 0.9)]:
+        a = bind.pim(g["cubes_V"], g["cubes_I"], g["cubes_T"], pts, direction=d)
+        b = bind.pim(g["cubes_V"], g["cubes_I"], g["cubes_T"], pts, direction=d, use_bvh=False)
+        np.testing.assert_array_equal(a, b)
+    A = formats.read_pre(os.path.join(GOLD, "join_A.pre"))
+    B = formats.read_pre(os.path.join(GOLD, "join_B.pre"))
+    np.testing.assert_array_equal(bind.edge_join(A.edges, B.vertices, B.indices, B.tri2obj),
+                                  bind.edge_join(A.edges, B.vertices, B.indices, B.tri2obj, use_bvh=False))
+    np.testing.assert_array_equal(bind.containment(B, A.vertices, A.indices, A.tri2obj, swap=True),
+                                  bind.containment(B, A.vertices, A.indices, A.tri2obj, swap=True, use_bvh=False))
+
+
+def _det3(u, v, w):
+    return (u[0] * (v[1] * w[2] - v[2] * w[1]) - u[1] * (v[0] * w[2] - v[2] * w[0]) +
+            u[2] * (v[0] * w[1] - v[1] * w[0]))
+
+
+def _sign(x):
+    return (x > 0) - (x < 0)
+
+
+def test_orient_exact_against_rationals():
+    """orc_orient = sign det[d, a-o, b-o] evaluated exactly (float inputs as rationals)."""
+    rng = np.random.default_rng(13)
+    cases = []
+    for _ in range(400):
+        d, o, a = rng.standard_normal((3, 3)).astype(np.float32)
+        kind = rng.integers(0, 4)
+        if kind == 0:
+            b = rng.standard_normal(3).astype(np.float32)
+        elif kind == 1:      # b on the plane through o spanned by d and a-o (rounded to float)
+            s, t = rng.standard_normal(2)
+            b = (o.astype(np.float64) + s * d + t * (a.astype(np.float64) - o)).astype(np.float32)
+        elif kind == 2:      # tiny and huge magnitudes
+            sc = np.float32(10.0 ** rng.integers(-30, 30))
+            d, o, a, b = [(x * sc).astype(np.float32) for x in rng.standard_normal((4, 3))]
+        else:                # integer grid: many exact zeros
+            d, o, a, b = [rng.integers(-2, 3, size=3).astype(np.float32) for _ in range(4)]
+        cases.append((d, o, a, b))
+    for d, o, a, b in cases:
+        F = [[Fraction(float(x)) for x in v] for v in (d, o, a, b)]
+        dd, oo, aa, bb = F
+        ex = _det3(dd, [aa[k] - oo[k] for k in range(3)], [bb[k] - oo[k] for k in range(3)])
+        assert bind.orient(d, o, a, b) == _sign(ex)
+
+
+def test_perturbed_sign_rules():
+    """The symbolic tie-break: the sign of det[d, a-o, b-o], else of -det[d, e_kx, b-a], else
+    of -det[d, e_ky, b-a]; swapping a and b negates it; it is 0 only when b-a is parallel to d."""
+    rng = np.random.default_rng(17)
+    for _ in range(600):
+        d, o, a, b = [rng.integers(-2, 3, size=3).astype(np.float32) for _ in range(4)]
+        if not d.any():
+            continue
+        kz = 2
+        if abs(d[0]) > abs(d[kz]):
+            kz = 0
+        if abs(d[1]) > abs(d[kz]):
+            kz = 1
+        kx, ky = (kz + 1) % 3, (kz + 2) % 3
+        D, O, A, Bv = [[Fraction(float(x)) for x in v] for v in (d, o, a, b)]
+        ba = [Bv[k] - A[k] for k in range(3)]
+        ex = _sign(_det3(D, [A[k] - O[k] for k in range(3)], [Bv[k] - O[k] for k in range(3)]))
+        if ex == 0:
+            ex = -_sign(_det3(D, [int(k == kx) for k in range(3)], ba))
+        if ex == 0:
+            ex = -_sign(_det3(D, [int(k == ky) for k in range(3)], ba))
+        s = bind.perturbed_sign(d, o, a, b)
+        assert s == ex
+        assert bind.perturbed_sign(d, o, b, a) == -s
+        cross = np.cross(d.astype(np.float64), (b - a).astype(np.float64))
+        assert (s == 0) == (not cross.any())
+
+
+@pytest.mark.parametrize("direction", [(0, 0, 1), (0, 0, -1), (1, 0, 0), (0, -1, 0)])
+def test_watertight_parity_on_shared_edges_and_vertices(direction):
+    """Rays that run exactly through the shared edges and vertices of a one-cube-thick
+    layer of 3x2 cubes (and along their side faces) classify the origin as the perturbed
+    origin o + delta*e_kx + delta^2*e_ky lies: no crossing is counted twice or missed.
+    (The layer is one cube thick along the ray: coincident faces across a layer boundary
+    lie at the same distance and the hit chain counts them once, by design.)"""
+    d = np.array(direction, np.float32)
+    kz = int(np.argmax(np.abs(d)))
+    kx, ky = (kz + 1) % 3, (kz + 2) % 3
+    n = np.ones(3, int)
+    n[kx], n[ky] = 3, 2
+    g = synth.cube_grid(int(n[0]), int(n[1]), int(n[2]), edges=False)
+    rng = np.random.default_rng(23)
+    m = 3000
+    pts = np.empty((m, 3), np.float32)
+    pts[:, kz] = rng.uniform(-0.5, n[kz] + 0.5, m)
+    for ax in (kx, ky):
+        on_line = rng.random(m) < 0.7
+        pts[:, ax] = np.where(on_line, rng.integers(-1, n[ax] + 2, m), rng.uniform(-0.5, n[ax] + 0.5, m))
+    pts[:, kz] = np.where(np.abs(pts[:, kz] - np.round(pts[:, kz])) < 1e-3, pts[:, kz] + 0.01, pts[:, kz])
+    inside = np.ones(m, bool)
+    for ax in (kx, ky):      # perturbed upward: closed below, open above
+        inside &= (pts[:, ax] >= 0) & (pts[:, ax] < n[ax])
+    inside &= (pts[:, kz] > 0) & (pts[:, kz] < n[kz])
+    got = bind.pim(g.vertices, g.indices, g.tri2obj, pts, direction=direction, use_bvh=False)
+    np.testing.assert_array_equal(got >= 0, inside)
+
+
+def test_estimate_pairs_alpha_rule(meta):
+    """The estimate is raw * alpha with alpha from the reference host code; a grid of zeros
+    gives zero."""
+    A = formats.read_pre(os.path.join(GOLD, "join_A.pre"))
+    zero = formats.Grid(A.grid.min_bound, A.grid.max_bound, A.grid.resolution, np.zeros_like(A.grid.cells))
+    est, raw = bind.estimate_pairs(zero, zero)
+    assert est == 0 and raw == 0.0
+    est, raw = bind.estimate_pairs(A.grid, A.grid, alpha_correction=False)
+    assert est == int(round(raw)) or abs(est - raw) <= 1
+
+
+# ---------------------------------------------------------------------- executables
+
+@pytest.fixture(scope="module")
+def cli_bin():
+    try:
+        build.build_lib()
+        build.build_cli()
+    except Exception as e:  # nvcc or g++ missing on this machine
+        pytest.skip(f"cannot build the executables: {e}")
+    return build.BIN
+
+
+@pytest.mark.parametrize("app", build.CLI_APPS)
+def test_cli_help(cli_bin, app):
+    r = subprocess.run([os.path.join(cli_bin, app), "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0
+    assert r.stdout.startswith("Usage: ")
+    assert "--output" in r.stdout
+
+
+@pytest.mark.parametrize("app,flag", [("raytracer", "--geometry"), ("raytracer_filter_refine", "--geometry"),
+                                      ("raytracer_mesh_overlap", "--mesh1"),
+                                      ("raytracer_overlap_estimated", "--mesh1"),
+                                      ("raytracer_overlap_direct_estimation", "--mesh1"),
+                                      ("raytracer_intersection_estimated", "--mesh1")])
+def test_cli_missing_input(cli_bin, app, flag):
+    r = subprocess.run([os.path.join(cli_bin, app)], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0
+    assert flag in (r.stderr + r.stdout)
