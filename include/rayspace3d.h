@@ -33,7 +33,7 @@ typedef enum rs_status {
     RS_ERR_ITER_LIMIT = 5,      /* an iteration budget ran out; result not valid */
     RS_ERR_FORMAT = 6,          /* malformed input file */
     RS_ERR_OOM = 7,             /* device allocation failed */
-    RS_ERR_TARGET_OVERFLOW = 8, /* containment ray crossed more distinct targets than supported */
+    RS_ERR_TARGET_OVERFLOW = 8, /* reserved: containment handles any number of distinct targets */
     RS_ERR_TOO_LARGE = 9        /* input larger than a fixed-capacity entry point accepts */
 } rs_status;
 
@@ -130,7 +130,8 @@ int rs_containment(const rs_bvh* target, const float* d_src_vertices, uint64_t s
  * (query/src/utilities/PairHitTracking.h:31-150, ContainmentTracking.h:22-120): for every
  * source object o < capacity, d_candidate_counts[o] = number of distinct target objects the
  * ray crossed, and d_target_ids/d_target_hits[o*max_targets + j] = the odd-parity targets
- * (first-crossed order) and how many of their triangles the ray crossed; -1/0 where unused.
+ * (traversal order within passes of 32 ids) and how many of their triangles the ray crossed;
+ * -1/0 where unused.
  * RS_ERR_OUTPUT_OVERFLOW if the source set has more than `capacity` objects. */
 int rs_containment_tracked(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,
                            const uint32_t* d_src_indices, uint64_t src_nF, const int32_t* d_src_tri2obj,

@@ -47,6 +47,9 @@ def lib():
                                     ctypes.POINTER(ctypes.POINTER(U64)), ctypes.POINTER(U64), I, I]
         L.orc_containment.argtypes = [P, U64, P, U64, P, P, U64, P, U64, P, I,
                                       ctypes.POINTER(ctypes.POINTER(U64)), ctypes.POINTER(U64), I, I]
+        L.orc_containment_diag.argtypes = [P, U64, P, U64, P, P, U64, P, U64, P, P, U64,
+                                           ctypes.POINTER(ctypes.POINTER(U64)),
+                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_uint32)), ctypes.POINTER(U64), I]
         L.orc_estimate_raw.argtypes = [P, P, U64, F, F, F]
         L.orc_estimate_raw.restype = ctypes.c_double
         L.orc_estimate_pairs.argtypes = [P, P, U64, P, P, P, F, F, I, ctypes.POINTER(ctypes.c_double)]
@@ -104,6 +107,25 @@ def containment(src_geom, V, I, T, swap=False, threads=None, use_bvh=True):
     lib().orc_containment(_p(sV), len(sV), _p(sI), len(sI), _p(sT), _p(V), len(V), _p(I), len(I), _p(T),
                           int(swap), ctypes.byref(kp), ctypes.byref(nk), threads or os.cpu_count(), int(use_bvh))
     return _take_keys(kp, nk)
+
+
+def containment_diag(src_geom, V, I, T, threads=None):
+    """(candidates[nObj], odd keys (src<<32|tgt) sorted, crossed-triangle count per key)."""
+    sV, sI, sT = _c(src_geom.vertices, np.float32), _c(src_geom.indices, np.uint32), _c(src_geom.tri2obj, np.int32)
+    V, I, T = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32)
+    n_obj = int(sT.max()) + 1 if len(sT) else 0
+    cand = np.zeros(max(n_obj, 1), np.uint32)
+    kp = ctypes.POINTER(ctypes.c_uint64)()
+    hp = ctypes.POINTER(ctypes.c_uint32)()
+    nk = ctypes.c_uint64()
+    rc = lib().orc_containment_diag(_p(sV), len(sV), _p(sI), len(sI), _p(sT), _p(V), len(V), _p(I), len(I), _p(T),
+                                    _p(cand), len(cand), ctypes.byref(kp), ctypes.byref(hp), ctypes.byref(nk),
+                                    threads or os.cpu_count())
+    assert rc == 0
+    n = int(nk.value)
+    hits = np.ctypeslib.as_array(hp, shape=(max(n, 1),))[:n].copy() if n else np.zeros(0, np.uint32)
+    lib().orc_free(ctypes.cast(hp, ctypes.c_void_p))
+    return cand[:n_obj], _take_keys(kp, nk), hits
 
 
 def overlap_join(A, B, threads=None, use_bvh=True):

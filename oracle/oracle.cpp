@@ -622,9 +622,18 @@ int orc_edge_join(const float* starts, const float* ends, const int32_t* offsets
     return 0;
 }
 
-int orc_containment(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uint64_t srcNF, const int32_t* srcT2O,
-                    const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* tri2obj,
-                    int swap, uint64_t** keys, uint64_t* nkeys, int nthreads, int use_bvh) {
+// Per-source diagnostics of the tracked containment (PairHitTracking.h:31-150):
+// candidates[o] = distinct target objects the ray crossed; odd-parity targets with the
+// number of their triangles the ray crossed.
+struct ContainDiag {
+    std::vector<uint32_t> candidates;
+    std::vector<std::vector<std::pair<uint32_t, uint32_t>>> odd;  // (target, hits) per source
+};
+
+static void containment_run(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uint64_t srcNF,
+                            const int32_t* srcT2O, const float* V, uint64_t nV, const uint32_t* I, uint64_t nF,
+                            const int32_t* tri2obj, int swap, std::vector<uint64_t>& all, ContainDiag* diag,
+                            int nthreads, int use_bvh) {
     Mesh src{srcV, srcNV, srcI, srcNF, srcT2O};
     Mesh m{V, nV, I, nF, tri2obj};
     // raytracer_intersection_estimated_main.cpp:539-552: lowest triangle index per object.
@@ -639,6 +648,10 @@ int orc_containment(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uin
     CpuBvh bvh;
     if (use_bvh) build_bvh(m, bvh);
     std::vector<std::vector<uint64_t>> perObj(nObj);
+    if (diag) {
+        diag->candidates.assign(nObj, 0);
+        diag->odd.assign(nObj, {});
+    }
     parallel_for(nObj, nthreads, [&](uint64_t b, uint64_t e) {
         std::vector<Hit> hits;
         std::vector<uint32_t> tg;
@@ -656,21 +669,57 @@ int orc_containment(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uin
             for (size_t i = 0; i < tg.size();) {
                 size_t j = i;
                 while (j < tg.size() && tg[j] == tg[i]) ++j;
+                if (diag) ++diag->candidates[o];
                 if ((j - i) & 1) {
                     uint64_t key = swap ? (((uint64_t)tg[i] << 32) | (uint32_t)o) : (((uint64_t)o << 32) | tg[i]);
                     perObj[o].push_back(key);
+                    if (diag) diag->odd[o].push_back({tg[i], (uint32_t)(j - i)});
                 }
                 i = j;
             }
         }
     });
-    std::vector<uint64_t> all;
+    all.clear();
     for (auto& v : perObj) all.insert(all.end(), v.begin(), v.end());
     std::sort(all.begin(), all.end());
     all.erase(std::unique(all.begin(), all.end()), all.end());
+}
+
+static void give_keys(const std::vector<uint64_t>& all, uint64_t** keys, uint64_t* nkeys) {
     *nkeys = all.size();
     *keys = (uint64_t*)std::malloc(sizeof(uint64_t) * (all.size() ? all.size() : 1));
     if (!all.empty()) std::memcpy(*keys, all.data(), sizeof(uint64_t) * all.size());
+}
+
+int orc_containment(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uint64_t srcNF, const int32_t* srcT2O,
+                    const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* tri2obj,
+                    int swap, uint64_t** keys, uint64_t* nkeys, int nthreads, int use_bvh) {
+    std::vector<uint64_t> all;
+    containment_run(srcV, srcNV, srcI, srcNF, srcT2O, V, nV, I, nF, tri2obj, swap, all, nullptr, nthreads, use_bvh);
+    give_keys(all, keys, nkeys);
+    return 0;
+}
+
+int orc_containment_diag(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uint64_t srcNF,
+                         const int32_t* srcT2O, const float* V, uint64_t nV, const uint32_t* I, uint64_t nF,
+                         const int32_t* tri2obj, uint32_t* out_candidates, uint64_t capacity,
+                         uint64_t** odd_keys, uint32_t** odd_hits, uint64_t* n_odd, int nthreads) {
+    std::vector<uint64_t> all;
+    ContainDiag dg;
+    containment_run(srcV, srcNV, srcI, srcNF, srcT2O, V, nV, I, nF, tri2obj, 0, all, &dg, nthreads, 1);
+    if (dg.candidates.size() > capacity) return 1;
+    std::copy(dg.candidates.begin(), dg.candidates.end(), out_candidates);
+    std::vector<std::pair<uint64_t, uint32_t>> flat;
+    for (uint64_t o = 0; o < dg.odd.size(); ++o)
+        for (auto& th : dg.odd[o]) flat.push_back({(o << 32) | th.first, th.second});
+    std::sort(flat.begin(), flat.end());
+    *n_odd = flat.size();
+    *odd_keys = (uint64_t*)std::malloc(sizeof(uint64_t) * (flat.size() ? flat.size() : 1));
+    *odd_hits = (uint32_t*)std::malloc(sizeof(uint32_t) * (flat.size() ? flat.size() : 1));
+    for (size_t i = 0; i < flat.size(); ++i) {
+        (*odd_keys)[i] = flat[i].first;
+        (*odd_hits)[i] = flat[i].second;
+    }
     return 0;
 }
 

@@ -54,6 +54,15 @@ int orc_containment(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uin
                     const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* tri2obj,
                     int swap, uint64_t** keys, uint64_t* nkeys, int nthreads, int use_bvh);
 
+/* Containment (swap=0) with the per-source diagnostics of the tracked variant
+ * (query/src/utilities/PairHitTracking.h:31-150): out_candidates[o] = distinct target
+ * objects crossed (capacity >= number of source objects, else returns 1); the odd-parity
+ * (source<<32 | target) keys, sorted, with the number of the target's triangles crossed. */
+int orc_containment_diag(const float* srcV, uint64_t srcNV, const uint32_t* srcI, uint64_t srcNF,
+                         const int32_t* srcT2O, const float* V, uint64_t nV, const uint32_t* I, uint64_t nF,
+                         const int32_t* tri2obj, uint32_t* out_candidates, uint64_t capacity,
+                         uint64_t** odd_keys, uint32_t** odd_hits, uint64_t* n_odd, int nthreads);
+
 /* Grid estimator raw sum (float per-cell values summed in double, index order). */
 double orc_estimate_raw(const void* cellsA, const void* cellsB, uint64_t ncells,
                         float cellVolume, float epsilon, float gamma);

@@ -8,12 +8,10 @@
 //      unique by construction;
 //   3. stable radix sort of the 32 Morton bits only (4 passes; ids stay ascending
 //      within equal codes);
-//   4. Karras' binary radix tree over the sorted keys;
-//   5. the triangles in leaf order (3 x float4 each);
-//   6. bottom-up box refit that starts from leaf groups (subtrees of <= leaf_size
-//      triangles, whose boxes are read straight from the leaf-ordered triangles),
-//      with one acquire-release arrival counter per node;
-//   7. emission of 64-byte nodes in which the leaf groups become leaves.
+//   4. one bottom-up pass (k_build_up) that writes the triangles in leaf order
+//      (3 x float4 each), builds the binary radix tree over the sorted keys
+//      agglomeratively and refits its boxes on the way up, emitting 64-byte nodes
+//      in which subtrees of <= leaf_size triangles become leaves.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -135,138 +133,109 @@ __global__ void k_morton(const float* __restrict__ V, uint64_t nV, const uint32_
     keys[t] = ((uint64_t)code << 32) | (uint32_t)t;
 }
 
-__device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, int n, int i, int j) {
-    if (j < 0 || j >= n) return -1;
-    const uint64_t a = keys[i], b = keys[j];
-    if (a == b) return 64 + __clz((unsigned)(i ^ j));
-    return __clzll((long long)(a ^ b));
+// Length of the common prefix of sorted keys i and i+1 (keys are distinct).
+__device__ __forceinline__ int split_prefix(const uint64_t* __restrict__ keys, int i) {
+    return __clzll((long long)(__ldg(&keys[i]) ^ __ldg(&keys[i + 1])));
 }
 
-// Karras 2012, "Maximizing parallelism in the construction of BVHs, octrees and k-d trees".
-// Internal nodes 0..n-2, leaves n-1..2n-2.
-__global__ void k_karras(const uint64_t* __restrict__ keys, int n, int* __restrict__ left, int* __restrict__ right,
-                         int* __restrict__ parent, int2* __restrict__ range) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = delta(keys, n, i, i - d);
-    int lmax = 2;
-    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
-    const int j = i + l * d;
-    const int dnode = delta(keys, n, i, j);
-    int s = 0;
-    int t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
-    } while (t > 1);
-    const int gamma = i + s * d + (d < 0 ? -1 : 0);
-    const int lo = min(i, j), hi = max(i, j);
-    const int lc = (lo == gamma) ? (n - 1 + gamma) : gamma;
-    const int rc = (hi == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
-    left[i] = lc;
-    right[i] = rc;
-    parent[lc] = i;
-    parent[rc] = i;
-    range[i] = make_int2(lo, hi);
+__device__ __forceinline__ int exchange_acq_rel(int* p, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
 }
 
-// Bottom-up refit from the leaf groups.  One thread per internal node p whose range
-// is larger than leaf_size (and the root): each child of p that spans <= leaf_size
-// triangles is a leaf group whose box is the union of its triangles, contiguous in
-// leaf order.  The thread stores that box and arrives at p; the second arrival at a
-// node merges both children and moves up.  Each arrival publishes its box with a
-// release fence before the counter increment; the second arrival's loads depend on
-// the increment's result and bypass L1.
-__device__ __forceinline__ void arrive(int node, float4 lo, float4 hi, int p, const int* __restrict__ left,
-                                       const int* __restrict__ right, const int* __restrict__ parent,
-                                       float4* __restrict__ blo, float4* __restrict__ bhi, int* __restrict__ flags) {
-    while (p >= 0) {
-        __threadfence();
-        if (atomicAdd(&flags[p], 1) == 0) return;
-        const int other = (__ldcg(&left[p]) == node) ? __ldcg(&right[p]) : __ldcg(&left[p]);
-        const float4 ol = __ldcg(&blo[other]), oh = __ldcg(&bhi[other]);
-        lo = make_float4(fminf(lo.x, ol.x), fminf(lo.y, ol.y), fminf(lo.z, ol.z), 0.f);
-        hi = make_float4(fmaxf(hi.x, oh.x), fmaxf(hi.y, oh.y), fmaxf(hi.z, oh.z), 0.f);
-        __stcg(&blo[p], lo);
-        __stcg(&bhi[p], hi);
-        node = p;
-        p = __ldcg(&parent[p]);
-    }
-}
-
-__global__ void k_refit(const float4* __restrict__ tris, int n, int leaf_size, const int* __restrict__ left,
-                        const int* __restrict__ right, const int* __restrict__ parent, const int2* __restrict__ range,
-                        float4* __restrict__ blo, float4* __restrict__ bhi, int* __restrict__ flags) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n - 1) return;
-    const int2 rp = range[p];
-    if (p != 0 && rp.y - rp.x + 1 <= leaf_size) return;  // inside a leaf group
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
-        const int c = side == 0 ? left[p] : right[p];
-        int first, size;
-        if (c >= n - 1) {
-            first = c - (n - 1);
-            size = 1;
-        } else {
-            const int2 rc = range[c];
-            first = rc.x;
-            size = rc.y - rc.x + 1;
-        }
-        if (size > leaf_size) continue;
-        float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-        for (int k = first; k < first + size; ++k) {
-#pragma unroll
-            for (int v = 0; v < 3; ++v) {
-                const float4 q = tris[3 * (size_t)k + v];
-                lo = make_float4(fminf(lo.x, q.x), fminf(lo.y, q.y), fminf(lo.z, q.z), 0.f);
-                hi = make_float4(fmaxf(hi.x, q.x), fmaxf(hi.y, q.y), fmaxf(hi.z, q.z), 0.f);
-            }
-        }
-        __stcg(&blo[c], lo);
-        __stcg(&bhi[c], hi);
-        arrive(c, lo, hi, p, left, right, parent, blo, bhi, flags);
-    }
-}
-
-__device__ __forceinline__ void child_entry(int c, int n, int leaf_size, const int2* __restrict__ range,
-                                            int& idx, int& cnt) {
-    if (c >= n - 1) {
-        idx = c - (n - 1);
-        cnt = 1;
-        return;
-    }
-    const int2 r = range[c];
-    const int size = r.y - r.x + 1;
-    if (size <= leaf_size) {
-        idx = r.x;
-        cnt = size;
+// A node slot holds its two children: side 0 in a.xyzw b.xy (box) and d.xy (entry),
+// side 1 in b.zw c.xyzw and d.zw.  The two sides occupy disjoint bytes, so the two
+// children of a node can write their halves concurrently.
+__device__ __forceinline__ void store_half(BNode* nd, int side, const float lo[3], const float hi[3], int idx,
+                                           int cnt) {
+    char* b = reinterpret_cast<char*>(nd);
+    if (side == 0) {
+        *reinterpret_cast<float4*>(b) = make_float4(lo[0], lo[1], lo[2], hi[0]);
+        *reinterpret_cast<float2*>(b + 16) = make_float2(hi[1], hi[2]);
+        *reinterpret_cast<int2*>(b + 48) = make_int2(idx, cnt);
     } else {
-        idx = c;
-        cnt = 0;
+        *reinterpret_cast<float2*>(b + 24) = make_float2(lo[0], lo[1]);
+        *reinterpret_cast<float4*>(b + 32) = make_float4(lo[2], hi[0], hi[1], hi[2]);
+        *reinterpret_cast<int2*>(b + 56) = make_int2(idx, cnt);
     }
 }
 
-__global__ void k_emit_nodes(int n, int leaf_size, const int* __restrict__ left, const int* __restrict__ right,
-                             const int2* __restrict__ range, const float4* __restrict__ blo,
-                             const float4* __restrict__ bhi, BNode* __restrict__ nodes) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int l = left[i], r = right[i];
-    int i0, c0, i1, c1;
-    child_entry(l, n, leaf_size, range, i0, c0);
-    child_entry(r, n, leaf_size, range, i1, c1);
-    const float4 l0 = blo[l], h0 = bhi[l], l1 = blo[r], h1 = bhi[r];
-    BNode nd;
-    nd.a = make_float4(l0.x, l0.y, l0.z, h0.x);
-    nd.b = make_float4(h0.y, h0.z, l1.x, l1.y);
-    nd.c = make_float4(l1.z, h1.x, h1.y, h1.z);
-    nd.d = make_int4(i0, c0, i1, c1);
-    nodes[i] = nd;
+__device__ __forceinline__ void load_half(const BNode* nd, int side, float lo[3], float hi[3]) {
+    const char* b = reinterpret_cast<const char*>(nd);
+    if (side == 0) {
+        const float4 a = __ldcg(reinterpret_cast<const float4*>(b));
+        const float2 c = __ldcg(reinterpret_cast<const float2*>(b + 16));
+        lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = a.w, hi[1] = c.x, hi[2] = c.y;
+    } else {
+        const float2 a = __ldcg(reinterpret_cast<const float2*>(b + 24));
+        const float4 c = __ldcg(reinterpret_cast<const float4*>(b + 32));
+        lo[0] = a.x, lo[1] = a.y, lo[2] = c.x, hi[0] = c.y, hi[1] = c.z, hi[2] = c.w;
+    }
+}
+
+// Bottom-up construction of the binary radix tree over the sorted keys, fused with
+// the emission of the leaf-ordered triangles and the box refit (agglomerative LBVH,
+// Apetrei 2014, "Fast and Simple Agglomerative LBVH Construction").  Thread k starts
+// at leaf k with range [k, k].  A subtree [l, r] joins the neighbouring split whose
+// keys share the longer prefix: split r (it is the left child) or split l-1 (the
+// right child); a split with no neighbour on one side takes the other.  This yields
+// the same tree as Karras' top-down construction.  At split p the child writes its
+// box and entry into its half of node slot p+1, then exchanges its outer range bound
+// in xchg[p] with acquire-release semantics; the first arrival stops, the second reads
+// its sibling's half, merges the boxes and continues with the parent's range.
+// Subtrees of <= leaf_size triangles are entered as leaves (first triangle, count);
+// larger ones by their slot (count 0).  The subtree [0, n-1] is copied to slot 0.
+__global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, uint64_t nV,
+                                                 const uint32_t* __restrict__ I, const int32_t* __restrict__ t2o,
+                                                 const uint64_t* __restrict__ keys, int n, int leaf_size,
+                                                 float4* __restrict__ tris, BNode* __restrict__ nodes,
+                                                 int* __restrict__ xchg) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t t = (uint32_t)(__ldg(&keys[k]) & 0xffffffffull);
+    const uint64_t last = nV - 1;
+    const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last), i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
+                   i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
+    float a[3], b[3], c[3], lo[3], hi[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        a[q] = V[3 * i0 + q];
+        b[q] = V[3 * i1 + q];
+        c[q] = V[3 * i2 + q];
+        lo[q] = fminf(fminf(a[q], b[q]), c[q]);
+        hi[q] = fmaxf(fmaxf(a[q], b[q]), c[q]);
+    }
+    tris[3 * (uint64_t)k] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
+    tris[3 * (uint64_t)k + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
+    tris[3 * (uint64_t)k + 2] = make_float4(c[0], c[1], c[2], 0.0f);
+    int l = k, r = k, self = 0;
+    for (;;) {
+        const int size = r - l + 1;
+        if (l == 0 && r == n - 1) {
+            const float4* src = reinterpret_cast<const float4*>(nodes + self);
+            float4* dst = reinterpret_cast<float4*>(nodes);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dst[q] = __ldcg(src + q);
+            return;
+        }
+        const bool left_child = (l == 0) ? true : (r == n - 1) ? false : split_prefix(keys, r) > split_prefix(keys, l - 1);
+        const int p = left_child ? r : l - 1;
+        BNode* nd = nodes + (p + 1);
+        store_half(nd, left_child ? 0 : 1, lo, hi, size <= leaf_size ? l : self, size <= leaf_size ? size : 0);
+        const int other = exchange_acq_rel(&xchg[p], left_child ? l : r);
+        if (other < 0) return;
+        float olo[3], ohi[3];
+        load_half(nd, left_child ? 1 : 0, olo, ohi);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            lo[q] = fminf(lo[q], olo[q]);
+            hi[q] = fmaxf(hi[q], ohi[q]);
+        }
+        if (left_child) r = other;
+        else l = other;
+        self = p + 1;
+    }
 }
 
 __global__ void k_emit_tris(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I,
@@ -348,15 +317,13 @@ extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t
     const int n = (int)nF;
     int* bounds = nullptr;  // 12 ordered-int bounds, then the bad-index flag
     uint64_t* keys = nullptr;
-    int *left = nullptr, *right = nullptr, *parent = nullptr, *flags = nullptr;
-    int2* range = nullptr;
-    float4 *blo = nullptr, *bhi = nullptr;
+    int* xchg = nullptr;
     cudaError_t e = cudaSuccess;
     int hb[13];
     const int grid = 4 * sm_count();
-    h->n_nodes = n >= 2 ? (uint64_t)(n - 1) : 1;
+    h->n_nodes = n >= 2 ? (uint64_t)n : 1;  // slot 0 = root, slot p+1 = split p
     h->n_tris = (uint64_t)n;
-    prof_begin(P_BVH_BUILD, s);
+    const int ptok = prof_begin(P_BVH_BUILD, s);
     e = alloc(&h->nodes, h->n_nodes, s);
     if (e == cudaSuccess) e = alloc(&h->tris, 3 * (size_t)n, s);
     if (e == cudaSuccess) e = alloc(&bounds, 13, s);
@@ -376,28 +343,17 @@ extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t
         }
     } else {
         const int nb = (n + kT - 1) / kT;
-        const int nbi = (n - 1 + kT - 1) / kT;
         e = alloc(&keys, n, s);
-        if (e == cudaSuccess) e = alloc(&left, n - 1, s);
-        if (e == cudaSuccess) e = alloc(&right, n - 1, s);
-        if (e == cudaSuccess) e = alloc(&parent, 2 * (size_t)n - 1, s);
-        if (e == cudaSuccess) e = alloc(&flags, n - 1, s);
-        if (e == cudaSuccess) e = alloc(&range, n - 1, s);
-        if (e == cudaSuccess) e = alloc(&blo, 2 * (size_t)n - 1, s);
-        if (e == cudaSuccess) e = alloc(&bhi, 2 * (size_t)n - 1, s);
+        if (e == cudaSuccess) e = alloc(&xchg, n - 1, s);
         if (e != cudaSuccess) goto fail;
         launch(k_morton, nb, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys);
         e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32);
         if (e != cudaSuccess) goto fail;
-        cudaMemsetAsync(parent, 0xff, (2 * (size_t)n - 1) * sizeof(int), s);
-        cudaMemsetAsync(flags, 0, (size_t)(n - 1) * sizeof(int), s);
-        launch(k_karras, nbi, kT, 0, s, keys, n, left, right, parent, range);
-        launch(k_emit_tris, nb, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys, n, h->tris);
-        launch(k_refit, nbi, kT, 0, s, (const float4*)h->tris, n, leaf_size, left, right, parent, range, blo, bhi,
-               flags);
-        launch(k_emit_nodes, nbi, kT, 0, s, n, leaf_size, left, right, range, blo, bhi, h->nodes);
+        cudaMemsetAsync(xchg, 0xff, (size_t)(n - 1) * sizeof(int), s);
+        launch(k_build_up, nb, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys, n, leaf_size,
+               h->tris, h->nodes, xchg);
     }
-    prof_end(P_BVH_BUILD, s);
+    prof_end(P_BVH_BUILD, s, ptok);
     e = cudaGetLastError();
     // One host round trip: vertex bounds for the filter box and the bad-index flag.
     if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
@@ -406,13 +362,7 @@ extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t
 fail:
     if (bounds) cudaFreeAsync(bounds, s);
     if (keys) cudaFreeAsync(keys, s);
-    if (left) cudaFreeAsync(left, s);
-    if (right) cudaFreeAsync(right, s);
-    if (parent) cudaFreeAsync(parent, s);
-    if (flags) cudaFreeAsync(flags, s);
-    if (range) cudaFreeAsync(range, s);
-    if (blo) cudaFreeAsync(blo, s);
-    if (bhi) cudaFreeAsync(bhi, s);
+    if (xchg) cudaFreeAsync(xchg, s);
     const bool bad = (e == cudaSuccess) && hb[12] != 0;
     if (e != cudaSuccess || bad) {
         if (h->nodes) cudaFreeAsync(h->nodes, s);

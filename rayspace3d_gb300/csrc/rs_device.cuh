@@ -30,7 +30,7 @@ enum : uint32_t {
     ST_HIT_OVERFLOW = 1u << 1,   // a per-ray hit list overflowed (handled by a fallback pass)
     ST_STACK_OVERFLOW = 1u << 2, // a traversal stack overflowed (result invalid)
     ST_ITER_LIMIT = 1u << 3,     // an iteration budget ran out (result invalid)
-    ST_TARGET_OVERFLOW = 1u << 4 // containment: more distinct targets than the per-ray list holds
+    ST_TARGET_OVERFLOW = 1u << 4 // reserved (containment handles any number of targets in passes)
 };
 
 // ---------------------------------------------------------------------------

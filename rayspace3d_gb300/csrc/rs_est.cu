@@ -99,11 +99,11 @@ int estimate_device(const void* d_a, const void* d_b, uint64_t n, float cell_vol
     double* part = nullptr;
     cudaError_t e = dmalloc((void**)&part, (kBlocks * kSums + kSums) * sizeof(double), s);
     if (e != cudaSuccess) return to_status(e);
-    prof_begin(P_ESTIMATE, s);
+    const int ptok = prof_begin(P_ESTIMATE, s);
     launch(k_estimate, kBlocks, kT, 0, s, reinterpret_cast<const uint4*>(d_a), reinterpret_cast<const uint4*>(d_b), n,
                                       cell_volume, eps, gamma, part);
     launch(k_estimate_final, 1, 256, 0, s, part, part + kBlocks * kSums);
-    prof_end(P_ESTIMATE, s);
+    prof_end(P_ESTIMATE, s, ptok);
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out, part + kBlocks * kSums, kSums * sizeof(double), cudaMemcpyDeviceToHost, s);

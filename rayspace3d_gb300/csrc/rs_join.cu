@@ -92,7 +92,7 @@ __global__ void k_max_obj(const int32_t* __restrict__ t2o, uint64_t nF, int* __r
 // Optional per-source outputs of the containment pass (the reference's pair-hit and
 // containment-tracking buffers, query/src/utilities/PairHitTracking.h,
 // ContainmentTracking.h): distinct targets crossed, and the odd-parity targets with
-// their crossing counts in first-crossed order.
+// their crossing counts (traversal order within each pass).
 struct Tracking {
     int max_targets;
     int32_t* target_ids;      // [nObj * max_targets], -1 where unused
@@ -122,63 +122,89 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
     if (vi >= nV) return;
     const Ray r = make_ray(V[3 * (uint64_t)vi], V[3 * (uint64_t)vi + 1], V[3 * (uint64_t)vi + 2], 0.0f, 0.0f, 1.0f,
                            1e-4f, 1e10f);
-    int32_t tgt[kTargets];
+    // Parity per target object in passes of at most kTargets objects: pass p tracks the
+    // kTargets smallest object ids (as uint32) above the largest id of pass p-1.  A list
+    // member is inserted at its first crossing and never evicted (evictions only drop the
+    // largest member for a smaller newcomer, and the largest only decreases), so every
+    // tracked parity is complete; a pass that had to turn an id away runs another pass.
+    uint32_t tgt[kTargets];
     uint32_t hits[TRACK ? kTargets : 1];
-    uint32_t par = 0;  // parity bit per list entry
-    int nt = 0;
-    bool ovf = false;
-    unsigned int crossings = 0;
-    const bool ok = traverse<2>(nodes, max_steps, r, [&](int f, int cnt) {
-        for (int k = f; k < f + cnt; ++k) {
-            float a[3], b[3], c[3];
-            uint32_t tid;
-            int32_t obj;
-            load_tri(tris, k, a, b, c, tid, obj);
-            float t;
-            if (!hit_triangle<2>(r, a, b, c, t)) continue;
-            ++crossings;
-            int j = 0;
-            for (; j < nt; ++j)
-                if (tgt[j] == obj) break;
-            if (j < nt) {
-                par ^= 1u << j;
-                if (TRACK) ++hits[j];
-            } else if (nt < kTargets) {
-                tgt[nt] = obj;
-                if (TRACK) hits[nt] = 1;
-                par |= 1u << nt;
-                ++nt;
-            } else {
-                ovf = true;
+    uint32_t lo = 0;
+    bool bounded = false;
+    unsigned int crossings = 0, candidates = 0;
+    int out = 0;
+    for (;;) {
+        uint32_t par = 0;  // parity bit per list entry
+        int nt = 0;
+        bool more = false;
+        const bool ok = traverse<2>(nodes, max_steps, r, [&](int f, int cnt) {
+            for (int k = f; k < f + cnt; ++k) {
+                float a[3], b[3], c[3];
+                uint32_t tid;
+                int32_t obj;
+                load_tri(tris, k, a, b, c, tid, obj);
+                const uint32_t id = (uint32_t)obj;
+                if (bounded && id <= lo) continue;
+                if (more && nt == kTargets && (bounded || !table.stats)) {  // above every member of a full list
+                    uint32_t mx = 0;
+                    for (int j = 0; j < nt; ++j) mx = max(mx, tgt[j]);
+                    if (id > mx) continue;
+                }
+                float t;
+                if (!hit_triangle<2>(r, a, b, c, t)) continue;
+                if (!bounded) ++crossings;
+                int j = 0;
+                for (; j < nt; ++j)
+                    if (tgt[j] == id) break;
+                if (j < nt) {
+                    par ^= 1u << j;
+                    if (TRACK) ++hits[j];
+                } else if (nt < kTargets) {
+                    tgt[nt] = id;
+                    if (TRACK) hits[nt] = 1;
+                    par |= 1u << nt;
+                    ++nt;
+                } else {
+                    more = true;
+                    int jm = 0;
+                    for (int q = 1; q < nt; ++q)
+                        if (tgt[q] > tgt[jm]) jm = q;
+                    if (id < tgt[jm]) {
+                        tgt[jm] = id;
+                        if (TRACK) hits[jm] = 1;
+                        par |= 1u << jm;
+                    }
+                }
+            }
+        });
+        if (!ok) {
+            atomicOr(table.status, ST_STACK_OVERFLOW);
+            return;
+        }
+        candidates += (unsigned int)nt;
+        uint32_t mx = 0;
+        for (int j = 0; j < nt; ++j) {
+            mx = max(mx, tgt[j]);
+            if (!((par >> j) & 1u)) continue;
+            const unsigned long long key = swap ? (((unsigned long long)tgt[j] << 32) | (uint32_t)o)
+                                                : (((unsigned long long)(uint32_t)o << 32) | tgt[j]);
+            table_insert(table, key);
+            if (TRACK && out < trk.max_targets) {
+                trk.target_ids[o * trk.max_targets + out] = (int32_t)tgt[j];
+                trk.target_hits[o * trk.max_targets + out] = hits[j];
+                ++out;
             }
         }
-    });
-    if (!ok) {
-        atomicOr(table.status, ST_STACK_OVERFLOW);
-        return;
-    }
-    if (ovf) {
-        atomicOr(table.status, ST_TARGET_OVERFLOW);
-        return;
+        if (!more) break;
+        lo = mx;
+        bounded = true;
     }
     if (table.stats) {
         atomicAdd(&table.stats[4], 1ull);
         if (crossings) atomicAdd(&table.stats[5], (unsigned long long)crossings);
-        if (nt) atomicAdd(&table.stats[6], (unsigned long long)nt);
+        if (candidates) atomicAdd(&table.stats[6], (unsigned long long)candidates);
     }
-    int out = 0;
-    for (int j = 0; j < nt; ++j) {
-        if (!((par >> j) & 1u)) continue;
-        const unsigned long long key = swap ? (((unsigned long long)(uint32_t)tgt[j] << 32) | (uint32_t)o)
-                                            : (((unsigned long long)(uint32_t)o << 32) | (uint32_t)tgt[j]);
-        table_insert(table, key);
-        if (TRACK && out < trk.max_targets) {
-            trk.target_ids[o * trk.max_targets + out] = tgt[j];
-            trk.target_hits[o * trk.max_targets + out] = hits[j];
-            ++out;
-        }
-    }
-    if (TRACK) trk.candidates[o] = (uint32_t)nt;
+    if (TRACK) trk.candidates[o] = candidates;
 }
 
 }  // namespace
@@ -206,10 +232,10 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
                             int swap, rs_pairset* ps, cudaStream_t s) {
     if (nE == 0 || target->n_tris == 0) return cudaSuccess;
     const unsigned grid = (unsigned)((nE + kT - 1) / kT);
-    prof_begin(P_EDGE_JOIN, s);
+    const int ptok = prof_begin(P_EDGE_JOIN, s);
     launch(k_edge_join, grid, kT, 0, s, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, target->nodes,
            max_steps(target), target->tris, swap, table_view(ps));
-    prof_end(P_EDGE_JOIN, s);
+    prof_end(P_EDGE_JOIN, s, ptok);
     return cudaGetLastError();
 }
 
@@ -264,7 +290,7 @@ static int containment_impl(const rs_bvh* target, const float* d_src_vertices, u
             launch(k_first_tri_init, (unsigned)((nObj + 255) / 256), 256, 0, s, first, nObj);
             launch(k_first_tri, (unsigned)((src_nF + 255) / 256), 256, 0, s, d_src_tri2obj, src_nF, first, nObj);
             const unsigned grid = (unsigned)((nObj + kT - 1) / kT);
-            prof_begin(P_CONTAINMENT, s);
+            const int ptok = prof_begin(P_CONTAINMENT, s);
             if (trk)
                 launch(k_containment<true>, grid, kT, 0, s, d_src_vertices, src_nV, d_src_indices, (const int32_t*)first,
                        nObj, (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap,
@@ -273,7 +299,7 @@ static int containment_impl(const rs_bvh* target, const float* d_src_vertices, u
                 launch(k_containment<false>, grid, kT, 0, s, d_src_vertices, src_nV, d_src_indices, (const int32_t*)first,
                        nObj, (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap,
                        table_view(ps), Tracking{0, nullptr, nullptr, nullptr});
-            prof_end(P_CONTAINMENT, s);
+            prof_end(P_CONTAINMENT, s, ptok);
             e = cudaGetLastError();
         }
     }

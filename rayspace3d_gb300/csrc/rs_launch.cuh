@@ -32,8 +32,8 @@ enum ProfId { P_EDGE_JOIN = 0, P_CONTAINMENT = 1, P_PIM = 2, P_BVH_BUILD = 3, P_
 
 // Records an event pair around one launch when profiling is on; prof_collect()
 // (called after the stream has been synchronised) accumulates the elapsed time.
-void prof_begin(int id, cudaStream_t s);
-void prof_end(int id, cudaStream_t s);
+int prof_begin(int id, cudaStream_t s);          // returns a token for prof_end
+void prof_end(int id, cudaStream_t s, int token);
 void prof_collect();
 
 }  // namespace rs

@@ -147,7 +147,7 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
     if (n == 0) return RS_OK;
     uint64_t* tmp = nullptr;
     uint64_t* dcount = nullptr;
-    prof_begin(P_FINALIZE, s);
+    const int ptok = prof_begin(P_FINALIZE, s);
     e = dmalloc((void**)&tmp, n * sizeof(uint64_t), s);
     if (e == cudaSuccess) e = dmalloc((void**)&dcount, sizeof(uint64_t), s);
     if (e == cudaSuccess) e = compact_u64(reinterpret_cast<const uint64_t*>(ps->slots), ps->capacity, kEmptyKey, tmp,
@@ -159,7 +159,7 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
     const uint64_t ncopy = std::min<uint64_t>(n, capacity);
     if (e == cudaSuccess && ncopy)
         e = cudaMemcpyAsync(d_keys, tmp, ncopy * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
-    prof_end(P_FINALIZE, s);
+    prof_end(P_FINALIZE, s, ptok);
     if (tmp) cudaFreeAsync(tmp, s);
     if (dcount) cudaFreeAsync(dcount, s);
     cudaError_t e2 = cudaStreamSynchronize(s);

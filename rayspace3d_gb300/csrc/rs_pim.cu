@@ -485,7 +485,7 @@ cudaError_t launch_pim(const rs_bvh* bvh, const float* pts, uint64_t n, float dx
                        unsigned long long* ovf_count, cudaStream_t s) {
     const unsigned grid = (unsigned)((n + kT - 1) / kT);
     constexpr int GA = AXIS < 0 ? 0 : AXIS;
-    prof_begin(P_PIM, s);
+    const int ptok = prof_begin(P_PIM, s);
     if (AXIS >= 0 && bvh->cgrid[GA].built) {
         const rs_column_grid& cg = bvh->cgrid[GA];
         GridView g{cg.u0, cg.v0, cg.su, cg.sv, cg.u1, cg.v1, cg.gu, cg.gv, cg.start, cg.list};
@@ -495,7 +495,7 @@ cudaError_t launch_pim(const rs_bvh* bvh, const float* pts, uint64_t n, float dx
         launch(k_pim<AXIS, FILTER>, grid, kT, 0, s, pts, n, dx, dy, dz, bvh->nodes, max_steps(bvh),
                (const float4*)bvh->tris, box, obj, in, status, ovf_list, ovf_count);
     }
-    prof_end(P_PIM, s);
+    prof_end(P_PIM, s, ptok);
     launch(k_pim_fallback<AXIS>, 2 * sm_count(), 128, 0, s, pts, dx, dy, dz, bvh->nodes, max_steps(bvh),
            (const float4*)bvh->tris, obj, in, status, ovf_list, ovf_count);
     return cudaGetLastError();

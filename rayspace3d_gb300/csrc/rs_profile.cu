@@ -1,5 +1,7 @@
 // rs_profile.cu -- launch counter and the opt-in per-kernel event profiler.
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "rs_engine.h"
 #include "rs_prims.cuh"
@@ -34,9 +36,12 @@ cudaError_t dmalloc(void** p, size_t bytes, cudaStream_t s) {
 }
 
 namespace {
+// One event pair per profiled launch between collections; launches on several
+// streams may be open at once (each begin returns its own token).
 struct Slot {
-    cudaEvent_t a = nullptr, b = nullptr;
-    bool pending = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    std::vector<char> done;  // 0 open, 1 ended, 2 collected
+    size_t used = 0;
     double total_ms = 0.0;
     uint64_t launches = 0;
 };
@@ -45,34 +50,50 @@ bool g_on = false;
 Slot g_slots[P_COUNT];
 }  // namespace
 
-void prof_begin(int id, cudaStream_t s) {
+int prof_begin(int id, cudaStream_t s) {
     std::lock_guard<std::mutex> g(g_mu);
-    if (!g_on) return;
+    if (!g_on) return -1;
     Slot& sl = g_slots[id];
-    if (!sl.a) {
-        cudaEventCreate(&sl.a);
-        cudaEventCreate(&sl.b);
+    if (sl.used == sl.ev.size()) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (cudaEventCreate(&a) != cudaSuccess) return -1;
+        if (cudaEventCreate(&b) != cudaSuccess) {
+            cudaEventDestroy(a);
+            return -1;
+        }
+        sl.ev.push_back({a, b});
+        sl.done.push_back(0);
     }
-    cudaEventRecord(sl.a, s);
+    const int tok = (int)sl.used++;
+    sl.done[tok] = 0;
+    cudaEventRecord(sl.ev[tok].first, s);
+    return tok;
 }
 
-void prof_end(int id, cudaStream_t s) {
+void prof_end(int id, cudaStream_t s, int tok) {
     std::lock_guard<std::mutex> g(g_mu);
-    if (!g_on || !g_slots[id].a) return;
-    cudaEventRecord(g_slots[id].b, s);
-    g_slots[id].pending = true;
+    Slot& sl = g_slots[id];
+    if (tok < 0 || (size_t)tok >= sl.used) return;
+    cudaEventRecord(sl.ev[tok].second, s);
+    sl.done[tok] = 1;
 }
 
 void prof_collect() {
     std::lock_guard<std::mutex> g(g_mu);
     for (Slot& sl : g_slots) {
-        if (!sl.pending) continue;
-        float ms = 0.0f;
-        if (cudaEventSynchronize(sl.b) == cudaSuccess && cudaEventElapsedTime(&ms, sl.a, sl.b) == cudaSuccess) {
-            sl.total_ms += ms;
-            sl.launches += 1;
+        bool all = true;
+        for (size_t i = 0; i < sl.used; ++i) {
+            if (sl.done[i] == 0) all = false;  // still open on some stream
+            if (sl.done[i] != 1) continue;
+            float ms = 0.0f;
+            if (cudaEventSynchronize(sl.ev[i].second) == cudaSuccess &&
+                cudaEventElapsedTime(&ms, sl.ev[i].first, sl.ev[i].second) == cudaSuccess) {
+                sl.total_ms += ms;
+                sl.launches += 1;
+            }
+            sl.done[i] = 2;
         }
-        sl.pending = false;
+        if (all) sl.used = 0;
     }
 }
 
@@ -91,7 +112,7 @@ extern "C" int rs_profile_reset(void) {
     for (auto& sl : rs::g_slots) {
         sl.total_ms = 0.0;
         sl.launches = 0;
-        sl.pending = false;
+        sl.used = 0;
     }
     return RS_OK;
 }
