@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--pim-points", type=int, default=1_000_000)
     ap.add_argument("--no-pim", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -261,6 +262,8 @@ def run_engine(args, rank, world, local):
 
     # Parity spot check of this run's output against the previous device-resident result.
     assert int(out.numel()) == n_pairs
+    with torch.cuda.stream(stream):
+        rc = recheck(L, lambda: (step(da, db), torch.cuda.synchronize()))
 
     # Roofline of the join's dominant kernel, k_edge_join (one launch per direction;
     # the BVH build is a chain of smaller kernels).  Algorithmic bytes per launch: the
@@ -288,6 +291,7 @@ def run_engine(args, rank, world, local):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e_s, 6), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
+        "recheck": rc,
         "kernels": {k: {kk: round(vv, 5) if isinstance(vv, float) else vv for kk, vv in v.items()}
                     for k, v in prof.items()},
         "roofline": roof,
@@ -296,30 +300,47 @@ def run_engine(args, rank, world, local):
     return result, A, B
 
 
-def run_pim(args, local):
+def recheck(L, fn):
+    """Runs fn once with triangle-test counting on; returns the recheck statistics."""
+    import ctypes
+    L.rs_recheck_reset()
+    L.rs_recheck_enable(1)
+    try:
+        fn()
+    finally:
+        L.rs_recheck_enable(0)
+    ex, tests = ctypes.c_uint64(), ctypes.c_uint64()
+    L.rs_recheck_read(ctypes.byref(ex), ctypes.byref(tests))
+    return {"exact_edge_signs": ex.value, "triangle_tests": tests.value,
+            "rate_per_test": (ex.value / tests.value) if tests.value else 0.0}
+
+
+def run_pim(args, local, n_points, direction, reps=20):
+    """Point-in-mesh on one level-4 icosphere: kernel time (profiler), stream time and
+    end-to-end time with the points copied in from pinned host memory."""
     import ctypes
 
     import torch
     from rayspace3d_gb300 import _lib, api, synth
 
     L = _lib.load()
-    g, pts = synth.pim_workload(args.pim_points, level=4, seed=0)
+    g, pts = synth.pim_workload(n_points, level=4, seed=0)
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
         dg = api.DeviceGeometry(g)
         bvh = api.Bvh(dg, stream=stream)
         dp = torch.from_numpy(pts).cuda()
         obj = torch.empty(len(pts), dtype=torch.int32, device="cuda")
+        inside = torch.empty(len(pts), dtype=torch.uint8, device="cuda")
         for _ in range(3):
-            api.point_in_mesh(bvh, dp, out_obj=obj, stream=stream)
+            api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside, stream=stream)
         torch.cuda.synchronize()
         L.rs_profile_reset()
         L.rs_profile_enable(1)
-        reps = 20
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(reps):
-            api.point_in_mesh(bvh, dp, out_obj=obj, stream=stream)
+            api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside, stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
         L.rs_profile_enable(0)
@@ -328,25 +349,76 @@ def run_pim(args, local):
         cnt = ctypes.c_uint64()
         L.rs_profile_read(2, ctypes.byref(kms), ctypes.byref(cnt))
         kavg = kms.value / max(cnt.value, 1)
-        # end to end: points from pinned host memory, objects back
         hp = torch.from_numpy(pts).pin_memory()
-        hobj = torch.empty(len(pts), dtype=torch.int32).pin_memory()
+        hin = torch.empty(len(pts), dtype=torch.uint8).pin_memory()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(reps):
             dp.copy_(hp, non_blocking=True)
-            api.point_in_mesh(bvh, dp, out_obj=obj, stream=stream)
-            hobj.copy_(obj, non_blocking=True)
+            api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside, stream=stream)
+            hin.copy_(inside, non_blocking=True)
         torch.cuda.synchronize()
         e2e = (time.perf_counter() - t0) / reps
+        rc = recheck(L, lambda: (api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside,
+                                                   stream=stream), torch.cuda.synchronize()))
     hbm, kind = peaks()
     nbytes = 13 * len(pts) + 12 * dg.nV + 16 * dg.nF
-    return {"workload": f"{len(pts)} points uniform in [-1.5,1.5]^3, level-4 icosphere (5120 triangles), +Z rays",
+    axis = "xyz"[int(np.argmax(np.abs(direction)))]
+    return {"workload": f"{len(pts)} points uniform in [-1.5,1.5]^3, level-4 icosphere (5120 triangles), "
+                        f"+{axis} rays, seed 0",
             "mpts_s": round(len(pts) / (ms * 1e-3) / 1e6, 2), "ms": round(ms, 4),
             "kernel_ms": round(kavg, 4), "inside_frac": round(float((obj >= 0).float().mean().item()), 5),
             "e2e_mpts_s": round(len(pts) / e2e / 1e6, 2),
+            "e2e_bytes_per_call": {"h2d": 12 * len(pts), "d2h": len(pts)},
+            "recheck": rc,
             "roofline": {"bound": "hbm", "achieved": round(nbytes / (kavg * 1e-3) / 1e9, 2), "peak": hbm,
                          "unit": "GB/s", "frac": round(nbytes / (kavg * 1e-3) / 1e9 / hbm, 5),
-                         "algorithmic_bytes_per_launch": nbytes, "peak_source": kind + " hbm_gbs"}}, (g, pts)
+                         "algorithmic_bytes_per_launch": nbytes, "peak_source": kind + " hbm_gbs"}}
+
+
+def run_join_variant(args, world_size, steps=5):
+    """The overlap join at another world size (device-resident), pairs and recheck rate."""
+    import torch
+    from rayspace3d_gb300 import _lib, api, synth
+
+    L = _lib.load()
+    A, B = synth.overlap_workload(n_objects=args.objects, level=2, world=world_size, seed=1,
+                                  grid_resolution=args.grid)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+        cache = {}
+
+        def step():
+            est, _ = api.estimate_pairs(da, db, stream=stream)
+            size = api.hash_size_pow2(est)
+            ps = cache.get(size)
+            if ps is None:
+                ps = cache[size] = api.PairSet(size, pow2=True, stream=stream)
+            ba, bb = api.Bvh(da, stream=stream), api.Bvh(db, stream=stream)
+            api.overlap_join(ba, bb, ps, stream=stream)
+            keys = ps.finalize(order=1, stream=stream)
+            ba.close()
+            bb.close()
+            return keys, est
+
+        for _ in range(3):
+            keys, est = step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            keys, est = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        rc = recheck(L, lambda: (step(), torch.cuda.synchronize()))
+    n_pairs = int(keys.numel())
+    return {"workload": f"overlap join: {args.objects} + {args.objects} level-2 icospheres, world {world_size:g}^3, "
+                        f"seed 1, {args.grid}^3 grid",
+            "seconds": round(ms / 1e3, 6), "pairs": n_pairs, "estimated_pairs": int(est),
+            "selectivity": n_pairs / float(args.objects) ** 2,
+            "edge_rays_per_join": int(da.nE + db.nE), "recheck": rc}
 
 
 def cpu_join_sample(A, B, frac=0.02, threads=None):
@@ -410,7 +482,12 @@ def main():
         return
     result, A, B = run_engine(args, rank, world, local)
     if not args.no_pim:
-        result["pim"], _ = run_pim(args, local)
+        result["pim"] = run_pim(args, local, args.pim_points, (1.0, 0.0, 0.0))
+        result["pim_z"] = run_pim(args, local, args.pim_points, (0.0, 0.0, 1.0))
+        if not args.no_variants:
+            result["pim_100m"] = run_pim(args, local, 100_000_000, (1.0, 0.0, 0.0), reps=5)
+    if not args.no_variants:
+        result["join_w80"] = run_join_variant(args, 80.7)
     if rank == 0 and not args.no_cpu_baseline:
         v, meta = cpu_join_sample(A, B, frac=0.01)
         result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": meta["cores"], "kind": "port",

@@ -200,6 +200,14 @@ int rs_profile_enable(int on);
 int rs_profile_reset(void);
 int rs_profile_read(int kernel, double* total_ms, uint64_t* launches);
 
+/* Recheck rate of the exact hit contract (no counterpart in the reference): the number of
+ * edge signs the FP32 error filter could not decide and that were re-evaluated exactly
+ * (always counted), and the number of ray/triangle tests (counted while enabled; costs one
+ * atomic per ray).  Rate = exact_signs / (3 * triangle_tests) at most. */
+int rs_recheck_enable(int on);
+int rs_recheck_reset(void);
+int rs_recheck_read(uint64_t* exact_signs, uint64_t* triangle_tests);
+
 /* ========================================================================== */
 /* 2. Reference-compatible helpers (same names and signatures as the reference) */
 /* ========================================================================== */

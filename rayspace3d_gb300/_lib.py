@@ -61,6 +61,9 @@ SIGNATURES = {
     "rs_profile_enable": (I, [I]),
     "rs_profile_reset": (I, []),
     "rs_profile_read": (I, [I, ctypes.POINTER(ctypes.c_double), PU64]),
+    "rs_recheck_enable": (I, [I]),
+    "rs_recheck_reset": (I, []),
+    "rs_recheck_read": (I, [PU64, PU64]),
     "exclusive_scan_gpu": (ctypes.c_longlong, [P, P, I]),
     "merge_and_deduplicate_pairs_gpu": (ctypes.c_longlong, [P, ctypes.c_longlong, P, ctypes.c_longlong, P]),
     "compact_hash_table_pairs": (I, [P, ctypes.c_ulonglong, P, I]),

@@ -34,6 +34,42 @@ enum : uint32_t {
 };
 
 // ---------------------------------------------------------------------------
+// Recheck statistics, one copy per translation unit: [0] edge signs that the FP32
+// filter could not decide (always counted: the exact path is rare), [1] triangle
+// tests (counted while g_recheck_on is set, one warp-aggregated atomic per thread).
+// ---------------------------------------------------------------------------
+static __device__ unsigned long long g_recheck[2];
+static __device__ int g_recheck_on;
+
+__device__ __forceinline__ void note_exact() { atomicAdd(&g_recheck[0], 1ull); }
+
+__device__ __forceinline__ void add_tests(unsigned int n) {
+    if (!__ldcg(&g_recheck_on)) return;
+    const unsigned int mask = __activemask();
+    const unsigned int sum = __reduce_add_sync(mask, n);
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&g_recheck[1], (unsigned long long)sum);
+}
+
+// Host side: op 0 = disable, 1 = enable, 2 = reset, 3 = read into out[2] (adds).
+static inline int recheck_op(int op, unsigned long long* out) {
+    if (op == 0 || op == 1) {
+        const int v = op;
+        return (int)cudaMemcpyToSymbol(g_recheck_on, &v, sizeof(v));
+    }
+    if (op == 2) {
+        const unsigned long long z[2] = {0, 0};
+        return (int)cudaMemcpyToSymbol(g_recheck, z, sizeof(z));
+    }
+    unsigned long long v[2] = {0, 0};
+    const cudaError_t e = cudaMemcpyFromSymbol(v, g_recheck, sizeof(v));
+    if (e == cudaSuccess && out) {
+        out[0] += v[0];
+        out[1] += v[1];
+    }
+    return (int)e;
+}
+
+// ---------------------------------------------------------------------------
 // Exact FP64 building blocks (Knuth two-sum, FMA two-product, Shewchuk
 // grow-expansion).  Intrinsics keep the compiler from re-associating them.
 // ---------------------------------------------------------------------------
@@ -75,6 +111,7 @@ __device__ __forceinline__ int expansion_sign(const double* e, int m) {
 // by value so callers never have to keep them addressable in local memory.
 static __device__ __noinline__ int orient_exact(float d0, float d1, float d2, float o0, float o1, float o2,
                                                 float a0, float a1, float a2, float b0, float b1, float b2) {
+    note_exact();
     const float d[3] = {d0, d1, d2}, o[3] = {o0, o1, o2}, a[3] = {a0, a1, a2}, b[3] = {b0, b1, b2};
     double e[40];
     int m = 0;
@@ -105,6 +142,7 @@ static __device__ __noinline__ int orient_exact(float d0, float d1, float d2, fl
 // Components are picked with selects so no operand array is indexed by a variable.
 static __device__ __noinline__ int axis_det_exact(int k, float d0, float d1, float d2, float a0, float a1, float a2,
                                                   float b0, float b1, float b2) {
+    note_exact();
     const float di = k == 0 ? d1 : (k == 1 ? d2 : d0), dj = k == 0 ? d2 : (k == 1 ? d0 : d1);
     const float ai = k == 0 ? a1 : (k == 1 ? a2 : a0), aj = k == 0 ? a2 : (k == 1 ? a0 : a1);
     const float bi = k == 0 ? b1 : (k == 1 ? b2 : b0), bj = k == 0 ? b2 : (k == 1 ? b0 : b1);

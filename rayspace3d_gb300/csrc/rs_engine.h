@@ -55,5 +55,8 @@ constexpr int kMetaWords = 16;
 // Upper bound on the node visits of one traversal of a valid tree.
 inline uint32_t max_steps(const rs_bvh* b) { return (uint32_t)(2 * b->n_nodes + 8); }
 int to_status(cudaError_t e);
+// Recheck statistics of the translation units that run hit tests (see rs_device.cuh).
+int recheck_pim(int op, unsigned long long* out);
+int recheck_join(int op, unsigned long long* out);
 int status_from_bits(uint32_t bits);
 }  // namespace rs

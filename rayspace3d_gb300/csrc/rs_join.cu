@@ -40,8 +40,9 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
     const int32_t* src = sources + offsets[i];
     int32_t last[4] = {INT_MIN, INT_MIN, INT_MIN, INT_MIN};
     int lp = 0;
-    unsigned int crossings = 0;
+    unsigned int crossings = 0, tests = 0;
     const bool ok = traverse<-1>(nodes, max_steps, r, [&](int first, int cnt) {
+        tests += (unsigned int)cnt;
         for (int k = first; k < first + cnt; ++k) {
             float a[3], b[3], c[3];
             uint32_t tid;
@@ -62,6 +63,7 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
         }
     });
     if (!ok) atomicOr(table.status, ST_STACK_OVERFLOW);
+    add_tests(tests);
     if (table.stats) {
         atomicAdd(&table.stats[2], 1ull);
         if (crossings) atomicAdd(&table.stats[3], (unsigned long long)crossings);
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
     uint32_t hits[TRACK ? kTargets : 1];
     uint32_t lo = 0;
     bool bounded = false;
-    unsigned int crossings = 0, candidates = 0;
+    unsigned int crossings = 0, candidates = 0, tests = 0;
     int out = 0;
     for (;;) {
         uint32_t par = 0;  // parity bit per list entry
@@ -151,6 +153,7 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
                     if (id > mx) continue;
                 }
                 float t;
+                ++tests;
                 if (!hit_triangle<2>(r, a, b, c, t)) continue;
                 if (!bounded) ++crossings;
                 int j = 0;
@@ -199,6 +202,7 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
         lo = mx;
         bounded = true;
     }
+    add_tests(tests);
     if (table.stats) {
         atomicAdd(&table.stats[4], 1ull);
         if (crossings) atomicAdd(&table.stats[5], (unsigned long long)crossings);
@@ -208,6 +212,8 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
 }
 
 }  // namespace
+
+int recheck_join(int op, unsigned long long* out) { return recheck_op(op, out); }
 
 PairTable table_view(rs_pairset* ps) {
     PairTable t;

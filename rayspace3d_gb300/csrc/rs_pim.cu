@@ -152,7 +152,9 @@ __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint6
         return;
     }
     HitList hl;
+    unsigned int tests = 0;
     const bool ok = traverse<AXIS>(nodes, max_steps, r, [&](int first, int cnt) {
+        tests += (unsigned int)cnt;
         for (int k = first; k < first + cnt; ++k) {
             float a[3], b[3], c[3];
             uint32_t tid;
@@ -162,6 +164,7 @@ __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint6
             if (hit_triangle<AXIS>(r, a, b, c, t)) hl.add(t, tid, obj);
         }
     });
+    add_tests(tests);
     if (!ok) {
         atomicOr(status, ST_STACK_OVERFLOW);
         return;
@@ -235,6 +238,7 @@ __global__ void __launch_bounds__(kT) k_pim_grid(const float* __restrict__ pts, 
     const uint32_t pre = inc - cnt;
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
     __syncwarp();
+    add_tests(lane == 0 ? total : 0u);
     for (uint32_t base = 0; base < total; base += 32) {
         const uint32_t j = base + lane;
         // Owner of work item j: the last lane whose prefix is <= j.
@@ -599,6 +603,9 @@ __global__ void k_hit_scatter(const int32_t* __restrict__ obj, uint64_t n, const
 }
 
 }  // namespace
+
+int recheck_pim(int op, unsigned long long* out) { return recheck_op(op, out); }
+
 }  // namespace rs
 
 // ---------------------------------------------------------------------------

@@ -288,3 +288,25 @@ def test_containment_beyond_32_targets(cuda):
     api.containment(bt, api.DeviceGeometry(src), ps, swap=True)
     np.testing.assert_array_equal(np.sort(ps.finalize().cpu().numpy().astype(np.uint64)),
                                   bind.containment(src, tgt.vertices, tgt.indices, tgt.tri2obj, swap=True))
+
+
+def test_recheck_counters(cuda, golden):
+    """Points snapped onto shared cube edges and vertices need the exact path; the counters
+    see it, and results stay equal to the oracle's."""
+    L = _lib.load()
+    cubes = _geom(golden, "cubes_")
+    pts = golden["cubes_pts"]
+    L.rs_recheck_reset()
+    L.rs_recheck_enable(1)
+    try:
+        got = _gpu_pim(cubes, pts)
+    finally:
+        L.rs_recheck_enable(0)
+    ex, tests = ctypes.c_uint64(), ctypes.c_uint64()
+    assert L.rs_recheck_read(ctypes.byref(ex), ctypes.byref(tests)) == 0
+    np.testing.assert_array_equal(got, golden["cubes_z"])
+    assert tests.value > 0 and ex.value > 0
+    assert ex.value <= 3 * tests.value + 3 * 12 * len(pts)
+    L.rs_recheck_reset()
+    assert L.rs_recheck_read(ctypes.byref(ex), ctypes.byref(tests)) == 0
+    assert ex.value == 0 and tests.value == 0
