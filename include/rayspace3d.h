@@ -56,6 +56,15 @@ const char* rs_version(void);
 int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
                  const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream);
 int rs_bvh_destroy(rs_bvh* bvh);
+
+/* Asynchronous build (no counterpart in the reference): queues the same build on `stream`
+ * and returns at once.  Queries on any stream are ordered after the build automatically;
+ * rs_bvh_wait blocks until it is done and returns its status (RS_ERR_INVALID for
+ * out-of-range vertex indices, which rs_bvh_build reports directly).  Two builds on two
+ * streams run concurrently. */
+int rs_bvh_build_async(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                       const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream);
+int rs_bvh_wait(const rs_bvh* bvh);
 /* Number of triangles, nodes, engine-owned device bytes, and the bounds of all vertices. */
 int rs_bvh_info(const rs_bvh* bvh, uint64_t* n_tri, uint64_t* n_nodes, uint64_t* bytes,
                 float* h_min3, float* h_max3);
@@ -187,6 +196,13 @@ int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_ends
                     const rs_bvh* B, const float* d_startsB, const float* d_endsB, const int32_t* d_offsetsB,
                     const int32_t* d_countsB, const int32_t* d_sourcesB, uint64_t nEB,
                     int direction, int with_containment, rs_pairset* ps, void* stream);
+
+/* Broad phase of rs_overlap_join (no counterpart in the reference), on by default: each
+ * object's box is tested against the other set's triangle boxes, both widened by more
+ * than the edge payload's quantisation and the slab arithmetic's rounding; edges whose
+ * source objects overlap nothing are not traced.  The pair set is the same with it on or
+ * off; rs_set_overlap_cull(0) traces every edge. */
+int rs_set_overlap_cull(int on);
 
 /* Status text for a code. */
 const char* rs_status_string(int status);

@@ -36,6 +36,8 @@ SIGNATURES = {
     "rs_version": (ctypes.c_char_p, []),
     "rs_status_string": (ctypes.c_char_p, [I]),
     "rs_bvh_build": (I, [P, U64, P, U64, P, I, PP, P]),
+    "rs_bvh_build_async": (I, [P, U64, P, U64, P, I, PP, P]),
+    "rs_bvh_wait": (I, [P]),
     "rs_bvh_destroy": (I, [P]),
     "rs_bvh_info": (I, [P, PU64, PU64, PU64, P, P]),
     "rs_pim": (I, [P, P, U64, F, F, F, P, P, P]),
@@ -62,6 +64,7 @@ SIGNATURES = {
     "rs_profile_reset": (I, []),
     "rs_profile_read": (I, [I, ctypes.POINTER(ctypes.c_double), PU64]),
     "rs_recheck_enable": (I, [I]),
+    "rs_set_overlap_cull": (I, [I]),
     "rs_recheck_reset": (I, []),
     "rs_recheck_read": (I, [PU64, PU64]),
     "exclusive_scan_gpu": (ctypes.c_longlong, [P, P, I]),

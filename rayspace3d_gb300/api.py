@@ -77,12 +77,18 @@ class DeviceGeometry:
 class Bvh:
     """Engine-owned BVH over a DeviceGeometry (which must stay alive)."""
 
-    def __init__(self, geom: DeviceGeometry, leaf_size: int = 0, stream=None):
+    def __init__(self, geom: DeviceGeometry, leaf_size: int = 0, stream=None, asynchronous: bool = False):
+        """asynchronous=True queues the build on `stream` and returns at once (rs_bvh_build_async);
+        queries are ordered after it, wait() reports its status."""
         self.geom = geom
         h = ctypes.c_void_p()
-        _check(_lib.load().rs_bvh_build(_ptr(geom.V), geom.nV, _ptr(geom.I), geom.nF, _ptr(geom.T), leaf_size,
-                                        ctypes.byref(h), _stream(stream)), "rs_bvh_build")
+        fn = _lib.load().rs_bvh_build_async if asynchronous else _lib.load().rs_bvh_build
+        _check(fn(_ptr(geom.V), geom.nV, _ptr(geom.I), geom.nF, _ptr(geom.T), leaf_size, ctypes.byref(h),
+                  _stream(stream)), "rs_bvh_build")
         self.handle = h
+
+    def wait(self):
+        _check(_lib.load().rs_bvh_wait(self.handle), "rs_bvh_wait")
 
     def info(self):
         nt, nn, nb = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()

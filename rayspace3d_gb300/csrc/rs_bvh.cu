@@ -3,9 +3,9 @@
 // Replaces OptixAccelerationStructure::buildInternal
 // (query/src/optix/OptixAccelerationStructure.cpp:22-68), which builds one
 // triangle GAS over every triangle of a .pre set.  Steps:
-//   1. per-triangle boxes, scene bounds of triangle centres and of all vertices;
-//   2. keys = 32-bit Morton code of the centre (11/11/10 bits) << 32 | triangle id,
-//      unique by construction;
+//   1. bounds of all vertices;
+//   2. keys = 32-bit Morton code of each triangle box's centre (11/11/10 bits, in the
+//      vertex bounds) << 32 | triangle id, unique by construction;
 //   3. stable radix sort of the 32 Morton bits only (4 passes; ids stay ascending
 //      within equal codes);
 //   4. one bottom-up pass (k_build_up) that writes the triangles in leaf order
@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 
 #include "rs_engine.h"
@@ -54,7 +55,10 @@ __device__ __forceinline__ void block_minmax_atomic(float mn[3], float mx[3], in
     }
 }
 
-__global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, int* bounds) {
+// Bounds of all vertices (bounds[6..11]) and the largest object id (max_obj), grid-stride
+// with one atomic per warp.
+__global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, const int32_t* __restrict__ t2o,
+                                uint64_t nF, int* bounds, int* max_obj) {
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nV; i += (uint64_t)gridDim.x * blockDim.x) {
 #pragma unroll
@@ -65,6 +69,11 @@ __global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, int* b
         }
     }
     block_minmax_atomic(mn, mx, bounds + 6);
+    int mo = -1;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nF; t += (uint64_t)gridDim.x * blockDim.x)
+        mo = max(mo, t2o[t]);
+    mo = __reduce_max_sync(0xffffffffu, mo);
+    if ((threadIdx.x & 31) == 0 && mo >= 0) atomicMax(max_obj, mo);
 }
 
 // Indices are clamped so a malformed index buffer cannot read out of bounds; the
@@ -82,26 +91,6 @@ __device__ __forceinline__ void tri_box(const float* __restrict__ V, uint64_t nV
     }
 }
 
-__global__ void k_centroid_bounds(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I,
-                                  uint64_t nF, int* bounds, unsigned int* bad_index) {
-    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nF; t += (uint64_t)gridDim.x * blockDim.x) {
-        if (I[3 * t] >= nV || I[3 * t + 1] >= nV || I[3 * t + 2] >= nV) {
-            atomicOr(bad_index, 1u);
-            continue;
-        }
-        float lo[3], hi[3];
-        tri_box(V, nV, I, t, lo, hi);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float c = 0.5f * lo[k] + 0.5f * hi[k];
-            mn[k] = fminf(mn[k], c);
-            mx[k] = fmaxf(mx[k], c);
-        }
-    }
-    block_minmax_atomic(mn, mx, bounds);
-}
-
 __device__ __forceinline__ uint32_t spread10(uint32_t x) {
     x &= 0x3ffu;
     x = (x | (x << 16)) & 0x030000ffu;
@@ -111,26 +100,31 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
     return x;
 }
 
+// Keys of the triangles: the Morton code of the box centre quantised in the bounds of
+// all vertices, << 32 | triangle id.  Also flags out-of-range vertex indices.
 __global__ void k_morton(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I, uint64_t nF,
-                         const int* __restrict__ bounds, uint64_t* __restrict__ keys) {
+                         const int* __restrict__ bounds, uint64_t* __restrict__ keys,
+                         unsigned int* __restrict__ bad_index) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (t >= nF) return;
-    float lo[3], hi[3];
-    tri_box(V, nV, I, t, lo, hi);
-    uint32_t q[3];
-    const float scale[3] = {2048.0f, 2048.0f, 1024.0f};
+    if (t < nF) {
+        if (I[3 * t] >= nV || I[3 * t + 1] >= nV || I[3 * t + 2] >= nV) atomicOr(bad_index, 1u);
+        float lo[3], hi[3];
+        tri_box(V, nV, I, t, lo, hi);
+        uint32_t q[3];
+        const float scale[3] = {2048.0f, 2048.0f, 1024.0f};
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float cmin = ord_flt(bounds[k]), cmax = ord_flt(bounds[3 + k]);
-        const float ext = cmax - cmin;
-        const float c = 0.5f * lo[k] + 0.5f * hi[k];
-        float u = ext > 0.0f ? (c - cmin) / ext : 0.0f;
-        u = fminf(fmaxf(u, 0.0f), 1.0f);
-        q[k] = (uint32_t)fminf(u * scale[k], scale[k] - 1.0f);
+        for (int k = 0; k < 3; ++k) {
+            const float cmin = ord_flt(bounds[6 + k]), cmax = ord_flt(bounds[9 + k]);
+            const float ext = cmax - cmin;
+            const float c = 0.5f * lo[k] + 0.5f * hi[k];
+            float u = ext > 0.0f ? (c - cmin) / ext : 0.0f;
+            u = fminf(fmaxf(u, 0.0f), 1.0f);
+            q[k] = (uint32_t)fminf(u * scale[k], scale[k] - 1.0f);
+        }
+        const uint32_t code = ((q[0] >> 10) << 31) | ((q[1] >> 10) << 30) | (spread10(q[0]) << 2) |
+                              (spread10(q[1]) << 1) | spread10(q[2]);
+        keys[t] = ((uint64_t)code << 32) | (uint32_t)t;
     }
-    const uint32_t code = ((q[0] >> 10) << 31) | ((q[1] >> 10) << 30) | (spread10(q[0]) << 2) |
-                          (spread10(q[1]) << 1) | spread10(q[2]);
-    keys[t] = ((uint64_t)code << 32) | (uint32_t)t;
 }
 
 // Length of the common prefix of sorted keys i and i+1 (keys are distinct).
@@ -174,42 +168,119 @@ __device__ __forceinline__ void load_half(const BNode* nd, int side, float lo[3]
     }
 }
 
+__device__ __forceinline__ void store_node(BNode* nd, const float lo0[3], const float hi0[3], int i0, int c0,
+                                           const float lo1[3], const float hi1[3], int i1, int c1) {
+    nd->a = make_float4(lo0[0], lo0[1], lo0[2], hi0[0]);
+    nd->b = make_float4(hi0[1], hi0[2], lo1[0], lo1[1]);
+    nd->c = make_float4(lo1[2], hi1[0], hi1[1], hi1[2]);
+    nd->d = make_int4(i0, c0, i1, c1);
+}
+
 // Bottom-up construction of the binary radix tree over the sorted keys, fused with
 // the emission of the leaf-ordered triangles and the box refit (agglomerative LBVH,
 // Apetrei 2014, "Fast and Simple Agglomerative LBVH Construction").  Thread k starts
 // at leaf k with range [k, k].  A subtree [l, r] joins the neighbouring split whose
 // keys share the longer prefix: split r (it is the left child) or split l-1 (the
 // right child); a split with no neighbour on one side takes the other.  This yields
-// the same tree as Karras' top-down construction.  At split p the child writes its
-// box and entry into its half of node slot p+1, then exchanges its outer range bound
-// in xchg[p] with acquire-release semantics; the first arrival stops, the second reads
-// its sibling's half, merges the boxes and continues with the parent's range.
-// Subtrees of <= leaf_size triangles are entered as leaves (first triangle, count);
-// larger ones by their slot (count 0).  The subtree [0, n-1] is copied to slot 0.
+// the same tree as Karras' top-down construction.
+//
+// Merges inside a warp's 32 leaves run first, in lock-step rounds without memory
+// fences: a subtree is owned by the lane of its leftmost leaf, so a left child finds
+// its right sibling at lane r+1 and merges when that lane holds a complete subtree
+// that chose the same split; the split prefixes come from the lanes by shuffle.  The
+// rounds end when no merge happens.  The remaining subtrees meet their siblings across
+// warps: at split p the child writes its box and entry into its half of node slot
+// p+1, then exchanges its outer range bound in xchg[p] with acquire-release
+// semantics; the first arrival stops, the second reads its sibling's half, merges and
+// continues.  Every split therefore sees exactly one merge, in the warp or through
+// xchg.  Subtrees of <= leaf_size triangles are entered as leaves (first triangle,
+// count), larger ones by their slot (count 0); slot 0 receives the root.
 __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, uint64_t nV,
                                                  const uint32_t* __restrict__ I, const int32_t* __restrict__ t2o,
                                                  const uint64_t* __restrict__ keys, int n, int leaf_size,
                                                  float4* __restrict__ tris, BNode* __restrict__ nodes,
                                                  int* __restrict__ xchg) {
+    __shared__ int s_absorbed[kT];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t t = (uint32_t)(__ldg(&keys[k]) & 0xffffffffull);
-    const uint64_t last = nV - 1;
-    const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last), i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
-                   i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
-    float a[3], b[3], c[3], lo[3], hi[3];
+    const int lane = threadIdx.x & 31;
+    const int base = k - lane;
+    const bool valid = k < n;
+    float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+    if (valid) {
+        const uint32_t t = (uint32_t)(__ldg(&keys[k]) & 0xffffffffull);
+        const uint64_t last = nV - 1;
+        const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last),
+                       i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
+                       i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
+        float a[3], b[3], c[3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        a[q] = V[3 * i0 + q];
-        b[q] = V[3 * i1 + q];
-        c[q] = V[3 * i2 + q];
-        lo[q] = fminf(fminf(a[q], b[q]), c[q]);
-        hi[q] = fmaxf(fmaxf(a[q], b[q]), c[q]);
+        for (int q = 0; q < 3; ++q) {
+            a[q] = V[3 * i0 + q];
+            b[q] = V[3 * i1 + q];
+            c[q] = V[3 * i2 + q];
+            lo[q] = fminf(fminf(a[q], b[q]), c[q]);
+            hi[q] = fmaxf(fmaxf(a[q], b[q]), c[q]);
+        }
+        tris[3 * (uint64_t)k] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
+        tris[3 * (uint64_t)k + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
+        tris[3 * (uint64_t)k + 2] = make_float4(c[0], c[1], c[2], 0.0f);
     }
-    tris[3 * (uint64_t)k] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
-    tris[3 * (uint64_t)k + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
-    tris[3 * (uint64_t)k + 2] = make_float4(c[0], c[1], c[2], 0.0f);
+    // Split prefixes: lane j holds split base+j; split base-1 is broadcast.
+    const int d_own = (k < n - 1) ? split_prefix(keys, k) : -1;
+    const int d_left = __shfl_sync(0xffffffffu, (lane == 0 && base > 0 && base - 1 < n - 1) ? split_prefix(keys, base - 1)
+                                                                                          : -1, 0);
     int l = k, r = k, self = 0;
+    bool active = valid;
+    for (;;) {
+        // Choose the parent split of the owned subtree (only meaningful when active).
+        const bool root = active && l == 0 && r == n - 1;
+        const int dr = __shfl_sync(0xffffffffu, d_own, min(max(r - base, 0), 31));
+        const int dl_in = __shfl_sync(0xffffffffu, d_own, min(max(l - 1 - base, 0), 31));
+        const int dl = (l - 1 == base - 1) ? d_left : dl_in;
+        const bool left_child = (l == 0) ? true : (r == n - 1) ? false : dr > dl;
+        // Sibling of a left child: the subtree owned by lane r+1-base.
+        const int sl = min(max(r + 1 - base, 0), 31);
+        const int o_active = __shfl_sync(0xffffffffu, (int)(active && !root), sl);
+        const int o_l = __shfl_sync(0xffffffffu, l, sl);
+        const int o_r = __shfl_sync(0xffffffffu, r, sl);
+        const int o_left = __shfl_sync(0xffffffffu, (int)left_child, sl);
+        const int o_self = __shfl_sync(0xffffffffu, self, sl);
+        float olo[3], ohi[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            olo[q] = __shfl_sync(0xffffffffu, lo[q], sl);
+            ohi[q] = __shfl_sync(0xffffffffu, hi[q], sl);
+        }
+        const bool merge = active && !root && left_child && r + 1 - base <= 31 && o_active && o_l == r + 1 && !o_left;
+        s_absorbed[threadIdx.x] = 0;
+        __syncwarp();
+        if (merge) s_absorbed[threadIdx.x - lane + (r + 1 - base)] = 1;
+        __syncwarp();
+        const bool absorbed = s_absorbed[threadIdx.x] != 0;
+        __syncwarp();
+        if (merge) {
+            const int p = r;
+            const int size0 = r - l + 1, size1 = o_r - o_l + 1;
+            store_node(nodes + (p + 1), lo, hi, size0 <= leaf_size ? l : self, size0 <= leaf_size ? size0 : 0, olo,
+                       ohi, size1 <= leaf_size ? o_l : o_self, size1 <= leaf_size ? size1 : 0);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                lo[q] = fminf(lo[q], olo[q]);
+                hi[q] = fmaxf(hi[q], ohi[q]);
+            }
+            r = o_r;
+            self = p + 1;
+            if (l == 0 && r == n - 1) {
+                const BNode nd = nodes[self];
+                nodes[0] = nd;
+                active = false;
+            }
+        }
+        if (absorbed) active = false;
+        if (!__any_sync(0xffffffffu, merge)) break;
+    }
+    if (!active) return;
+    // Cross-warp merges through the exchange array.
     for (;;) {
         const int size = r - l + 1;
         if (l == 0 && r == n - 1) {
@@ -296,80 +367,24 @@ int status_from_bits(uint32_t bits) {
 
 using namespace rs;
 
-extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
-                            const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream) {
-    if (!out) return RS_ERR_INVALID;
-    *out = nullptr;
-    if ((nF && (!d_indices || !d_tri2obj || !d_vertices)) || (nV && !d_vertices)) return RS_ERR_INVALID;
-    if (nF && nV == 0) return RS_ERR_INVALID;               // every index would be out of range
-    if (nF >= (uint64_t)0x7fffffff) return RS_ERR_INVALID;  // node/leaf indices are int32
-    if (leaf_size == 0) leaf_size = 4;
-    if (leaf_size < 1 || leaf_size > 8) return RS_ERR_INVALID;
-    cudaStream_t s = (cudaStream_t)stream;
-    rs_bvh* h = new rs_bvh();
-    h->V = d_vertices;
-    h->nV = nV;
-    h->I = d_indices;
-    h->nF = nF;
-    h->t2o = d_tri2obj;
-    h->leaf_size = leaf_size;
-    cudaGetDevice(&h->device);
-    const int n = (int)nF;
-    int* bounds = nullptr;  // 12 ordered-int bounds, then the bad-index flag
-    uint64_t* keys = nullptr;
-    int* xchg = nullptr;
-    cudaError_t e = cudaSuccess;
-    int hb[13];
-    const int grid = 4 * sm_count();
-    h->n_nodes = n >= 2 ? (uint64_t)n : 1;  // slot 0 = root, slot p+1 = split p
-    h->n_tris = (uint64_t)n;
-    const int ptok = prof_begin(P_BVH_BUILD, s);
-    e = alloc(&h->nodes, h->n_nodes, s);
-    if (e == cudaSuccess) e = alloc(&h->tris, 3 * (size_t)n, s);
-    if (e == cudaSuccess) e = alloc(&bounds, 13, s);
-    if (e != cudaSuccess) goto fail;
-    launch(k_init_bounds, 1, 32, 0, s, bounds);
-    cudaMemsetAsync(bounds + 12, 0, sizeof(int), s);
-    if (nV) launch(k_vertex_bounds, grid, kT, 0, s, d_vertices, nV, bounds);
-    if (nF) launch(k_centroid_bounds, grid, kT, 0, s, d_vertices, nV, d_indices, nF, bounds,
-                   reinterpret_cast<unsigned int*>(bounds + 12));
-    if (n <= 1) {
-        launch(k_small_root, 1, 1, 0, s, d_vertices, nV, d_indices, n, h->nodes);
-        if (n == 1) {
-            e = alloc(&keys, 1, s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(keys, 0, sizeof(uint64_t), s);
-            if (e == cudaSuccess) launch(k_emit_tris, 1, 32, 0, s, d_vertices, nV, d_indices, d_tri2obj,
-                                         (const uint64_t*)keys, 1, h->tris);
-        }
-    } else {
-        const int nb = (n + kT - 1) / kT;
-        e = alloc(&keys, n, s);
-        if (e == cudaSuccess) e = alloc(&xchg, n - 1, s);
-        if (e != cudaSuccess) goto fail;
-        launch(k_morton, nb, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys);
-        e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32);
-        if (e != cudaSuccess) goto fail;
-        cudaMemsetAsync(xchg, 0xff, (size_t)(n - 1) * sizeof(int), s);
-        launch(k_build_up, nb, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys, n, leaf_size,
-               h->tris, h->nodes, xchg);
-    }
-    prof_end(P_BVH_BUILD, s, ptok);
-    e = cudaGetLastError();
-    // One host round trip: vertex bounds for the filter box and the bad-index flag.
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    prof_collect();
-fail:
-    if (bounds) cudaFreeAsync(bounds, s);
-    if (keys) cudaFreeAsync(keys, s);
-    if (xchg) cudaFreeAsync(xchg, s);
-    const bool bad = (e == cudaSuccess) && hb[12] != 0;
-    if (e != cudaSuccess || bad) {
-        if (h->nodes) cudaFreeAsync(h->nodes, s);
-        if (h->tris) cudaFreeAsync(h->tris, s);
-        cudaStreamSynchronize(s);
-        delete h;
-        return bad ? RS_ERR_INVALID : to_status(e);
+namespace rs {
+
+std::mutex g_bvh_mu;
+
+// Reads an asynchronous build's result words once the build has finished: vertex bounds,
+// object count and the bad-index flag.  Returns the build's status.
+int bvh_ready(const rs_bvh* ch) {
+    rs_bvh* h = const_cast<rs_bvh*>(ch);
+    std::lock_guard<std::mutex> g(g_bvh_mu);
+    if (!h->pending) return h->build_status;
+    int hb[14];
+    cudaError_t e = cudaEventSynchronize(h->done);
+    if (e == cudaSuccess) std::memcpy(hb, h->pending, sizeof(hb));
+    pinned_slot_release(h->pending);
+    h->pending = nullptr;
+    if (e != cudaSuccess) {
+        h->build_status = to_status(e);
+        return h->build_status;
     }
     for (int k = 0; k < 3; ++k) {
         auto dec = [](int i) {
@@ -381,8 +396,142 @@ fail:
         h->vmin[k] = dec(hb[6 + k]);
         h->vmax[k] = dec(hb[9 + k]);
     }
+    h->n_obj = hb[13] >= 0 ? (uint64_t)hb[13] + 1 : 0;
+    h->build_status = hb[12] != 0 ? RS_ERR_INVALID : RS_OK;
+    return h->build_status;
+}
+
+// Orders work queued on stream s after the handle's build.
+int bvh_use(const rs_bvh* h, cudaStream_t s) {
+    if (h->build_status != RS_OK) return h->build_status;
+    if (h->done && cudaStreamWaitEvent(s, h->done, 0) != cudaSuccess) return RS_ERR_CUDA;
+    return RS_OK;
+}
+
+static void bvh_free(rs_bvh* h) {
+    if (h->done) cudaEventSynchronize(h->done);
+    pinned_slot_release(h->pending);
+    if (h->nodes) cudaFree(h->nodes);
+    if (h->tris) cudaFree(h->tris);
+    for (auto& g : h->cgrid) {
+        if (g.start) cudaFree(g.start);
+        if (g.list) cudaFree(g.list);
+    }
+    if (h->done) cudaEventDestroy(h->done);
+    delete h;
+}
+
+static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                      const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, cudaStream_t s, bool async) {
+
+    if (!out) return RS_ERR_INVALID;
+    *out = nullptr;
+    if ((nF && (!d_indices || !d_tri2obj || !d_vertices)) || (nV && !d_vertices)) return RS_ERR_INVALID;
+    if (nF && nV == 0) return RS_ERR_INVALID;               // every index would be out of range
+    if (nF >= (uint64_t)0x7fffffff) return RS_ERR_INVALID;  // node/leaf indices are int32
+    if (leaf_size == 0) leaf_size = 4;
+    if (leaf_size < 1 || leaf_size > 8) return RS_ERR_INVALID;
+    rs_bvh* h = new rs_bvh();
+    h->V = d_vertices;
+    h->nV = nV;
+    h->I = d_indices;
+    h->nF = nF;
+    h->t2o = d_tri2obj;
+    h->leaf_size = leaf_size;
+    cudaGetDevice(&h->device);
+    const int n = (int)nF;
+    int* bounds = nullptr;  // [6..11] vertex bounds (ordered ints), [12] bad-index flag, [13] max object
+    uint64_t* keys = nullptr;
+    int* xchg = nullptr;
+    cudaError_t e = cudaSuccess;
+    int* slot = nullptr;
+    const int grid = 4 * sm_count();
+    h->n_nodes = n >= 2 ? (uint64_t)n : 1;  // slot 0 = root, slot p+1 = split p
+    h->n_tris = (uint64_t)n;
+    const int ptok = prof_begin(P_BVH_BUILD, s);
+    e = alloc(&h->nodes, h->n_nodes, s);
+    if (e == cudaSuccess) e = alloc(&h->tris, 3 * (size_t)n, s);
+    if (e == cudaSuccess) e = alloc(&bounds, 14, s);
+    if (e != cudaSuccess) goto fail;
+    launch(k_init_bounds, 1, 32, 0, s, bounds);
+    cudaMemsetAsync(bounds + 12, 0, sizeof(int), s);
+    cudaMemsetAsync(bounds + 13, 0xff, sizeof(int), s);
+    if (nV || nF) launch(k_vertex_bounds, grid, kT, 0, s, d_vertices, nV, d_tri2obj, nF, bounds, bounds + 13);
+    if (n <= 1) {
+        launch(k_small_root, 1, 1, 0, s, d_vertices, nV, d_indices, n, h->nodes);
+        if (n == 1) {
+            e = alloc(&keys, 1, s);
+            if (e == cudaSuccess) launch(k_morton, 1, 32, 0, s, d_vertices, nV, d_indices, nF, bounds, keys,
+                                         reinterpret_cast<unsigned int*>(bounds + 12));
+            if (e == cudaSuccess) launch(k_emit_tris, 1, 32, 0, s, d_vertices, nV, d_indices, d_tri2obj,
+                                         (const uint64_t*)keys, 1, h->tris);
+        }
+    } else {
+        const int nb = (n + kT - 1) / kT;
+        e = alloc(&keys, n, s);
+        if (e == cudaSuccess) e = alloc(&xchg, n - 1, s);
+        if (e != cudaSuccess) goto fail;
+        launch(k_morton, nb, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys,
+               reinterpret_cast<unsigned int*>(bounds + 12));
+        e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32);
+        if (e != cudaSuccess) goto fail;
+        cudaMemsetAsync(xchg, 0xff, (size_t)(n - 1) * sizeof(int), s);
+        launch(k_build_up, nb, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys, n, leaf_size,
+               h->tris, h->nodes, xchg);
+    }
+    prof_end(P_BVH_BUILD, s, ptok);
+    e = cudaGetLastError();
+    // The result words go to a pinned slot, read by bvh_ready() after the build's event.
+    if (e == cudaSuccess) {
+        slot = pinned_slot_acquire();
+        if (!slot) e = cudaErrorMemoryAllocation;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(slot, bounds, 14 * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
+fail:
+    if (keys) cudaFreeAsync(keys, s);
+    if (xchg) cudaFreeAsync(xchg, s);
+    if (bounds) cudaFreeAsync(bounds, s);
+    if (e != cudaSuccess) {
+        if (h->nodes) cudaFreeAsync(h->nodes, s);
+        if (h->tris) cudaFreeAsync(h->tris, s);
+        h->nodes = nullptr;
+        h->tris = nullptr;
+        cudaStreamSynchronize(s);
+        pinned_slot_release(slot);
+        if (h->done) cudaEventDestroy(h->done);
+        delete h;
+        return to_status(e);
+    }
+    h->pending = slot;
+    if (!async) {
+        const int st = bvh_ready(h);
+        prof_collect();
+        if (st != RS_OK) {
+            bvh_free(h);
+            return st;
+        }
+    }
     *out = h;
     return RS_OK;
+}
+
+}  // namespace rs
+
+extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                            const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream) {
+    return rs::build_impl(d_vertices, nV, d_indices, nF, d_tri2obj, leaf_size, out, (cudaStream_t)stream, false);
+}
+
+extern "C" int rs_bvh_build_async(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                                  const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream) {
+    return rs::build_impl(d_vertices, nV, d_indices, nF, d_tri2obj, leaf_size, out, (cudaStream_t)stream, true);
+}
+
+extern "C" int rs_bvh_wait(const rs_bvh* bvh) {
+    if (!bvh) return RS_ERR_INVALID;
+    return rs::bvh_ready(bvh);
 }
 
 extern "C" int rs_bvh_destroy(rs_bvh* bvh) {
@@ -390,20 +539,16 @@ extern "C" int rs_bvh_destroy(rs_bvh* bvh) {
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(bvh->device);
-    if (bvh->nodes) cudaFree(bvh->nodes);
-    if (bvh->tris) cudaFree(bvh->tris);
-    for (auto& g : bvh->cgrid) {
-        if (g.start) cudaFree(g.start);
-        if (g.list) cudaFree(g.list);
-    }
+    rs::bvh_free(bvh);
     cudaSetDevice(prev);
-    delete bvh;
     return RS_OK;
 }
 
 extern "C" int rs_bvh_info(const rs_bvh* bvh, uint64_t* n_tri, uint64_t* n_nodes, uint64_t* bytes,
                            float* h_min3, float* h_max3) {
     if (!bvh) return RS_ERR_INVALID;
+    const int st = rs::bvh_ready(bvh);
+    if (st != RS_OK) return st;
     if (n_tri) *n_tri = bvh->n_tris;
     if (n_nodes) *n_nodes = bvh->n_nodes;
     if (bytes) *bytes = bvh->n_nodes * sizeof(BNode) + bvh->n_tris * 3 * sizeof(float4);

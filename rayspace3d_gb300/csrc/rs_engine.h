@@ -35,7 +35,15 @@ struct rs_bvh {
     // Bounds of all vertices (the reference's BoundingBox::computeFromGeometry).
     float vmin[3] = {0, 0, 0};
     float vmax[3] = {0, 0, 0};
+    // Largest object id + 1 over the triangles (0 when there are none).
+    uint64_t n_obj = 0;
     int device = 0;
+    // Completion of the build, and its device result words until bvh_ready() has read
+    // them (asynchronous builds); the fields above that come from them (vmin, vmax,
+    // n_obj) are valid only after bvh_ready().
+    cudaEvent_t done = nullptr;
+    int* pending = nullptr;
+    int build_status = RS_OK;
 };
 
 struct rs_pairset {
@@ -55,6 +63,17 @@ constexpr int kMetaWords = 16;
 // Upper bound on the node visits of one traversal of a valid tree.
 inline uint32_t max_steps(const rs_bvh* b) { return (uint32_t)(2 * b->n_nodes + 8); }
 int to_status(cudaError_t e);
+// Asynchronous builds: bvh_ready() waits for the build and reads its host-side results
+// (returns the build status); bvh_use() orders stream s after the build.
+int bvh_ready(const rs_bvh* h);
+int bvh_use(const rs_bvh* h, cudaStream_t s);
+// Broad-phase flags for one edge direction: cand[o] != 0 for source objects o that may
+// have a partner; no culling when cand is null.
+struct EdgeCull {
+    const uint8_t* cand = nullptr;
+    uint64_t n_obj = 0;
+};
+
 // Recheck statistics of the translation units that run hit tests (see rs_device.cuh).
 int recheck_pim(int op, unsigned long long* out);
 int recheck_join(int op, unsigned long long* out);

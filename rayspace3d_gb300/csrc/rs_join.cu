@@ -25,9 +25,22 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
                                                   const int32_t* __restrict__ counts,
                                                   const int32_t* __restrict__ sources, uint64_t nE,
                                                   const BNode* __restrict__ nodes, uint32_t max_steps,
-                                                  const float4* __restrict__ tris, int swap, PairTable table) {
+                                                  const float4* __restrict__ tris, int swap, PairTable table,
+                                                  const uint8_t* __restrict__ cull, uint64_t n_cull) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= nE) return;
+    if (cull) {
+        // Broad phase: an edge whose source objects have no candidate partner cannot
+        // cross a target triangle (see k_cull_query).
+        const int ns = counts[i];
+        const int32_t* sp = sources + offsets[i];
+        bool any = false;
+        for (int q = 0; q < ns && !any; ++q) {
+            const int32_t so = sp[q];
+            any = (so < 0 || (uint64_t)so >= n_cull) ? true : cull[so] != 0;
+        }
+        if (!any) return;
+    }
     const float sx = starts[3 * i], sy = starts[3 * i + 1], sz = starts[3 * i + 2];
     const float ex = ends[3 * i], ey = ends[3 * i + 1], ez = ends[3 * i + 2];
     // distance3f / normalize3f of mesh_overlap_edges.cu:47-60 as individually rounded operations.
@@ -89,6 +102,144 @@ __global__ void k_max_obj(const int32_t* __restrict__ t2o, uint64_t nF, int* __r
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+// --- broad phase of the overlap join ---------------------------------------------------
+//
+// If the slab test of an edge ray passes for a triangle box, each coordinate range of
+// the ray's segment [1e-6, len + 1e-6] comes within 1.1e-6 + 7u*L of that box (u =
+// 2^-24, L = edge length; the slab, direction and length arithmetic rounds at most
+// seven times relative to L).  The segment lies in the box of every source object of
+// the edge up to the edge payload's 1e-5 endpoint quantisation (a shared edge carries
+// its first object's endpoints).  Boxes are therefore compared widened: the triangle
+// box by kCullRel * (largest |coordinate| + extent) per axis, the object box by that
+// and kCullAbs; the sum covers 1.2e-5 + 7u*L more than five times over (L <= the
+// object box's extent).  An object whose widened box overlaps no widened triangle box
+// of the other set cannot be the source of a pair, so its edges are not traced.  Each
+// set's flags come from its own objects' queries against the other set's BVH.
+
+constexpr float kCullAbs = 1e-4f;
+constexpr float kCullRel = 4e-6f;
+constexpr int kCullBudget = 256;  // BVH nodes one object's query may visit before giving up
+
+__global__ void k_obj_box_init(int* __restrict__ box, uint64_t n_obj) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < 6 * n_obj) box[i] = (i % 6) < 3 ? 0x7fffffff : (int)0x80000000;
+}
+
+__device__ __forceinline__ int f2ord(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+// Object boxes from the leaf-ordered triangles (consecutive leaves mostly share an
+// object, so lanes with equal objects reduce first and one lane updates the box).
+__global__ void k_obj_boxes(const float4* __restrict__ tris, uint64_t n, int* __restrict__ box, uint64_t n_obj) {
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 p = __ldg(&tris[3 * k]), q = __ldg(&tris[3 * k + 1]), r = __ldg(&tris[3 * k + 2]);
+    const int32_t obj = __float_as_int(q.w);
+    int v[6] = {f2ord(fminf(fminf(p.x, q.x), r.x)), f2ord(fminf(fminf(p.y, q.y), r.y)),
+                f2ord(fminf(fminf(p.z, q.z), r.z)), f2ord(fmaxf(fmaxf(p.x, q.x), r.x)),
+                f2ord(fmaxf(fmaxf(p.y, q.y), r.y)), f2ord(fmaxf(fmaxf(p.z, q.z), r.z))};
+    const unsigned int peers = __match_any_sync(__activemask(), obj);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        v[c] = __reduce_min_sync(peers, v[c]);
+        v[3 + c] = __reduce_max_sync(peers, v[3 + c]);
+    }
+    if ((int)(threadIdx.x & 31) != __ffs(peers) - 1) return;
+    if (obj < 0 || (uint64_t)obj >= n_obj) return;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        atomicMin(&box[6 * (uint64_t)obj + c], v[c]);
+        atomicMax(&box[6 * (uint64_t)obj + 3 + c], v[3 + c]);
+    }
+}
+
+__device__ __forceinline__ float cull_margin(float l, float h) {
+    return kCullRel * (fmaxf(fabsf(l), fabsf(h)) + (h - l));
+}
+
+// [l, h] widened by its margin overlaps the (already widened) query box.
+__device__ __forceinline__ bool cull_overlap(float l0, float l1, float l2, float h0, float h1, float h2,
+                                             const float* qlo, const float* qhi) {
+    const float m0 = cull_margin(l0, h0), m1 = cull_margin(l1, h1), m2 = cull_margin(l2, h2);
+    return l0 - m0 <= qhi[0] && h0 + m0 >= qlo[0] && l1 - m1 <= qhi[1] && h1 + m1 >= qlo[1] &&
+           l2 - m2 <= qhi[2] && h2 + m2 >= qlo[2];
+}
+
+// One thread per object of one set: does its widened box overlap any widened triangle
+// box of the other set's BVH?  cand[o] = 1 on the first overlap, or when the query runs
+// out of its node budget or stack; 0 otherwise.  Node boxes contain their triangles'
+// boxes and the widening grows with the box, so node culling is conservative.
+__global__ void k_cull_query(const int* __restrict__ box, uint64_t n_obj, const BNode* __restrict__ nodes,
+                             uint32_t max_steps, const float4* __restrict__ tris, uint8_t* __restrict__ cand) {
+    const uint64_t a = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (a >= n_obj) return;
+    float qlo[3], qhi[3];
+    bool empty = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float l = ord2f(box[6 * a + c]), h = ord2f(box[6 * a + 3 + c]);
+        empty |= !(l <= h);
+        const float m = kCullAbs + cull_margin(l, h);
+        qlo[c] = l - m;
+        qhi[c] = h + m;
+    }
+    if (empty) {  // no triangle of this object, hence no edges
+        cand[a] = 0;
+        return;
+    }
+    int stack[kStack];
+    int sp = 0, node = 0;
+    uint8_t result = 0;
+    for (uint32_t step = 0;; ++step) {
+        if (step > max_steps || step > (uint32_t)kCullBudget) {
+            result = 1;
+            break;
+        }
+        const float4 na = __ldg(&nodes[node].a), nb = __ldg(&nodes[node].b), nc = __ldg(&nodes[node].c);
+        const int4 nd = __ldg(&nodes[node].d);
+        bool h0 = cull_overlap(na.x, na.y, na.z, na.w, nb.x, nb.y, qlo, qhi);
+        bool h1 = cull_overlap(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, qlo, qhi);
+#pragma unroll 1
+        for (int side = 0; side < 2 && !result; ++side) {
+            const bool h = side == 0 ? h0 : h1;
+            const int first = side == 0 ? nd.x : nd.z, cnt = side == 0 ? nd.y : nd.w;
+            if (!h || cnt == 0) continue;
+            for (int k = first; k < first + cnt; ++k) {
+                const float4 p = __ldg(&tris[3 * (size_t)k]), q = __ldg(&tris[3 * (size_t)k + 1]),
+                             r = __ldg(&tris[3 * (size_t)k + 2]);
+                if (cull_overlap(fminf(fminf(p.x, q.x), r.x), fminf(fminf(p.y, q.y), r.y),
+                                 fminf(fminf(p.z, q.z), r.z), fmaxf(fmaxf(p.x, q.x), r.x),
+                                 fmaxf(fmaxf(p.y, q.y), r.y), fmaxf(fmaxf(p.z, q.z), r.z), qlo, qhi)) {
+                    result = 1;
+                    break;
+                }
+            }
+        }
+        if (result) break;
+        if (nd.y > 0) h0 = false;
+        if (nd.w > 0) h1 = false;
+        if (h0 && h1) {
+            if (sp == kStack) {
+                result = 1;
+                break;
+            }
+            stack[sp++] = nd.z;
+            node = nd.x;
+        } else if (h0) {
+            node = nd.x;
+        } else if (h1) {
+            node = nd.z;
+        } else {
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    cand[a] = result;
 }
 
 // Optional per-source outputs of the containment pass (the reference's pair-hit and
@@ -235,14 +386,29 @@ namespace rs {
 // Launches one edge-ray direction without waiting for it (status lands in the table's meta word).
 cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const float* d_ends,
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
-                            int swap, rs_pairset* ps, cudaStream_t s) {
+                            int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull) {
     if (nE == 0 || target->n_tris == 0) return cudaSuccess;
     const unsigned grid = (unsigned)((nE + kT - 1) / kT);
     const int ptok = prof_begin(P_EDGE_JOIN, s);
     launch(k_edge_join, grid, kT, 0, s, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, target->nodes,
-           max_steps(target), target->tris, swap, table_view(ps));
+           max_steps(target), target->tris, swap, table_view(ps), (const uint8_t*)cull.cand, cull.n_obj);
     prof_end(P_EDGE_JOIN, s, ptok);
     return cudaGetLastError();
+}
+
+// Broad-phase flags of `src`'s objects against `other`'s BVH (one query per object).
+cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cudaStream_t s) {
+    int* box = nullptr;
+    cudaError_t e = dmalloc((void**)&box, 6 * src->n_obj * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    launch(k_obj_box_init, (unsigned)((6 * src->n_obj + 255) / 256), 256, 0, s, box, src->n_obj);
+    launch(k_obj_boxes, (unsigned)((src->n_tris + 255) / 256), 256, 0, s, (const float4*)src->tris, src->n_tris,
+           box, src->n_obj);
+    launch(k_cull_query, (unsigned)((src->n_obj + kT - 1) / kT), kT, 0, s, (const int*)box, src->n_obj,
+           (const BNode*)other->nodes, max_steps(other), (const float4*)other->tris, cand);
+    e = cudaGetLastError();
+    cudaFreeAsync(box, s);
+    return e;
 }
 
 // Waits for the stream and turns the table's status bits into an rs_status.
@@ -263,7 +429,10 @@ extern "C" int rs_edge_join(const rs_bvh* target, const float* d_starts, const f
     if (!target || !ps || (nE && (!d_starts || !d_ends || !d_offsets || !d_counts || !d_sources)))
         return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = edge_join_async(target, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, swap, ps, s);
+    const int st = bvh_use(target, s);
+    if (st != RS_OK) return st;
+    cudaError_t e = edge_join_async(target, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, swap, ps, s,
+                                    EdgeCull{});
     return table_status(ps, s, e);
 }
 
@@ -272,6 +441,8 @@ static int containment_impl(const rs_bvh* target, const float* d_src_vertices, u
                             rs_pairset* ps, const Tracking* trk, uint64_t trk_capacity, cudaStream_t s) {
     if (!target || !ps || (src_nF && (!d_src_vertices || !d_src_indices || !d_src_tri2obj))) return RS_ERR_INVALID;
     if (src_nF == 0 || target->n_tris == 0) return RS_OK;
+    const int st = bvh_use(target, s);
+    if (st != RS_OK) return st;
     int* dmx = nullptr;
     int32_t* first = nullptr;
     int hmx = -1;

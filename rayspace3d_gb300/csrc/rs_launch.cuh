@@ -33,6 +33,9 @@ enum ProfId { P_EDGE_JOIN = 0, P_CONTAINMENT = 1, P_PIM = 2, P_BVH_BUILD = 3, P_
 // Records an event pair around one launch when profiling is on; prof_collect()
 // (called after the stream has been synchronised) accumulates the elapsed time.
 int prof_begin(int id, cudaStream_t s);          // returns a token for prof_end
+// Pinned host slots of 16 ints (nullptr when pinned memory is unavailable).
+int* pinned_slot_acquire();
+void pinned_slot_release(int* p);
 void prof_end(int id, cudaStream_t s, int token);
 void prof_collect();
 

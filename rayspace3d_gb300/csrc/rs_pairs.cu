@@ -18,7 +18,9 @@ namespace rs {
 PairTable table_view(rs_pairset* ps);
 cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const float* d_ends,
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
-                            int swap, rs_pairset* ps, cudaStream_t s);
+                            int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull);
+cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cudaStream_t s);
+bool g_overlap_cull = true;
 int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e);
 
 namespace {
@@ -179,6 +181,31 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
     const bool a2b = direction == 0 || direction == 1;
     const bool b2a = direction == 0 || direction == 2;
     cudaStream_t s = (cudaStream_t)stream;
+    {
+        int st = bvh_ready(A);  // the broad phase needs the object counts
+        if (st == RS_OK) st = bvh_ready(B);
+        if (st == RS_OK) st = bvh_use(A, s);
+        if (st == RS_OK) st = bvh_use(B, s);
+        if (st != RS_OK) return st;
+    }
+    // Broad phase once per call (it does not depend on the table, so reruns after growth
+    // reuse it): object boxes of each set against the other set's triangle boxes.
+    uint8_t* cand = nullptr;  // [A objects | B objects]
+    EdgeCull cullA, cullB;
+    if (g_overlap_cull && A->n_obj && B->n_obj && A->n_tris && B->n_tris) {
+        cudaError_t e = dmalloc((void**)&cand, A->n_obj + B->n_obj, s);
+        if (e == cudaSuccess && a2b) e = cull_async(A, B, cand, s);
+        if (e == cudaSuccess && b2a) e = cull_async(B, A, cand + A->n_obj, s);
+        if (e == cudaSuccess) {
+            if (a2b) cullA = EdgeCull{cand, A->n_obj};
+            if (b2a) cullB = EdgeCull{cand + A->n_obj, B->n_obj};
+        } else {
+            cudaGetLastError();  // culling is an optimisation: run without it
+        }
+    }
+    auto release = [&]() {
+        if (cand) cudaFreeAsync(cand, s);
+    };
     for (int attempt = 0; attempt < 8; ++attempt) {
         // Order of executeHashQuery (raytracer_intersection_estimated_main.cpp:107-158): overlap A->B,
         // overlap B->A, containment A->B, containment B->A.  The two edge directions are queued
@@ -186,23 +213,35 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
         cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
         if (e == cudaSuccess && a2b)
-            e = edge_join_async(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s);
+            e = edge_join_async(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s, cullA);
         if (e == cudaSuccess && b2a)
-            e = edge_join_async(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, s);
+            e = edge_join_async(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, s, cullB);
         int st = table_status(ps, s, e);
         if (with_containment) {
             if (st == RS_OK && a2b) st = rs_containment(B, A->V, A->nV, A->I, A->nF, A->t2o, 0, ps, stream);
             if (st == RS_OK && b2a) st = rs_containment(A, B->V, B->nV, B->I, B->nF, B->t2o, 1, ps, stream);
         }
-        if (st != RS_ERR_TABLE_FULL) return st;
+        if (st != RS_ERR_TABLE_FULL) {
+            release();
+            return st;
+        }
         // Grow and rerun: the table keeps the hashing variant, with four times the slots.
         uint64_t cap = ps->capacity * 4;
         if (!ps->pow2 && cap % 2 == 0) cap += 1;
-        if (cap > (1ull << 34)) return RS_ERR_TABLE_FULL;
+        if (cap > (1ull << 34)) break;
         e = alloc_slots(ps, cap, s);
-        if (e != cudaSuccess) return to_status(e);
+        if (e != cudaSuccess) {
+            release();
+            return to_status(e);
+        }
     }
+    release();
     return RS_ERR_TABLE_FULL;
+}
+
+extern "C" int rs_set_overlap_cull(int on) {
+    g_overlap_cull = on != 0;
+    return RS_OK;
 }
 
 extern "C" int rs_pairset_set_tracking(rs_pairset* ps, int on) {

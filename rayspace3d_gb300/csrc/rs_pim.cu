@@ -527,6 +527,9 @@ int pim_impl(const rs_bvh* cbvh, const float* pts, uint64_t n, float dx, float d
     if (n == 0) return RS_OK;
     if (n > 0xffffffffull) return RS_ERR_INVALID;
     rs_bvh* bvh = const_cast<rs_bvh*>(cbvh);
+    int st = filter ? bvh_ready(bvh) : RS_OK;
+    if (st == RS_OK) st = bvh_use(bvh, s);
+    if (st != RS_OK) return st;
     if (filter && bvh->nV == 0) {
         cudaError_t e = cudaSuccess;
         if (obj) e = cudaMemsetAsync(obj, 0xff, n * sizeof(int32_t), s);
@@ -662,6 +665,9 @@ extern "C" int rs_pim_noalloc(const rs_bvh* bvh, const float* d_points, uint64_t
     if (n > kNoAllocMaxPoints) return RS_ERR_TOO_LARGE;
     if (n == 0) return RS_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    int st = filtered ? bvh_ready(bvh) : RS_OK;
+    if (st == RS_OK) st = bvh_use(bvh, s);
+    if (st != RS_OK) return st;
     if (filtered && bvh->nV == 0) {
         cudaError_t e = cudaSuccess;
         if (d_obj) e = cudaMemsetAsync(d_obj, 0xff, n * sizeof(int32_t), s);

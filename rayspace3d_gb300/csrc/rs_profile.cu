@@ -35,6 +35,32 @@ cudaError_t dmalloc(void** p, size_t bytes, cudaStream_t s) {
     return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
+// Small pinned host slots (16 ints) that asynchronous builds copy their result words
+// into, so reading them needs only the build's event.  Slots come from 256-slot pinned
+// blocks allocated on demand and are recycled.
+namespace {
+std::mutex g_slot_mu;
+std::vector<int*> g_free_slots;
+}  // namespace
+
+int* pinned_slot_acquire() {
+    std::lock_guard<std::mutex> g(g_slot_mu);
+    if (g_free_slots.empty()) {
+        int* block = nullptr;
+        if (cudaMallocHost((void**)&block, 256 * 16 * sizeof(int)) != cudaSuccess) return nullptr;
+        for (int i = 255; i >= 0; --i) g_free_slots.push_back(block + 16 * i);
+    }
+    int* p = g_free_slots.back();
+    g_free_slots.pop_back();
+    return p;
+}
+
+void pinned_slot_release(int* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> g(g_slot_mu);
+    g_free_slots.push_back(p);
+}
+
 namespace {
 // One event pair per profiled launch between collections; launches on several
 // streams may be open at once (each begin returns its own token).

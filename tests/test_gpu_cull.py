@@ -1,0 +1,77 @@
+"""The overlap join's broad phase: the pair set is identical with culling on and off and
+equal to the oracle's, on contact-heavy inputs (face-sharing and touching cubes, shared
+edges, objects that only touch within the edge payload's quantisation) and on a query that
+exhausts its node budget (one object whose box covers the whole other set)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import bind
+from rayspace3d_gb300 import _lib, api, formats, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _join(A, B, cull, containment=False):
+    L = _lib.load()
+    L.rs_set_overlap_cull(1 if cull else 0)
+    try:
+        ba, bb = api.Bvh(api.DeviceGeometry(A)), api.Bvh(api.DeviceGeometry(B))
+        ps = api.PairSet(1 << 12)
+        api.overlap_join(ba, bb, ps, with_containment=containment)
+        torch.cuda.synchronize()
+        return np.sort(ps.finalize().cpu().numpy().astype(np.uint64))
+    finally:
+        L.rs_set_overlap_cull(1)
+
+
+def _check(A, B, containment=False):
+    want = bind.intersection_join(A, B) if containment else bind.overlap_join(A, B)
+    on = _join(A, B, True, containment)
+    off = _join(A, B, False, containment)
+    np.testing.assert_array_equal(off, want)
+    np.testing.assert_array_equal(on, want)
+    return want
+
+
+def _shift(g, d, grid=False):
+    V = (g.vertices + np.asarray(d, np.float32)).astype(np.float32)
+    return synth.make_geometry(V, g.indices, g.tri2obj)
+
+
+@pytest.mark.parametrize("offset", [(1.0, 0.0, 0.0), (0.5, 0.5, 0.0), (0.0, 0.0, 1.0), (1.0, 1.0, 1.0),
+                                    (2.0, 0.0, 0.0), (3.0, 0.0, 0.0), (1e-5, 0.0, 0.0), (3.0 + 4e-6, 0.0, 0.0),
+                                    (0.25, 0.0, 0.75)])
+def test_cull_on_touching_cubes(cuda, offset):
+    A = synth.cube_grid(3, 2, 2)
+    B = _shift(synth.cube_grid(3, 2, 2), offset)
+    _check(A, B)
+
+
+def test_cull_on_random_spheres_and_intersection(cuda):
+    for seed, world in [(21, 6.0), (22, 15.0), (23, 40.0)]:
+        A, B = synth.overlap_workload(n_objects=200, level=1, world=world, seed=seed)
+        _check(A, B)
+    A, B = synth.overlap_workload(n_objects=150, level=1, world=10.0, seed=24)
+    _check(A, B, containment=True)
+
+
+def test_cull_with_shared_edges(cuda):
+    """Edges shared by several objects (quantised-equal endpoints) carry the first
+    object's endpoints; every source must still see its pairs."""
+    g = synth.cube_grid(4, 1, 1)
+    assert (g.edges.counts > 1).any()
+    B = _shift(synth.cube_grid(2, 2, 2), (1.5, -0.5, 0.25))
+    _check(g, B)
+    _check(B, g)
+
+
+def test_cull_budget_exhausted(cuda):
+    """One huge sphere around a cloud of small ones: its query visits more nodes than the
+    budget allows, which must switch culling off for the other side, not drop pairs."""
+    rng = np.random.default_rng(5)
+    small = synth.sphere_set(400, 2, 0.2, 0.6, 20.0, rng)
+    v, f = synth.icosphere(3)
+    big = synth.make_geometry((v * 9.0 + 10.0).astype(np.float32), f, np.zeros(len(f), np.int32))
+    _check(big, small)
+    _check(small, big)

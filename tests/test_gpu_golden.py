@@ -310,3 +310,48 @@ def test_recheck_counters(cuda, golden):
     L.rs_recheck_reset()
     assert L.rs_recheck_read(ctypes.byref(ex), ctypes.byref(tests)) == 0
     assert ex.value == 0 and tests.value == 0
+
+
+def test_async_builds_on_two_streams(cuda, golden, join_sets):
+    """rs_bvh_build_async on two streams, then a join on a third: the engine orders the
+    join after both builds; results equal the oracle's."""
+    A, B = join_sets
+    da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+    torch.cuda.synchronize()
+    s1, s2, s3 = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    ba = api.Bvh(da, stream=s1, asynchronous=True)
+    bb = api.Bvh(db, stream=s2, asynchronous=True)
+    ps = api.PairSet(1 << 12, stream=s3)
+    api.overlap_join(ba, bb, ps, with_containment=True, stream=s3)
+    keys = np.sort(ps.finalize(stream=s3).cpu().numpy().astype(np.uint64))
+    np.testing.assert_array_equal(keys, golden["join_intersection"])
+    ba.wait()
+    bb.wait()
+    info = ba.info()
+    assert info["triangles"] == len(A.indices)
+    np.testing.assert_array_equal(np.array(info["min"], np.float32), A.vertices.min(axis=0))
+    # point-in-mesh straight after an asynchronous build on another stream
+    geo = _geom(golden, "pim_")
+    bp = api.Bvh(api.DeviceGeometry(geo), stream=s1, asynchronous=True)
+    obj, _ = api.point_in_mesh(bp, torch.from_numpy(golden["pim_pts"]).cuda(), stream=s2)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(obj.cpu().numpy(), golden["pim_z"])
+
+
+def test_out_of_range_vertex_index(cuda):
+    """An index past the vertex array is reported, synchronously by rs_bvh_build and by
+    rs_bvh_wait after an asynchronous build (the kernels clamp every index)."""
+    L = _lib.load()
+    V = torch.tensor([[0, 0, 0], [1, 0, 0], [0, 1, 0]], dtype=torch.float32, device="cuda")
+    I = torch.tensor([[0, 1, 2], [0, 1, 7]], dtype=torch.int32, device="cuda")
+    T = torch.zeros(2, dtype=torch.int32, device="cuda")
+    h = ctypes.c_void_p()
+    assert L.rs_bvh_build(V.data_ptr(), 3, I.data_ptr(), 2, T.data_ptr(), 0, ctypes.byref(h), None) == \
+        _lib.RS_ERR_INVALID
+    assert not h.value
+    assert L.rs_bvh_build_async(V.data_ptr(), 3, I.data_ptr(), 2, T.data_ptr(), 0, ctypes.byref(h), None) == 0
+    assert L.rs_bvh_wait(h) == _lib.RS_ERR_INVALID
+    pts = torch.zeros((4, 3), dtype=torch.float32, device="cuda")
+    obj = torch.empty(4, dtype=torch.int32, device="cuda")
+    assert L.rs_pim(h, pts.data_ptr(), 4, 0.0, 0.0, 1.0, obj.data_ptr(), None, None) == _lib.RS_ERR_INVALID
+    assert L.rs_bvh_destroy(h) == 0
