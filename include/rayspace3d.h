@@ -207,6 +207,36 @@ int rs_set_overlap_cull(int on);
 /* Status text for a code. */
 const char* rs_status_string(int status);
 
+/* Batched queries in one persistent launch (no counterpart in the reference, which
+ * launches and synchronises per query: RayLauncher.cpp:39-64, MeshIntersectionLauncher.cpp:
+ * 279-328).  Point-in-mesh queries and edge-ray directions of any sizes are split into
+ * chunks that the warps of one persistent kernel pull from a global counter; rays with
+ * more than 8 crossings are resolved exactly by a second launch.  An unchanged batch is
+ * captured as a CUDA graph on its first submit (on a non-default stream) and replayed
+ * afterwards.  Inputs, outputs and pair sets stay owned by the caller and must outlive
+ * the batch; edge queries insert into their pair set, which the caller clears. */
+typedef struct rs_batch rs_batch;
+int rs_batch_create(rs_batch** out);
+int rs_batch_destroy(rs_batch* batch);
+int rs_batch_add_pim(rs_batch* batch, const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy,
+                     float dz, int32_t* d_obj, uint8_t* d_inside, int* index);
+int rs_batch_add_edges(rs_batch* batch, const rs_bvh* target, const float* d_starts, const float* d_ends,
+                       const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
+                       int swap, rs_pairset* ps, int* index);
+/* chunk: rays a warp takes per pull (multiple of 32, default 64); stack_depth: 32 or 64
+ * traversal stack entries (default 64); use_graph: capture and replay (default 1). */
+int rs_batch_set_options(rs_batch* batch, int chunk, int stack_depth, int use_graph);
+int rs_batch_submit(rs_batch* batch, void* stream);
+/* Waits for the last submit; per-query statuses into h_status (nullable); returns the
+ * first failing one. */
+int rs_batch_wait(rs_batch* batch, int* h_status);
+/* Times the batch over BVH leaf sizes {2,4,8,16}, chunks {32,64,128} and stack depths
+ * {32,64} (three runs each, configurations whose queries fail are skipped), keeps the
+ * fastest (rebuilding the batch's BVHs with its leaf size when it differs from the
+ * caller's) and reports it. */
+int rs_batch_autotune(rs_batch* batch, int* h_leaf_size, int* h_chunk, int* h_stack_depth, double* h_ms,
+                      void* stream);
+
 /* Diagnostics (no counterpart in the reference).  rs_launch_count: kernels launched by this
  * library since load.  rs_profile_*: when enabled, device time of the main kernels is
  * accumulated with CUDA events on the launching stream; ids 0 edge join, 1 containment,

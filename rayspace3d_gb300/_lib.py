@@ -65,6 +65,15 @@ SIGNATURES = {
     "rs_profile_read": (I, [I, ctypes.POINTER(ctypes.c_double), PU64]),
     "rs_recheck_enable": (I, [I]),
     "rs_set_overlap_cull": (I, [I]),
+    "rs_batch_create": (I, [PP]),
+    "rs_batch_destroy": (I, [P]),
+    "rs_batch_add_pim": (I, [P, P, P, U64, F, F, F, P, P, ctypes.POINTER(I)]),
+    "rs_batch_add_edges": (I, [P, P, P, P, P, P, P, U64, I, P, ctypes.POINTER(I)]),
+    "rs_batch_set_options": (I, [P, I, I, I]),
+    "rs_batch_submit": (I, [P, P]),
+    "rs_batch_wait": (I, [P, ctypes.POINTER(I)]),
+    "rs_batch_autotune": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
+                              ctypes.POINTER(ctypes.c_double), P]),
     "rs_recheck_reset": (I, []),
     "rs_recheck_read": (I, [PU64, PU64]),
     "exclusive_scan_gpu": (ctypes.c_longlong, [P, P, I]),

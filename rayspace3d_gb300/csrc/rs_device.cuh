@@ -333,7 +333,7 @@ constexpr int kStack = 64;
 // of a shared-memory array).  A valid tree visits each node at most once, so
 // `max_steps` (the node count) bounds the loop even if the node array were corrupt.
 // Returns false on stack overflow or an exhausted step budget.
-template <int AXIS, class F>
+template <int AXIS, int STACK = kStack, class F>
 __device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNode* __restrict__ nodes,
                                               uint32_t max_steps, const Ray& r, F&& on_leaf) {
     int sp = 0;
@@ -352,7 +352,7 @@ __device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNod
         if (h0 && nd.y > 0) { on_leaf(nd.x, nd.y); h0 = false; }
         if (h1 && nd.w > 0) { on_leaf(nd.z, nd.w); h1 = false; }
         if (h0 && h1) {
-            if (sp == kStack) return false;
+            if (sp == STACK) return false;
             stack[sp * stride] = nd.z;
             ++sp;
             node = nd.x;
@@ -369,11 +369,11 @@ __device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNod
     return true;
 }
 
-template <int AXIS, class F>
+template <int AXIS, int STACK = kStack, class F>
 __device__ __forceinline__ bool traverse(const BNode* __restrict__ nodes, uint32_t max_steps, const Ray& r,
                                          F&& on_leaf) {
-    int stack[kStack];
-    return traverse_with<AXIS>(stack, 1, nodes, max_steps, r, on_leaf);
+    int stack[STACK];
+    return traverse_with<AXIS, STACK>(stack, 1, nodes, max_steps, r, on_leaf);
 }
 
 __device__ __forceinline__ void load_tri(const float4* __restrict__ tris, int k, float* a, float* b, float* c,

@@ -13,6 +13,7 @@
 
 #include "rs_engine.h"
 #include "rs_prims.cuh"
+#include "rs_query_core.cuh"
 
 namespace rs {
 namespace {
@@ -41,46 +42,7 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
         }
         if (!any) return;
     }
-    const float sx = starts[3 * i], sy = starts[3 * i + 1], sz = starts[3 * i + 2];
-    const float ex = ends[3 * i], ey = ends[3 * i + 1], ez = ends[3 * i + 2];
-    // distance3f / normalize3f of mesh_overlap_edges.cu:47-60 as individually rounded operations.
-    const float dx = __fsub_rn(ex, sx), dy = __fsub_rn(ey, sy), dz = __fsub_rn(ez, sz);
-    const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-    if (len < 1e-6f) return;
-    const Ray r = make_ray(sx, sy, sz, __fdiv_rn(dx, len), __fdiv_rn(dy, len), __fdiv_rn(dz, len), 1e-6f,
-                           __fadd_rn(len, 1e-6f));
-    const int nsrc = counts[i];
-    const int32_t* src = sources + offsets[i];
-    int32_t last[4] = {INT_MIN, INT_MIN, INT_MIN, INT_MIN};
-    int lp = 0;
-    unsigned int crossings = 0, tests = 0;
-    const bool ok = traverse<-1>(nodes, max_steps, r, [&](int first, int cnt) {
-        tests += (unsigned int)cnt;
-        for (int k = first; k < first + cnt; ++k) {
-            float a[3], b[3], c[3];
-            uint32_t tid;
-            int32_t obj;
-            load_tri(tris, k, a, b, c, tid, obj);
-            float t;
-            if (!hit_triangle<-1>(r, a, b, c, t)) continue;
-            ++crossings;
-            if (obj == last[0] || obj == last[1] || obj == last[2] || obj == last[3]) continue;
-            last[lp] = obj;
-            lp = (lp + 1) & 3;
-            for (int q = 0; q < nsrc; ++q) {
-                const uint32_t sobj = (uint32_t)src[q];
-                const unsigned long long key = swap ? (((unsigned long long)(uint32_t)obj << 32) | sobj)
-                                                    : (((unsigned long long)sobj << 32) | (uint32_t)obj);
-                table_insert(table, key);
-            }
-        }
-    });
-    if (!ok) atomicOr(table.status, ST_STACK_OVERFLOW);
-    add_tests(tests);
-    if (table.stats) {
-        atomicAdd(&table.stats[2], 1ull);
-        if (crossings) atomicAdd(&table.stats[3], (unsigned long long)crossings);
-    }
+    edge_ray<kStack>(starts, ends, offsets, counts, sources, i, nodes, max_steps, tris, swap, table);
 }
 
 __global__ void k_first_tri_init(int32_t* __restrict__ first, uint64_t nObj) {

@@ -26,91 +26,12 @@
 
 #include "rs_engine.h"
 #include "rs_prims.cuh"
+#include "rs_query_core.cuh"
 
 namespace rs {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kHits = 8;
-constexpr float kEps = 1e-6f;
-constexpr float kTmax = 1e16f;
-constexpr int kFallbackIters = 1 << 16;
-
-struct BoxMesh {
-    float v[12][9];  // 12 triangles x (a,b,c)
-};
-
-__device__ __forceinline__ bool hit_less(float t0, uint32_t i0, float t1, uint32_t i1) {
-    return t0 < t1 || (t0 == t1 && i0 < i1);
-}
-
-// Advance rule of raytracing.cu:23-60 on hits sorted by (t, id): a hit counts when
-// t >= threshold; the next threshold is t + 1e-6, or the next float when that does
-// not advance.
-struct Chain {
-    float thr = kEps;
-    uint32_t count = 0;
-    int32_t first_obj = -1;
-    __device__ __forceinline__ void step(float t, int32_t obj) {
-        if (t >= thr && t < kTmax) {
-            if (count == 0) first_obj = obj;
-            ++count;
-            float nt = __fadd_rn(t, kEps);
-            if (!(nt > t)) nt = nextafterf(t, INFINITY);
-            thr = nt;
-        }
-    }
-};
-
-// Up to kHits crossings in registers: predicated append, sorting network at the end.
-struct HitList {
-    float t[kHits];
-    uint32_t id[kHits];
-    int32_t obj[kHits];
-    int n = 0;
-    bool ovf = false;
-    __device__ __forceinline__ void add(float tt, uint32_t ii, int32_t oo) {
-        if (n >= kHits) {
-            ovf = true;
-            return;
-        }
-#pragma unroll
-        for (int j = 0; j < kHits; ++j)
-            if (j == n) {
-                t[j] = tt;
-                id[j] = ii;
-                obj[j] = oo;
-            }
-        ++n;
-    }
-    // Odd-even transposition sort of all kHits slots (empty slots sort last).
-    __device__ __forceinline__ Chain finish() {
-#pragma unroll
-        for (int j = 0; j < kHits; ++j)
-            if (j >= n) {
-                t[j] = INFINITY;
-                id[j] = 0xffffffffu;
-                obj[j] = -1;
-            }
-#pragma unroll
-        for (int r = 0; r < kHits; ++r) {
-#pragma unroll
-            for (int j = r & 1; j + 1 < kHits; j += 2) {
-                if (hit_less(t[j + 1], id[j + 1], t[j], id[j])) {
-                    const float tt = t[j]; t[j] = t[j + 1]; t[j + 1] = tt;
-                    const uint32_t ii = id[j]; id[j] = id[j + 1]; id[j + 1] = ii;
-                    const int32_t oo = obj[j]; obj[j] = obj[j + 1]; obj[j + 1] = oo;
-                }
-            }
-        }
-        Chain c;
-#pragma unroll
-        for (int j = 0; j < kHits; ++j)
-            if (j < n) c.step(t[j], obj[j]);
-        return c;
-    }
-};
-
 template <int AXIS>
 __device__ __forceinline__ bool box_filter(const float* __restrict__ box, const Ray& r) {
     HitList hl;
@@ -131,11 +52,6 @@ __device__ __forceinline__ bool box_filter(const float* __restrict__ box, const 
     return (ch.count & 1) != 0;
 }
 
-__device__ __forceinline__ void write_result(const Chain& ch, uint64_t i, int32_t* out_obj, uint8_t* out_in) {
-    const bool inside = (ch.count & 1) != 0;
-    if (out_obj) out_obj[i] = inside ? ch.first_obj : -1;
-    if (out_in) out_in[i] = inside ? 1 : 0;
-}
 
 template <int AXIS, bool FILTER>
 __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint64_t n, float dx, float dy, float dz,
@@ -153,17 +69,7 @@ __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint6
     }
     HitList hl;
     unsigned int tests = 0;
-    const bool ok = traverse<AXIS>(nodes, max_steps, r, [&](int first, int cnt) {
-        tests += (unsigned int)cnt;
-        for (int k = first; k < first + cnt; ++k) {
-            float a[3], b[3], c[3];
-            uint32_t tid;
-            int32_t obj;
-            load_tri(tris, k, a, b, c, tid, obj);
-            float t;
-            if (hit_triangle<AXIS>(r, a, b, c, t)) hl.add(t, tid, obj);
-        }
-    });
+    const bool ok = pim_collect<AXIS, kStack>(nodes, max_steps, tris, r, hl, tests);
     add_tests(tests);
     if (!ok) {
         atomicOr(status, ST_STACK_OVERFLOW);
@@ -290,8 +196,7 @@ __global__ void __launch_bounds__(kT) k_pim_grid(const float* __restrict__ pts, 
     write_result(hl.finish(), i, out_obj, out_in);
 }
 
-// Exact fallback for rays with more than kHits crossings: each round re-traverses
-// the BVH and takes the smallest (t, id) above the previous one.
+// Exact fallback for rays with more than kHits crossings (pim_fallback_ray).
 template <int AXIS>
 __global__ void __launch_bounds__(kT) k_pim_fallback(const float* __restrict__ pts, float dx, float dy, float dz,
                                                      const BNode* __restrict__ nodes, uint32_t max_steps,
@@ -306,45 +211,7 @@ __global__ void __launch_bounds__(kT) k_pim_fallback(const float* __restrict__ p
         const uint32_t i = ovf_list[q];
         const Ray r = make_ray(pts[3 * (uint64_t)i], pts[3 * (uint64_t)i + 1], pts[3 * (uint64_t)i + 2], dx, dy, dz,
                                kEps, kTmax);
-        Chain ch;
-        float pt = -INFINITY;
-        uint32_t pid = 0;
-        bool have_prev = false;
-        int it = 0;
-        for (; it < kFallbackIters; ++it) {
-            float bt = INFINITY;
-            uint32_t bid = 0xffffffffu;
-            int32_t bobj = -1;
-            bool found = false;
-            const bool ok = traverse<AXIS>(nodes, max_steps, r, [&](int first, int c) {
-                for (int k = first; k < first + c; ++k) {
-                    float a[3], b[3], cc[3];
-                    uint32_t tid;
-                    int32_t obj;
-                    load_tri(tris, k, a, b, cc, tid, obj);
-                    float t;
-                    if (!hit_triangle<AXIS>(r, a, b, cc, t)) continue;
-                    if (have_prev && !hit_less(pt, pid, t, tid)) continue;
-                    if (!found || hit_less(t, tid, bt, bid)) {
-                        found = true;
-                        bt = t;
-                        bid = tid;
-                        bobj = obj;
-                    }
-                }
-            });
-            if (!ok) {
-                atomicOr(status, ST_STACK_OVERFLOW);
-                break;
-            }
-            if (!found) break;
-            ch.step(bt, bobj);
-            pt = bt;
-            pid = bid;
-            have_prev = true;
-        }
-        if (it == kFallbackIters) atomicOr(status, ST_ITER_LIMIT);
-        write_result(ch, i, out_obj, out_in);
+        pim_fallback_ray<AXIS, kStack>(nodes, max_steps, tris, r, status, out_obj, out_in, i);
     }
 }
 
