@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--pim-points", type=int, default=1_000_000)
     ap.add_argument("--no-pim", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--batch-full", action="store_true", help="batched workload at its full size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -431,6 +432,130 @@ def run_join_variant(args, world_size, steps=5):
             "edge_rays_per_join": int(da.nE + db.nE), "recheck": rc}
 
 
+def run_batch(args, full: bool):
+    """The batched, degeneracy-heavy configuration in one persistent launch (rs_batch_*):
+    256 point-in-mesh queries over meshes of 80..81,920 triangles (icosphere levels 1-6,
+    and face-sharing cube blocks), point counts log-uniform in [1e4, 4e6] (full) or
+    [1e4, 1e6] (default), 20 % snapped onto vertices, edges and faces, +x/+y/+z and
+    oblique rays; plus both edge directions of 64 (full) or 16 (default) overlap joins of
+    level-2 icospheres, objects per side log-uniform in [1e3, 5e4] (full) or [1e3, 2e4],
+    world scaled to the 10k-in-1000^3 density, one in eight a pair of face-sharing cube
+    blocks offset by half a cube.  Everything is generated on the device (gen.py).  The
+    autotuner picks leaf size, chunk and stack depth first; then the batch is replayed
+    as a CUDA graph and timed.  A sample of queries is checked against the
+    single-query entry points."""
+    import ctypes
+
+    import torch
+    from rayspace3d_gb300 import _lib, api, gen, synth
+
+    L = _lib.load()
+    rng = np.random.default_rng(4)
+    n_pim, n_join = 256, (64 if full else 16)
+    pmax, omax = (4e6, 5e4) if full else (1e6, 2e4)
+    keep = []
+    meshes = []
+    queries = []  # (mesh index, points, direction)
+    for q in range(n_pim):
+        if q % 10 == 9:
+            nx, ny, nz = (int(v) for v in rng.integers(1, 9, size=3))
+            g = synth.cube_grid(nx, ny, nz, edges=False)
+            dg = api.DeviceGeometry(g)
+        else:
+            level = int(rng.integers(1, 7))
+            dg = gen.instanced_set(1, level, 1.0, 1.0, 0.0, seed=1000 + q)
+        meshes.append(dg)
+        n = int(np.exp(rng.uniform(np.log(1e4), np.log(pmax))))
+        pts = gen.mesh_points(dg, n, seed=2000 + q, frac_snapped=0.2)
+        k = q % 4
+        d = [(1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0), None][k]
+        if d is None:
+            v = rng.standard_normal(3)
+            v /= np.linalg.norm(v)
+            d = tuple(float(x) for x in v)
+        queries.append((q, pts, d))
+    joins = []
+    for j in range(n_join):
+        if j % 8 == 7:
+            A = api.DeviceGeometry(synth.cube_grid(20, 20, 5))
+            gb = synth.cube_grid(20, 20, 5)
+            gb = synth.make_geometry(gb.vertices + np.float32(0.5), gb.indices, gb.tri2obj)
+            B = api.DeviceGeometry(gb)
+        else:
+            n = int(np.exp(rng.uniform(np.log(1e3), np.log(omax))))
+            w = 1000.0 * (n / 1e4) ** (1.0 / 3.0)
+            A = gen.instanced_set(n, 2, 0.5, 2.0, w, seed=3000 + 2 * j)
+            B = gen.instanced_set(n, 2, 0.5, 2.0, w, seed=3001 + 2 * j)
+        joins.append((A, B))
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        bvhs = [api.Bvh(dg, stream=stream) for dg in meshes]
+        jb = [(api.Bvh(A, stream=stream), api.Bvh(B, stream=stream)) for A, B in joins]
+        sets = [api.PairSet(1 << 20, stream=stream) for _ in joins]
+        outs = []
+        h = ctypes.c_void_p()
+        L.rs_batch_create(ctypes.byref(h))
+        for (q, pts, d) in queries:
+            obj = torch.empty(len(pts), dtype=torch.int32, device="cuda")
+            ins = torch.empty(len(pts), dtype=torch.uint8, device="cuda")
+            L.rs_batch_add_pim(h, bvhs[q].handle, pts.data_ptr(), len(pts), *d, obj.data_ptr(), ins.data_ptr(), None)
+            outs.append((obj, ins))
+        for (A, B), (ba, bb), ps in zip(joins, jb, sets):
+            L.rs_batch_add_edges(h, bb.handle, *A.edge_ptrs(), A.nE, 0, ps.handle, None)
+            L.rs_batch_add_edges(h, ba.handle, *B.edge_ptrs(), B.nE, 1, ps.handle, None)
+        sp = ctypes.c_void_p(stream.cuda_stream)
+        leaf, ch, sd, tms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        t0 = time.perf_counter()
+        rc_tune = L.rs_batch_autotune(h, ctypes.byref(leaf), ctypes.byref(ch), ctypes.byref(sd), ctypes.byref(tms),
+                                      sp)
+        tune_s = time.perf_counter() - t0
+        nq = n_pim + 2 * n_join
+        st = (ctypes.c_int * nq)()
+        for ps in sets:
+            ps.clear(stream=stream)
+        rc = L.rs_batch_submit(h, sp)  # captures the graph
+        rc = rc or L.rs_batch_wait(h, st)
+        reps = 5
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            L.rs_batch_submit(h, sp)
+        e1.record(stream)
+        rc = rc or L.rs_batch_wait(h, st)
+        ms = e0.elapsed_time(e1) / reps
+        rc_stats = recheck(L, lambda: (L.rs_batch_submit(h, sp), L.rs_batch_wait(h, st)))
+        # Spot checks against the single-query entry points.
+        checks = 0
+        for i in list(range(0, n_pim, 37)):
+            q, pts, d = queries[i]
+            o, _ = api.point_in_mesh(bvhs[q], pts, direction=d, stream=stream)
+            torch.cuda.synchronize()
+            assert torch.equal(o, outs[i][0]), f"batch point-in-mesh query {i} differs"
+            checks += 1
+        for j in list(range(0, n_join, 5)) + [7]:
+            if j >= n_join:
+                continue
+            ref = api.PairSet(1 << 20, stream=stream)
+            api.overlap_join(jb[j][0], jb[j][1], ref, stream=stream)
+            a = ref.finalize(stream=stream).cpu().numpy()
+            b = sets[j].finalize(stream=stream).cpu().numpy()
+            assert np.array_equal(np.sort(a), np.sort(b)), f"batch join {j} differs"
+            checks += 1
+        L.rs_batch_destroy(h)
+    n_pts = sum(len(p) for _, p, _ in queries)
+    n_edges = sum(A.nE + B.nE for A, B in joins)
+    n_tris_join = sum(A.nF + B.nF for A, B in joins)
+    return {"workload": ("full" if full else "default") + f": {n_pim} point-in-mesh queries ({n_pts} points, "
+                        f"20 % snapped) + {n_join} overlap joins ({n_edges} edge rays, {n_tris_join} triangles), "
+                        "one persistent launch replayed as a CUDA graph",
+            "status": int(rc), "ms": round(ms, 3), "mrays_s": round((n_pts + n_edges) / (ms * 1e-3) / 1e6, 1),
+            "points": int(n_pts), "edge_rays": int(n_edges),
+            "autotune": {"status": int(rc_tune), "leaf_size": leaf.value, "chunk": ch.value,
+                         "stack_depth": sd.value, "best_ms": round(tms.value, 3), "seconds": round(tune_s, 2)},
+            "recheck": rc_stats, "spot_checks_passed": checks}
+
+
 def cpu_join_sample(A, B, frac=0.02, threads=None):
     """Oracle overlap join on a bounded sample of both edge sets, extrapolated to one
     full join: 2 x CPU BVH build + (sampled traversal time / frac)."""
@@ -498,6 +623,7 @@ def main():
             result["pim_100m"] = run_pim(args, local, 100_000_000, (1.0, 0.0, 0.0), reps=5)
     if not args.no_variants:
         result["join_w80"] = run_join_variant(args, 80.7)
+        result["batch"] = run_batch(args, args.batch_full)
     if rank == 0 and not args.no_cpu_baseline:
         v, meta = cpu_join_sample(A, B, frac=0.01)
         result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": meta["cores"], "kind": "port",

@@ -68,6 +68,20 @@ class DeviceGeometry:
             raw = np.ascontiguousarray(g.grid.cells).view(np.uint8)
             self.cells = torch.from_numpy(raw.copy()).to(dev)
 
+    @classmethod
+    def from_tensors(cls, V: torch.Tensor, I: torch.Tensor, T: torch.Tensor, edges=None,
+                     cells: Optional[torch.Tensor] = None) -> "DeviceGeometry":
+        """Wraps device tensors (float32 V[n,3], int32/uint32-bits I[m,3], int32 T[m], optional
+        edge tuple (starts, ends, offsets, counts, sources) and raw grid cells) without copies."""
+        self = cls.__new__(cls)
+        self.host = None
+        self.V, self.I, self.T = V.contiguous(), I.contiguous(), T.contiguous()
+        self.nV, self.nF = int(V.shape[0]), int(I.shape[0])
+        self.edges = tuple(t.contiguous() for t in edges) if edges is not None else None
+        self.nE = int(self.edges[0].shape[0]) if self.edges is not None else 0
+        self.cells = cells
+        return self
+
     def edge_ptrs(self):
         if self.edges is None:
             raise ValueError("geometry has no precomputed edge payload")

@@ -7,7 +7,8 @@
 // kernel (a few CTAs per SM) has each warp pull the next chunk from a global atomic
 // counter and trace its rays with the same per-ray bodies as the single-query kernels
 // (rs_query_core.cuh), so queries of very uneven sizes share the GPU without a launch
-// or a tail per query.  Points whose rays cross more than 8 triangles go to one
+// or a tail per query.  Axis-aligned point-in-mesh queries read the handle's column
+// grid (built at the first submit), others traverse the BVH.  Points whose rays cross more than 8 triangles go to one
 // overflow list that a second launch resolves exactly.  The launches of an unchanged
 // batch are captured once as a CUDA graph and replayed.  rs_batch_autotune times the
 // batch over BVH leaf sizes, chunk sizes and traversal stack depths and keeps the best.
@@ -46,6 +47,8 @@ struct BatchQuery {
     uint64_t n;
     uint64_t first_chunk;
     unsigned int* status;
+    int use_grid;  // axis-aligned point-in-mesh through the handle's column grid
+    GridView grid;
 };
 
 __device__ __forceinline__ int find_query(const BatchQuery* __restrict__ q, int nq, uint64_t chunk) {
@@ -83,7 +86,9 @@ template <int STACK>
 __global__ void __launch_bounds__(kBT) k_batch(const BatchQuery* __restrict__ q, int nq, uint64_t total_chunks,
                                                int chunk, unsigned long long* __restrict__ next,
                                                uint2* __restrict__ ovf, unsigned long long* __restrict__ ovf_count) {
+    __shared__ GridWarpSlots slots[kBT / 32];
     const int lane = threadIdx.x & 31;
+    GridWarpSlots& sl = slots[threadIdx.x >> 5];
     for (;;) {
         unsigned long long c = 0;
         if (lane == 0) c = atomicAdd(next, 1ull);
@@ -93,6 +98,29 @@ __global__ void __launch_bounds__(kBT) k_batch(const BatchQuery* __restrict__ q,
         const BatchQuery& Q = q[qi];
         const uint64_t r0 = (c - Q.first_chunk) * (uint64_t)chunk;
         const uint64_t r1 = min(r0 + (uint64_t)chunk, Q.n);
+        if (Q.kind == 0 && Q.use_grid) {
+            // Warp-cooperative rounds of 32 points: every lane takes part in each round.
+            for (uint64_t base = r0; base < r1; base += 32) {
+                const uint64_t i = base + lane;
+                const bool valid = i < r1;
+                float p[3] = {0.0f, 0.0f, 0.0f};
+                if (valid) {
+                    p[0] = Q.pts[3 * i];
+                    p[1] = Q.pts[3 * i + 1];
+                    p[2] = Q.pts[3 * i + 2];
+                }
+                auto spill = [&]() {
+                    const unsigned long long slot = atomicAdd(ovf_count, 1ull);
+                    if (slot < kOverflowCap) ovf[slot] = make_uint2((uint32_t)qi, (uint32_t)i);
+                    else atomicOr(Q.status, ST_HIT_OVERFLOW);
+                };
+                if (Q.axis == 0) pim_grid_warp<0>(Q.grid, Q.tris, p, valid, valid, i, Q.obj, Q.in, sl, spill);
+                else if (Q.axis == 1) pim_grid_warp<1>(Q.grid, Q.tris, p, valid, valid, i, Q.obj, Q.in, sl, spill);
+                else pim_grid_warp<2>(Q.grid, Q.tris, p, valid, valid, i, Q.obj, Q.in, sl, spill);
+                __syncwarp();
+            }
+            continue;
+        }
         for (uint64_t i = r0 + lane; i < r1; i += 32) {
             if (Q.kind == 1) {
                 edge_ray<STACK>(Q.starts, Q.ends, Q.offsets, Q.counts, Q.sources, i, Q.nodes, Q.max_steps, Q.tris,
@@ -131,6 +159,8 @@ __global__ void __launch_bounds__(kBT) k_batch_fallback(const BatchQuery* __rest
 }  // namespace
 
 PairTable table_view(rs_pairset* ps);
+
+int recheck_batch(int op, unsigned long long* out) { return recheck_op(op, out); }
 
 }  // namespace rs
 
@@ -194,7 +224,7 @@ void release_device(rs_batch* b) {
     b->dirty = true;
 }
 
-int commit(rs_batch* b) {
+int commit(rs_batch* b, cudaStream_t s) {
     if (!b->dirty) return RS_OK;
     release_device(b);
     const int nq = (int)b->items.size();
@@ -226,6 +256,13 @@ int commit(rs_batch* b) {
             q.pts = it.pts;
             q.obj = it.obj;
             q.in = it.in;
+            if (q.axis >= 0 && h->n_tris > 0) {
+                const int g = ensure_grid(h, q.axis, s);
+                if (g != RS_OK) return g;
+                const rs_column_grid& cg = h->cgrid[q.axis];
+                q.use_grid = 1;
+                q.grid = GridView{cg.u0, cg.v0, cg.su, cg.sv, cg.u1, cg.v1, cg.gu, cg.gv, cg.start, cg.list};
+            }
         } else {
             q.axis = -1;
             q.starts = it.starts;
@@ -259,6 +296,15 @@ int commit(rs_batch* b) {
     return RS_OK;
 }
 
+// One fallback thread per possible overflow entry, up to the list's capacity (the count
+// is only known on the device; threads past it return at once).
+unsigned fallback_grid(const rs_batch* b) {
+    uint64_t pim = 0;
+    for (const rs_batch_item& it : b->items)
+        if (it.kind == 0) pim += it.n;
+    return (unsigned)std::max<uint64_t>(1, (std::min(pim, kOverflowCap) + kBT - 1) / kBT);
+}
+
 // The launches of one submit: counters, per-query statuses, outputs of queries against
 // empty meshes, the persistent kernel and the overflow fallback.
 cudaError_t enqueue(rs_batch* b, cudaStream_t s) {
@@ -276,12 +322,12 @@ cudaError_t enqueue(rs_batch* b, cudaStream_t s) {
         if (b->stack == 32) {
             launch(k_batch<32>, b->grid, kBT, 0, s, (const BatchQuery*)b->d_q, nq, b->total_chunks, b->chunk,
                    b->d_counters, b->d_ovf, b->d_counters + 1);
-            if (b->d_ovf) launch(k_batch_fallback<32>, 2 * sm_count(), kBT, 0, s, (const BatchQuery*)b->d_q,
+            if (b->d_ovf) launch(k_batch_fallback<32>, fallback_grid(b), kBT, 0, s, (const BatchQuery*)b->d_q,
                                  (const uint2*)b->d_ovf, (const unsigned long long*)b->d_counters + 1);
         } else {
             launch(k_batch<64>, b->grid, kBT, 0, s, (const BatchQuery*)b->d_q, nq, b->total_chunks, b->chunk,
                    b->d_counters, b->d_ovf, b->d_counters + 1);
-            if (b->d_ovf) launch(k_batch_fallback<64>, 2 * sm_count(), kBT, 0, s, (const BatchQuery*)b->d_q,
+            if (b->d_ovf) launch(k_batch_fallback<64>, fallback_grid(b), kBT, 0, s, (const BatchQuery*)b->d_q,
                                  (const uint2*)b->d_ovf, (const unsigned long long*)b->d_counters + 1);
         }
     }
@@ -366,7 +412,7 @@ extern "C" int rs_batch_set_options(rs_batch* b, int chunk, int stack_depth, int
 extern "C" int rs_batch_submit(rs_batch* b, void* stream) {
     if (!b) return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
-    const int st = commit(b);
+    const int st = commit(b, s);
     if (st != RS_OK) return st;
     for (const rs_batch_item& it : b->items) {
         const int u = bvh_use(effective(b, it.bvh), s);

@@ -112,11 +112,40 @@ __device__ __forceinline__ int expansion_sign(const double* e, int m) {
 static __device__ __noinline__ int orient_exact(float d0, float d1, float d2, float o0, float o1, float o2,
                                                 float a0, float a1, float a2, float b0, float b1, float b2) {
     note_exact();
+    // a == o, b == o or a == b makes a-o, b-o dependent: the determinant is exactly zero
+    // (points snapped onto mesh vertices hit this for every incident edge).
+    if ((a0 == o0 && a1 == o1 && a2 == o2) || (b0 == o0 && b1 == o1 && b2 == o2) ||
+        (a0 == b0 && a1 == b1 && a2 == b2))
+        return 0;
     const float d[3] = {d0, d1, d2}, o[3] = {o0, o1, o2}, a[3] = {a0, a1, a2}, b[3] = {b0, b1, b2};
-    double e[40];
-    int m = 0;
     const float* X[3] = {a, b, o};
     const float* Y[3] = {b, o, a};
+    // FP64 filter: each of the 36 terms d_k * (X_i Y_j) has an exact float-by-float product
+    // and one rounding (relative 2^-53), the sum of 36 terms 35 more, so
+    // |sum - det| <= 36 * 2^-53 * sum|terms| (1 + 2^-50); 40 * 2^-53 is used.
+    {
+        double sum = 0.0, mag = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int i = (k + 1) % 3, j = (k + 2) % 3;
+            const double dk = (double)d[k];
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                const double p = __dmul_rn(dk, __dmul_rn((double)X[s][i], (double)Y[s][j]));
+                const double q = __dmul_rn(dk, __dmul_rn((double)X[s][j], (double)Y[s][i]));
+                sum = __dadd_rn(sum, __dsub_rn(p, q));
+                mag = __dadd_rn(mag, __dadd_rn(fabs(p), fabs(q)));
+            }
+        }
+        // Products of floats neither underflow nor overflow in FP64; mag == 0 means every
+        // term, hence the determinant, is exactly zero.
+        if (mag == 0.0) return 0;
+        const double bound = __dmul_rn(mag, 40.0 * 1.1102230246251565e-16);
+        if (sum > bound) return 1;
+        if (sum < -bound) return -1;
+    }
+    double e[40];
+    int m = 0;
 #pragma unroll 1
     for (int k = 0; k < 3; ++k) {
         if (d[k] == 0.0f) continue;
@@ -155,6 +184,98 @@ static __device__ __noinline__ int axis_det_exact(int k, float d0, float d1, flo
     return expansion_sign(e, m);
 }
 
+// Adds b into the expansion e[0..M) of exactly M components (zeros kept), giving M+1
+// components; with compile-time M every index is static, so e stays in registers.
+template <int M>
+__device__ __forceinline__ void grow_fixed(double* e, double b) {
+    double q = b;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        double h;
+        q = two_sum(q, e[i], h);
+        e[i] = h;
+    }
+    e[M] = q;
+}
+
+// The same in FP32 (Knuth two-sum in float), for the float expansion below.
+__device__ __forceinline__ float two_sum_f(float a, float b, float& err) {
+    float s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    float aa = __fsub_rn(s, bb);
+    err = __fadd_rn(__fsub_rn(a, aa), __fsub_rn(b, bb));
+    return s;
+}
+
+template <int M>
+__device__ __forceinline__ void grow_fixed_f(float* e, float b) {
+    float q = b;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        float h;
+        q = two_sum_f(q, e[i], h);
+        e[i] = h;
+    }
+    e[M] = q;
+}
+
+// Exact sign of A_i B_j - A_j B_i with A = a - o, B = b - o (the determinant for a ray
+// along +e_AXIS), expanded into six products of input coordinates:
+//   a_i b_j - a_j b_i - a_i o_j + a_j o_i - o_i b_j + o_j b_i.
+// Coincident or axis-parallel collinear inputs are exact zeros without arithmetic.
+// When every nonzero coordinate lies in [2^-50, 2^50], each product is exactly the sum
+// of two floats (FMA two-product: no overflow, and the error term is a multiple of
+// 2^-146, above the subnormal spacing), and the twelve parts are summed exactly as a
+// float expansion (Shewchuk grow-expansion, zeros kept, registers only): FP32 throughput
+// on this part is many times its FP64 throughput.  Otherwise each product is exact in
+// FP64 and the six are summed as an FP64 expansion.
+__device__ __forceinline__ bool in_f32_range(float x) {
+    const float ax = fabsf(x);
+    return ax == 0.0f || (ax >= 8.881784197001252e-16f && ax <= 1.125899906842624e15f);
+}
+
+static __device__ __noinline__ int orient2_exact(float ai, float aj, float bi, float bj, float oi, float oj) {
+    note_exact();
+    if ((ai == oi && aj == oj) || (bi == oi && bj == oj) || (ai == bi && aj == bj) || (ai == oi && bi == oi) ||
+        (aj == oj && bj == oj))
+        return 0;
+    if (in_f32_range(ai) && in_f32_range(aj) && in_f32_range(bi) && in_f32_range(bj) && in_f32_range(oi) &&
+        in_f32_range(oj)) {
+        const float x[6] = {ai, -aj, -ai, aj, -oi, oj};
+        const float y[6] = {bj, bi, oj, oi, bj, bi};
+        float e[12];
+        e[0] = __fmul_rn(x[0], y[0]);
+        grow_fixed_f<1>(e, __fmaf_rn(x[0], y[0], -e[0]));
+#define RS_TWO_PROD_GROW(K, M)                                   \
+    {                                                            \
+        const float p = __fmul_rn(x[K], y[K]);                   \
+        grow_fixed_f<M>(e, p);                                   \
+        grow_fixed_f<M + 1>(e, __fmaf_rn(x[K], y[K], -p));       \
+    }
+        RS_TWO_PROD_GROW(1, 2)
+        RS_TWO_PROD_GROW(2, 4)
+        RS_TWO_PROD_GROW(3, 6)
+        RS_TWO_PROD_GROW(4, 8)
+        RS_TWO_PROD_GROW(5, 10)
+#undef RS_TWO_PROD_GROW
+#pragma unroll
+        for (int i = 11; i >= 0; --i)
+            if (e[i] != 0.0f) return e[i] > 0.0f ? 1 : -1;
+        return 0;
+    }
+    double e[6];
+    e[0] = __dmul_rn((double)ai, (double)bj);
+    grow_fixed<1>(e, -__dmul_rn((double)aj, (double)bi));
+    grow_fixed<2>(e, -__dmul_rn((double)ai, (double)oj));
+    grow_fixed<3>(e, __dmul_rn((double)aj, (double)oi));
+    grow_fixed<4>(e, -__dmul_rn((double)oi, (double)bj));
+    grow_fixed<5>(e, __dmul_rn((double)oj, (double)bi));
+#pragma unroll
+    for (int i = 5; i >= 0; --i)
+        if (e[i] != 0.0) return e[i] > 0.0 ? 1 : -1;
+    return 0;
+}
+
 // FP32 filter for det[d, a-o, b-o].  Roundings on any elementary product are at
 // most 7 (two input differences, product, difference, scale by d, two sums), so
 // |computed - exact| <= 7.01u * M with u = 2^-24 and M the float magnitude sum;
@@ -190,6 +311,10 @@ __device__ __forceinline__ int orient_sign(const float* d, const float* o, const
     if (mag > 7.888609052210118e-31f && mag < 3.0e38f) {  // 2^-100 < M < overflow
         if (det > bound) return 1;
         if (det < -bound) return -1;
+    }
+    if (AXIS >= 0) {
+        const int i = (AXIS + 1) % 3, j = (AXIS + 2) % 3;
+        return orient2_exact(a[i], a[j], b[i], b[j], o[i], o[j]);
     }
     return orient_exact(d[0], d[1], d[2], o[0], o[1], o[2], a[0], a[1], a[2], b[0], b[1], b[2]);
 }

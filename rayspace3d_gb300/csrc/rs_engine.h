@@ -67,6 +67,8 @@ int to_status(cudaError_t e);
 // (returns the build status); bvh_use() orders stream s after the build.
 int bvh_ready(const rs_bvh* h);
 int bvh_use(const rs_bvh* h, cudaStream_t s);
+// Builds the column grid of +e_axis rays for the handle if it does not exist yet.
+int ensure_grid(const rs_bvh* h, int axis, cudaStream_t s);
 // Broad-phase flags for one edge direction: cand[o] != 0 for source objects o that may
 // have a partner; no culling when cand is null.
 struct EdgeCull {
@@ -77,5 +79,6 @@ struct EdgeCull {
 // Recheck statistics of the translation units that run hit tests (see rs_device.cuh).
 int recheck_pim(int op, unsigned long long* out);
 int recheck_join(int op, unsigned long long* out);
+int recheck_batch(int op, unsigned long long* out);
 int status_from_bits(uint32_t bits);
 }  // namespace rs

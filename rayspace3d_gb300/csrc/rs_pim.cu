@@ -82,20 +82,6 @@ __global__ void __launch_bounds__(kT) k_pim(const float* __restrict__ pts, uint6
     write_result(hl.finish(), i, out_obj, out_in);
 }
 
-struct GridView {
-    float u0, v0, su, sv, u1, v1;
-    int gu, gv;
-    const uint32_t* start;
-    const uint32_t* list;
-};
-
-// Monotone cell index: identical for triangle boxes and query points.
-__device__ __forceinline__ int cell_of(float x, float x0, float s, int g) {
-    float f = floorf(__fmul_rn(__fsub_rn(x, x0), s));
-    f = fminf(fmaxf(f, 0.0f), (float)(g - 1));
-    return (int)f;
-}
-
 // Warp-cooperative column-grid query.  Each warp owns 32 points; their candidate
 // lists are flattened into one (point, triangle) work list with a warp scan, so every
 // lane tests one candidate per round however unevenly the candidates are spread over
@@ -109,91 +95,21 @@ __global__ void __launch_bounds__(kT) k_pim_grid(const float* __restrict__ pts, 
                                                  int32_t* __restrict__ out_obj, uint8_t* __restrict__ out_in,
                                                  uint32_t* __restrict__ ovf_list,
                                                  unsigned long long* __restrict__ ovf_count) {
-    __shared__ float s_t[kWarps][kHits][32];
-    __shared__ uint32_t s_id[kWarps][kHits][32];
-    __shared__ int32_t s_obj[kWarps][kHits][32];
-    __shared__ int s_n[kWarps][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __shared__ GridWarpSlots slots[kWarps];
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const bool valid = i < n;
-    constexpr int U = (AXIS + 1) % 3, V = (AXIS + 2) % 3;
     float p[3] = {0.0f, 0.0f, 0.0f};
     if (valid) {
         p[0] = pts[3 * i];
         p[1] = pts[3 * i + 1];
         p[2] = pts[3 * i + 2];
     }
-    const float dx = AXIS == 0 ? 1.0f : 0.0f, dy = AXIS == 1 ? 1.0f : 0.0f, dz = AXIS == 2 ? 1.0f : 0.0f;
     bool keep = valid;
-    if (FILTER && valid) keep = box_filter<AXIS>(box, make_ray(p[0], p[1], p[2], dx, dy, dz, kEps, kTmax));
-    uint32_t b = 0, cnt = 0;
-    // A crossed triangle's projected box contains the point, and all boxes lie in [u0,u1]x[v0,v1].
-    if (keep && p[U] >= g.u0 && p[U] <= g.u1 && p[V] >= g.v0 && p[V] <= g.v1) {
-        const int c = cell_of(p[V], g.v0, g.sv, g.gv) * g.gu + cell_of(p[U], g.u0, g.su, g.gu);
-        b = __ldg(&g.start[c]);
-        cnt = __ldg(&g.start[c + 1]) - b;
-    }
-    s_n[w][lane] = 0;
-    // Warp exclusive scan of the candidate counts.
-    uint32_t inc = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-    }
-    const uint32_t pre = inc - cnt;
-    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-    __syncwarp();
-    add_tests(lane == 0 ? total : 0u);
-    for (uint32_t base = 0; base < total; base += 32) {
-        const uint32_t j = base + lane;
-        // Owner of work item j: the last lane whose prefix is <= j.
-        int owner = 0;
-#pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-            const uint32_t pc = __shfl_sync(0xffffffffu, pre, owner + step);
-            if (pc <= j) owner += step;
-        }
-        const uint32_t ob = __shfl_sync(0xffffffffu, b, owner);
-        const uint32_t opre = __shfl_sync(0xffffffffu, pre, owner);
-        const float ox = __shfl_sync(0xffffffffu, p[0], owner);
-        const float oy = __shfl_sync(0xffffffffu, p[1], owner);
-        const float oz = __shfl_sync(0xffffffffu, p[2], owner);
-        if (j < total) {
-            const int k = (int)__ldg(&g.list[ob + (j - opre)]);
-            float a[3], bb[3], cc[3];
-            uint32_t tid;
-            int32_t obj;
-            load_tri(tris, k, a, bb, cc, tid, obj);
-            const Ray r = make_ray(ox, oy, oz, dx, dy, dz, kEps, kTmax);
-            float t;
-            if (hit_triangle<AXIS>(r, a, bb, cc, t)) {
-                const int slot = atomicAdd(&s_n[w][owner], 1);
-                if (slot < kHits) {
-                    s_t[w][slot][owner] = t;
-                    s_id[w][slot][owner] = tid;
-                    s_obj[w][slot][owner] = obj;
-                }
-            }
-        }
-    }
-    __syncwarp();
-    if (!valid) return;
-    const int nh = s_n[w][lane];
-    if (nh > kHits) {
-        ovf_list[atomicAdd(ovf_count, 1ull)] = (uint32_t)i;
-        return;
-    }
-    HitList hl;
-#pragma unroll
-    for (int q = 0; q < kHits; ++q)
-        if (q < nh) {
-            hl.t[q] = s_t[w][q][lane];
-            hl.id[q] = s_id[w][q][lane];
-            hl.obj[q] = s_obj[w][q][lane];
-        }
-    hl.n = nh;
-    write_result(hl.finish(), i, out_obj, out_in);
+    if (FILTER && valid)
+        keep = box_filter<AXIS>(box, make_ray(p[0], p[1], p[2], AXIS == 0 ? 1.0f : 0.0f, AXIS == 1 ? 1.0f : 0.0f,
+                                              AXIS == 2 ? 1.0f : 0.0f, kEps, kTmax));
+    pim_grid_warp<AXIS>(g, tris, p, valid, keep, i, out_obj, out_in, slots[threadIdx.x >> 5],
+                        [&]() { ovf_list[atomicAdd(ovf_count, 1ull)] = (uint32_t)i; });
 }
 
 // Exact fallback for rays with more than kHits crossings (pim_fallback_ray).
@@ -367,7 +283,9 @@ cudaError_t launch_pim(const rs_bvh* bvh, const float* pts, uint64_t n, float dx
                (const float4*)bvh->tris, box, obj, in, status, ovf_list, ovf_count);
     }
     prof_end(P_PIM, s, ptok);
-    launch(k_pim_fallback<AXIS>, 2 * sm_count(), 128, 0, s, pts, dx, dy, dz, bvh->nodes, max_steps(bvh),
+    // One thread per possible overflow entry (the count is only known on the device);
+    // threads past it return at once.
+    launch(k_pim_fallback<AXIS>, (unsigned)((n + kT - 1) / kT), kT, 0, s, pts, dx, dy, dz, bvh->nodes, max_steps(bvh),
            (const float4*)bvh->tris, obj, in, status, ovf_list, ovf_count);
     return cudaGetLastError();
 }
@@ -409,13 +327,9 @@ int pim_impl(const rs_bvh* cbvh, const float* pts, uint64_t n, float dx, float d
     if (dz == 1.0f && zx && zy) axis = 2;
     else if (dx == 1.0f && zy && zz) axis = 0;
     else if (dy == 1.0f && zx && zz) axis = 1;
-    if (axis >= 0 && bvh->n_tris > 0 && !bvh->cgrid[axis].built) {
-        // The column grid is built once per handle and axis, like the index build of the reference.
-        std::lock_guard<std::mutex> g(g_grid_mu);
-        if (!bvh->cgrid[axis].built) {
-            cudaError_t e = axis == 0 ? build_grid<0>(bvh, s) : (axis == 1 ? build_grid<1>(bvh, s) : build_grid<2>(bvh, s));
-            if (e != cudaSuccess) return to_status(e);
-        }
+    if (axis >= 0) {
+        st = ensure_grid(bvh, axis, s);
+        if (st != RS_OK) return st;
     }
     unsigned long long* meta = nullptr;  // [0] status, [1] overflow count, then the 12 box triangles
     uint32_t* ovf = nullptr;
@@ -473,6 +387,20 @@ __global__ void k_hit_scatter(const int32_t* __restrict__ obj, uint64_t n, const
 }
 
 }  // namespace
+
+// The column grid of one axis is built once per handle, like the index build of the
+// reference (allocates and synchronises the stream).
+int ensure_grid(const rs_bvh* cbvh, int axis, cudaStream_t s) {
+    rs_bvh* bvh = const_cast<rs_bvh*>(cbvh);
+    if (axis < 0 || axis > 2 || bvh->n_tris == 0 || bvh->cgrid[axis].built) return RS_OK;
+    std::lock_guard<std::mutex> g(g_grid_mu);
+    if (!bvh->cgrid[axis].built) {
+        cudaError_t e = axis == 0 ? build_grid<0>(bvh, s) : (axis == 1 ? build_grid<1>(bvh, s) : build_grid<2>(bvh, s));
+        if (e != cudaSuccess) return to_status(e);
+    }
+    return RS_OK;
+}
+
 
 int recheck_pim(int op, unsigned long long* out) { return recheck_op(op, out); }
 

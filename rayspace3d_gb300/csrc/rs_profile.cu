@@ -155,12 +155,14 @@ extern "C" int rs_profile_read(int kernel, double* total_ms, uint64_t* launches)
 extern "C" int rs_recheck_enable(int on) {
     int e = rs::recheck_pim(on ? 1 : 0, nullptr);
     if (e == 0) e = rs::recheck_join(on ? 1 : 0, nullptr);
+    if (e == 0) e = rs::recheck_batch(on ? 1 : 0, nullptr);
     return rs::to_status((cudaError_t)e);
 }
 
 extern "C" int rs_recheck_reset(void) {
     int e = rs::recheck_pim(2, nullptr);
     if (e == 0) e = rs::recheck_join(2, nullptr);
+    if (e == 0) e = rs::recheck_batch(2, nullptr);
     return rs::to_status((cudaError_t)e);
 }
 
@@ -168,6 +170,7 @@ extern "C" int rs_recheck_read(uint64_t* exact_signs, uint64_t* triangle_tests) 
     unsigned long long v[2] = {0, 0};
     int e = rs::recheck_pim(3, v);
     if (e == 0) e = rs::recheck_join(3, v);
+    if (e == 0) e = rs::recheck_batch(3, v);
     if (e != 0) return rs::to_status((cudaError_t)e);
     if (exact_signs) *exact_signs = v[0];
     if (triangle_tests) *triangle_tests = v[1];

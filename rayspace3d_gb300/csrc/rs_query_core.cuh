@@ -95,6 +95,120 @@ __device__ __forceinline__ void write_result(const Chain& ch, uint64_t i, int32_
     if (out_in) out_in[i] = inside ? 1 : 0;
 }
 
+struct GridView {
+    float u0, v0, su, sv, u1, v1;
+    int gu, gv;
+    const uint32_t* start;
+    const uint32_t* list;
+};
+
+// Monotone cell index: identical for triangle boxes and query points.
+__device__ __forceinline__ int cell_of(float x, float x0, float s, int g) {
+    float f = floorf(__fmul_rn(__fsub_rn(x, x0), s));
+    f = fminf(fmaxf(f, 0.0f), (float)(g - 1));
+    return (int)f;
+}
+
+// Candidates of a point from the column grid of the +e_AXIS direction (a crossed
+// triangle's projected box contains the point; all boxes lie in [u0,u1]x[v0,v1]).
+template <int AXIS>
+__device__ __forceinline__ void grid_cell(const GridView& g, const float* p, uint32_t& begin, uint32_t& count) {
+    constexpr int U = (AXIS + 1) % 3, V = (AXIS + 2) % 3;
+    begin = 0;
+    count = 0;
+    if (p[U] >= g.u0 && p[U] <= g.u1 && p[V] >= g.v0 && p[V] <= g.v1) {
+        const int c = cell_of(p[V], g.v0, g.sv, g.gv) * g.gu + cell_of(p[U], g.u0, g.su, g.gu);
+        begin = __ldg(&g.start[c]);
+        count = __ldg(&g.start[c + 1]) - begin;
+    }
+}
+
+// Shared-memory crossing slots of one warp for pim_grid_warp.
+struct GridWarpSlots {
+    float t[kHits][32];
+    uint32_t id[kHits][32];
+    int32_t obj[kHits][32];
+    int n[32];
+};
+
+// Warp-cooperative column-grid query of the warp's 32 points (all lanes call it; lanes
+// without a point pass valid = false, lanes whose point was filtered out keep = false).
+// The candidate lists are flattened into one (point, triangle) work list with a warp
+// scan, so every lane tests one candidate per round however unevenly candidates are
+// spread over the points.  Crossings go to per-point slots in shared memory; each lane
+// then sorts and counts its own point's, or calls overflow() when it has more than
+// kHits of them.
+template <int AXIS, class Ovf>
+__device__ __forceinline__ void pim_grid_warp(const GridView& g, const float4* __restrict__ tris, const float* p,
+                                              bool valid, bool keep, uint64_t i, int32_t* __restrict__ out_obj,
+                                              uint8_t* __restrict__ out_in, GridWarpSlots& sl, Ovf&& overflow) {
+    const int lane = threadIdx.x & 31;
+    const float dx = AXIS == 0 ? 1.0f : 0.0f, dy = AXIS == 1 ? 1.0f : 0.0f, dz = AXIS == 2 ? 1.0f : 0.0f;
+    uint32_t b = 0, cnt = 0;
+    if (keep) grid_cell<AXIS>(g, p, b, cnt);
+    sl.n[lane] = 0;
+    // Warp exclusive scan of the candidate counts.
+    uint32_t inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    const uint32_t pre = inc - cnt;
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    __syncwarp();
+    add_tests(lane == 0 ? total : 0u);
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t j = base + lane;
+        // Owner of work item j: the last lane whose prefix is <= j.
+        int owner = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t pc = __shfl_sync(0xffffffffu, pre, owner + step);
+            if (pc <= j) owner += step;
+        }
+        const uint32_t ob = __shfl_sync(0xffffffffu, b, owner);
+        const uint32_t opre = __shfl_sync(0xffffffffu, pre, owner);
+        const float ox = __shfl_sync(0xffffffffu, p[0], owner);
+        const float oy = __shfl_sync(0xffffffffu, p[1], owner);
+        const float oz = __shfl_sync(0xffffffffu, p[2], owner);
+        if (j < total) {
+            const int k = (int)__ldg(&g.list[ob + (j - opre)]);
+            float a[3], bb[3], cc[3];
+            uint32_t tid;
+            int32_t obj;
+            load_tri(tris, k, a, bb, cc, tid, obj);
+            const Ray r = make_ray(ox, oy, oz, dx, dy, dz, kEps, kTmax);
+            float t;
+            if (hit_triangle<AXIS>(r, a, bb, cc, t)) {
+                const int slot = atomicAdd(&sl.n[owner], 1);
+                if (slot < kHits) {
+                    sl.t[slot][owner] = t;
+                    sl.id[slot][owner] = tid;
+                    sl.obj[slot][owner] = obj;
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (!valid) return;
+    const int nh = sl.n[lane];
+    if (nh > kHits) {
+        overflow();
+        return;
+    }
+    HitList hl;
+#pragma unroll
+    for (int q = 0; q < kHits; ++q)
+        if (q < nh) {
+            hl.t[q] = sl.t[q][lane];
+            hl.id[q] = sl.id[q][lane];
+            hl.obj[q] = sl.obj[q][lane];
+        }
+    hl.n = nh;
+    write_result(hl.finish(), i, out_obj, out_in);
+}
+
 // Every crossing of ray r with t in [1e-6, 1e16] into hl (BVH traversal).  Returns false
 // on an exhausted traversal budget or stack.
 template <int AXIS, int STACK>
@@ -117,11 +231,57 @@ __device__ __forceinline__ bool pim_collect(const BNode* __restrict__ nodes, uin
 // Exact fallback for a ray with more than kHits crossings: each round re-traverses the
 // BVH and takes the smallest (t, id) above the previous one, so the crossings are
 // walked in the same order as the sorted list.
+constexpr int kLongHits = 64;
+
 template <int AXIS, int STACK>
 __device__ __forceinline__ void pim_fallback_ray(const BNode* __restrict__ nodes, uint32_t max_steps,
                                                  const float4* __restrict__ tris, const Ray& r,
                                                  unsigned int* __restrict__ status, int32_t* __restrict__ out_obj,
                                                  uint8_t* __restrict__ out_in, uint64_t i) {
+    // One traversal into a local list of up to kLongHits crossings, insertion-sorted by
+    // (t, id); only rays with more crossings walk them by re-traversal below.
+    {
+        float lt[kLongHits];
+        uint32_t lid[kLongHits];
+        int32_t lobj[kLongHits];
+        int n = 0;
+        bool more = false;
+        const bool ok = traverse<AXIS, STACK>(nodes, max_steps, r, [&](int first, int c) {
+            for (int k = first; k < first + c; ++k) {
+                float a[3], b[3], cc[3];
+                uint32_t tid;
+                int32_t obj;
+                load_tri(tris, k, a, b, cc, tid, obj);
+                float t;
+                if (!hit_triangle<AXIS>(r, a, b, cc, t)) continue;
+                if (n == kLongHits) {
+                    more = true;
+                    continue;
+                }
+                int j = n++;
+                while (j > 0 && hit_less(t, tid, lt[j - 1], lid[j - 1])) {
+                    lt[j] = lt[j - 1];
+                    lid[j] = lid[j - 1];
+                    lobj[j] = lobj[j - 1];
+                    --j;
+                }
+                lt[j] = t;
+                lid[j] = tid;
+                lobj[j] = obj;
+            }
+        });
+        if (!ok) {
+            atomicOr(status, ST_STACK_OVERFLOW);
+            write_result(Chain{}, i, out_obj, out_in);
+            return;
+        }
+        if (!more) {
+            Chain ch;
+            for (int j = 0; j < n; ++j) ch.step(lt[j], lobj[j]);
+            write_result(ch, i, out_obj, out_in);
+            return;
+        }
+    }
     Chain ch;
     float pt = -INFINITY;
     uint32_t pid = 0;

@@ -1,0 +1,120 @@
+"""Seeded synthetic workloads generated directly in device memory (torch on the GPU).
+
+For workloads too large to build on the host (the batched configuration: hundreds of
+millions of points and triangles): instanced icospheres and boxes with per-object
+transforms, their edge payloads, and query points with a share snapped exactly onto
+mesh vertices, edges and faces.  Instances of one template never share quantised
+edge endpoints (random transforms), so each object's unique template edges are its
+edge payload with the object as the only source -- the set that
+``EdgePreprocessor::extractEdges`` (preprocess/src/EdgePreprocessor.cpp:41-119) would
+produce, with its first-occurrence orientation, listed per object rather than in
+``std::map`` order.  Edge-ray results do not depend on the order.  Face-sharing cube
+blocks, whose edges are shared across objects, come from the host generator
+(``synth.cube_grid``) instead.
+"""
+from __future__ import annotations
+
+from typing import Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import synth
+from .api import DeviceGeometry
+
+_TEMPLATE = {}
+
+
+def _template(kind: str, level: int, device):
+    key = (kind, level, str(device))
+    if key not in _TEMPLATE:
+        if kind == "sphere":
+            v, f = synth.icosphere(level)
+        else:
+            v, f = synth.cube_mesh((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0))
+            v = v.astype(np.float64)
+        # Edges in face order (v0v1, v1v2, v2v0 of each face), each kept with the
+        # orientation of its first occurrence, as the reference's extraction does.
+        e = np.stack([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]], axis=1).reshape(-1, 2).astype(np.int64)
+        _, first = np.unique(np.sort(e, axis=1), axis=0, return_index=True)
+        e = e[np.sort(first)]
+        _TEMPLATE[key] = (torch.from_numpy(np.asarray(v, np.float64)).to(device),
+                          torch.from_numpy(np.asarray(f, np.int64)).to(device),
+                          torch.from_numpy(e).to(device))
+    return _TEMPLATE[key]
+
+
+def _rotations(g: torch.Generator, n: int, device) -> torch.Tensor:
+    q = torch.randn((n, 4), generator=g, device=device, dtype=torch.float64)
+    q = q / q.norm(dim=1, keepdim=True)
+    w, x, y, z = q.unbind(1)
+    R = torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w),
+                     2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w),
+                     2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], dim=1)
+    return R.view(n, 3, 3)
+
+
+def instanced_set(n_objects: int, level: int, r_lo: float, r_hi: float, world: float, seed: int,
+                  kind: str = "sphere", device="cuda") -> DeviceGeometry:
+    """n objects of one template (icosphere of `level`, or a box), radius log-uniform in
+    [r_lo, r_hi], Haar rotation, centre uniform in [0, world]^3; with edges."""
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    tv, tf, te = _template(kind, level, dev)
+    nv, nf, ne = tv.shape[0], tf.shape[0], te.shape[0]
+    radii = torch.exp(torch.empty(n_objects, device=dev, dtype=torch.float64).uniform_(
+        float(np.log(r_lo)), float(np.log(r_hi)), generator=g))
+    R = _rotations(g, n_objects, dev)
+    centers = torch.rand((n_objects, 3), generator=g, device=dev, dtype=torch.float64) * world
+    p = torch.einsum("nvk,njk->nvj", tv[None] * radii[:, None, None], R) + centers[:, None, :]
+    V = p.to(torch.float32).reshape(-1, 3).contiguous()
+    base = (torch.arange(n_objects, device=dev, dtype=torch.int64) * nv)
+    I = (tf[None] + base[:, None, None]).reshape(-1, 3).to(torch.int32).contiguous()
+    T = torch.arange(n_objects, device=dev, dtype=torch.int32).repeat_interleave(nf).contiguous()
+    ei = (te[None] + base[:, None, None]).reshape(-1, 2)
+    starts = V[ei[:, 0]].contiguous()
+    ends = V[ei[:, 1]].contiguous()
+    nE = n_objects * ne
+    offsets = torch.arange(nE, device=dev, dtype=torch.int32)
+    counts = torch.ones(nE, device=dev, dtype=torch.int32)
+    sources = torch.arange(n_objects, device=dev, dtype=torch.int32).repeat_interleave(ne).contiguous()
+    return DeviceGeometry.from_tensors(V, I, T, edges=(starts, ends, offsets, counts, sources))
+
+
+def mesh_points(dg: DeviceGeometry, n: int, seed: int, frac_snapped: float = 0.2, pad: float = 0.25,
+                device="cuda") -> torch.Tensor:
+    """n points uniform in the padded bounds of the mesh; a share placed exactly on
+    vertices, on edges (rounded convex combinations) and on faces."""
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    lo = dg.V.min(dim=0).values - pad
+    hi = dg.V.max(dim=0).values + pad
+    pts = lo + torch.rand((n, 3), generator=g, device=dev) * (hi - lo)
+    k = int(n * frac_snapped)
+    if k and dg.nF:
+        tri = dg.I[torch.randint(0, dg.nF, (k,), generator=g, device=dev)].long()
+        a, b, c = dg.V[tri[:, 0]].double(), dg.V[tri[:, 1]].double(), dg.V[tri[:, 2]].double()
+        which = torch.randint(0, 3, (k, 1), generator=g, device=dev)
+        w = torch.rand((k, 1), generator=g, device=dev, dtype=torch.float64)
+        u = -torch.log(torch.rand((k, 3), generator=g, device=dev, dtype=torch.float64).clamp_min(1e-300))
+        u = u / u.sum(dim=1, keepdim=True)
+        snap = torch.where(which == 0, a, torch.where(which == 1, a + w * (b - a),
+                                                      u[:, :1] * a + u[:, 1:2] * b + u[:, 2:] * c))
+        idx = torch.randperm(n, generator=g, device=dev)[:k]
+        pts[idx] = snap.to(torch.float32)
+    return pts.contiguous()
+
+
+def to_host_geometry(dg: DeviceGeometry):
+    """Host copy (for the oracle on small cases)."""
+    from .formats import Edges, Geometry
+    V = dg.V.cpu().numpy()
+    I = dg.I.cpu().numpy().view(np.uint32)
+    T = dg.T.cpu().numpy()
+    edges = None
+    if dg.edges is not None:
+        s, e, o, c, src = [t.cpu().numpy() for t in dg.edges]
+        edges = Edges(s, e, o, c, src)
+    return Geometry(V, I, T, total_triangles=len(I), edges=edges)

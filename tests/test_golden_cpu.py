@@ -351,3 +351,26 @@ def test_cli_missing_input(cli_bin, app, flag):
     r = subprocess.run([os.path.join(cli_bin, app)], capture_output=True, text=True, timeout=60)
     assert r.returncode != 0
     assert flag in (r.stderr + r.stdout)
+
+
+def test_device_generator_edges_match_extraction():
+    """The device generator lists each object's template edges; for instanced objects that
+    is the set the reference's extraction produces, with the same orientations, and
+    joins over either payload agree."""
+    torch = pytest.importorskip("torch")
+    from rayspace3d_gb300 import gen
+    for kind, level in (("sphere", 1), ("box", 0)):
+        dg = gen.instanced_set(40, level, 0.5, 2.0, 8.0, seed=5, kind=kind, device="cpu")
+        g = gen.to_host_geometry(dg)
+        ref = synth.extract_edges(g.vertices, g.indices, g.tri2obj)
+
+        def key_set(e):  # (source, start bits, end bits): oriented edges per source
+            src = e.sources[e.offsets]
+            return sorted(zip(src.tolist(), map(tuple, e.starts.view(np.uint32).tolist()),
+                              map(tuple, e.ends.view(np.uint32).tolist())))
+        assert np.all(ref.counts == 1)
+        assert key_set(ref) == key_set(g.edges)
+        other = synth.sphere_set(40, 1, 0.5, 2.0, 8.0, np.random.default_rng(6))
+        a = bind.edge_join(ref, other.vertices, other.indices, other.tri2obj)
+        b = bind.edge_join(g.edges, other.vertices, other.indices, other.tri2obj)
+        np.testing.assert_array_equal(a, b)
