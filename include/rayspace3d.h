@@ -237,6 +237,43 @@ int rs_batch_wait(rs_batch* batch, int* h_status);
 int rs_batch_autotune(rs_batch* batch, int* h_leaf_size, int* h_chunk, int* h_stack_depth, double* h_ms,
                       void* stream);
 
+/* Grid statistics on the GPU (generateGridStats, preprocess/src/preprocess_dataset.cpp:37-181)
+ * for a triangle set in device memory: d_cells receives resolution^3 GridCell records
+ * (16 B: u32 CenterCount, u32 TouchCount, f32 AvgSizeMean, f32 VolRatio; index
+ * (z*R+y)*R+x); the frame is [0, world_size]^3, or the bounds of all vertices when
+ * world_size <= 0 (h_bounds6 receives min xyz, max xyz; nullable).  Objects are ids
+ * 0..n_obj-1.  Per-cell float sums are taken in arrival order, so AvgSizeMean and VolRatio
+ * may differ from the reference's in the last bits; the counts are exact. */
+int rs_grid_stats(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                  const int32_t* d_tri2obj, uint64_t n_obj, int resolution, float world_size, void* d_cells,
+                  float* h_bounds6, void* stream);
+
+/* Learned selectivity estimator (no counterpart in the reference; BASELINE config 5): a
+ * 32768 -> 512 -> 512 -> 1 ReLU MLP on pooled grid features predicting log1p(pairs),
+ * trained and evaluated with the engine's BF16 tensor-core GEMM kernels (FP32 accumulate,
+ * FP32 master weights, Adam).  Features (rs_mlp_features): each grid pooled to 16^3
+ * blocks x {log1p sum CenterCount, log1p sum TouchCount, log1p TouchCount-weighted
+ * AvgSizeMean, TouchCount-weighted VolRatio}, side A then side B (32768 floats).
+ * Parameters are one FP32 array of rs_mlp_num_params() values: W1[512][32768], b1[512],
+ * W2[512][512], b2[512], W3[512], b3[1]. */
+typedef struct rs_mlp rs_mlp;
+int rs_mlp_create(uint64_t seed, rs_mlp** out);
+int rs_mlp_destroy(rs_mlp* mlp);
+uint64_t rs_mlp_num_params(void);
+int rs_mlp_get_params(const rs_mlp* mlp, float* h_params, float* h_grads);
+int rs_mlp_set_params(rs_mlp* mlp, const float* h_params);
+int rs_mlp_features(const void* d_cellsA, const void* d_cellsB, int resolution, float* d_out32768, void* stream);
+/* d_X: B rows of 32768 FP32 features; d_y: B predictions (log1p pairs). */
+int rs_mlp_forward(rs_mlp* mlp, const float* d_X, int B, float* d_y, void* stream);
+/* Mean squared error against d_target and its gradients (read with rs_mlp_get_params). */
+int rs_mlp_gradients(rs_mlp* mlp, const float* d_X, const float* d_target, int B, float* h_loss, void* stream);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on a minibatch. */
+int rs_mlp_train_step(rs_mlp* mlp, const float* d_X, const float* d_target, int B, float lr, float* h_loss,
+                      void* stream);
+/* Estimated pair count of two grids (expm1 of the prediction, rounded; h_log1p nullable). */
+int rs_estimate_mlp(rs_mlp* mlp, const void* d_cellsA, const void* d_cellsB, int resolution, int64_t* h_estimate,
+                    double* h_log1p, void* stream);
+
 /* Diagnostics (no counterpart in the reference).  rs_launch_count: kernels launched by this
  * library since load.  rs_profile_*: when enabled, device time of the main kernels is
  * accumulated with CUDA events on the launching stream; ids 0 edge join, 1 containment,

@@ -65,6 +65,17 @@ SIGNATURES = {
     "rs_profile_read": (I, [I, ctypes.POINTER(ctypes.c_double), PU64]),
     "rs_recheck_enable": (I, [I]),
     "rs_set_overlap_cull": (I, [I]),
+    "rs_grid_stats": (I, [P, U64, P, U64, P, U64, I, F, P, ctypes.POINTER(F), P]),
+    "rs_mlp_create": (I, [U64, PP]),
+    "rs_mlp_destroy": (I, [P]),
+    "rs_mlp_num_params": (U64, []),
+    "rs_mlp_get_params": (I, [P, ctypes.POINTER(F), ctypes.POINTER(F)]),
+    "rs_mlp_set_params": (I, [P, ctypes.POINTER(F)]),
+    "rs_mlp_features": (I, [P, P, I, P, P]),
+    "rs_mlp_forward": (I, [P, P, I, P, P]),
+    "rs_mlp_gradients": (I, [P, P, P, I, ctypes.POINTER(F), P]),
+    "rs_mlp_train_step": (I, [P, P, P, I, F, ctypes.POINTER(F), P]),
+    "rs_estimate_mlp": (I, [P, P, P, I, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double), P]),
     "rs_batch_create": (I, [PP]),
     "rs_batch_destroy": (I, [P]),
     "rs_batch_add_pim": (I, [P, P, P, U64, F, F, F, P, P, ctypes.POINTER(I)]),

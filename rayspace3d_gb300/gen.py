@@ -55,9 +55,10 @@ def _rotations(g: torch.Generator, n: int, device) -> torch.Tensor:
 
 
 def instanced_set(n_objects: int, level: int, r_lo: float, r_hi: float, world: float, seed: int,
-                  kind: str = "sphere", device="cuda") -> DeviceGeometry:
+                  kind: str = "sphere", device="cuda", centers: Optional[torch.Tensor] = None) -> DeviceGeometry:
     """n objects of one template (icosphere of `level`, or a box), radius log-uniform in
-    [r_lo, r_hi], Haar rotation, centre uniform in [0, world]^3; with edges."""
+    [r_lo, r_hi], Haar rotation, centre uniform in [0, world]^3 (or the given float64
+    centers[n,3]); with edges."""
     dev = torch.device(device)
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
@@ -66,7 +67,10 @@ def instanced_set(n_objects: int, level: int, r_lo: float, r_hi: float, world: f
     radii = torch.exp(torch.empty(n_objects, device=dev, dtype=torch.float64).uniform_(
         float(np.log(r_lo)), float(np.log(r_hi)), generator=g))
     R = _rotations(g, n_objects, dev)
-    centers = torch.rand((n_objects, 3), generator=g, device=dev, dtype=torch.float64) * world
+    if centers is None:
+        centers = torch.rand((n_objects, 3), generator=g, device=dev, dtype=torch.float64) * world
+    else:
+        centers = centers.to(device=dev, dtype=torch.float64)
     p = torch.einsum("nvk,njk->nvj", tv[None] * radii[:, None, None], R) + centers[:, None, :]
     V = p.to(torch.float32).reshape(-1, 3).contiguous()
     base = (torch.arange(n_objects, device=dev, dtype=torch.int64) * nv)
@@ -118,3 +122,40 @@ def to_host_geometry(dg: DeviceGeometry):
         s, e, o, c, src = [t.cpu().numpy() for t in dg.edges]
         edges = Edges(s, e, o, c, src)
     return Geometry(V, I, T, total_triangles=len(I), edges=edges)
+
+
+def concat(parts) -> DeviceGeometry:
+    """One set from several (object ids and vertex indices offset; edges included)."""
+    Vs, Is, Ts, E = [], [], [], [[], [], [], [], []]
+    voff = ooff = eoff = soff = 0
+    for g in parts:
+        Vs.append(g.V)
+        Is.append(g.I + voff)
+        Ts.append(g.T + ooff)
+        if g.edges is not None:
+            s, e, o, c, src = g.edges
+            E[0].append(s)
+            E[1].append(e)
+            E[2].append(o + soff)
+            E[3].append(c)
+            E[4].append(src + ooff)
+            soff += int(src.shape[0])
+        voff += g.nV
+        ooff += int(g.T.max().item()) + 1 if g.nF else 0
+    edges = tuple(torch.cat(x) for x in E) if E[0] else None
+    return DeviceGeometry.from_tensors(torch.cat(Vs), torch.cat(Is), torch.cat(Ts), edges=edges)
+
+
+def mixture_centers(n: int, k: int, world: float, seed: int, device="cuda") -> torch.Tensor:
+    """n centres from a Gaussian mixture of k components (means uniform in the world,
+    sigma log-uniform in [world/200, world/5], weights Dirichlet(1)), clipped to the world."""
+    dev = torch.device(device)
+    g = torch.Generator(device="cpu")
+    g.manual_seed(seed)
+    means = torch.rand((k, 3), generator=g, dtype=torch.float64) * world
+    sig = torch.exp(torch.empty(k, dtype=torch.float64).uniform_(float(np.log(world / 200)),
+                                                                  float(np.log(world / 5)), generator=g))
+    w = -torch.log(torch.rand(k, generator=g, dtype=torch.float64).clamp_min(1e-12))
+    comp = torch.multinomial(w / w.sum(), n, replacement=True, generator=g)
+    c = means[comp] + torch.randn((n, 3), generator=g, dtype=torch.float64) * sig[comp, None]
+    return c.clamp(0.0, world).to(dev)
