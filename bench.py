@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--no-pim", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--batch-full", action="store_true", help="batched workload at its full size")
+    ap.add_argument("--learned-full", action="store_true", help="learned estimator at its full size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -556,6 +557,84 @@ def run_batch(args, full: bool):
             "recheck": rc_stats, "spot_checks_passed": checks}
 
 
+def run_learned(args, full: bool):
+    """Learned selectivity estimator: dataset pairs (mixture-placed icospheres and boxes,
+    radii log-uniform in [0.1, 50], 1000^3 world; 1k..200k objects per side in the full
+    run, 1k..20k by default), labelled by the engine's exact joins; train on all but the
+    held-out pairs; errors of the network and of the grid estimator on the held-out ones;
+    tensor-core throughput of the forward pass (bound: BF16 tensor peak)."""
+    import ctypes
+
+    import torch
+    from rayspace3d_gb300 import _lib, learned
+
+    n_train, n_test = (2000, 200) if full else (240, 60)
+    n_hi = 200_000 if full else 20_000
+    t0 = time.perf_counter()
+    samples = [learned.make_sample(10_000 + i, 1000, n_hi) for i in range(n_train + n_test)]
+    gen_s = time.perf_counter() - t0
+    train, test = samples[:n_train], samples[n_train:]
+    t0 = time.perf_counter()
+    m, losses = learned.train(train, epochs=40 if full else 80, batch=64, lr=1e-3, seed=0)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    ev_test = learned.evaluate(m, test)
+    ev_train = learned.evaluate(m, train)
+    # Forward-pass throughput on a 256-row batch (2 * (32768*512 + 512*512 + 512) flop/row).
+    B = 256
+    X = torch.rand((B, learned.N_FEAT), device="cuda")
+    for _ in range(3):
+        m.forward(X)
+    torch.cuda.synchronize()
+    reps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        m.forward(X)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flop = 2.0 * B * (32768 * 512 + 512 * 512 + 512)
+    tflops = flop / (ms * 1e-3) / 1e12
+    peak = None
+    try:
+        with open(MEASURED_PEAKS) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        peak = 1900.0
+    # Estimator latency: grid estimator vs network, one pair.
+    s0 = test[0]
+    L = _lib.load()
+    rng = np.random.default_rng(10_000 + n_train)
+    A, na = learned.dataset_side(4 * (10_000 + n_train), 1000, n_hi, rng)
+    Bs, nb = learned.dataset_side(4 * (10_000 + n_train) + 3, 1000, n_hi, rng)
+    ca, cb = learned.grid_cells(A, na), learned.grid_cells(Bs, nb)
+    est, lg = ctypes.c_int64(), ctypes.c_double()
+    from rayspace3d_gb300 import api
+    for _ in range(3):
+        L.rs_estimate_mlp(m.h, ca.data_ptr(), cb.data_ptr(), learned.RES, ctypes.byref(est), ctypes.byref(lg), None)
+        api.estimate_grid(ca, cb, learned.RES ** 3, learned._cell_volume())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(20):
+        L.rs_estimate_mlp(m.h, ca.data_ptr(), cb.data_ptr(), learned.RES, ctypes.byref(est), ctypes.byref(lg), None)
+    mlp_ms = (time.perf_counter() - t0) / 20 * 1e3
+    t0 = time.perf_counter()
+    for _ in range(20):
+        api.estimate_grid(ca, cb, learned.RES ** 3, learned._cell_volume())
+    grid_ms = (time.perf_counter() - t0) / 20 * 1e3
+    m.close()
+    return {"workload": f"{n_train} training + {n_test} held-out dataset pairs, 1000..{n_hi} objects per side, "
+                        "128^3 grids pooled to 16^3x4 per side, MLP 32768-512-512-1 (BF16 weights, FP32 accumulate)",
+            "generation_s": round(gen_s, 1), "train_s": round(train_s, 2), "final_train_loss": round(losses[-1], 4),
+            "held_out": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in ev_test.items()},
+            "train_set": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in ev_train.items()},
+            "estimator_ms": {"mlp": round(mlp_ms, 3), "grid": round(grid_ms, 3)},
+            "roofline": {"bound": "tensor", "kernel": "k_gemm (mma.sync m16n8k16 bf16), forward pass B=256",
+                         "achieved": round(tflops, 2), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(tflops / peak, 5), "ms": round(ms, 4)}}
+
+
 def cpu_join_sample(A, B, frac=0.02, threads=None):
     """Oracle overlap join on a bounded sample of both edge sets, extrapolated to one
     full join: 2 x CPU BVH build + (sampled traversal time / frac)."""
@@ -624,6 +703,7 @@ def main():
     if not args.no_variants:
         result["join_w80"] = run_join_variant(args, 80.7)
         result["batch"] = run_batch(args, args.batch_full)
+        result["learned"] = run_learned(args, args.learned_full)
     if rank == 0 and not args.no_cpu_baseline:
         v, meta = cpu_join_sample(A, B, frac=0.01)
         result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": meta["cores"], "kind": "port",
