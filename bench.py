@@ -57,6 +57,7 @@ def parse_args():
     ap.add_argument("--no-variants", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--batch-full", action="store_true", help="batched workload at its full size")
     ap.add_argument("--learned-full", action="store_true", help="learned estimator at its full size")
+    ap.add_argument("--intersection-n", type=int, default=10_000, help="objects per set of the intersection join")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -557,6 +558,58 @@ def run_batch(args, full: bool):
             "recheck": rc_stats, "spot_checks_passed": checks}
 
 
+def run_intersection(args, n: int):
+    """Full intersection join at uneven sizes: n objects per set (10k by default; the
+    configuration names 100k, whose two resident BVHs at 112 B per triangle plus the
+    inputs exceed the GPU's memory) of icospheres with levels 1..5 (triangle counts
+    log-uniform), radii log-uniform in [0.2, 20], uniform in a 2000^3 world (scaled to keep
+    the density at smaller n), seed 2, 5 % of B planted strictly inside A objects.  One
+    step = both BVH builds (concurrent) + overlap both ways + containment both ways +
+    sorted pair list."""
+    import torch
+    from rayspace3d_gb300 import api, gen
+
+    world = 2000.0 * (n / 100_000) ** (1.0 / 3.0)
+    t0 = time.perf_counter()
+    A, B, planted = gen.intersection_sets(n, seed=2, world=world)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        ps = api.PairSet(1 << 20, stream=stream)
+
+        def step():
+            sa.wait_stream(stream)
+            sb.wait_stream(stream)
+            ba, bb = api.Bvh(A, stream=sa, asynchronous=True), api.Bvh(B, stream=sb, asynchronous=True)
+            ps.clear(stream=stream)
+            api.overlap_join(ba, bb, ps, with_containment=True, stream=stream)
+            keys = ps.finalize(stream=stream)
+            ba.close()
+            bb.close()
+            return keys
+
+        keys = step()
+        torch.cuda.synchronize()
+        steps = 3
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            keys = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+    k = keys.cpu().numpy().astype(np.uint64)
+    ks = set(int(x) for x in k)
+    found = sum(((a << 32) | b) in ks for a, b in planted)
+    return {"workload": f"full intersection: {n} + {n} icospheres of levels 1..5, radii 0.2..20, world {world:.0f}^3, "
+                        f"seed 2, {len(planted)} B objects planted inside A",
+            "seconds": round(ms / 1e3, 5), "pairs": int(len(k)), "planted_found": int(found),
+            "planted": len(planted), "triangles_per_set": [int(A.nF), int(B.nF)],
+            "edge_rays": int(A.nE + B.nE), "generation_s": round(gen_s, 1)}
+
+
 def run_learned(args, full: bool):
     """Learned selectivity estimator: dataset pairs (mixture-placed icospheres and boxes,
     radii log-uniform in [0.1, 50], 1000^3 world; 1k..200k objects per side in the full
@@ -704,6 +757,7 @@ def main():
         result["join_w80"] = run_join_variant(args, 80.7)
         result["batch"] = run_batch(args, args.batch_full)
         result["learned"] = run_learned(args, args.learned_full)
+        result["intersection"] = run_intersection(args, args.intersection_n)
     if rank == 0 and not args.no_cpu_baseline:
         v, meta = cpu_join_sample(A, B, frac=0.01)
         result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": meta["cores"], "kind": "port",

@@ -159,3 +159,84 @@ def mixture_centers(n: int, k: int, world: float, seed: int, device="cuda") -> t
     comp = torch.multinomial(w / w.sum(), n, replacement=True, generator=g)
     c = means[comp] + torch.randn((n, 3), generator=g, dtype=torch.float64) * sig[comp, None]
     return c.clamp(0.0, world).to(dev)
+
+
+def intersection_sets(n: int, seed: int, world: float = 2000.0, levels=(1, 2, 3, 4, 5), r_lo: float = 0.2,
+                      r_hi: float = 20.0, frac_inside: float = 0.05, device="cuda"):
+    """The full-intersection configuration: n objects per set, icospheres whose level is
+    drawn uniformly from `levels` (triangle counts log-uniform), radii log-uniform in
+    [r_lo, r_hi], centres uniform in [0, world]^3.  A share frac_inside of B is placed
+    strictly inside random A objects: radius 0.10..0.35 of the A radius, centre offset
+    below 0.9 (0.75 R_A - r_B), so the whole object stays within 0.8 R_A, inside the
+    inscribed sphere of any icosphere of level >= 1 (0.94 R).  Returns (A, B, planted),
+    planted = list of (a, b) object ids."""
+    rng = np.random.default_rng(seed)
+    dev = torch.device(device)
+
+    def draw(k):
+        lv = rng.choice(np.asarray(levels), size=k)
+        r = np.exp(rng.uniform(np.log(r_lo), np.log(r_hi), size=k))
+        c = rng.uniform(0.0, world, size=(k, 3))
+        return lv, r, c
+
+    la, ra, ca = draw(n)
+    lb, rb, cb = draw(n)
+    k_in = int(round(n * frac_inside))
+    inside_b = rng.choice(n, size=k_in, replace=False)
+    host_a = rng.integers(0, n, size=k_in)
+    planted = []
+    for b, a in zip(inside_b, host_a):
+        rb[b] = ra[a] * rng.uniform(0.10, 0.35)
+        v = rng.standard_normal(3)
+        v /= np.linalg.norm(v)
+        off = rng.uniform(0.0, 1.0) * 0.9 * (0.75 * ra[a] - rb[b])
+        cb[b] = ca[a] + v * off
+        planted.append((int(a), int(b)))
+
+    def build(lv, r, c, sseed):
+        # objects keep their ids: each level's objects are generated together and the
+        # vertex/index/edge blocks are reordered back to id order afterwards
+        parts, ids = [], []
+        for L in sorted(set(lv.tolist())):
+            idx = np.nonzero(lv == L)[0]
+            g = instanced_set(len(idx), int(L), 1.0, 1.0, 0.0, seed=sseed + int(L), device=device,
+                              centers=torch.from_numpy(c[idx]))
+            # radii: scale each object's vertices about its centre
+            nv = g.nV // len(idx)
+            cc = torch.from_numpy(c[idx]).to(dev)
+            rr = torch.from_numpy(r[idx]).to(dev)
+            Vd = g.V.double().view(len(idx), nv, 3)
+            Vd = (Vd - cc[:, None, :]) * rr[:, None, None] + cc[:, None, :]
+            V = Vd.to(torch.float32).reshape(-1, 3)
+            s, e, o, cnt, src = g.edges
+            ne = s.shape[0] // len(idx)
+            s = ((s.double().view(len(idx), ne, 3) - cc[:, None, :]) * rr[:, None, None] + cc[:, None, :]) \
+                .to(torch.float32).reshape(-1, 3)
+            e = ((e.double().view(len(idx), ne, 3) - cc[:, None, :]) * rr[:, None, None] + cc[:, None, :]) \
+                .to(torch.float32).reshape(-1, 3)
+            idmap = torch.from_numpy(idx.astype(np.int32)).to(dev)
+            T = idmap[g.T.long()]
+            src = idmap[src.long()]
+            parts.append(DeviceGeometry.from_tensors(V, g.I, T, edges=(s, e, o, cnt, src)))
+            ids.append(idx)
+        # concatenate without renumbering objects
+        Vs, Is, Ts, E = [], [], [], [[], [], [], [], []]
+        voff = soff = 0
+        for g in parts:
+            Vs.append(g.V)
+            Is.append(g.I + voff)
+            Ts.append(g.T)
+            s, e, o, cnt, src = g.edges
+            E[0].append(s)
+            E[1].append(e)
+            E[2].append(o + soff)
+            E[3].append(cnt)
+            E[4].append(src)
+            soff += int(src.shape[0])
+            voff += g.nV
+        return DeviceGeometry.from_tensors(torch.cat(Vs), torch.cat(Is), torch.cat(Ts),
+                                           edges=tuple(torch.cat(x) for x in E))
+
+    A = build(la, ra, ca, 100 * seed + 1)
+    B = build(lb, rb, cb, 100 * seed + 51)
+    return A, B, planted
