@@ -297,7 +297,7 @@ def run_engine(args, rank, world, local):
         "config": {"workload": WORKLOAD, "objects_per_set": args.objects, "world": args.world,
                    "edges_per_set": int(da.nE), "triangles_per_set": int(da.nF), "pairs": n_pairs,
                    "l2": "inputs larger than L2 (geometry ~487 MB + grids 64 MB per step)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"independent joins per rank x{world}"},
         "e2e": {"value": round(e2e_s, 6), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "recheck": rc,

@@ -9,6 +9,7 @@
 // __anyhit__ah_containment (mesh_intersection_anyhit.cu:46-240): one +Z ray per
 // source object, parity per target object kept in registers instead of a
 // 256-slot global scratch per object.
+#include <algorithm>
 #include <climits>
 
 #include "rs_engine.h"
@@ -26,23 +27,52 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
                                                   const int32_t* __restrict__ counts,
                                                   const int32_t* __restrict__ sources, uint64_t nE,
                                                   const BNode* __restrict__ nodes, uint32_t max_steps,
-                                                  const float4* __restrict__ tris, int swap, PairTable table,
-                                                  const uint8_t* __restrict__ cull, uint64_t n_cull) {
+                                                  const float4* __restrict__ tris, int swap, PairTable table) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= nE) return;
-    if (cull) {
-        // Broad phase: an edge whose source objects have no candidate partner cannot
-        // cross a target triangle (see k_cull_query).
+    edge_ray<kStack>(starts, ends, offsets, counts, sources, i, nodes, max_steps, tris, swap, table);
+}
+
+// Broad phase of one direction: the edges with at least one candidate source object
+// (k_cull_query) are appended to `live` (any order: the pair table deduplicates).  A
+// light kernel, so the dependent loads of many edges are in flight at once.
+__global__ void __launch_bounds__(256) k_edge_live(const int32_t* __restrict__ offsets,
+                                                   const int32_t* __restrict__ counts,
+                                                   const int32_t* __restrict__ sources, uint64_t nE,
+                                                   const uint8_t* __restrict__ cull, uint64_t n_cull,
+                                                   uint32_t* __restrict__ live, unsigned int* __restrict__ n_live) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    bool any = false;
+    if (i < nE) {
         const int ns = counts[i];
         const int32_t* sp = sources + offsets[i];
-        bool any = false;
         for (int q = 0; q < ns && !any; ++q) {
             const int32_t so = sp[q];
             any = (so < 0 || (uint64_t)so >= n_cull) ? true : cull[so] != 0;
         }
-        if (!any) return;
     }
-    edge_ray<kStack>(starts, ends, offsets, counts, sources, i, nodes, max_steps, tris, swap, table);
+    const unsigned int m = __ballot_sync(0xffffffffu, any);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(n_live, (unsigned int)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (any) live[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+}
+
+// Edge rays of the live list (grid-stride: the list length is only known on the device).
+__global__ void __launch_bounds__(kT) k_edge_join_live(const float* __restrict__ starts,
+                                                       const float* __restrict__ ends,
+                                                       const int32_t* __restrict__ offsets,
+                                                       const int32_t* __restrict__ counts,
+                                                       const int32_t* __restrict__ sources,
+                                                       const uint32_t* __restrict__ live,
+                                                       const unsigned int* __restrict__ n_live,
+                                                       const BNode* __restrict__ nodes, uint32_t max_steps,
+                                                       const float4* __restrict__ tris, int swap, PairTable table) {
+    const unsigned int n = *n_live;
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        edge_ray<kStack>(starts, ends, offsets, counts, sources, live[j], nodes, max_steps, tris, swap, table);
 }
 
 __global__ void k_first_tri_init(int32_t* __restrict__ first, uint64_t nObj) {
@@ -351,11 +381,32 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
                             int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull) {
     if (nE == 0 || target->n_tris == 0) return cudaSuccess;
     const unsigned grid = (unsigned)((nE + kT - 1) / kT);
-    const int ptok = prof_begin(P_EDGE_JOIN, s);
-    launch(k_edge_join, grid, kT, 0, s, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, target->nodes,
-           max_steps(target), target->tris, swap, table_view(ps), (const uint8_t*)cull.cand, cull.n_obj);
-    prof_end(P_EDGE_JOIN, s, ptok);
-    return cudaGetLastError();
+    if (!cull.cand || nE > 0xffffffffull) {
+        const int ptok = prof_begin(P_EDGE_JOIN, s);
+        launch(k_edge_join, grid, kT, 0, s, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, target->nodes,
+               max_steps(target), target->tris, swap, table_view(ps));
+        prof_end(P_EDGE_JOIN, s, ptok);
+        return cudaGetLastError();
+    }
+    // Live edges first, then rays for them only.
+    unsigned int* n_live = nullptr;
+    uint32_t* live = nullptr;
+    cudaError_t e = dmalloc((void**)&n_live, sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&live, nE * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(n_live, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+        const int ptok = prof_begin(P_EDGE_JOIN, s);
+        launch(k_edge_live, (unsigned)((nE + 255) / 256), 256, 0, s, d_offsets, d_counts, d_sources, nE,
+               (const uint8_t*)cull.cand, cull.n_obj, live, n_live);
+        launch(k_edge_join_live, (unsigned)std::min<uint64_t>(grid, 8ull * sm_count()), kT, 0, s, d_starts, d_ends,
+               d_offsets, d_counts, d_sources, (const uint32_t*)live, (const unsigned int*)n_live, target->nodes,
+               max_steps(target), target->tris, swap, table_view(ps));
+        prof_end(P_EDGE_JOIN, s, ptok);
+        e = cudaGetLastError();
+    }
+    if (live) cudaFreeAsync(live, s);
+    if (n_live) cudaFreeAsync(n_live, s);
+    return e;
 }
 
 // Broad-phase flags of `src`'s objects against `other`'s BVH (one query per object).
