@@ -177,3 +177,11 @@ def box_mesh(V):
     bi = np.empty((12, 3), np.uint32)
     lib().orc_box_mesh(_p(V), len(V), _p(bv), _p(bi))
     return bv, bi
+
+
+def containment_strict(A, B, threads=None, use_bvh=True):
+    """raytracer_containment: B objects inside A objects (B->A containment rays, as (a, b))
+    whose pair is not an overlap pair.  Returns (strict containment keys, overlap keys)."""
+    overlap = overlap_join(A, B, threads, use_bvh)
+    inside = containment(B, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh)
+    return np.setdiff1d(inside, overlap).astype(np.uint64), overlap

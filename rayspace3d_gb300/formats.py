@@ -151,26 +151,42 @@ def read_pre(path: str) -> Geometry:
     return Geometry(V, I, T, int(total), edges, grid)
 
 
+def _fgets_segments(data: bytes):
+    """The pieces a C ``fgets(buf, 1024, f)`` loop returns: lines ending at ``\n`` (kept),
+    with lines longer than 1023 bytes split into 1023-byte pieces."""
+    pos = 0
+    n = len(data)
+    while pos < n:
+        nl = data.find(b"\n", pos)
+        end = n if nl < 0 else nl + 1
+        while end - pos > 1023:
+            yield data[pos:pos + 1023].decode("latin-1")
+            pos += 1023
+        yield data[pos:end].decode("latin-1")
+        pos = end
+
+
 def read_points(path: str) -> np.ndarray:
-    """Parse a point file like PointIO.cpp:52-82: ``POINT``-prefixed lines read three
+    """Parse a point file like PointIO.cpp:33-62: ``POINT``-prefixed lines read three
     floats after the first ``(``; lines starting with a digit or ``-`` are bare
-    ``x y z``; blank lines and ``#`` comments are skipped.  Returns float32[N,3]."""
+    ``x y z``; blank lines and ``#`` comments are skipped; lines are read in fgets
+    pieces of at most 1023 characters.  Returns float32[N,3]."""
     out = []
-    with open(path, "r") as f:
-        for line in f:
-            s = line.lstrip(" \t")
-            if not s or s[0] in "\r\n#":
+    with open(path, "rb") as f:
+        data = f.read()
+    for line in _fgets_segments(data):
+        s = line.lstrip(" \t")
+        if not s or s[0] in "\r\n#":
+            continue
+        if s.startswith("POINT"):
+            k = s.find("(")
+            if k < 0:
                 continue
-            if s.startswith("POINT"):
-                k = s.find("(")
-                if k < 0:
-                    continue
-                vals = _strtof3(s[k + 1:])
+            out.append(_strtof3(s[k + 1:]))
+        elif "0" <= s[0] <= "9" or s[0] == "-":
+            vals = _strtof3(s)
+            if vals is not None and not (vals[0] is None):
                 out.append(vals)
-            elif s[0].isdigit() or s[0] == "-":
-                vals = _strtof3(s)
-                if vals is not None and not (vals[0] is None):
-                    out.append(vals)
     arr = np.array([[0.0 if v is None else v for v in p] for p in out if p is not None], dtype=np.float32)
     return arr.reshape(-1, 3)
 

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <fstream>
 #include <iomanip>
 #include <iostream>
@@ -103,54 +104,6 @@ bool requirePrecomputedEdges(const Geometry& g, const std::string& path, const c
               << std::endl;
     std::cerr << "Re-run preprocess_dataset to regenerate the .pre file with embedded edge payload." << std::endl;
     return false;
-}
-
-std::vector<float> loadPointDataset(const std::string& path) {
-    std::vector<float> pts;
-    if (path.empty()) {
-        std::cout << "No point dataset provided, using default test points" << std::endl;
-        return {0.0f, 0.0f, -1.0f, 0.5f, 0.5f, -1.0f, 1.0f, 1.0f, -1.0f};
-    }
-    std::cout << "=== Loading Point Dataset ===" << std::endl;
-    std::cout << "Loading points from: " << path << std::endl;
-    FILE* f = std::fopen(path.c_str(), "r");
-    if (!f) {
-        std::cerr << "Error: Could not open point dataset file: " << path << std::endl;
-        return pts;
-    }
-    pts.reserve(3 * 1000000);
-    char line[1024];
-    while (std::fgets(line, sizeof(line), f)) {
-        char* p = line;
-        while (*p == ' ' || *p == '\t') ++p;
-        if (*p == '\0' || *p == '\r' || *p == '\n' || *p == '#') continue;
-        if (std::strncmp(p, "POINT", 5) == 0) {
-            char* s = std::strchr(p, '(');
-            if (s) {
-                ++s;
-                char* e;
-                const float x = std::strtof(s, &e);
-                const float y = std::strtof(e, &e);
-                const float z = std::strtof(e, &e);
-                pts.push_back(x);
-                pts.push_back(y);
-                pts.push_back(z);
-            }
-        } else if ((*p >= '0' && *p <= '9') || *p == '-') {
-            char* e;
-            const float x = std::strtof(p, &e);
-            const float y = std::strtof(e, &e);
-            const float z = std::strtof(e, &e);
-            if (p != e) {
-                pts.push_back(x);
-                pts.push_back(y);
-                pts.push_back(z);
-            }
-        }
-    }
-    std::fclose(f);
-    std::cout << "Found " << pts.size() / 3 << " points." << std::endl;
-    return pts;
 }
 
 std::vector<std::string> splitPaths(const std::string& input) {

@@ -114,6 +114,18 @@ def main():
     p_pts = os.path.join(tmp, "points.bin")
     subprocess.run([drv, "points", p_txt, p_pts], check=True, stdout=subprocess.DEVNULL)
     out["points"] = read_vecs(p_pts, [("<f4", 3)])[0].reshape(-1, 3)
+    # long lines (split by the reader's 1023-byte fgets pieces), CR and CRLF endings, tabs
+    p_txt2 = os.path.join(HERE, "points_tricky.wkt")
+    with open(p_txt2, "wb") as f:
+        f.write(b"POINT (1 2 3)\r\n\tPOINT Z (4 5 6)\n")
+        f.write(b"POINT (" + b"7" * 1030 + b" 8 9)\n")
+        f.write(b" " * 1020 + b"POINT (10 11 12)\n")
+        f.write(b"-1 -2 -3\r-4 -5 -6\n")
+        f.write(b"1.5e2 2.5e-1 3\n#POINT (0 0 0)\n")
+        f.write(b"POINT(13 14 15)")
+    p_pts2 = os.path.join(tmp, "points2.bin")
+    subprocess.run([drv, "points", p_txt2, p_pts2], check=True, stdout=subprocess.DEVNULL)
+    out["points_tricky"] = read_vecs(p_pts2, [("<f4", 3)])[0].reshape(-1, 3)
     # 4. bounding-box mesh
     g, _ = synth.pim_workload(10, level=2)
     p_in = os.path.join(tmp, "box.bin")

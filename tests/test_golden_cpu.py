@@ -346,7 +346,8 @@ def test_cli_help(cli_bin, app):
                                       ("raytracer_mesh_overlap", "--mesh1"),
                                       ("raytracer_overlap_estimated", "--mesh1"),
                                       ("raytracer_overlap_direct_estimation", "--mesh1"),
-                                      ("raytracer_intersection_estimated", "--mesh1")])
+                                      ("raytracer_intersection_estimated", "--mesh1"),
+                                      ("raytracer_containment", "--mesh1")])
 def test_cli_missing_input(cli_bin, app, flag):
     r = subprocess.run([os.path.join(cli_bin, app)], capture_output=True, text=True, timeout=60)
     assert r.returncode != 0
@@ -374,3 +375,41 @@ def test_device_generator_edges_match_extraction():
         a = bind.edge_join(ref, other.vertices, other.indices, other.tri2obj)
         b = bind.edge_join(g.edges, other.vertices, other.indices, other.tri2obj)
         np.testing.assert_array_equal(a, b)
+
+
+_POINT_MAIN = textwrap.dedent("""
+    #include <cstdio>
+    #include <vector>
+    #include "rs_cli.h"
+    int main(int argc, char** argv) {
+        std::vector<float> p = rscli::loadPointDataset(argv[1]);
+        std::FILE* f = std::fopen(argv[2], "wb");
+        std::fwrite(p.data(), sizeof(float), p.size(), f);
+        std::fclose(f);
+        return 0;
+    }
+""")
+
+
+@pytest.mark.parametrize("name", ["points", "points_tricky"])
+def test_point_readers_match_reference_parser(golden, tmp_path, name):
+    """The executables' parallel point parser (host/common/point_io.cpp) and the Python
+    reader against the reference's own loadPointDataset output, on a file with long lines
+    (split into 1023-byte fgets pieces), CR and CRLF endings and tabs."""
+    wkt = os.path.join(GOLD, name + ".wkt")
+    np.testing.assert_array_equal(formats.read_points(wkt).view(np.uint32), golden[name].view(np.uint32))
+    src = tmp_path / "main.cpp"
+    exe = tmp_path / "points"
+    src.write_text(_POINT_MAIN)
+    host = os.path.join(ROOT, "rayspace3d_gb300", "host")
+    try:
+        subprocess.run(["g++", "-O1", "-std=c++17", "-pthread", "-I", host, "-I", os.path.join(ROOT, "include"),
+                        "-I", os.path.join(build.cuda_home(), "include"), str(src),
+                        os.path.join(host, "common", "point_io.cpp"), "-o", str(exe)], check=True,
+                       capture_output=True)
+    except (OSError, RuntimeError, subprocess.CalledProcessError) as e:
+        pytest.skip(f"cannot compile the parser: {e}")
+    out = tmp_path / "p.bin"
+    subprocess.run([str(exe), wkt, str(out)], check=True, capture_output=True)
+    got = np.fromfile(out, np.float32).reshape(-1, 3)
+    np.testing.assert_array_equal(got.view(np.uint32), golden[name].view(np.uint32))

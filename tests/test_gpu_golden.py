@@ -355,3 +355,34 @@ def test_out_of_range_vertex_index(cuda):
     obj = torch.empty(4, dtype=torch.int32, device="cuda")
     assert L.rs_pim(h, pts.data_ptr(), 4, 0.0, 0.0, 1.0, obj.data_ptr(), None, None) == _lib.RS_ERR_INVALID
     assert L.rs_bvh_destroy(h) == 0
+
+
+@pytest.mark.parametrize("include_overlap", [False, True])
+def test_cli_containment(cuda, cli, tmp_path, include_overlap):
+    """raytracer_containment on sets with B objects planted inside A objects: strict
+    containment pairs (and the overlap pairs) equal the oracle's."""
+    from rayspace3d_gb300 import gen
+    A, B, planted = gen.intersection_sets(400, seed=8, world=300.0, levels=(1, 2, 3))
+    ha, hb = gen.to_host_geometry(A), gen.to_host_geometry(B)
+    formats.write_pre(str(tmp_path / "a.pre"), ha)
+    formats.write_pre(str(tmp_path / "b.pre"), hb)
+    extra = ["--include-overlap-pairs"] if include_overlap else []
+    out = _run([cli("raytracer_containment"), "--mesh1", "a.pre", "--mesh2", "b.pre", "--output", "t.json",
+                "--runs", "2"] + extra, tmp_path)
+    strict, overlap = bind.containment_strict(ha, hb)
+    assert f"Containment pairs (B in A): {len(strict)}" in out
+    head, rows = _read_csv(tmp_path / "mesh_containment_results.csv")
+    if include_overlap:
+        assert head == ["a_object_id", "b_object_id", "pair_type"]
+        got_c = _keys([r[:2] for r in rows if r[2] == "containment"])
+        got_o = _keys([r[:2] for r in rows if r[2] == "overlap"])
+        np.testing.assert_array_equal(got_o, overlap)
+    else:
+        assert head == ["a_object_id", "b_object_id"]
+        got_c = _keys(rows)
+    np.testing.assert_array_equal(got_c, strict)
+    # planted objects that touch nothing else are strict containment pairs
+    keys = set(int(k) for k in strict) | set(int(k) for k in overlap)
+    assert all(((a << 32) | b) in keys for a, b in planted)
+    t = _timing(tmp_path / "t.json")
+    assert "build a index_1" in t["phases"] and "query_1" in t["phases"]
