@@ -242,13 +242,29 @@ int rs_batch_autotune(rs_batch* batch, int* h_leaf_size, int* h_chunk, int* h_st
  * (16 B: u32 CenterCount, u32 TouchCount, f32 AvgSizeMean, f32 VolRatio; index
  * (z*R+y)*R+x); the frame is [0, world_size]^3, or the bounds of all vertices when
  * world_size <= 0 (h_bounds6 receives min xyz, max xyz; nullable).  Objects are ids
- * 0..n_obj-1.  Per-cell float sums are taken in arrival order, so AvgSizeMean and VolRatio
- * may differ from the reference's in the last bits; the counts are exact. */
+ * 0..n_obj-1 (RS_ERR_INVALID if a valid triangle names another).  Bit-identical to the
+ * reference: per-object volumes are summed in triangle order and per-cell float sums in the
+ * reference's object visit order (its std::unordered_map iteration order). */
 int rs_grid_stats(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
                   const int32_t* d_tri2obj, uint64_t n_obj, int resolution, float world_size, void* d_cells,
                   float* h_bounds6, void* stream);
 
-/* Learned selectivity estimator (no counterpart in the reference; BASELINE config 5): a
+/* Unique-edge payload on the GPU (EdgePreprocessor::extractEdges,
+ * preprocess/src/EdgePreprocessor.cpp:41-119), identical to the reference's: edges keyed by
+ * their endpoints quantised with llround(x * 1e5) and ordered as the reference's std::map
+ * orders the keys; each edge's endpoints are those of its first occurrence (triangle order,
+ * edges v0v1, v1v2, v2v0) in that occurrence's orientation; sources are the distinct objects
+ * in first-seen order.  Triangles with an index >= nV are skipped.  Outputs: d_starts and
+ * d_ends (float3 per edge), d_offsets and d_counts (int32 per edge) and d_sources (int32 per
+ * source), each with room for `capacity` entries (3 * nF always suffices).  *h_nE and *h_nS
+ * receive the edge and source counts; RS_ERR_OUTPUT_OVERFLOW (outputs untouched) when either
+ * exceeds capacity; RS_ERR_TOO_LARGE above 715,827,882 triangles. */
+int rs_extract_edges(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                     const int32_t* d_tri2obj, float* d_starts, float* d_ends, int32_t* d_offsets,
+                     int32_t* d_counts, int32_t* d_sources, uint64_t capacity, uint64_t* h_nE, uint64_t* h_nS,
+                     void* stream);
+
+/* Learned selectivity estimator (no counterpart in the reference): a
  * 32768 -> 512 -> 512 -> 1 ReLU MLP on pooled grid features predicting log1p(pairs),
  * trained and evaluated with the engine's BF16 tensor-core GEMM kernels (FP32 accumulate,
  * FP32 master weights, Adam).  Features (rs_mlp_features): each grid pooled to 16^3

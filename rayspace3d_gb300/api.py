@@ -150,6 +150,26 @@ def compact_hits(obj: torch.Tensor, stream=None) -> Tuple[torch.Tensor, torch.Te
     return ids[:cnt.value], objs[:cnt.value]
 
 
+def extract_edges(V: torch.Tensor, I: torch.Tensor, T: torch.Tensor, stream=None):
+    """Unique-edge payload (starts, ends, offsets, counts, sources) of device-resident
+    triangles, identical to EdgePreprocessor::extractEdges
+    (preprocess/src/EdgePreprocessor.cpp:41-119)."""
+    nV, nF = int(V.shape[0]), int(I.shape[0])
+    cap = max(3 * nF, 1)
+    dev = V.device
+    starts = torch.empty((cap, 3), dtype=torch.float32, device=dev)
+    ends = torch.empty((cap, 3), dtype=torch.float32, device=dev)
+    offsets = torch.empty(cap, dtype=torch.int32, device=dev)
+    counts = torch.empty(cap, dtype=torch.int32, device=dev)
+    sources = torch.empty(cap, dtype=torch.int32, device=dev)
+    nE, nS = ctypes.c_uint64(), ctypes.c_uint64()
+    _check(_lib.load().rs_extract_edges(_ptr(V), nV, _ptr(I), nF, _ptr(T), _ptr(starts), _ptr(ends), _ptr(offsets),
+                                        _ptr(counts), _ptr(sources), cap, ctypes.byref(nE), ctypes.byref(nS),
+                                        _stream(stream)), "rs_extract_edges")
+    e, s = nE.value, nS.value
+    return starts[:e], ends[:e], offsets[:e], counts[:e], sources[:s]
+
+
 class PairSet:
     """Open-addressing table of pair keys (id1<<32 | id2)."""
 

@@ -31,7 +31,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-
 HOST_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
 
 CLI_APPS = ["raytracer", "raytracer_filter_refine", "raytracer_mesh_overlap", "raytracer_overlap_estimated",
-            "raytracer_overlap_direct_estimation", "raytracer_intersection_estimated", "raytracer_containment"]
+            "raytracer_overlap_direct_estimation", "raytracer_intersection_estimated", "raytracer_containment",
+            "preprocess_dataset"]
 
 
 def nvcc() -> str:

@@ -106,6 +106,46 @@ bool requirePrecomputedEdges(const Geometry& g, const std::string& path, const c
     return false;
 }
 
+bool writeBinaryFile(const std::string& path, const Geometry& g) {
+    std::ofstream out(path, std::ios::binary);
+    if (!out) {
+        std::cerr << "Error: Could not open file for writing: " << path << std::endl;
+        return false;
+    }
+    const bool edges = g.hasEdges();
+    uint32_t head[2] = {kMagic, 2};
+    uint64_t h[6] = {g.numVertices(), g.numTriangles(), (uint64_t)g.T.size(), edges ? g.numEdges() : 0,
+                     edges ? (uint64_t)g.sources.size() : 0, g.totalTriangles};
+    uint8_t flags[8] = {(uint8_t)(g.hasGrid ? 1 : 0), (uint8_t)(edges ? 1 : 0), 0, 0, 0, 0, 0, 0};
+    out.write(reinterpret_cast<const char*>(head), sizeof(head));
+    out.write(reinterpret_cast<const char*>(h), sizeof(h));
+    out.write(reinterpret_cast<const char*>(flags), sizeof(flags));
+    auto put = [&](const void* p, size_t bytes) {
+        if (bytes) out.write(reinterpret_cast<const char*>(p), (std::streamsize)bytes);
+    };
+    put(g.V.data(), g.V.size() * sizeof(float));
+    put(g.I.data(), g.I.size() * sizeof(uint32_t));
+    put(g.T.data(), g.T.size() * sizeof(int32_t));
+    if (edges) {
+        put(g.starts.data(), g.starts.size() * sizeof(float));
+        put(g.ends.data(), g.ends.size() * sizeof(float));
+        put(g.offsets.data(), g.offsets.size() * sizeof(int32_t));
+        put(g.counts.data(), g.counts.size() * sizeof(int32_t));
+        put(g.sources.data(), g.sources.size() * sizeof(int32_t));
+    }
+    if (g.hasGrid) {
+        float b[6] = {g.gmin[0], g.gmin[1], g.gmin[2], g.gmax[0], g.gmax[1], g.gmax[2]};
+        uint32_t r[4] = {g.res[0], g.res[1], g.res[2], 0};
+        put(b, sizeof(b));
+        put(r, sizeof(r));
+        if (g.cells.size() != (size_t)g.res[0] * g.res[1] * g.res[2])
+            std::cerr << "Warning: Grid cell count mismatch in write!" << std::endl;
+        put(g.cells.data(), g.cells.size() * sizeof(GridCellH));
+    }
+    out.close();
+    return static_cast<bool>(out);
+}
+
 std::vector<std::string> splitPaths(const std::string& input) {
     std::vector<std::string> out;
     std::stringstream ss(input);
@@ -233,11 +273,14 @@ void PerformanceTimer::writeResults(const std::string& filename) const {
         f << "      \"duration_ms\": " << std::fixed << std::setprecision(2) << (double)all[i]->us / 1000.0 << "\n";
         f << "    }" << (i + 1 < all.size() ? "," : "") << "\n";
     }
-    f << "  },\n  \"counters\": {\n";
-    for (size_t i = 0; i < counters_.size(); ++i)
-        f << "    \"" << lower(counters_[i].first) << "\": " << counters_[i].second
-          << (i + 1 < counters_.size() ? "," : "") << "\n";
     f << "  },\n";
+    if (writeCounters) {
+        f << "  \"counters\": {\n";
+        for (size_t i = 0; i < counters_.size(); ++i)
+            f << "    \"" << lower(counters_[i].first) << "\": " << counters_[i].second
+              << (i + 1 < counters_.size() ? "," : "") << "\n";
+        f << "  },\n";
+    }
     const long long total = getTotalDuration();
     if (total > 0) {
         f << "  \"total\": {\n    \"duration_us\": " << total << ",\n    \"duration_ms\": " << std::fixed

@@ -4,6 +4,7 @@
 //
 // Restates the reference's host-side formats and helpers in C++ over librs.so:
 //   .pre v2 / v1 reading        common/include/BinaryIO.h:14-180
+//   .pre v2 writing             common/include/BinaryIO.h:35-102
 //   point files                 query/src/runtime/PointIO.cpp:32-92
 //   phase timer + timing JSON   query/src/timer.cpp:1-192
 //   flag parsing                query/src/applications/app_cli_options.h:10-163
@@ -51,6 +52,9 @@ struct Geometry {
 // Version 1 files (48-byte header, no edges) are read as well.
 Geometry loadGeometryFromFile(const std::string& path);
 bool requirePrecomputedEdges(const Geometry& g, const std::string& path, const char* label);
+// RaySpace::IO::writeBinaryFile: version-2 layout, edge section when the payload is
+// present, grid section when hasGrid; struct padding is written as zeros.
+bool writeBinaryFile(const std::string& path, const Geometry& g);
 // Flat xyz floats; an empty path yields the reference's three default points.
 std::vector<float> loadPointDataset(const std::string& path);
 std::vector<std::string> splitPaths(const std::string& input);
@@ -64,6 +68,8 @@ public:
     void addMeasurement(const std::string& phase, long long us);
     void addCounter(const std::string& name, unsigned long long value);
     long long getTotalDuration() const;
+    // The preprocessing timer (common/src/timer.cpp:96-137) writes no "counters" object.
+    bool writeCounters = true;
 
 private:
     using clock = std::chrono::high_resolution_clock;

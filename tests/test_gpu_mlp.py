@@ -1,5 +1,4 @@
-"""Learned estimator (rs_grid_stats, rs_mlp_*): GPU grid statistics against the
-reference-exact restatement, pooled features, the tensor-core forward pass and gradients
+"""Learned estimator (rs_mlp_*): pooled features, the tensor-core forward pass and gradients
 against the float64 CPU restatement (oracle/mlp.py), training, and the gain over the
 grid estimator."""
 import ctypes
@@ -12,27 +11,6 @@ from oracle import mlp as omlp
 from rayspace3d_gb300 import _lib, api, formats, learned, synth
 
 pytestmark = pytest.mark.gpu
-
-
-@pytest.mark.parametrize("world", [20.0, -1.0])
-def test_grid_stats_gpu_matches_restatement(cuda, world):
-    rng = np.random.default_rng(3)
-    g = synth.sphere_set(300, 1, 0.2, 2.5, 20.0, rng, edges=False)
-    R = 16
-    want = synth.grid_stats(g.vertices, g.indices, g.tri2obj, R, world)
-    dg = api.DeviceGeometry(g)
-    cells = torch.empty(R ** 3 * 16, dtype=torch.uint8, device="cuda")
-    b = (ctypes.c_float * 6)()
-    assert _lib.load().rs_grid_stats(dg.V.data_ptr(), dg.nV, dg.I.data_ptr(), dg.nF, dg.T.data_ptr(), 300, R,
-                                     world, cells.data_ptr(), b, None) == 0
-    got = cells.cpu().numpy().view(formats.GRID_CELL_DTYPE)
-    np.testing.assert_array_equal(np.array(b[:3], np.float32), want.min_bound)
-    np.testing.assert_array_equal(np.array(b[3:], np.float32), want.max_bound)
-    np.testing.assert_array_equal(got["CenterCount"], want.cells["CenterCount"])
-    np.testing.assert_array_equal(got["TouchCount"], want.cells["TouchCount"])
-    # per-cell float sums in arrival order: a few ulps from the reference's order
-    np.testing.assert_allclose(got["AvgSizeMean"], want.cells["AvgSizeMean"], rtol=1e-5)
-    np.testing.assert_allclose(got["VolRatio"], want.cells["VolRatio"], rtol=1e-5)
 
 
 @pytest.mark.parametrize("R", [16, 40, 128])
