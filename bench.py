@@ -181,12 +181,13 @@ def run_engine(args, rank, world, local):
         da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
         torch.cuda.synchronize()
 
-        def step(ga, gb):
-            # The two builds run concurrently on their own streams, after the work already
-            # queued on `stream` (the inputs' copies in the end-to-end run); the join on
-            # `stream` is ordered after both builds by the engine.
-            sa.wait_stream(stream)
-            sb.wait_stream(stream)
+        def step(ga, gb, after_copies=False):
+            # The two builds run concurrently on their own streams (after the work already
+            # queued on `stream`, or, end to end, after their own geometry copies queued on
+            # those streams); the join on `stream` is ordered after both builds by the engine.
+            if not after_copies:
+                sa.wait_stream(stream)
+                sb.wait_stream(stream)
             ba = api.Bvh(ga, stream=sa, asynchronous=True)
             bb = api.Bvh(gb, stream=sb, asynchronous=True)
             est, _ = api.estimate_pairs(ga, gb, stream=stream)
@@ -248,11 +249,20 @@ def run_engine(args, rank, world, local):
             dst.cells = torch.empty_like(src.cells)
 
         def e2e_step():
+            # Each set's triangles are copied on its build stream, so a build starts as soon
+            # as its own geometry has landed; the grids (needed first, by the estimate) and
+            # then the edge payloads are copied on the join stream meanwhile.
+            for s, dst, tag in ((sa, ga2, "A"), (sb, gb2, "B")):
+                s.wait_stream(stream)
+                with torch.cuda.stream(s):
+                    for d, h in zip([dst.V, dst.I, dst.T], host[tag][:3]):
+                        d.copy_(h, non_blocking=True)
             for dst, tag in ((ga2, "A"), (gb2, "B")):
-                dts = [dst.V, dst.I, dst.T] + list(dst.edges) + [dst.cells]
-                for d, h in zip(dts, host[tag]):
+                dst.cells.copy_(host[tag][-1], non_blocking=True)
+            for dst, tag in ((ga2, "A"), (gb2, "B")):
+                for d, h in zip(dst.edges, host[tag][3:8]):
                     d.copy_(h, non_blocking=True)
-            k = step(ga2, gb2)
+            k = step(ga2, gb2, after_copies=True)
             out = k.cpu()
             return out
 
@@ -688,6 +698,61 @@ def run_learned(args, full: bool):
                          "frac": round(tflops / peak, 5), "ms": round(ms, 4)}}
 
 
+def run_prep(A, cpu: bool = True):
+    """GPU preprocessing of one overlap-join set (3.2 M triangles of the headline
+    workload): the unique-edge payload (rs_extract_edges) and 128^3 grid statistics over
+    the 1000^3 world (rs_grid_stats), both bit-identical to the reference's CPU code, timed
+    wall-clock per call with the triangles resident on the device; beside them the same
+    two steps by the single-threaded C++ restatement of the reference (std::map /
+    std::unordered_map, as the reference runs them), on the full set."""
+    import ctypes
+
+    import torch
+    from rayspace3d_gb300 import _lib, api
+
+    dg = api.DeviceGeometry(A)
+    L = _lib.load()
+    cells = torch.empty(128 ** 3 * 16, dtype=torch.uint8, device="cuda")
+    b = (ctypes.c_float * 6)()
+
+    def grid():
+        api._check(L.rs_grid_stats(dg.V.data_ptr(), dg.nV, dg.I.data_ptr(), dg.nF, dg.T.data_ptr(),
+                                   int(dg.T.max().item()) + 1, 128, 1000.0, cells.data_ptr(), b, None),
+                   "rs_grid_stats")
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    t_edges = timed(lambda: api.extract_edges(dg.V, dg.I, dg.T))
+    t_grid = timed(grid)
+    e = api.extract_edges(dg.V, dg.I, dg.T)
+    out = {"workload": "preprocessing of one overlap-join set: 10k level-2 icospheres (3.2 M triangles), "
+                       "unique edges + 128^3 grid over 1000^3",
+           "triangles": int(dg.nF), "edges": int(e[0].shape[0]), "sources": int(e[4].shape[0]),
+           "gpu_seconds": {"extract_edges": round(t_edges, 5), "grid_stats": round(t_grid, 5)},
+           "gpu_mtris_per_s": round(dg.nF / (t_edges + t_grid) / 1e6, 1)}
+    if cpu:
+        from oracle import bind
+        t0 = time.perf_counter()
+        bind.extract_edges(A.vertices, A.indices, A.tri2obj)
+        c_edges = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        bind.grid_stats(A.vertices, A.indices, A.tri2obj, 128, 1000.0)
+        c_grid = time.perf_counter() - t0
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "the full set",
+                               "seconds": {"extract_edges": round(c_edges, 3), "grid_stats": round(c_grid, 3)}}
+        out["speedup_vs_cpu"] = round((c_edges + c_grid) / (t_edges + t_grid), 1)
+    return out
+
+
 def cpu_join_sample(A, B, frac=0.02, threads=None):
     """Oracle overlap join on a bounded sample of both edge sets, extrapolated to one
     full join: 2 x CPU BVH build + (sampled traversal time / frac)."""
@@ -758,6 +823,7 @@ def main():
         result["batch"] = run_batch(args, args.batch_full)
         result["learned"] = run_learned(args, args.learned_full)
         result["intersection"] = run_intersection(args, args.intersection_n)
+        result["prep"] = run_prep(A, cpu=(rank == 0 and not args.no_cpu_baseline))
     if rank == 0 and not args.no_cpu_baseline:
         v, meta = cpu_join_sample(A, B, frac=0.01)
         result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": meta["cores"], "kind": "port",

@@ -249,6 +249,15 @@ int rs_grid_stats(const float* d_vertices, uint64_t nV, const uint32_t* d_indice
                   const int32_t* d_tri2obj, uint64_t n_obj, int resolution, float world_size, void* d_cells,
                   float* h_bounds6, void* stream);
 
+/* Legacy per-triangle overlap, one direction (mesh_overlap.cu:126-179, compiled but not
+ * launched by the reference's mains): every edge of every source triangle, in the
+ * triangle's own orientation (v0v1, v1v2, v2v0) and with the triangle's object as its
+ * source, is traced against `target` like an edge of rs_edge_join; shared edges are traced
+ * once per triangle.  Needs no precomputed edge payload.  RS_ERR_INVALID (pairs of the valid
+ * triangles still inserted) when a source index is >= nV. */
+int rs_triangle_join(const rs_bvh* target, const float* d_vertices, uint64_t nV, const uint32_t* d_indices,
+                     uint64_t nF, const int32_t* d_tri2obj, int swap, rs_pairset* ps, void* stream);
+
 /* Unique-edge payload on the GPU (EdgePreprocessor::extractEdges,
  * preprocess/src/EdgePreprocessor.cpp:41-119), identical to the reference's: edges keyed by
  * their endpoints quantised with llround(x * 1e5) and ordered as the reference's std::map

@@ -58,6 +58,10 @@ def lib():
         L.orc_perturbed_sign.argtypes = [P, P, P, P]
         L.orc_free.argtypes = [P]
         L.orc_box_mesh.argtypes = [P, U64, P, P]
+        PF, PI = ctypes.POINTER(ctypes.POINTER(F)), ctypes.POINTER(ctypes.POINTER(ctypes.c_int32))
+        L.orc_extract_edges.argtypes = [P, U64, P, U64, P, PF, PF, PI, PI, PI, ctypes.POINTER(U64),
+                                        ctypes.POINTER(U64)]
+        L.orc_grid_stats.argtypes = [P, U64, P, U64, P, I, F, P, P]
         _lib = L
     return _lib
 
@@ -185,3 +189,33 @@ def containment_strict(A, B, threads=None, use_bvh=True):
     overlap = overlap_join(A, B, threads, use_bvh)
     inside = containment(B, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh)
     return np.setdiff1d(inside, overlap).astype(np.uint64), overlap
+
+
+def extract_edges(V, I, T):
+    """(starts, ends, offsets, counts, sources) of EdgePreprocessor::extractEdges."""
+    V, I, T = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32)
+    L = lib()
+    ptr_f = [ctypes.POINTER(ctypes.c_float)() for _ in range(2)]
+    ptr_i = [ctypes.POINTER(ctypes.c_int32)() for _ in range(3)]
+    ne, ns = ctypes.c_uint64(), ctypes.c_uint64()
+    L.orc_extract_edges(_p(V), len(V), _p(I), len(I), _p(T), ctypes.byref(ptr_f[0]), ctypes.byref(ptr_f[1]),
+                        ctypes.byref(ptr_i[0]), ctypes.byref(ptr_i[1]), ctypes.byref(ptr_i[2]), ctypes.byref(ne),
+                        ctypes.byref(ns))
+    n_e, n_s = ne.value, ns.value
+    out = [np.ctypeslib.as_array(ptr_f[0], shape=(max(n_e, 1) * 3,))[:3 * n_e].reshape(-1, 3).copy(),
+           np.ctypeslib.as_array(ptr_f[1], shape=(max(n_e, 1) * 3,))[:3 * n_e].reshape(-1, 3).copy(),
+           np.ctypeslib.as_array(ptr_i[0], shape=(max(n_e, 1),))[:n_e].copy(),
+           np.ctypeslib.as_array(ptr_i[1], shape=(max(n_e, 1),))[:n_e].copy(),
+           np.ctypeslib.as_array(ptr_i[2], shape=(max(n_s, 1),))[:n_s].copy()]
+    for p in ptr_f + ptr_i:
+        L.orc_free(ctypes.cast(p, ctypes.c_void_p))
+    return out
+
+
+def grid_stats(V, I, T, res, world_size):
+    """(bounds float32[6], cells uint8[res^3 * 16]) of generateGridStats."""
+    V, I, T = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32)
+    cells = np.zeros(int(res) ** 3 * 16, np.uint8)
+    b = np.zeros(6, np.float32)
+    lib().orc_grid_stats(_p(V), len(V), _p(I), len(I), _p(T), int(res), float(world_size), _p(cells), _p(b))
+    return b, cells

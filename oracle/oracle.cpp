@@ -8,7 +8,10 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
+#include <map>
+#include <unordered_map>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -800,6 +803,151 @@ void orc_box_mesh(const float* V, uint64_t nV, float* out_v, uint32_t* out_i) {
     box_mesh(m, bv, bi, bo);
     std::memcpy(out_v, bv.data(), 24 * sizeof(float));
     std::memcpy(out_i, bi.data(), 36 * sizeof(uint32_t));
+}
+
+// ---------------------------------------------------------------------------
+// Preprocessing payloads.
+// ---------------------------------------------------------------------------
+int orc_extract_edges(const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* T,
+                      float** starts, float** ends, int32_t** offsets, int32_t** counts, int32_t** sources,
+                      uint64_t* nE, uint64_t* nS) {
+    using Q = std::array<long long, 3>;
+    struct Info {
+        uint32_t a, b;              // vertex ids of the first occurrence, in its orientation
+        std::vector<int32_t> objs;  // distinct, first-seen order
+    };
+    auto quant = [&](uint32_t v) {
+        Q q;
+        for (int k = 0; k < 3; ++k) q[k] = std::llround((double)V[3 * (uint64_t)v + k] * 1e5);
+        return q;
+    };
+    std::map<std::pair<Q, Q>, Info> edges;
+    for (uint64_t t = 0; t < nF; ++t) {
+        const uint32_t v[3] = {I[3 * t], I[3 * t + 1], I[3 * t + 2]};
+        if (v[0] >= nV || v[1] >= nV || v[2] >= nV) continue;
+        for (int e = 0; e < 3; ++e) {
+            const uint32_t a = v[e], b = v[(e + 1) % 3];
+            Q qa = quant(a), qb = quant(b);
+            if (qb < qa) std::swap(qa, qb);
+            auto ins = edges.try_emplace({qa, qb});
+            Info& info = ins.first->second;
+            if (ins.second) {
+                info.a = a;
+                info.b = b;
+            }
+            if (std::find(info.objs.begin(), info.objs.end(), T[t]) == info.objs.end()) info.objs.push_back(T[t]);
+        }
+    }
+    const uint64_t ne = edges.size();
+    uint64_t ns = 0;
+    for (const auto& kv : edges) ns += kv.second.objs.size();
+    *starts = (float*)std::malloc(std::max<uint64_t>(ne, 1) * 3 * sizeof(float));
+    *ends = (float*)std::malloc(std::max<uint64_t>(ne, 1) * 3 * sizeof(float));
+    *offsets = (int32_t*)std::malloc(std::max<uint64_t>(ne, 1) * sizeof(int32_t));
+    *counts = (int32_t*)std::malloc(std::max<uint64_t>(ne, 1) * sizeof(int32_t));
+    *sources = (int32_t*)std::malloc(std::max<uint64_t>(ns, 1) * sizeof(int32_t));
+    uint64_t i = 0, j = 0;
+    for (const auto& kv : edges) {
+        const Info& info = kv.second;
+        for (int k = 0; k < 3; ++k) {
+            (*starts)[3 * i + k] = V[3 * (uint64_t)info.a + k];
+            (*ends)[3 * i + k] = V[3 * (uint64_t)info.b + k];
+        }
+        (*offsets)[i] = (int32_t)j;
+        (*counts)[i] = (int32_t)info.objs.size();
+        for (int32_t o : info.objs) (*sources)[j++] = o;
+        ++i;
+    }
+    *nE = ne;
+    *nS = ns;
+    return 0;
+}
+
+void orc_grid_stats(const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* T, int res,
+                    float world_size, void* cells_out, float* bounds6) {
+    struct Cell {
+        uint32_t center, touch;
+        float avg, ratio;
+    };
+    struct Obj {
+        float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+        double vol = 0.0;
+    };
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (uint64_t v = 0; v < nV; ++v)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], V[3 * v + k]);
+            hi[k] = std::max(hi[k], V[3 * v + k]);
+        }
+    if (world_size > 0) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = 0.0f;
+            hi[k] = world_size;
+        }
+    }
+    float cs[3];
+    for (int k = 0; k < 3; ++k) {
+        cs[k] = (hi[k] - lo[k]) / (float)res;
+        bounds6[k] = lo[k];
+        bounds6[3 + k] = hi[k];
+    }
+    const uint64_t ncell = (uint64_t)res * res * res;
+    Cell* cells = static_cast<Cell*>(cells_out);
+    std::memset(cells, 0, ncell * sizeof(Cell));
+    auto valid = [&](uint64_t t) { return I[3 * t] < nV && I[3 * t + 1] < nV && I[3 * t + 2] < nV; };
+    std::unordered_map<int, Obj> objs;
+    for (uint64_t t = 0; t < nF; ++t) {
+        if (!valid(t)) continue;
+        Obj& o = objs[T[t]];
+        for (int c = 0; c < 3; ++c)
+            for (int k = 0; k < 3; ++k) {
+                const float x = V[3 * (uint64_t)I[3 * t + c] + k];
+                o.mn[k] = std::min(o.mn[k], x);
+                o.mx[k] = std::max(o.mx[k], x);
+            }
+    }
+    for (uint64_t t = 0; t < nF; ++t) {
+        if (!valid(t)) continue;
+        Obj& o = objs[T[t]];
+        float p[3][3];
+        for (int c = 0; c < 3; ++c)
+            for (int k = 0; k < 3; ++k) p[c][k] = V[3 * (uint64_t)I[3 * t + c] + k] - (o.mn[k] + o.mx[k]) * 0.5f;
+        const float cx = p[0][1] * p[1][2] - p[0][2] * p[1][1];
+        const float cy = p[0][2] * p[1][0] - p[0][0] * p[1][2];
+        const float cz = p[0][0] * p[1][1] - p[0][1] * p[1][0];
+        const float term = cx * p[2][0] + cy * p[2][1] + cz * p[2][2];
+        o.vol += term;
+    }
+    for (const auto& kv : objs) {
+        const Obj& o = kv.second;
+        const float w = o.mx[0] - o.mn[0], h = o.mx[1] - o.mn[1], d = o.mx[2] - o.mn[2];
+        float box = w * h * d;
+        if (box < 1e-9f) box = 1e-9f;
+        float ratio = (std::fabs((float)o.vol) / 6.0f) / box;
+        if (ratio > 1.0f) ratio = 1.0f;
+        const float avg = (w + h + d) / 3.0f;
+        int a[3], c0[3], c1[3];
+        for (int k = 0; k < 3; ++k) {
+            a[k] = (int)(((o.mn[k] + o.mx[k]) * 0.5f - lo[k]) / cs[k]);
+            c0[k] = std::max(0, (int)((o.mn[k] - lo[k]) / cs[k]));
+            c1[k] = std::min(res - 1, (int)((o.mx[k] - lo[k] - 1e-5f) / cs[k]));
+        }
+        if (a[0] >= 0 && a[0] < res && a[1] >= 0 && a[1] < res && a[2] >= 0 && a[2] < res)
+            cells[((uint64_t)a[2] * res + a[1]) * res + a[0]].center++;
+        for (int z = c0[2]; z <= c1[2]; ++z)
+            for (int y = c0[1]; y <= c1[1]; ++y)
+                for (int x = c0[0]; x <= c1[0]; ++x) {
+                    Cell& c = cells[((uint64_t)z * res + y) * res + x];
+                    c.touch++;
+                    c.avg += avg;
+                    c.ratio += ratio;
+                }
+    }
+    for (uint64_t i = 0; i < ncell; ++i)
+        if (cells[i].touch) {
+            cells[i].avg /= (float)cells[i].touch;
+            cells[i].ratio /= (float)cells[i].touch;
+        }
 }
 
 void orc_free(void* p) { std::free(p); }

@@ -14,6 +14,8 @@
  *   - sorted unique pair keys (query/src/cuda/mesh_query_deduplication.cu:56-120)
  *   - the grid selectivity estimator (query/src/cuda/estimated_overlap.cu:8-41,
  *     query/src/applications/raytracer_overlap_estimated_main.cpp:129-158,252-325)
+ *   - the preprocessing payloads: unique edges (preprocess/src/EdgePreprocessor.cpp:41-119)
+ *     and grid statistics (preprocess/src/preprocess_dataset.cpp:37-179)
  * under the engine's exact hit contract (exact-sign orientation predicates with
  * a symbolic-perturbation tie-break, float hit distance by a fixed operation
  * sequence clamped to the triangle's slab interval).  Its exact arithmetic is a
@@ -79,6 +81,18 @@ int orc_perturbed_sign(const float d[3], const float o[3], const float a[3], con
 /* The 12-triangle bounding-box mesh of all vertices (BoundingBox.cpp:4-50):
  * out_v float[24] (8 vertices), out_i uint32[36] (12 triangles). */
 void orc_box_mesh(const float* V, uint64_t nV, float* out_v, uint32_t* out_i);
+
+/* Unique-edge payload (EdgePreprocessor.cpp:41-119): an ordered map from the quantised
+ * endpoint pair to the first occurrence's endpoints and the distinct source objects in
+ * first-seen order.  Arrays are malloc'd (free with orc_free); *nE, *nS their lengths. */
+int orc_extract_edges(const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* T,
+                      float** starts, float** ends, int32_t** offsets, int32_t** counts, int32_t** sources,
+                      uint64_t* nE, uint64_t* nS);
+
+/* Grid statistics (preprocess_dataset.cpp:37-179) into res^3 16-byte cells; bounds6
+ * receives the frame (min xyz, max xyz). */
+void orc_grid_stats(const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* T, int res,
+                    float world_size, void* cells, float* bounds6);
 
 void orc_free(void* p);
 

@@ -66,6 +66,7 @@ SIGNATURES = {
     "rs_recheck_enable": (I, [I]),
     "rs_set_overlap_cull": (I, [I]),
     "rs_grid_stats": (I, [P, U64, P, U64, P, U64, I, F, P, ctypes.POINTER(F), P]),
+    "rs_triangle_join": (I, [P, P, U64, P, U64, P, I, P, P]),
     "rs_extract_edges": (I, [P, U64, P, U64, P, P, P, P, P, P, U64, PU64, PU64, P]),
     "rs_mlp_create": (I, [U64, PP]),
     "rs_mlp_destroy": (I, [P]),

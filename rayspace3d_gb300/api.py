@@ -220,6 +220,13 @@ def containment(target: Bvh, source: DeviceGeometry, ps: PairSet, swap: bool = F
                                       _ptr(source.T), int(swap), ps.handle, _stream(stream)), "rs_containment")
 
 
+def triangle_join(target: Bvh, source: DeviceGeometry, ps: PairSet, swap: bool = False, stream=None) -> None:
+    """Legacy per-triangle overlap (mesh_overlap.cu:126-179): the source triangles' own edges
+    traced against target, (source object, target object) keys, or swapped."""
+    _check(_lib.load().rs_triangle_join(target.handle, _ptr(source.V), source.nV, _ptr(source.I), source.nF,
+                                        _ptr(source.T), int(swap), ps.handle, _stream(stream)), "rs_triangle_join")
+
+
 def overlap_join(A: Bvh, B: Bvh, ps: PairSet, direction: int = 0, with_containment: bool = False,
                  stream=None) -> None:
     """Both edge directions (and containment when asked) into ps, growing it on overflow."""

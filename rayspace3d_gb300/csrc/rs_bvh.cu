@@ -56,22 +56,50 @@ __device__ __forceinline__ void block_minmax_atomic(float mn[3], float mx[3], in
 }
 
 // Bounds of all vertices (bounds[6..11]) and the largest object id (max_obj), grid-stride
-// with one atomic per warp.
+// with one atomic per warp.  The xyz array is read as float4 when it is 16-byte aligned:
+// float f of the flat array is component f % 3, and float4 q starts at component q % 3.
+__device__ __forceinline__ void fold_component(float mn[3], float mx[3], int c, float v) {
+    // c is 0, 1 or 2; selects keep the three accumulators in registers.
+    mn[0] = c == 0 ? fminf(mn[0], v) : mn[0];
+    mx[0] = c == 0 ? fmaxf(mx[0], v) : mx[0];
+    mn[1] = c == 1 ? fminf(mn[1], v) : mn[1];
+    mx[1] = c == 1 ? fmaxf(mx[1], v) : mx[1];
+    mn[2] = c == 2 ? fminf(mn[2], v) : mn[2];
+    mx[2] = c == 2 ? fmaxf(mx[2], v) : mx[2];
+}
+
 __global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, const int32_t* __restrict__ t2o,
                                 uint64_t nF, int* bounds, int* max_obj) {
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nV; i += (uint64_t)gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float v = V[3 * i + k];
-            mn[k] = fminf(mn[k], v);
-            mx[k] = fmaxf(mx[k], v);
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t nf = 3 * nV;
+    uint64_t done = 0;
+    if ((reinterpret_cast<uintptr_t>(V) & 15u) == 0) {
+        const float4* V4 = reinterpret_cast<const float4*>(V);
+        const uint64_t n4 = nf / 4;
+        for (uint64_t q = tid; q < n4; q += stride) {
+            const float4 v = __ldg(&V4[q]);
+            const int c = (int)(q % 3);
+            fold_component(mn, mx, c, v.x);
+            fold_component(mn, mx, c == 2 ? 0 : c + 1, v.y);
+            fold_component(mn, mx, c == 0 ? 2 : c - 1, v.z);
+            fold_component(mn, mx, c, v.w);
         }
+        done = 4 * n4;
     }
+    for (uint64_t f = done + tid; f < nf; f += stride) fold_component(mn, mx, (int)(f % 3), V[f]);
     block_minmax_atomic(mn, mx, bounds + 6);
     int mo = -1;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nF; t += (uint64_t)gridDim.x * blockDim.x)
-        mo = max(mo, t2o[t]);
+    if ((reinterpret_cast<uintptr_t>(t2o) & 15u) == 0) {
+        const int4* T4 = reinterpret_cast<const int4*>(t2o);
+        for (uint64_t q = tid; q < nF / 4; q += stride) {
+            const int4 t = __ldg(&T4[q]);
+            mo = max(max(mo, max(t.x, t.y)), max(t.z, t.w));
+        }
+        for (uint64_t t = 4 * (nF / 4) + tid; t < nF; t += stride) mo = max(mo, t2o[t]);
+    } else {
+        for (uint64_t t = tid; t < nF; t += stride) mo = max(mo, t2o[t]);
+    }
     mo = __reduce_max_sync(0xffffffffu, mo);
     if ((threadIdx.x & 31) == 0 && mo >= 0) atomicMax(max_obj, mo);
 }
@@ -176,6 +204,12 @@ __device__ __forceinline__ void store_node(BNode* nd, const float lo0[3], const 
     nd->d = make_int4(i0, c0, i1, c1);
 }
 
+// A subtree left open by the block phase of k_build_up: box, leaf range, node slot.
+struct OpenTree {
+    float lo[3], hi[3];
+    int l, r, self;
+};
+
 // Bottom-up construction of the binary radix tree over the sorted keys, fused with
 // the emission of the leaf-ordered triangles and the box refit (agglomerative LBVH,
 // Apetrei 2014, "Fast and Simple Agglomerative LBVH Construction").  Thread k starts
@@ -199,7 +233,7 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
                                                  const uint32_t* __restrict__ I, const int32_t* __restrict__ t2o,
                                                  const uint64_t* __restrict__ keys, int n, int leaf_size,
                                                  float4* __restrict__ tris, BNode* __restrict__ nodes,
-                                                 int* __restrict__ xchg) {
+                                                 OpenTree* __restrict__ open, unsigned int* __restrict__ n_open) {
     __shared__ int s_absorbed[kT];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -279,33 +313,135 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
         if (absorbed) active = false;
         if (!__any_sync(0xffffffffu, merge)) break;
     }
-    if (!active) return;
-    // Cross-warp merges through the exchange array.
-    for (;;) {
-        const int size = r - l + 1;
-        if (l == 0 && r == n - 1) {
-            const float4* src = reinterpret_cast<const float4*>(nodes + self);
-            float4* dst = reinterpret_cast<float4*>(nodes);
+    // Block rounds: the subtrees still open after the warp rounds meet siblings owned by
+    // other warps of the block through shared memory, in lock-step rounds separated by
+    // block barriers.  The owner of a subtree is still the thread of its leftmost leaf,
+    // so l == k, r stays inside the block, and the sibling of a left child is owned by
+    // thread r + 1 - bb.
+    {
+        __shared__ int s_d[kT + 1];  // split prefixes of splits bb-1 .. bb+kT-1
+        __shared__ int s_r[kT], s_self[kT];
+        __shared__ float s_box[6][kT];
+        __shared__ unsigned char s_state[kT];  // bit 0: open subtree, bit 1: left child
+        __shared__ unsigned char s_abs[kT];
+        const int bb = blockIdx.x * blockDim.x;
+        const int tid = threadIdx.x;
+        s_d[tid + 1] = d_own;
+        if (tid == 0) s_d[0] = (bb > 0 && bb - 1 < n - 1) ? split_prefix(keys, bb - 1) : -1;
+        s_abs[tid] = 0;
+        __syncthreads();
+        for (int round = 0; round < kT; ++round) {
+            bool left_child = false;
+            if (active) {
+                const int dr = s_d[r - bb + 1], dl = s_d[l - bb];
+                left_child = (l == 0) ? true : (r == n - 1) ? false : dr > dl;
+            }
+            s_r[tid] = r;
+            s_self[tid] = self;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) dst[q] = __ldcg(src + q);
-            return;
+            for (int q = 0; q < 3; ++q) {
+                s_box[q][tid] = lo[q];
+                s_box[3 + q][tid] = hi[q];
+            }
+            s_state[tid] = (unsigned char)((active ? 1 : 0) | (left_child ? 2 : 0));
+            __syncthreads();
+            bool merged = false;
+            const int sib = r + 1 - bb;
+            if (active && left_child && sib < kT && r + 1 < n && s_state[sib] == 1) {
+                const int p = r;
+                const int o_r = s_r[sib];
+                const int size0 = r - l + 1, size1 = o_r - r;
+                float olo[3], ohi[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    olo[q] = s_box[q][sib];
+                    ohi[q] = s_box[3 + q][sib];
+                }
+                store_node(nodes + (p + 1), lo, hi, size0 <= leaf_size ? l : self, size0 <= leaf_size ? size0 : 0,
+                           olo, ohi, size1 <= leaf_size ? r + 1 : s_self[sib], size1 <= leaf_size ? size1 : 0);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    lo[q] = fminf(lo[q], olo[q]);
+                    hi[q] = fmaxf(hi[q], ohi[q]);
+                }
+                r = o_r;
+                self = p + 1;
+                s_abs[sib] = 1;
+                merged = true;
+                if (l == 0 && r == n - 1) {
+                    const BNode nd = nodes[self];
+                    nodes[0] = nd;
+                    active = false;
+                }
+            }
+            __syncthreads();
+            if (s_abs[tid]) {
+                active = false;
+                s_abs[tid] = 0;
+            }
+            if (!__syncthreads_or(merged)) break;
         }
-        const bool left_child = (l == 0) ? true : (r == n - 1) ? false : split_prefix(keys, r) > split_prefix(keys, l - 1);
-        const int p = left_child ? r : l - 1;
-        BNode* nd = nodes + (p + 1);
-        store_half(nd, left_child ? 0 : 1, lo, hi, size <= leaf_size ? l : self, size <= leaf_size ? size : 0);
-        const int other = exchange_acq_rel(&xchg[p], left_child ? l : r);
-        if (other < 0) return;
-        float olo[3], ohi[3];
-        load_half(nd, left_child ? 1 : 0, olo, ohi);
+    }
+    // Subtrees still open go to the cross-block phase (k_build_cross), packed densely so
+    // that its latency-bound walks do not hold this kernel's blocks.
+    const unsigned m = __ballot_sync(0xffffffffu, active);
+    if (!m) return;
+    unsigned int slot = 0;
+    if (lane == __ffs(m) - 1) slot = atomicAdd(n_open, (unsigned int)__popc(m));
+    slot = __shfl_sync(0xffffffffu, slot, __ffs(m) - 1) + __popc(m & ((1u << lane) - 1u));
+    if (!active) return;
+    OpenTree& o = open[slot];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        o.lo[q] = lo[q];
+        o.hi[q] = hi[q];
+    }
+    o.l = l;
+    o.r = r;
+    o.self = self;
+}
+
+// Cross-block merges through the exchange array, one open subtree per thread.
+__global__ void __launch_bounds__(kT) k_build_cross(const uint64_t* __restrict__ keys, int n, int leaf_size,
+                                                    BNode* __restrict__ nodes, int* __restrict__ xchg,
+                                                    const OpenTree* __restrict__ open,
+                                                    const unsigned int* __restrict__ n_open) {
+    const unsigned int count = *n_open;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        float lo[3], hi[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            lo[q] = fminf(lo[q], olo[q]);
-            hi[q] = fmaxf(hi[q], ohi[q]);
+            lo[q] = open[i].lo[q];
+            hi[q] = open[i].hi[q];
         }
-        if (left_child) r = other;
-        else l = other;
-        self = p + 1;
+        int l = open[i].l, r = open[i].r, self = open[i].self;
+        for (;;) {
+            const int size = r - l + 1;
+            if (l == 0 && r == n - 1) {
+                const float4* src = reinterpret_cast<const float4*>(nodes + self);
+                float4* dst = reinterpret_cast<float4*>(nodes);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) dst[q] = __ldcg(src + q);
+                break;
+            }
+            const bool left_child =
+                (l == 0) ? true : (r == n - 1) ? false : split_prefix(keys, r) > split_prefix(keys, l - 1);
+            const int p = left_child ? r : l - 1;
+            BNode* nd = nodes + (p + 1);
+            store_half(nd, left_child ? 0 : 1, lo, hi, size <= leaf_size ? l : self, size <= leaf_size ? size : 0);
+            const int other = exchange_acq_rel(&xchg[p], left_child ? l : r);
+            if (other < 0) break;
+            float olo[3], ohi[3];
+            load_half(nd, left_child ? 1 : 0, olo, ohi);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                lo[q] = fminf(lo[q], olo[q]);
+                hi[q] = fmaxf(hi[q], ohi[q]);
+            }
+            if (left_child) r = other;
+            else l = other;
+            self = p + 1;
+        }
     }
 }
 
@@ -397,7 +533,8 @@ int bvh_ready(const rs_bvh* ch) {
         h->vmax[k] = dec(hb[9 + k]);
     }
     h->n_obj = hb[13] >= 0 ? (uint64_t)hb[13] + 1 : 0;
-    h->build_status = hb[12] != 0 ? RS_ERR_INVALID : RS_OK;
+    // [12]: bit 0 an index out of range, bit 1 a failed sort (bounded wait ran out).
+    h->build_status = (hb[12] & 2) ? RS_ERR_ITER_LIMIT : hb[12] != 0 ? RS_ERR_INVALID : RS_OK;
     return h->build_status;
 }
 
@@ -443,6 +580,8 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     int* bounds = nullptr;  // [6..11] vertex bounds (ordered ints), [12] bad-index flag, [13] max object
     uint64_t* keys = nullptr;
     int* xchg = nullptr;
+    OpenTree* open = nullptr;
+    unsigned int* n_open = nullptr;
     cudaError_t e = cudaSuccess;
     int* slot = nullptr;
     const int grid = 4 * sm_count();
@@ -473,11 +612,19 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
         if (e != cudaSuccess) goto fail;
         launch(k_morton, nb, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys,
                reinterpret_cast<unsigned int*>(bounds + 12));
-        e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32);
+        e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32, reinterpret_cast<uint32_t*>(bounds + 12), 2u);
         if (e != cudaSuccess) goto fail;
         cudaMemsetAsync(xchg, 0xff, (size_t)(n - 1) * sizeof(int), s);
+        // Open subtrees per block: at most two per level of the tree (64 key bits), so
+        // n / 2 bounds them for blocks of 256 leaves.
+        e = alloc(&open, (size_t)n / 2 + kT, s);
+        if (e == cudaSuccess) e = alloc(&n_open, 1, s);
+        if (e != cudaSuccess) goto fail;
+        cudaMemsetAsync(n_open, 0, sizeof(unsigned int), s);
         launch(k_build_up, nb, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys, n, leaf_size,
-               h->tris, h->nodes, xchg);
+               h->tris, h->nodes, open, n_open);
+        launch(k_build_cross, 4 * sm_count(), kT, 0, s, (const uint64_t*)keys, n, leaf_size, h->nodes, xchg,
+               (const OpenTree*)open, (const unsigned int*)n_open);
     }
     prof_end(P_BVH_BUILD, s, ptok);
     e = cudaGetLastError();
@@ -492,6 +639,8 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
 fail:
     if (keys) cudaFreeAsync(keys, s);
     if (xchg) cudaFreeAsync(xchg, s);
+    if (open) cudaFreeAsync(open, s);
+    if (n_open) cudaFreeAsync(n_open, s);
     if (bounds) cudaFreeAsync(bounds, s);
     if (e != cudaSuccess) {
         if (h->nodes) cudaFreeAsync(h->nodes, s);

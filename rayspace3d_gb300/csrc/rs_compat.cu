@@ -67,8 +67,14 @@ extern "C" long long merge_and_deduplicate_pairs_gpu(const void* d_results1, lon
     if (dmalloc((void**)&cnt, sizeof(uint64_t), 0) != cudaSuccess) return 0;
     if (unique_sorted_u64(keys, (size_t)total, cnt, 0) == cudaSuccess)
         cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, 0);
+    uint32_t sort_err = 0;
+    sort_error_read(&sort_err, 0);
     cudaFreeAsync(cnt, 0);
     cudaStreamSynchronize(0);
+    if (sort_err) {  // a failed sort: report no result, as on an allocation failure
+        sort_error_clear(0);
+        return 0;
+    }
     return (long long)h;
 }
 

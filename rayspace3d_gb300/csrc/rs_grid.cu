@@ -426,7 +426,13 @@ extern "C" int rs_grid_stats(const float* d_vertices, uint64_t nV, const uint32_
         launch(k_gs_cell_sums, (unsigned)((n + kGT - 1) / kGT), kGT, 0, s, (const uint64_t*)cell_key,
                (const uint32_t*)rank, n, (const ObjCells*)oc, (uint32_t*)d_cells);
     }
+    uint32_t sort_err = 0;
     e = cudaGetLastError();
+    if (e == cudaSuccess) e = sort_error_read(&sort_err, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && sort_err) {
+        sort_error_clear(s);
+        return RS_ERR_ITER_LIMIT;
+    }
     return to_status(e);
 }

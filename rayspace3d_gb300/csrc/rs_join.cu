@@ -33,6 +33,24 @@ __global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ star
     edge_ray<kStack>(starts, ends, offsets, counts, sources, i, nodes, max_steps, tris, swap, table);
 }
 
+// Legacy per-triangle overlap (mesh_overlap.cu:126-179): record r = 3 t + e is edge e of
+// source triangle t.  Triangles with an index >= nV set *bad and are skipped.
+__global__ void __launch_bounds__(kT) k_tri_edge_join(const float* __restrict__ V, uint64_t nV,
+                                                      const uint32_t* __restrict__ I,
+                                                      const int32_t* __restrict__ T, uint64_t m,
+                                                      const BNode* __restrict__ nodes, uint32_t max_steps,
+                                                      const float4* __restrict__ tris, int swap, PairTable table,
+                                                      unsigned int* __restrict__ bad) {
+    const uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    const uint64_t t = r / 3;
+    if (I[3 * t] >= nV || I[3 * t + 1] >= nV || I[3 * t + 2] >= nV) {
+        if (r % 3 == 0) atomicOr(bad, 1u);
+        return;
+    }
+    triangle_edge_ray<kStack>(V, I, T, r, nodes, max_steps, tris, swap, table);
+}
+
 // Broad phase of one direction: the edges with at least one candidate source object
 // (k_cull_query) are appended to `live` (any order: the pair table deduplicates).  A
 // light kernel, so the dependent loads of many edges are in flight at once.
@@ -447,6 +465,32 @@ extern "C" int rs_edge_join(const rs_bvh* target, const float* d_starts, const f
     cudaError_t e = edge_join_async(target, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, swap, ps, s,
                                     EdgeCull{});
     return table_status(ps, s, e);
+}
+
+extern "C" int rs_triangle_join(const rs_bvh* target, const float* d_vertices, uint64_t nV, const uint32_t* d_indices,
+                                uint64_t nF, const int32_t* d_tri2obj, int swap, rs_pairset* ps, void* stream) {
+    if (!target || !ps || (nF && (!d_vertices || !d_indices || !d_tri2obj))) return RS_ERR_INVALID;
+    const uint64_t m = 3 * nF;
+    if (m == 0 || target->n_tris == 0) return RS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int st = bvh_use(target, s);
+    if (st != RS_OK) return st;
+    unsigned int* bad = nullptr;
+    unsigned int hbad = 0;
+    cudaError_t e = dmalloc((void**)&bad, sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+        const int ptok = prof_begin(P_EDGE_JOIN, s);
+        launch(k_tri_edge_join, (unsigned)((m + kT - 1) / kT), kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, m,
+               target->nodes, max_steps(target), target->tris, swap, table_view(ps), bad);
+        prof_end(P_EDGE_JOIN, s, ptok);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    if (bad) cudaFreeAsync(bad, s);
+    const int r = table_status(ps, s, e);
+    if (r == RS_OK && hbad) return RS_ERR_INVALID;
+    return r;
 }
 
 static int containment_impl(const rs_bvh* target, const float* d_src_vertices, uint64_t src_nV,

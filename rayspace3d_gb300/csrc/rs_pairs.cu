@@ -164,10 +164,16 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
     prof_end(P_FINALIZE, s, ptok);
     if (tmp) cudaFreeAsync(tmp, s);
     if (dcount) cudaFreeAsync(dcount, s);
+    uint32_t sort_err = 0;
+    if (e == cudaSuccess) e = sort_error_read(&sort_err, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
     prof_collect();
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return to_status(e);
+    if (sort_err) {
+        sort_error_clear(s);
+        return RS_ERR_ITER_LIMIT;
+    }
     *h_count = n;
     return n > capacity ? RS_ERR_OUTPUT_OVERFLOW : RS_OK;
 }

@@ -292,9 +292,15 @@ extern "C" int rs_extract_edges(const float* d_vertices, uint64_t nV, const uint
             launch(k_keep, nbv, kPT, 0, s, (const uint64_t*)keys, (const uint32_t*)val2, mv, keep);
             e = exclusive_scan_u32(keep, kpos, mv, tot + 1, s);
         }
+        uint32_t sort_err = 0;
         if (e == cudaSuccess) e = cudaMemcpyAsync(htot, tot, 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = sort_error_read(&sort_err, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return to_status(e);
+        if (sort_err) {
+            sort_error_clear(s);
+            return RS_ERR_ITER_LIMIT;
+        }
         *h_nE = htot[0];
         *h_nS = htot[1];
         if (htot[0] > capacity || htot[1] > capacity) return RS_ERR_OUTPUT_OVERFLOW;

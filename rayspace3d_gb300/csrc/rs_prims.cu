@@ -2,10 +2,13 @@
 //
 // Replaces the thrust sort/unique/scan/reduce calls of the reference
 // (query/src/cuda/mesh_query_deduplication.cu:56-90, scan_utils.cu:11-28) with
-// the engine's own kernels.  Tiles are 4096 elements (256 threads x 16 items);
-// the radix scatter ranks keys per warp with __match_any_sync so every pass is
-// stable.
+// the engine's own kernels.  Scan and compaction tiles are 4096 elements (256 threads
+// x 16 items); the radix sort is a onesweep LSD sort whose passes rank keys per warp
+// with __match_any_sync, so every pass is stable.
 #include "rs_prims.cuh"
+
+#include <algorithm>
+#include <mutex>
 
 namespace rs {
 namespace {
@@ -22,85 +25,193 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-__global__ void __launch_bounds__(kThreads) k_radix_hist(const uint64_t* __restrict__ keys, size_t n, int shift,
-                                                          uint32_t* __restrict__ hist, int num_tiles) {
-    __shared__ uint32_t sh[kWarps][256];
-    for (int i = threadIdx.x; i < kWarps * 256; i += kThreads) (&sh[0][0])[i] = 0;
-    __syncthreads();
-    const int w = threadIdx.x >> 5;
-    const size_t base = (size_t)blockIdx.x * kTile;
-#pragma unroll
-    for (int it = 0; it < kItems; ++it) {
-        const size_t idx = base + (size_t)it * kThreads + threadIdx.x;
-        if (idx < n) atomicAdd(&sh[w][(uint32_t)(keys[idx] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    uint32_t s = 0;
-#pragma unroll
-    for (int ww = 0; ww < kWarps; ++ww) s += sh[ww][threadIdx.x];
-    hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = s;
+// ---------------------------------------------------------------------------
+// Onesweep LSD radix sort: one histogram kernel for every digit of the sort, then
+// one kernel per 8-bit digit.  A block takes the next tile (ids in start order),
+// counts its digits per warp, publishes the tile's per-digit counts, learns the counts
+// of all earlier tiles by decoupled look-back (each status word carries a count and a
+// flag: aggregate of that tile alone, or inclusive prefix through it), ranks its keys
+// stably into shared memory by digit and writes them out in digit runs.  A block only
+// ever waits on tiles that started before it, and every wait is bounded: past the
+// limit the block records the failure in the error word and stops waiting.
+// ---------------------------------------------------------------------------
+constexpr int kOsItems = 12;
+constexpr int kOsTile = kThreads * kOsItems;  // 3072 keys
+constexpr int kOsWarpSpan = 32 * kOsItems;
+constexpr int kMaxPasses = 8;
+constexpr unsigned long long kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62, kCountMask = (1ull << 62) - 1;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t os_digit(uint64_t k, int shift, int end_bit) {
+    const int w = min(8, end_bit - shift);
+    return (uint32_t)(k >> shift) & ((1u << w) - 1u);
 }
 
-__global__ void __launch_bounds__(kThreads) k_radix_scatter(const uint64_t* __restrict__ kin,
-                                                             const uint32_t* __restrict__ vin,
-                                                             uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                             size_t n, int shift, const uint32_t* __restrict__ offs,
-                                                             int num_tiles) {
-    __shared__ uint32_t cnt[kWarps][256];
-    for (int i = threadIdx.x; i < kWarps * 256; i += kThreads) (&cnt[0][0])[i] = 0;
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Counts of every digit of every pass (hist[p * 256 + d]).
+__global__ void __launch_bounds__(kThreads) k_os_hist(const uint64_t* __restrict__ keys, size_t n, int begin_bit,
+                                                       int end_bit, int passes, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kMaxPasses * 256];
+    for (int i = threadIdx.x; i < passes * 256; i += kThreads) sh[i] = 0;
     __syncthreads();
+    for (size_t i = blockIdx.x * (size_t)kThreads + threadIdx.x; i < n; i += (size_t)gridDim.x * kThreads) {
+        const uint64_t k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p * 256 + os_digit(k, begin_bit + 8 * p, end_bit)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += kThreads)
+        if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// In place: each pass's 256 counts become exclusive digit offsets (one warp per pass).
+__global__ void __launch_bounds__(256) k_os_offsets(uint32_t* __restrict__ hist, int passes) {
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t base = (size_t)blockIdx.x * kTile + (size_t)w * kWarpSpan;
-    uint64_t k[kItems];
-    uint32_t v[kItems];
+    for (int p = w; p < passes; p += 8) {
+        uint32_t* h = hist + p * 256;
+        uint32_t c[8], sum = 0;
 #pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-        const size_t idx = base + (size_t)r * 32 + lane;
-        k[r] = 0;
-        v[r] = 0;
-        if (idx < n) {
-            k[r] = kin[idx];
-            if (vin) v[r] = vin[idx];
+        for (int j = 0; j < 8; ++j) {
+            c[j] = h[lane * 8 + j];
+            sum += c[j];
+        }
+        uint32_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        uint32_t run = x - sum;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            h[lane * 8 + j] = run;
+            run += c[j];
         }
     }
-    // Pass A: per-warp digit counts.
+}
+
+__global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+                                                       uint32_t* __restrict__ vout, size_t n, int shift, int end_bit,
+                                                       const uint32_t* __restrict__ digit_base,
+                                                       unsigned long long* __restrict__ status,
+                                                       unsigned int* __restrict__ tile_ctr,
+                                                       uint32_t* __restrict__ err, uint32_t err_bit) {
+    __shared__ uint64_t s_keys[kOsTile];
+    __shared__ uint32_t s_vals[kOsTile];
+    __shared__ uint32_t s_cnt[kWarps][256];
+    __shared__ uint32_t s_dstart[256];
+    __shared__ uint32_t s_gbase[256];
+    __shared__ uint32_t s_wsum[kWarps];
+    __shared__ unsigned int s_tile;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    for (int i = tid; i < kWarps * 256; i += kThreads) (&s_cnt[0][0])[i] = 0;
+    __syncthreads();
+    const unsigned int tile = s_tile;
+    const size_t base = (size_t)tile * kOsTile + (size_t)w * kOsWarpSpan;
+    uint64_t k[kOsItems];
+    uint32_t v[kOsItems];
+    uint32_t dg[kOsItems];
 #pragma unroll
-    for (int r = 0; r < kItems; ++r) {
+    for (int r = 0; r < kOsItems; ++r) {
         const size_t idx = base + (size_t)r * 32 + lane;
         const bool valid = idx < n;
-        const uint32_t dg = valid ? ((uint32_t)(k[r] >> shift) & 255u) : (256u + lane);
-        const unsigned peers = __match_any_sync(0xffffffffu, dg);
-        if (valid && lane == __ffs(peers) - 1) cnt[w][dg] += __popc(peers);
+        k[r] = valid ? kin[idx] : 0ull;
+        v[r] = (valid && vin) ? vin[idx] : 0u;
+        dg[r] = valid ? os_digit(k[r], shift, end_bit) : (256u + lane);
+    }
+    // Per-warp digit counts.
+#pragma unroll
+    for (int r = 0; r < kOsItems; ++r) {
+        const unsigned peers = __match_any_sync(0xffffffffu, dg[r]);
+        if (dg[r] < 256u && lane == __ffs(peers) - 1) s_cnt[w][dg[r]] += __popc(peers);
         __syncwarp();
     }
     __syncthreads();
-    {
-        uint32_t run = offs[(size_t)threadIdx.x * num_tiles + blockIdx.x];
+    // Thread d: the tile's count of digit d, per-warp offsets within the digit, publication.
+    const int d = tid;
+    uint32_t tc = 0;
 #pragma unroll
-        for (int ww = 0; ww < kWarps; ++ww) {
-            const uint32_t c = cnt[ww][threadIdx.x];
-            cnt[ww][threadIdx.x] = run;
-            run += c;
-        }
+    for (int ww = 0; ww < kWarps; ++ww) {
+        const uint32_t c = s_cnt[ww][d];
+        s_cnt[ww][d] = tc;
+        tc += c;
     }
+    unsigned long long* mine = status + (size_t)tile * 256 + d;
+    st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | tc);
+    // Tile-local start of each digit's run: exclusive scan of tc over the digits.
+    {
+        uint32_t x = tc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_wsum[w] = x;
+        __syncthreads();
+        uint32_t before = 0;
+#pragma unroll
+        for (int ww = 0; ww < kWarps; ++ww)
+            if (ww < w) before += s_wsum[ww];
+        s_dstart[d] = before + x - tc;
+    }
+    // Decoupled look-back over the earlier tiles.
+    unsigned long long prefix = 0;
+    if (tile > 0) {
+        long long j = (long long)tile - 1;
+        uint32_t spins = 0;
+        while (j >= 0) {
+            const unsigned long long sv = ld_relaxed(status + (size_t)j * 256 + d);
+            const unsigned long long f = sv & ~kCountMask;
+            if (f == 0ull) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(err, err_bit);
+                    break;
+                }
+                continue;
+            }
+            prefix += sv & kCountMask;
+            if (f == kFlagPre) break;
+            --j;
+        }
+        st_relaxed(mine, kFlagPre | (prefix + tc));
+    }
+    s_gbase[d] = digit_base[d] + (uint32_t)prefix;
     __syncthreads();
-    // Pass B: stable ranks and scatter.
+    // Stable ranks into shared memory, digit-major.
     const unsigned lt = lanemask_lt();
 #pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-        const size_t idx = base + (size_t)r * 32 + lane;
-        const bool valid = idx < n;
-        const uint32_t dg = valid ? ((uint32_t)(k[r] >> shift) & 255u) : (256u + lane);
-        const unsigned peers = __match_any_sync(0xffffffffu, dg);
+    for (int r = 0; r < kOsItems; ++r) {
+        const unsigned peers = __match_any_sync(0xffffffffu, dg[r]);
+        const bool valid = dg[r] < 256u;
         uint32_t pos = 0;
-        if (valid) pos = cnt[w][dg] + __popc(peers & lt);
+        if (valid) pos = s_dstart[dg[r]] + s_cnt[w][dg[r]] + __popc(peers & lt);
         __syncwarp();
-        if (valid && lane == __ffs(peers) - 1) cnt[w][dg] += __popc(peers);
+        if (valid && lane == __ffs(peers) - 1) s_cnt[w][dg[r]] += __popc(peers);
         __syncwarp();
         if (valid) {
-            kout[pos] = k[r];
-            if (vout) vout[pos] = v[r];
+            s_keys[pos] = k[r];
+            s_vals[pos] = v[r];
         }
+    }
+    __syncthreads();
+    // Digit runs out to their global positions.
+    const size_t t0 = (size_t)tile * kOsTile;
+    const uint32_t tn = (uint32_t)min((size_t)kOsTile, n - t0);
+    for (uint32_t i = tid; i < tn; i += kThreads) {
+        const uint64_t kk = s_keys[i];
+        const uint32_t dd = os_digit(kk, shift, end_bit);
+        const size_t pos = (size_t)s_gbase[dd] + (i - s_dstart[dd]);
+        kout[pos] = kk;
+        if (vout) vout[pos] = s_vals[i];
     }
 }
 
@@ -329,31 +440,61 @@ int sm_count() {
     return cached;
 }
 
-cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit) {
+uint32_t* sort_error_word() {
+    static uint32_t* words[64] = {};
+    static std::mutex mu;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> g(mu);
+    if (!words[dev]) {
+        uint32_t* p = nullptr;
+        if (cudaMalloc((void**)&p, sizeof(uint32_t)) != cudaSuccess) return nullptr;
+        if (cudaMemset(p, 0, sizeof(uint32_t)) != cudaSuccess) return nullptr;
+        words[dev] = p;
+    }
+    return words[dev];
+}
+
+cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit,
+                           uint32_t* err, uint32_t err_bit) {
     if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
+    if (n > 0xffffffffull || end_bit > 64 || begin_bit < 0) return cudaErrorInvalidValue;
+    if (!err) {
+        err = sort_error_word();
+        err_bit = 1;
+        if (!err) return cudaErrorMemoryAllocation;
+    }
     const int passes = (end_bit - begin_bit + 7) / 8;
-    const size_t tiles = (n + kTile - 1) / kTile;
+    const size_t tiles = (n + kOsTile - 1) / kOsTile;
     uint64_t* k2 = nullptr;
     uint32_t* v2 = nullptr;
     uint32_t* hist = nullptr;
+    unsigned long long* status = nullptr;
+    unsigned int* ctr = nullptr;
+    const size_t status_bytes = (size_t)passes * tiles * 256 * sizeof(unsigned long long);
     cudaError_t e = dmalloc((void**)&k2, n * sizeof(uint64_t), s);
     if (e == cudaSuccess && vals) e = dmalloc((void**)&v2, n * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = dmalloc((void**)&hist, 256 * tiles * sizeof(uint32_t), s);
-    if (e != cudaSuccess) {
-        if (k2) cudaFreeAsync(k2, s);
-        if (v2) cudaFreeAsync(v2, s);
-        return e;
+    if (e == cudaSuccess) e = dmalloc((void**)&hist, passes * 256 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&status, status_bytes, s);
+    if (e == cudaSuccess) e = dmalloc((void**)&ctr, passes * sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, passes * 256 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, status_bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, passes * sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+        const unsigned hb = (unsigned)std::min<size_t>(tiles, 4 * (size_t)sm_count());
+        launch(k_os_hist, hb, kThreads, 0, s, (const uint64_t*)keys, n, begin_bit, end_bit, passes, hist);
+        launch(k_os_offsets, 1, 256, 0, s, hist, passes);
+        e = cudaGetLastError();
     }
     uint64_t* ka = keys;
     uint64_t* kb = k2;
     uint32_t* va = vals;
     uint32_t* vb = v2;
     for (int p = 0; p < passes && e == cudaSuccess; ++p) {
-        const int shift = begin_bit + 8 * p;
-        launch(k_radix_hist, (unsigned)tiles, kThreads, 0, s, ka, n, shift, hist, (int)tiles);
-        e = scan_impl<uint32_t, uint32_t>(hist, hist, 256 * tiles, nullptr, s);
-        if (e != cudaSuccess) break;
-        launch(k_radix_scatter, (unsigned)tiles, kThreads, 0, s, ka, va, kb, vb, n, shift, hist, (int)tiles);
+        launch(k_os_pass, (unsigned)tiles, kThreads, 0, s, (const uint64_t*)ka, (const uint32_t*)va, kb, vb, n,
+               begin_bit + 8 * p, end_bit, (const uint32_t*)(hist + p * 256), status + (size_t)p * tiles * 256,
+               ctr + p, err, err_bit);
         e = cudaGetLastError();
         uint64_t* tk = ka; ka = kb; kb = tk;
         uint32_t* tv = va; va = vb; vb = tv;
@@ -362,10 +503,21 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit
         e = cudaMemcpyAsync(keys, ka, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
         if (e == cudaSuccess && vals) e = cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
     }
-    cudaFreeAsync(hist, s);
-    cudaFreeAsync(k2, s);
-    if (v2) cudaFreeAsync(v2, s);
+    for (void* q : {(void*)k2, (void*)v2, (void*)hist, (void*)status, (void*)ctr})
+        if (q) cudaFreeAsync(q, s);
     return e;
+}
+
+cudaError_t sort_error_read(uint32_t* h_word, cudaStream_t s) {
+    uint32_t* w = sort_error_word();
+    if (!w) return cudaErrorMemoryAllocation;
+    return cudaMemcpyAsync(h_word, w, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+}
+
+cudaError_t sort_error_clear(cudaStream_t s) {
+    uint32_t* w = sort_error_word();
+    if (!w) return cudaErrorMemoryAllocation;
+    return cudaMemsetAsync(w, 0, sizeof(uint32_t), s);
 }
 
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, cudaStream_t s) {

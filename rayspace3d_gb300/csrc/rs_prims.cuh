@@ -9,10 +9,15 @@
 namespace rs {
 
 // Stable LSD radix sort of 64-bit keys (and optional 32-bit values) on bits
-// [begin_bit, end_bit), 8 bits per pass, in place.  Temporaries come from the
-// library's memory pool.
+// [begin_bit, end_bit), 8 bits per pass, in place; n < 2^32.  Temporaries come from the
+// library's memory pool.  A pass whose bounded look-back wait ran out ORs err_bit into
+// *err (a device word; null = the library's word, read with sort_error_read): the
+// result is then invalid.
 cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s,
-                           int begin_bit = 0);
+                           int begin_bit = 0, uint32_t* err = nullptr, uint32_t err_bit = 1);
+// Queues a copy of the library's sort error word (nonzero after a failed sort) to h_word.
+cudaError_t sort_error_read(uint32_t* h_word, cudaStream_t s);
+cudaError_t sort_error_clear(cudaStream_t s);
 
 // Full 64-bit ascending sort of keys: a single-block bitonic sort for small inputs,
 // the radix sort otherwise.

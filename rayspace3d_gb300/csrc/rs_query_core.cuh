@@ -325,22 +325,18 @@ __device__ __forceinline__ void pim_fallback_ray(const BNode* __restrict__ nodes
 
 // Edge ray i of mesh_overlap_edges.cu:106-216: every target object crossed with t in
 // [1e-6, len + 1e-6] is paired with every source object of the edge.
+// The segment (sx,sy,sz) -> (ex,ey,ez) with its nsrc source objects src[0..nsrc).
 template <int STACK>
-__device__ __forceinline__ void edge_ray(const float* __restrict__ starts, const float* __restrict__ ends,
-                                         const int32_t* __restrict__ offsets, const int32_t* __restrict__ counts,
-                                         const int32_t* __restrict__ sources, uint64_t i,
-                                         const BNode* __restrict__ nodes, uint32_t max_steps,
-                                         const float4* __restrict__ tris, int swap, const PairTable& table) {
-    const float sx = starts[3 * i], sy = starts[3 * i + 1], sz = starts[3 * i + 2];
-    const float ex = ends[3 * i], ey = ends[3 * i + 1], ez = ends[3 * i + 2];
+__device__ __forceinline__ void segment_ray(float sx, float sy, float sz, float ex, float ey, float ez,
+                                            const int32_t* __restrict__ src, int nsrc,
+                                            const BNode* __restrict__ nodes, uint32_t max_steps,
+                                            const float4* __restrict__ tris, int swap, const PairTable& table) {
     // distance3f / normalize3f of mesh_overlap_edges.cu:47-60 as individually rounded operations.
     const float dx = __fsub_rn(ex, sx), dy = __fsub_rn(ey, sy), dz = __fsub_rn(ez, sz);
     const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
     if (len < 1e-6f) return;
     const Ray r = make_ray(sx, sy, sz, __fdiv_rn(dx, len), __fdiv_rn(dy, len), __fdiv_rn(dz, len), 1e-6f,
                            __fadd_rn(len, 1e-6f));
-    const int nsrc = counts[i];
-    const int32_t* src = sources + offsets[i];
     int32_t last[4] = {INT_MIN, INT_MIN, INT_MIN, INT_MIN};
     int lp = 0;
     unsigned int crossings = 0, tests = 0;
@@ -371,6 +367,31 @@ __device__ __forceinline__ void edge_ray(const float* __restrict__ starts, const
         atomicAdd(&table.stats[2], 1ull);
         if (crossings) atomicAdd(&table.stats[3], (unsigned long long)crossings);
     }
+}
+
+template <int STACK>
+__device__ __forceinline__ void edge_ray(const float* __restrict__ starts, const float* __restrict__ ends,
+                                         const int32_t* __restrict__ offsets, const int32_t* __restrict__ counts,
+                                         const int32_t* __restrict__ sources, uint64_t i,
+                                         const BNode* __restrict__ nodes, uint32_t max_steps,
+                                         const float4* __restrict__ tris, int swap, const PairTable& table) {
+    segment_ray<STACK>(starts[3 * i], starts[3 * i + 1], starts[3 * i + 2], ends[3 * i], ends[3 * i + 1],
+                       ends[3 * i + 2], sources + offsets[i], counts[i], nodes, max_steps, tris, swap, table);
+}
+
+// Edge e of triangle t of a source mesh, in the triangle's own orientation (v0v1, v1v2,
+// v2v0), with the triangle's object as its one source: the legacy per-triangle overlap
+// (mesh_overlap.cu:126-179), which traces shared edges once per triangle.
+template <int STACK>
+__device__ __forceinline__ void triangle_edge_ray(const float* __restrict__ V, const uint32_t* __restrict__ I,
+                                                  const int32_t* __restrict__ T, uint64_t r,
+                                                  const BNode* __restrict__ nodes, uint32_t max_steps,
+                                                  const float4* __restrict__ tris, int swap, const PairTable& table) {
+    const uint64_t t = r / 3;
+    const int e = (int)(r % 3);
+    const uint64_t a = I[3 * t + e], b = I[3 * t + (e == 2 ? 0 : e + 1)];
+    segment_ray<STACK>(V[3 * a], V[3 * a + 1], V[3 * a + 2], V[3 * b], V[3 * b + 1], V[3 * b + 2], T + t, 1, nodes,
+                       max_steps, tris, swap, table);
 }
 
 }  // namespace

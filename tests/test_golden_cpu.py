@@ -49,6 +49,38 @@ def test_extract_edges_matches_reference(golden, case):
     np.testing.assert_array_equal(e.sources, golden[p + "sources"])
 
 
+@pytest.mark.parametrize("case", ["cube_grid", "spheres", "soup"])
+def test_oracle_extract_edges_matches_reference(golden, case):
+    """The oracle's C++ restatement of extractEdges (the preprocessing CPU baseline)."""
+    p = f"edges_{case}_"
+    got = bind.extract_edges(golden[p + "V"], golden[p + "I"], golden[p + "T"])
+    for a, k in zip(got, ("starts", "ends", "offsets", "counts", "sources")):
+        assert a.tobytes() == np.asarray(golden[p + k]).astype(a.dtype).tobytes(), k
+
+
+@pytest.mark.parametrize("case", ["fixed", "auto", "outside"])
+def test_oracle_grid_stats_matches_reference(golden, case):
+    """The oracle's C++ restatement of generateGridStats, bit for bit."""
+    p = f"grid_{case}_"
+    res, world = golden[p + "params"]
+    b, cells = bind.grid_stats(golden[p + "V"], golden[p + "I"], golden[p + "T"], int(res), float(world))
+    assert b.tobytes() == golden[p + "bounds"].astype(np.float32).tobytes()
+    assert cells.tobytes() == golden[p + "cells"].tobytes()
+
+
+def test_oracle_preprocessing_agrees_with_restatement_on_shuffled_sets():
+    rng = np.random.default_rng(4)
+    g = synth.sphere_set(300, 1, 0.3, 4.0, 40.0, rng, edges=False)
+    p = rng.permutation(len(g.indices))
+    V, I, T = g.vertices, g.indices[p], g.tri2obj[p]
+    e = synth.extract_edges(V, I, T)
+    got = bind.extract_edges(V, I, T)
+    for a, w in zip(got, (e.starts, e.ends, e.offsets, e.counts, e.sources)):
+        assert a.tobytes() == np.asarray(w).astype(a.dtype).tobytes()
+    b, cells = bind.grid_stats(V, I, T, 16, -1.0)
+    assert cells.tobytes() == synth.grid_stats(V, I, T, 16, -1.0).cells.tobytes()
+
+
 @pytest.mark.parametrize("case", ["fixed", "auto", "outside"])
 def test_grid_stats_matches_reference(golden, case):
     """generateGridStats (preprocess/src/preprocess_dataset.cpp:37-181), bit for bit,

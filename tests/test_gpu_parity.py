@@ -35,9 +35,14 @@ def _check_pim(g, pts, direction=(0.0, 0.0, 1.0), filtered=False, leaf=0):
 def test_radix_sort_matches_numpy(cuda):
     from rayspace3d_gb300 import _lib as L
     rng = np.random.default_rng(5)
-    for n in (1, 7, 4096, 4097, 100_003):
-        keys = rng.integers(0, 2 ** 63, size=n, dtype=np.int64)
-        keys[: n // 3] = keys[0]  # many duplicates
+    cases = [(n, "wide") for n in (1, 7, 3071, 3072, 3073, 4096, 4097, 100_003, 2_000_003)]
+    cases += [(1_500_001, "narrow")]
+    for n, kind in cases:
+        if kind == "wide":
+            keys = rng.integers(0, 2 ** 63, size=n, dtype=np.int64)
+            keys[: n // 3] = keys[0]  # many duplicates
+        else:  # few distinct values in a middle digit range: long runs per digit
+            keys = (rng.integers(0, 300, size=n, dtype=np.int64) << 40) | rng.integers(0, 5, size=n, dtype=np.int64)
         t = torch.from_numpy(keys.copy()).cuda()
         out = torch.empty_like(t)
         # merge_and_deduplicate_pairs_gpu sorts the 8-byte records as u64 and uniques them
