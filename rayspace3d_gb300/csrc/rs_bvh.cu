@@ -8,10 +8,13 @@
 //      vertex bounds) << 32 | triangle id, unique by construction;
 //   3. stable radix sort of the 32 Morton bits only (4 passes; ids stay ascending
 //      within equal codes);
-//   4. one bottom-up pass (k_build_up) that writes the triangles in leaf order
-//      (3 x float4 each), builds the binary radix tree over the sorted keys
-//      agglomeratively and refits its boxes on the way up, emitting 64-byte nodes
-//      in which subtrees of <= leaf_size triangles become leaves.
+//   4. groups of leaf_size / 2 consecutive sorted triangles; a bottom-up pass
+//      (k_build_up) writes the triangles in leaf order (3 x float4 each), builds the
+//      binary radix tree over the groups' keys agglomeratively and refits its boxes on
+//      the way up, emitting 64-byte nodes in which subtrees of <= leaf_size triangles
+//      become leaves, as far as one block of groups reaches;
+//   5. k_build_cross joins the subtrees left open across blocks.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -155,9 +158,10 @@ __global__ void k_morton(const float* __restrict__ V, uint64_t nV, const uint32_
     }
 }
 
-// Length of the common prefix of sorted keys i and i+1 (keys are distinct).
-__device__ __forceinline__ int split_prefix(const uint64_t* __restrict__ keys, int i) {
-    return __clzll((long long)(__ldg(&keys[i]) ^ __ldg(&keys[i + 1])));
+// Length of the common prefix of the keys of groups g and g+1 (the keys of their first
+// triangles, distinct by construction).
+__device__ __forceinline__ int group_prefix(const uint64_t* __restrict__ keys, int g, int L) {
+    return __clzll((long long)(__ldg(&keys[(size_t)g * L]) ^ __ldg(&keys[(size_t)(g + 1) * L])));
 }
 
 __device__ __forceinline__ int exchange_acq_rel(int* p, int v) {
@@ -204,99 +208,115 @@ __device__ __forceinline__ void store_node(BNode* nd, const float lo0[3], const 
     nd->d = make_int4(i0, c0, i1, c1);
 }
 
-// A subtree left open by the block phase of k_build_up: box, leaf range, node slot.
+// Leaf groups of L consecutive sorted triangles.  The entry of the child subtree over
+// groups [a, b] with node slot `slot`: a subtree of at most `leaf` triangles is a leaf
+// (first triangle, count), a larger one an inner node (slot, 0).
+struct Groups {
+    int n, L, leaf;
+    __device__ __forceinline__ int tris(int a, int b) const { return min(n, (b + 1) * L) - a * L; }
+    __device__ __forceinline__ int idx(int a, int b, int slot) const { return tris(a, b) <= leaf ? a * L : slot; }
+    __device__ __forceinline__ int cnt(int a, int b) const {
+        const int c = tris(a, b);
+        return c <= leaf ? c : 0;
+    }
+};
+
+// A subtree left open by k_build_up: box, group range, node slot.
 struct OpenTree {
     float lo[3], hi[3];
     int l, r, self;
 };
 
-// Bottom-up construction of the binary radix tree over the sorted keys, fused with
-// the emission of the leaf-ordered triangles and the box refit (agglomerative LBVH,
-// Apetrei 2014, "Fast and Simple Agglomerative LBVH Construction").  Thread k starts
-// at leaf k with range [k, k].  A subtree [l, r] joins the neighbouring split whose
-// keys share the longer prefix: split r (it is the left child) or split l-1 (the
-// right child); a split with no neighbour on one side takes the other.  This yields
-// the same tree as Karras' top-down construction.
+// Bottom-up construction of the binary radix tree over the leaf groups, fused with the
+// emission of the leaf-ordered triangles and the box refit (agglomerative LBVH, Apetrei
+// 2014, "Fast and Simple Agglomerative LBVH Construction").  Its leaves are groups of L
+// consecutive sorted triangles (group g = sorted triangles [gL, gL+L)), ordered by the
+// key of their first triangle; the tree is the radix tree of those group keys, the same
+// tree Karras' top-down construction gives, and subtrees of <= leaf triangles are
+// entered as leaves by their parents.  Thread k owns group k and starts with
+// the subtree [k, k].  A subtree [l, r] joins the neighbouring split whose keys share the
+// longer prefix: split r (it is the left child) or split l-1 (the right child); a split
+// with no neighbour on one side takes the other.
 //
-// Merges inside a warp's 32 leaves run first, in lock-step rounds without memory
-// fences: a subtree is owned by the lane of its leftmost leaf, so a left child finds
-// its right sibling at lane r+1 and merges when that lane holds a complete subtree
-// that chose the same split; the split prefixes come from the lanes by shuffle.  The
-// rounds end when no merge happens.  The remaining subtrees meet their siblings across
-// warps: at split p the child writes its box and entry into its half of node slot
-// p+1, then exchanges its outer range bound in xchg[p] with acquire-release
-// semantics; the first arrival stops, the second reads its sibling's half, merges and
-// continues.  Every split therefore sees exactly one merge, in the warp or through
-// xchg.  Subtrees of <= leaf_size triangles are entered as leaves (first triangle,
-// count), larger ones by their slot (count 0); slot 0 receives the root.
+// Merges inside the block run in lock-step rounds through shared memory: a subtree is
+// owned by the thread of its leftmost group, so a left child finds its right sibling at
+// thread r+1 and merges when that thread holds a complete subtree that chose the same
+// split.  The rounds end when no merge happens; the subtrees still open go to
+// k_build_cross.  Node slot p+1 holds split p, slot 0 the root.
 __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, uint64_t nV,
                                                  const uint32_t* __restrict__ I, const int32_t* __restrict__ t2o,
-                                                 const uint64_t* __restrict__ keys, int n, int leaf_size,
+                                                 const uint64_t* __restrict__ keys, Groups G, int nG,
                                                  float4* __restrict__ tris, BNode* __restrict__ nodes,
                                                  OpenTree* __restrict__ open, unsigned int* __restrict__ n_open) {
-    __shared__ int s_absorbed[kT];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    const int base = k - lane;
-    const bool valid = k < n;
-    float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+    __shared__ int s_d[kT + 1];  // split prefixes of splits bb-1 .. bb+kT-1
+    __shared__ int s_r[kT], s_self[kT];
+    __shared__ float s_box[6][kT];
+    __shared__ unsigned char s_state[kT];  // bit 0: open subtree, bit 1: left child
+    __shared__ unsigned char s_abs[kT];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int bb = blockIdx.x * kT;
+    const int k = bb + tid;
+    const bool valid = k < nG;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     if (valid) {
-        const uint32_t t = (uint32_t)(__ldg(&keys[k]) & 0xffffffffull);
+        const int j0 = k * G.L, j1 = min(G.n, j0 + G.L);
         const uint64_t last = nV - 1;
-        const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last),
-                       i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
-                       i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
-        float a[3], b[3], c[3];
+        for (int j = j0; j < j1; ++j) {
+            const uint32_t t = (uint32_t)(__ldg(&keys[j]) & 0xffffffffull);
+            const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last),
+                           i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
+                           i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
+            float a[3], b[3], c[3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            a[q] = V[3 * i0 + q];
-            b[q] = V[3 * i1 + q];
-            c[q] = V[3 * i2 + q];
-            lo[q] = fminf(fminf(a[q], b[q]), c[q]);
-            hi[q] = fmaxf(fmaxf(a[q], b[q]), c[q]);
+            for (int q = 0; q < 3; ++q) {
+                a[q] = V[3 * i0 + q];
+                b[q] = V[3 * i1 + q];
+                c[q] = V[3 * i2 + q];
+                lo[q] = fminf(lo[q], fminf(fminf(a[q], b[q]), c[q]));
+                hi[q] = fmaxf(hi[q], fmaxf(fmaxf(a[q], b[q]), c[q]));
+            }
+            tris[3 * (uint64_t)j] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
+            tris[3 * (uint64_t)j + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
+            tris[3 * (uint64_t)j + 2] = make_float4(c[0], c[1], c[2], 0.0f);
         }
-        tris[3 * (uint64_t)k] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
-        tris[3 * (uint64_t)k + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
-        tris[3 * (uint64_t)k + 2] = make_float4(c[0], c[1], c[2], 0.0f);
     }
-    // Split prefixes: lane j holds split base+j; split base-1 is broadcast.
-    const int d_own = (k < n - 1) ? split_prefix(keys, k) : -1;
-    const int d_left = __shfl_sync(0xffffffffu, (lane == 0 && base > 0 && base - 1 < n - 1) ? split_prefix(keys, base - 1)
-                                                                                          : -1, 0);
+    s_d[tid + 1] = (k < nG - 1) ? group_prefix(keys, k, G.L) : -1;
+    if (tid == 0) s_d[0] = (bb > 0 && bb - 1 < nG - 1) ? group_prefix(keys, bb - 1, G.L) : -1;
+    s_abs[tid] = 0;
     int l = k, r = k, self = 0;
-    bool active = valid;
-    for (;;) {
-        // Choose the parent split of the owned subtree (only meaningful when active).
-        const bool root = active && l == 0 && r == n - 1;
-        const int dr = __shfl_sync(0xffffffffu, d_own, min(max(r - base, 0), 31));
-        const int dl_in = __shfl_sync(0xffffffffu, d_own, min(max(l - 1 - base, 0), 31));
-        const int dl = (l - 1 == base - 1) ? d_left : dl_in;
-        const bool left_child = (l == 0) ? true : (r == n - 1) ? false : dr > dl;
-        // Sibling of a left child: the subtree owned by lane r+1-base.
-        const int sl = min(max(r + 1 - base, 0), 31);
-        const int o_active = __shfl_sync(0xffffffffu, (int)(active && !root), sl);
-        const int o_l = __shfl_sync(0xffffffffu, l, sl);
-        const int o_r = __shfl_sync(0xffffffffu, r, sl);
-        const int o_left = __shfl_sync(0xffffffffu, (int)left_child, sl);
-        const int o_self = __shfl_sync(0xffffffffu, self, sl);
-        float olo[3], ohi[3];
+    bool active = valid && nG > 1;  // a single group is the root's only child (k_one_group_root)
+    __syncthreads();
+    for (int round = 0; round < kT; ++round) {
+        bool left_child = false;
+        if (active) {
+            const int dr = s_d[r - bb + 1], dl = s_d[l - bb];
+            left_child = (l == 0) ? true : (r == nG - 1) ? false : dr > dl;
+        }
+        s_r[tid] = r;
+        s_self[tid] = self;
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            olo[q] = __shfl_sync(0xffffffffu, lo[q], sl);
-            ohi[q] = __shfl_sync(0xffffffffu, hi[q], sl);
+            s_box[q][tid] = lo[q];
+            s_box[3 + q][tid] = hi[q];
         }
-        const bool merge = active && !root && left_child && r + 1 - base <= 31 && o_active && o_l == r + 1 && !o_left;
-        s_absorbed[threadIdx.x] = 0;
-        __syncwarp();
-        if (merge) s_absorbed[threadIdx.x - lane + (r + 1 - base)] = 1;
-        __syncwarp();
-        const bool absorbed = s_absorbed[threadIdx.x] != 0;
-        __syncwarp();
-        if (merge) {
+        s_state[tid] = (unsigned char)((active ? 1 : 0) | (left_child ? 2 : 0));
+        __syncthreads();
+        bool merged = false;
+        const int sib = r + 1 - bb;
+        if (active && left_child && sib < kT && r + 1 < nG && s_state[sib] == 1) {
             const int p = r;
-            const int size0 = r - l + 1, size1 = o_r - o_l + 1;
-            store_node(nodes + (p + 1), lo, hi, size0 <= leaf_size ? l : self, size0 <= leaf_size ? size0 : 0, olo,
-                       ohi, size1 <= leaf_size ? o_l : o_self, size1 <= leaf_size ? size1 : 0);
+            const int o_r = s_r[sib];
+            float olo[3], ohi[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                olo[q] = s_box[q][sib];
+                ohi[q] = s_box[3 + q][sib];
+            }
+            // A node of <= leaf triangles is entered as a leaf by its parent, so its slot is
+            // only written when it is larger (or the root).
+            if (G.tris(l, o_r) > G.leaf || (l == 0 && o_r == nG - 1))
+                store_node(nodes + (p + 1), lo, hi, G.idx(l, r, self), G.cnt(l, r), olo, ohi,
+                           G.idx(r + 1, o_r, s_self[sib]), G.cnt(r + 1, o_r));
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 lo[q] = fminf(lo[q], olo[q]);
@@ -304,86 +324,23 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
             }
             r = o_r;
             self = p + 1;
-            if (l == 0 && r == n - 1) {
+            s_abs[sib] = 1;
+            merged = true;
+            if (l == 0 && r == nG - 1) {
                 const BNode nd = nodes[self];
                 nodes[0] = nd;
                 active = false;
             }
         }
-        if (absorbed) active = false;
-        if (!__any_sync(0xffffffffu, merge)) break;
-    }
-    // Block rounds: the subtrees still open after the warp rounds meet siblings owned by
-    // other warps of the block through shared memory, in lock-step rounds separated by
-    // block barriers.  The owner of a subtree is still the thread of its leftmost leaf,
-    // so l == k, r stays inside the block, and the sibling of a left child is owned by
-    // thread r + 1 - bb.
-    {
-        __shared__ int s_d[kT + 1];  // split prefixes of splits bb-1 .. bb+kT-1
-        __shared__ int s_r[kT], s_self[kT];
-        __shared__ float s_box[6][kT];
-        __shared__ unsigned char s_state[kT];  // bit 0: open subtree, bit 1: left child
-        __shared__ unsigned char s_abs[kT];
-        const int bb = blockIdx.x * blockDim.x;
-        const int tid = threadIdx.x;
-        s_d[tid + 1] = d_own;
-        if (tid == 0) s_d[0] = (bb > 0 && bb - 1 < n - 1) ? split_prefix(keys, bb - 1) : -1;
-        s_abs[tid] = 0;
         __syncthreads();
-        for (int round = 0; round < kT; ++round) {
-            bool left_child = false;
-            if (active) {
-                const int dr = s_d[r - bb + 1], dl = s_d[l - bb];
-                left_child = (l == 0) ? true : (r == n - 1) ? false : dr > dl;
-            }
-            s_r[tid] = r;
-            s_self[tid] = self;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                s_box[q][tid] = lo[q];
-                s_box[3 + q][tid] = hi[q];
-            }
-            s_state[tid] = (unsigned char)((active ? 1 : 0) | (left_child ? 2 : 0));
-            __syncthreads();
-            bool merged = false;
-            const int sib = r + 1 - bb;
-            if (active && left_child && sib < kT && r + 1 < n && s_state[sib] == 1) {
-                const int p = r;
-                const int o_r = s_r[sib];
-                const int size0 = r - l + 1, size1 = o_r - r;
-                float olo[3], ohi[3];
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    olo[q] = s_box[q][sib];
-                    ohi[q] = s_box[3 + q][sib];
-                }
-                store_node(nodes + (p + 1), lo, hi, size0 <= leaf_size ? l : self, size0 <= leaf_size ? size0 : 0,
-                           olo, ohi, size1 <= leaf_size ? r + 1 : s_self[sib], size1 <= leaf_size ? size1 : 0);
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    lo[q] = fminf(lo[q], olo[q]);
-                    hi[q] = fmaxf(hi[q], ohi[q]);
-                }
-                r = o_r;
-                self = p + 1;
-                s_abs[sib] = 1;
-                merged = true;
-                if (l == 0 && r == n - 1) {
-                    const BNode nd = nodes[self];
-                    nodes[0] = nd;
-                    active = false;
-                }
-            }
-            __syncthreads();
-            if (s_abs[tid]) {
-                active = false;
-                s_abs[tid] = 0;
-            }
-            if (!__syncthreads_or(merged)) break;
+        if (s_abs[tid]) {
+            active = false;
+            s_abs[tid] = 0;
         }
+        if (!__syncthreads_or(merged)) break;
     }
-    // Subtrees still open go to the cross-block phase (k_build_cross), packed densely so
-    // that its latency-bound walks do not hold this kernel's blocks.
+    // Open subtrees are packed densely for k_build_cross, so that its latency-bound walks
+    // do not hold this kernel's blocks.
     const unsigned m = __ballot_sync(0xffffffffu, active);
     if (!m) return;
     unsigned int slot = 0;
@@ -401,8 +358,11 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
     o.self = self;
 }
 
-// Cross-block merges through the exchange array, one open subtree per thread.
-__global__ void __launch_bounds__(kT) k_build_cross(const uint64_t* __restrict__ keys, int n, int leaf_size,
+// Cross-block merges, one open subtree per thread: at split p the child writes its box and
+// entry into its half of node slot p+1, then exchanges its outer range bound in xchg[p]
+// with acquire-release semantics; the first arrival stops, the second reads its sibling's
+// half, merges and continues.  Every split therefore sees exactly one merge.
+__global__ void __launch_bounds__(kT) k_build_cross(const uint64_t* __restrict__ keys, Groups G, int nG,
                                                     BNode* __restrict__ nodes, int* __restrict__ xchg,
                                                     const OpenTree* __restrict__ open,
                                                     const unsigned int* __restrict__ n_open) {
@@ -416,8 +376,7 @@ __global__ void __launch_bounds__(kT) k_build_cross(const uint64_t* __restrict__
         }
         int l = open[i].l, r = open[i].r, self = open[i].self;
         for (;;) {
-            const int size = r - l + 1;
-            if (l == 0 && r == n - 1) {
+            if (l == 0 && r == nG - 1) {
                 const float4* src = reinterpret_cast<const float4*>(nodes + self);
                 float4* dst = reinterpret_cast<float4*>(nodes);
 #pragma unroll
@@ -425,10 +384,10 @@ __global__ void __launch_bounds__(kT) k_build_cross(const uint64_t* __restrict__
                 break;
             }
             const bool left_child =
-                (l == 0) ? true : (r == n - 1) ? false : split_prefix(keys, r) > split_prefix(keys, l - 1);
+                (l == 0) ? true : (r == nG - 1) ? false : group_prefix(keys, r, G.L) > group_prefix(keys, l - 1, G.L);
             const int p = left_child ? r : l - 1;
             BNode* nd = nodes + (p + 1);
-            store_half(nd, left_child ? 0 : 1, lo, hi, size <= leaf_size ? l : self, size <= leaf_size ? size : 0);
+            store_half(nd, left_child ? 0 : 1, lo, hi, G.idx(l, r, self), G.cnt(l, r));
             const int other = exchange_acq_rel(&xchg[p], left_child ? l : r);
             if (other < 0) break;
             float olo[3], ohi[3];
@@ -445,36 +404,33 @@ __global__ void __launch_bounds__(kT) k_build_cross(const uint64_t* __restrict__
     }
 }
 
-__global__ void k_emit_tris(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I,
-                            const int32_t* __restrict__ t2o, const uint64_t* __restrict__ order, int n,
-                            float4* __restrict__ tris) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t t = (uint32_t)(order[k] & 0xffffffffull);
-    const uint64_t last = nV - 1;
-    const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last), i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
-                   i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
-    const float* a = V + 3 * (uint64_t)i0;
-    const float* b = V + 3 * (uint64_t)i1;
-    const float* c = V + 3 * (uint64_t)i2;
-    tris[3 * (uint64_t)k] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
-    tris[3 * (uint64_t)k + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
-    tris[3 * (uint64_t)k + 2] = make_float4(c[0], c[1], c[2], 0.0f);
-}
-
-// Root for n <= 1: child 0 is the single leaf (if any), child 1 an empty box.
-__global__ void k_small_root(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I, int n,
-                             BNode* nodes) {
+// Root of a set that is one group (1 <= n <= group size): child 0 is the leaf of all n sorted
+// triangles, child 1 an empty box that the slab test always rejects.
+__global__ void k_one_group_root(const float4* __restrict__ tris, int n, BNode* nodes) {
     const float inf = INFINITY;
     float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-    if (n == 1) tri_box(V, nV, I, 0, lo, hi);
+    for (int j = 0; j < n; ++j)
+        for (int v = 0; v < 3; ++v) {
+            const float4 p = tris[3 * j + v];
+            lo[0] = fminf(lo[0], p.x), lo[1] = fminf(lo[1], p.y), lo[2] = fminf(lo[2], p.z);
+            hi[0] = fmaxf(hi[0], p.x), hi[1] = fmaxf(hi[1], p.y), hi[2] = fmaxf(hi[2], p.z);
+        }
     BNode nd;
     nd.a = make_float4(lo[0], lo[1], lo[2], hi[0]);
     nd.b = make_float4(hi[1], hi[2], inf, inf);
     nd.c = make_float4(inf, -inf, -inf, -inf);
-    nd.d = make_int4(0, n == 1 ? 1 : 0, 0, 0);
-    // An empty child must never be entered: its count is 0 and its box is empty,
-    // so the slab test rejects it before the index is used.
+    nd.d = make_int4(0, n, 0, 0);
+    nodes[0] = nd;
+}
+
+// Root of an empty set: two empty children.
+__global__ void k_empty_root(BNode* nodes) {
+    const float inf = INFINITY;
+    BNode nd;
+    nd.a = make_float4(inf, inf, inf, -inf);
+    nd.b = make_float4(-inf, -inf, inf, inf);
+    nd.c = make_float4(inf, -inf, -inf, -inf);
+    nd.d = make_int4(0, 0, 0, 0);
     nodes[0] = nd;
 }
 
@@ -585,7 +541,11 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     cudaError_t e = cudaSuccess;
     int* slot = nullptr;
     const int grid = 4 * sm_count();
-    h->n_nodes = n >= 2 ? (uint64_t)n : 1;  // slot 0 = root, slot p+1 = split p
+    // Leaf groups of half the leaf size: the radix tree over the groups decides which
+    // subtrees of <= leaf_size triangles become leaves.
+    const int group = std::max(1, leaf_size / 2);
+    const int nG = (n + group - 1) / group;
+    h->n_nodes = nG >= 2 ? (uint64_t)nG : 1;          // slot 0 = root, slot p+1 = split p
     h->n_tris = (uint64_t)n;
     const int ptok = prof_begin(P_BVH_BUILD, s);
     e = alloc(&h->nodes, h->n_nodes, s);
@@ -596,35 +556,30 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     cudaMemsetAsync(bounds + 12, 0, sizeof(int), s);
     cudaMemsetAsync(bounds + 13, 0xff, sizeof(int), s);
     if (nV || nF) launch(k_vertex_bounds, grid, kT, 0, s, d_vertices, nV, d_tri2obj, nF, bounds, bounds + 13);
-    if (n <= 1) {
-        launch(k_small_root, 1, 1, 0, s, d_vertices, nV, d_indices, n, h->nodes);
-        if (n == 1) {
-            e = alloc(&keys, 1, s);
-            if (e == cudaSuccess) launch(k_morton, 1, 32, 0, s, d_vertices, nV, d_indices, nF, bounds, keys,
-                                         reinterpret_cast<unsigned int*>(bounds + 12));
-            if (e == cudaSuccess) launch(k_emit_tris, 1, 32, 0, s, d_vertices, nV, d_indices, d_tri2obj,
-                                         (const uint64_t*)keys, 1, h->tris);
-        }
+    if (n == 0) {
+        launch(k_empty_root, 1, 1, 0, s, h->nodes);
     } else {
-        const int nb = (n + kT - 1) / kT;
+        const Groups G{n, group, leaf_size};
         e = alloc(&keys, n, s);
-        if (e == cudaSuccess) e = alloc(&xchg, n - 1, s);
+        if (e == cudaSuccess) e = alloc(&xchg, std::max(nG - 1, 1), s);
+        // Open subtrees per block: at most two per level of the tree (64 key bits), so
+        // nG / 2 + kT bounds them for blocks of kT groups.
+        if (e == cudaSuccess) e = alloc(&open, (size_t)nG / 2 + kT, s);
+        if (e == cudaSuccess) e = alloc(&n_open, 1, s);
         if (e != cudaSuccess) goto fail;
-        launch(k_morton, nb, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys,
+        launch(k_morton, (n + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys,
                reinterpret_cast<unsigned int*>(bounds + 12));
         e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32, reinterpret_cast<uint32_t*>(bounds + 12), 2u);
         if (e != cudaSuccess) goto fail;
-        cudaMemsetAsync(xchg, 0xff, (size_t)(n - 1) * sizeof(int), s);
-        // Open subtrees per block: at most two per level of the tree (64 key bits), so
-        // n / 2 bounds them for blocks of 256 leaves.
-        e = alloc(&open, (size_t)n / 2 + kT, s);
-        if (e == cudaSuccess) e = alloc(&n_open, 1, s);
-        if (e != cudaSuccess) goto fail;
+        cudaMemsetAsync(xchg, 0xff, (size_t)std::max(nG - 1, 1) * sizeof(int), s);
         cudaMemsetAsync(n_open, 0, sizeof(unsigned int), s);
-        launch(k_build_up, nb, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys, n, leaf_size,
-               h->tris, h->nodes, open, n_open);
-        launch(k_build_cross, 4 * sm_count(), kT, 0, s, (const uint64_t*)keys, n, leaf_size, h->nodes, xchg,
-               (const OpenTree*)open, (const unsigned int*)n_open);
+        launch(k_build_up, (nG + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys,
+               G, nG, h->tris, h->nodes, open, n_open);
+        if (nG == 1)
+            launch(k_one_group_root, 1, 1, 0, s, (const float4*)h->tris, n, h->nodes);
+        else
+            launch(k_build_cross, 4 * sm_count(), kT, 0, s, (const uint64_t*)keys, G, nG, h->nodes, xchg,
+                   (const OpenTree*)open, (const unsigned int*)n_open);
     }
     prof_end(P_BVH_BUILD, s, ptok);
     e = cudaGetLastError();

@@ -41,6 +41,7 @@ constexpr int kOsWarpSpan = 32 * kOsItems;
 constexpr int kMaxPasses = 8;
 constexpr unsigned long long kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62, kCountMask = (1ull << 62) - 1;
 constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr int kLookAhead = 8;
 
 __device__ __forceinline__ uint32_t os_digit(uint64_t k, int shift, int end_bit) {
     const int w = min(8, end_bit - shift);
@@ -163,24 +164,35 @@ __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restr
             if (ww < w) before += s_wsum[ww];
         s_dstart[d] = before + x - tc;
     }
-    // Decoupled look-back over the earlier tiles.
+    // Decoupled look-back over the earlier tiles, kLookAhead status words in flight at a
+    // time: aggregates are summed until an inclusive prefix is met; a word not yet
+    // published stops the batch, and the walk resumes from it.
     unsigned long long prefix = 0;
     if (tile > 0) {
         long long j = (long long)tile - 1;
         uint32_t spins = 0;
-        while (j >= 0) {
-            const unsigned long long sv = ld_relaxed(status + (size_t)j * 256 + d);
-            const unsigned long long f = sv & ~kCountMask;
-            if (f == 0ull) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, err_bit);
-                    break;
-                }
-                continue;
+        bool found = false;
+        while (!found) {
+            unsigned long long sv[kLookAhead];
+#pragma unroll
+            for (int q = 0; q < kLookAhead; ++q)
+                sv[q] = (j - q >= 0) ? ld_relaxed(status + (size_t)(j - q) * 256 + d) : 0ull;
+            int used = 0;
+#pragma unroll
+            for (int q = 0; q < kLookAhead; ++q) {
+                if (found || used != q || j - q < 0) continue;
+                const unsigned long long f = sv[q] & ~kCountMask;
+                if (f == 0ull) continue;
+                prefix += sv[q] & kCountMask;
+                ++used;
+                if (f == kFlagPre) found = true;
             }
-            prefix += sv & kCountMask;
-            if (f == kFlagPre) break;
-            --j;
+            if (found) break;
+            if (used == 0 && ++spins > kSpinLimit) {
+                atomicOr(err, err_bit);
+                break;
+            }
+            j -= used;
         }
         st_relaxed(mine, kFlagPre | (prefix + tc));
     }
