@@ -102,7 +102,7 @@ class Clocks:
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
@@ -753,6 +753,21 @@ def run_prep(A, cpu: bool = True):
     return out
 
 
+def combine_ranks(result: dict, world: int, device) -> dict:
+    """N ranks, each running its own joins (independent units, no data-path collective):
+    the step time is the slowest rank's, and whole-job seconds per join is that time
+    divided by the N joins completed in it.  The end-to-end value combines the same way."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([result["ms_per_step"], result["e2e"]["value"]], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    slow_ms, slow_e2e = float(t[0].item()), float(t[1].item())
+    result["ms_per_step"] = round(slow_ms, 4)
+    result["value"] = round(slow_ms / 1e3 / world, 6)
+    result["e2e"]["value"] = round(slow_e2e / world, 6)
+    return result
+
+
 def cpu_join_sample(A, B, frac=0.02, threads=None):
     """Oracle overlap join on a bounded sample of both edge sets, extrapolated to one
     full join: 2 x CPU BVH build + (sampled traversal time / frac)."""
@@ -785,11 +800,8 @@ def cpu_join_sample(A, B, frac=0.02, threads=None):
 def main():
     args = parse_args()
     rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        backend = "nccl" if args.impl == "engine" else "gloo"
-        dist.init_process_group(backend=backend)
     if args.impl == "reference":
+        # The CPU arm has no collective: rank 0 alone runs and prints, the other ranks exit.
         if rank != 0:
             return
         A, B = make_workload(args)
@@ -812,6 +824,9 @@ def main():
                         "CPU port of the same exact tests on all host threads"}
         print(json.dumps(line))
         return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl")
     result, A, B = run_engine(args, rank, world, local)
     if not args.no_pim:
         result["pim"] = run_pim(args, local, args.pim_points, (1.0, 0.0, 0.0))
@@ -829,14 +844,7 @@ def main():
         result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": meta["cores"], "kind": "port",
                                   "sample": meta["sample"]}
     if world > 1:
-        # N independent replicas, one join each per step: whole-job seconds per join is the
-        # slowest rank's step time divided by the joins all ranks completed in it.
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([result["ms_per_step"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        result["ms_per_step"] = round(float(t.item()), 4)
-        result["value"] = round(float(t.item()) / 1e3 / world, 6)
+        combine_ranks(result, world, "cuda")
     if rank == 0:
         print(json.dumps(result))
 
