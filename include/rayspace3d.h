@@ -51,8 +51,9 @@ const char* rs_version(void);
  * Replaces OptixAccelerationStructure::buildInternal (query/src/optix/OptixAccelerationStructure.cpp:22-68),
  * fed by GeometryUploader::upload (query/src/geometry/GeometryUploader.cpp:12-34).
  * d_vertices: float32[nV*3]; d_indices: uint32[nF*3]; d_tri2obj: int32[nF].  The three
- * arrays stay owned by the caller and must outlive the handle.  leaf_size in [1,8]
- * (0 = default 4).  Fails with RS_ERR_INVALID if an index is >= nV. */
+ * arrays stay owned by the caller and must outlive the handle.  leaf_size in [1,16]
+ * (0 = default 2): subtrees of at most leaf_size triangles become leaves.  Fails with
+ * RS_ERR_INVALID if an index is >= nV. */
 int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
                  const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream);
 int rs_bvh_destroy(rs_bvh* bvh);

@@ -522,7 +522,9 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     if ((nF && (!d_indices || !d_tri2obj || !d_vertices)) || (nV && !d_vertices)) return RS_ERR_INVALID;
     if (nF && nV == 0) return RS_ERR_INVALID;               // every index would be out of range
     if (nF >= (uint64_t)0x7fffffff) return RS_ERR_INVALID;  // node/leaf indices are int32
-    if (leaf_size == 0) leaf_size = 4;
+    // Default 2: the exact triangle test costs more than a node visit, so small leaves
+    // trace fastest on dense joins (4 doubles the edge-ray time at selectivity 1e-4).
+    if (leaf_size == 0) leaf_size = 2;
     if (leaf_size < 1 || leaf_size > 16) return RS_ERR_INVALID;
     rs_bvh* h = new rs_bvh();
     h->V = d_vertices;

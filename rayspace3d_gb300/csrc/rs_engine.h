@@ -30,7 +30,7 @@ struct rs_bvh {
     uint64_t n_nodes = 0;
     float4* tris = nullptr;
     uint64_t n_tris = 0;
-    int leaf_size = 4;
+    int leaf_size = 2;
     rs_column_grid cgrid[3];
     // Bounds of all vertices (the reference's BoundingBox::computeFromGeometry).
     float vmin[3] = {0, 0, 0};
