@@ -181,10 +181,10 @@ def run_engine(args, rank, world, local):
         da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
         torch.cuda.synchronize()
 
-        def step(ga, gb, after_copies=False):
+        def step(ga, gb, after_copies=False, edges_ready=None):
             # The two builds run concurrently on their own streams (after the work already
-            # queued on `stream`, or, end to end, after their own geometry copies queued on
-            # those streams); the join on `stream` is ordered after both builds by the engine.
+            # queued on `stream`, or, end to end, after their own geometry copies); the join
+            # on `stream` is ordered after both builds by the engine.
             if not after_copies:
                 sa.wait_stream(stream)
                 sb.wait_stream(stream)
@@ -197,6 +197,8 @@ def run_engine(args, rank, world, local):
             if ps is None:
                 ps = api.PairSet(size, pow2=True, stream=stream)
                 pairs_out[key] = ps
+            if edges_ready is not None:
+                stream.wait_event(edges_ready)
             api.overlap_join(ba, bb, ps, stream=stream)
             keys = ps.finalize(order=1, stream=stream)
             ba.close()
@@ -226,7 +228,8 @@ def run_engine(args, rank, world, local):
         L.rs_profile_enable(0)
         dev_ms = ev0.elapsed_time(ev1) / args.steps
         prof = {}
-        for kid, name in enumerate(["edge_join", "containment", "pim", "bvh_build", "finalize", "estimate"]):
+        for kid, name in enumerate(["edge_join", "containment", "pim", "bvh_build", "finalize", "estimate",
+                                    "build_up"]):
             import ctypes
             ms = ctypes.c_double()
             cnt = ctypes.c_uint64()
@@ -248,21 +251,30 @@ def run_engine(args, rank, world, local):
             dst.edges = tuple(torch.empty_like(t) for t in src.edges)
             dst.cells = torch.empty_like(src.cells)
 
+        sc = torch.cuda.Stream(device=dev)
+        ev = {k: torch.cuda.Event() for k in ("A", "B", "cells", "edges")}
+
         def e2e_step():
-            # Each set's triangles are copied on its build stream, so a build starts as soon
-            # as its own geometry has landed; the grids (needed first, by the estimate) and
-            # then the edge payloads are copied on the join stream meanwhile.
-            for s, dst, tag in ((sa, ga2, "A"), (sb, gb2, "B")):
-                s.wait_stream(stream)
-                with torch.cuda.stream(s):
+            # All inputs go over one copy stream, in the order the step needs them: each
+            # set's triangles (its build starts when they land), the grids (the estimate and
+            # the table sizing run while the edge payloads are still in flight), the edges.
+            sc.wait_stream(stream)
+            with torch.cuda.stream(sc):
+                for dst, tag in ((ga2, "A"), (gb2, "B")):
                     for d, h in zip([dst.V, dst.I, dst.T], host[tag][:3]):
                         d.copy_(h, non_blocking=True)
-            for dst, tag in ((ga2, "A"), (gb2, "B")):
-                dst.cells.copy_(host[tag][-1], non_blocking=True)
-            for dst, tag in ((ga2, "A"), (gb2, "B")):
-                for d, h in zip(dst.edges, host[tag][3:8]):
-                    d.copy_(h, non_blocking=True)
-            k = step(ga2, gb2, after_copies=True)
+                    ev[tag].record(sc)
+                for dst, tag in ((ga2, "A"), (gb2, "B")):
+                    dst.cells.copy_(host[tag][-1], non_blocking=True)
+                ev["cells"].record(sc)
+                for dst, tag in ((ga2, "A"), (gb2, "B")):
+                    for d, h in zip(dst.edges, host[tag][3:8]):
+                        d.copy_(h, non_blocking=True)
+                ev["edges"].record(sc)
+            sa.wait_event(ev["A"])
+            sb.wait_event(ev["B"])
+            stream.wait_event(ev["cells"])
+            k = step(ga2, gb2, after_copies=True, edges_ready=ev["edges"])
             out = k.cpu()
             return out
 
@@ -284,20 +296,35 @@ def run_engine(args, rank, world, local):
     with torch.cuda.stream(stream):
         rc = recheck(L, lambda: (step(da, db), torch.cuda.synchronize()))
 
-    # Roofline of the join's dominant kernel, k_edge_join (one launch per direction;
-    # the BVH build is a chain of smaller kernels).  Algorithmic bytes per launch: the
-    # source edge payload, the target geometry once, and 8 B per pair-table insert.
+    # Roofline of the join's dominant kernel by the launch list, k_build_up (the bottom-up
+    # tree of each BVH build; two launches per join, one per set, on two concurrent
+    # streams).  Algorithmic bytes per launch: the set's triangles read once (12 B per
+    # vertex, 16 B index triple and object id per triangle), the sorted 8 B keys, the 48 B
+    # leaf-ordered triangles written, and 64 B for each tree node over more than
+    # leaf_size triangles (at least nF / leaf_size - 1 of them).
     hbm, peak_kind = peaks()
     roof = None
+    p = prof.get("build_up")
+    if p:
+        leaf = 2
+        per_launch = sum(12.0 * g.nV + (16.0 + 8.0 + 48.0) * g.nF + 64.0 * (g.nF / leaf - 1) for g in (da, db)) / 2.0
+        achieved = per_launch / (p["avg_ms"] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": "k_build_up", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 5), "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
+                "algorithmic_bytes_per_launch": int(per_launch), "avg_launch_ms": round(p["avg_ms"], 4),
+                "traffic": profiled_traffic("k_build_up", args.objects)}
+    # The edge rays (both kernels of one direction: live-edge compaction and rays for the
+    # live edges), against the bytes they would move if every edge were traced: the
+    # source edge payload, the target geometry once and 8 B per pair-table insert.
+    roof_edges = None
     p = prof.get("edge_join")
     if p:
         per_launch = (join_bytes(da, db) + join_bytes(db, da)) / 2.0 + 8.0 * n_pairs / 2.0
         achieved = per_launch / (p["avg_ms"] * 1e-3) / 1e9
-        traffic = profiled_traffic("k_edge_join", args.objects)
-        roof = {"bound": "hbm", "kernel": "k_edge_join", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 5), "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                "algorithmic_bytes_per_launch": int(per_launch), "avg_launch_ms": round(p["avg_ms"], 4),
-                "traffic": traffic}
+        roof_edges = {"bound": "hbm", "kernel": "k_edge_live + k_edge_join_live", "achieved": round(achieved, 2),
+                      "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5),
+                      "algorithmic_bytes_per_launch": int(per_launch), "avg_launch_ms": round(p["avg_ms"], 4),
+                      "traffic": profiled_traffic("k_edge_join", args.objects)}
 
     result = {
         "metric": METRIC, "value": round(dev_ms / 1e3, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -314,6 +341,7 @@ def run_engine(args, rank, world, local):
         "kernels": {k: {kk: round(vv, 5) if isinstance(vv, float) else vv for kk, vv in v.items()}
                     for k, v in prof.items()},
         "roofline": roof,
+        "roofline_edge_rays": roof_edges,
         "clocks": clk.summary(),
     }
     return result, A, B

@@ -575,8 +575,10 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
         if (e != cudaSuccess) goto fail;
         cudaMemsetAsync(xchg, 0xff, (size_t)std::max(nG - 1, 1) * sizeof(int), s);
         cudaMemsetAsync(n_open, 0, sizeof(unsigned int), s);
+        const int utok = prof_begin(P_BUILD_UP, s);
         launch(k_build_up, (nG + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys,
                G, nG, h->tris, h->nodes, open, n_open);
+        prof_end(P_BUILD_UP, s, utok);
         if (nG == 1)
             launch(k_one_group_root, 1, 1, 0, s, (const float4*)h->tris, n, h->nodes);
         else
