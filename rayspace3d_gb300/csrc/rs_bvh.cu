@@ -77,16 +77,35 @@ __global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, const 
     const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t nf = 3 * nV;
     uint64_t done = 0;
+    // Four independent loads in flight per thread and iteration; the component of float4
+    // q is q % 3, advanced incrementally (4 = 1 mod 3).
+    constexpr int U = 4;
     if ((reinterpret_cast<uintptr_t>(V) & 15u) == 0) {
         const float4* V4 = reinterpret_cast<const float4*>(V);
         const uint64_t n4 = nf / 4;
-        for (uint64_t q = tid; q < n4; q += stride) {
-            const float4 v = __ldg(&V4[q]);
-            const int c = (int)(q % 3);
-            fold_component(mn, mx, c, v.x);
-            fold_component(mn, mx, c == 2 ? 0 : c + 1, v.y);
-            fold_component(mn, mx, c == 0 ? 2 : c - 1, v.z);
-            fold_component(mn, mx, c, v.w);
+        const int s3 = (int)(stride % 3), step3 = (int)((U * stride) % 3);
+        int c0 = (int)(tid % 3);
+        for (uint64_t q0 = tid; q0 < n4; q0 += U * stride) {
+            float4 v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint64_t q = q0 + u * stride;
+                v[u] = q < n4 ? __ldg(&V4[q]) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            int c = c0;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (q0 + u * stride < n4) {
+                    fold_component(mn, mx, c, v[u].x);
+                    fold_component(mn, mx, c == 2 ? 0 : c + 1, v[u].y);
+                    fold_component(mn, mx, c == 0 ? 2 : c - 1, v[u].z);
+                    fold_component(mn, mx, c, v[u].w);
+                }
+                c += s3;
+                c = c >= 3 ? c - 3 : c;
+            }
+            c0 += step3;
+            c0 = c0 >= 3 ? c0 - 3 : c0;
         }
         done = 4 * n4;
     }
@@ -95,13 +114,20 @@ __global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, const 
     int mo = -1;
     if ((reinterpret_cast<uintptr_t>(t2o) & 15u) == 0) {
         const int4* T4 = reinterpret_cast<const int4*>(t2o);
-        for (uint64_t q = tid; q < nF / 4; q += stride) {
-            const int4 t = __ldg(&T4[q]);
-            mo = max(max(mo, max(t.x, t.y)), max(t.z, t.w));
+        const uint64_t n4 = nF / 4;
+        for (uint64_t q0 = tid; q0 < n4; q0 += U * stride) {
+            int4 t[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint64_t q = q0 + u * stride;
+                t[u] = q < n4 ? __ldg(&T4[q]) : make_int4(-1, -1, -1, -1);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) mo = max(max(mo, max(t[u].x, t[u].y)), max(t[u].z, t[u].w));
         }
-        for (uint64_t t = 4 * (nF / 4) + tid; t < nF; t += stride) mo = max(mo, t2o[t]);
+        for (uint64_t q = 4 * n4 + tid; q < nF; q += stride) mo = max(mo, t2o[q]);
     } else {
-        for (uint64_t t = tid; t < nF; t += stride) mo = max(mo, t2o[t]);
+        for (uint64_t q = tid; q < nF; q += stride) mo = max(mo, t2o[q]);
     }
     mo = __reduce_max_sync(0xffffffffu, mo);
     if ((threadIdx.x & 31) == 0 && mo >= 0) atomicMax(max_obj, mo);

@@ -63,9 +63,16 @@ __global__ void __launch_bounds__(kThreads) k_os_hist(const uint64_t* __restrict
     __shared__ uint32_t sh[kMaxPasses * 256];
     for (int i = threadIdx.x; i < passes * 256; i += kThreads) sh[i] = 0;
     __syncthreads();
-    for (size_t i = blockIdx.x * (size_t)kThreads + threadIdx.x; i < n; i += (size_t)gridDim.x * kThreads) {
-        const uint64_t k = keys[i];
-        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p * 256 + os_digit(k, begin_bit + 8 * p, end_bit)], 1u);
+    const size_t stride = (size_t)gridDim.x * kThreads;
+    for (size_t i0 = blockIdx.x * (size_t)kThreads + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        uint64_t k[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) k[u] = i0 + u * stride < n ? keys[i0 + u * stride] : 0ull;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i0 + u * stride < n)
+                for (int p = 0; p < passes; ++p)
+                    atomicAdd(&sh[p * 256 + os_digit(k[u], begin_bit + 8 * p, end_bit)], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < passes * 256; i += kThreads)
@@ -98,6 +105,7 @@ __global__ void __launch_bounds__(256) k_os_offsets(uint32_t* __restrict__ hist,
     }
 }
 
+template <bool VALS>
 __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                                                        uint32_t* __restrict__ vout, size_t n, int shift, int end_bit,
@@ -120,20 +128,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restr
     const size_t base = (size_t)tile * kOsTile + (size_t)w * kOsWarpSpan;
     uint64_t k[kOsItems];
     uint32_t v[kOsItems];
-    uint32_t dg[kOsItems];
+    unsigned peers[kOsItems];  // lanes of the warp holding the same digit in item r
 #pragma unroll
     for (int r = 0; r < kOsItems; ++r) {
         const size_t idx = base + (size_t)r * 32 + lane;
         const bool valid = idx < n;
         k[r] = valid ? kin[idx] : 0ull;
-        v[r] = (valid && vin) ? vin[idx] : 0u;
-        dg[r] = valid ? os_digit(k[r], shift, end_bit) : (256u + lane);
+        if (VALS) v[r] = valid ? vin[idx] : 0u;
     }
-    // Per-warp digit counts.
+    // Per-warp digit counts (an invalid key gets a digit of its own: 256 + lane).
 #pragma unroll
     for (int r = 0; r < kOsItems; ++r) {
-        const unsigned peers = __match_any_sync(0xffffffffu, dg[r]);
-        if (dg[r] < 256u && lane == __ffs(peers) - 1) s_cnt[w][dg[r]] += __popc(peers);
+        const bool valid = base + (size_t)r * 32 + lane < n;
+        const uint32_t dg = valid ? os_digit(k[r], shift, end_bit) : (256u + lane);
+        peers[r] = __match_any_sync(0xffffffffu, dg);
+        if (valid && lane == __ffs(peers[r]) - 1) s_cnt[w][dg] += __popc(peers[r]);
         __syncwarp();
     }
     __syncthreads();
@@ -202,16 +211,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restr
     const unsigned lt = lanemask_lt();
 #pragma unroll
     for (int r = 0; r < kOsItems; ++r) {
-        const unsigned peers = __match_any_sync(0xffffffffu, dg[r]);
-        const bool valid = dg[r] < 256u;
+        const bool valid = base + (size_t)r * 32 + lane < n;
+        const uint32_t dg = os_digit(k[r], shift, end_bit);
         uint32_t pos = 0;
-        if (valid) pos = s_dstart[dg[r]] + s_cnt[w][dg[r]] + __popc(peers & lt);
+        if (valid) pos = s_dstart[dg] + s_cnt[w][dg] + __popc(peers[r] & lt);
         __syncwarp();
-        if (valid && lane == __ffs(peers) - 1) s_cnt[w][dg[r]] += __popc(peers);
+        if (valid && lane == __ffs(peers[r]) - 1) s_cnt[w][dg] += __popc(peers[r]);
         __syncwarp();
         if (valid) {
             s_keys[pos] = k[r];
-            s_vals[pos] = v[r];
+            if (VALS) s_vals[pos] = v[r];
         }
     }
     __syncthreads();
@@ -223,7 +232,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restr
         const uint32_t dd = os_digit(kk, shift, end_bit);
         const size_t pos = (size_t)s_gbase[dd] + (i - s_dstart[dd]);
         kout[pos] = kk;
-        if (vout) vout[pos] = s_vals[i];
+        if (VALS) vout[pos] = s_vals[i];
     }
 }
 
@@ -504,7 +513,8 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit
     uint32_t* va = vals;
     uint32_t* vb = v2;
     for (int p = 0; p < passes && e == cudaSuccess; ++p) {
-        launch(k_os_pass, (unsigned)tiles, kThreads, 0, s, (const uint64_t*)ka, (const uint32_t*)va, kb, vb, n,
+        auto kern = vals ? k_os_pass<true> : k_os_pass<false>;
+        launch(kern, (unsigned)tiles, kThreads, 0, s, (const uint64_t*)ka, (const uint32_t*)va, kb, vb, n,
                begin_bit + 8 * p, end_bit, (const uint32_t*)(hist + p * 256), status + (size_t)p * tiles * 256,
                ctr + p, err, err_bit);
         e = cudaGetLastError();
