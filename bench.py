@@ -597,13 +597,14 @@ def run_batch(args, full: bool):
 
 
 def run_intersection(args, n: int):
-    """Full intersection join at uneven sizes: n objects per set (10k by default; the
-    configuration names 100k, whose two resident BVHs at 112 B per triangle plus the
-    inputs exceed the GPU's memory) of icospheres with levels 1..5 (triangle counts
-    log-uniform), radii log-uniform in [0.2, 20], uniform in a 2000^3 world (scaled to keep
-    the density at smaller n), seed 2, 5 % of B planted strictly inside A objects.  One
-    step = both BVH builds (concurrent) + overlap both ways + containment both ways +
-    sorted pair list."""
+    """Full intersection join at uneven sizes: n objects per set (10k by default, the
+    configuration's 100k with --intersection-n 100000) of icospheres with levels 1..5
+    (triangle counts log-uniform), radii log-uniform in [0.2, 20], uniform in a 2000^3
+    world (scaled to keep the density at smaller n), seed 2, 5 % of B planted strictly
+    inside A objects.  One step = both BVH builds (concurrent) + overlap both ways +
+    containment both ways + sorted pair list.  The device memory the step needs (both
+    BVHs at 112 B per triangle and the builds' scratch) is checked against the free memory
+    after generation; a size that does not fit is reported as skipped."""
     import torch
     from rayspace3d_gb300 import api, gen
 
@@ -612,6 +613,14 @@ def run_intersection(args, n: int):
     A, B, planted = gen.intersection_sets(n, seed=2, world=world)
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
+    torch.cuda.empty_cache()  # generation temporaries back to the driver for the builds
+    free0, total = torch.cuda.mem_get_info()
+    # BVH 112 B/triangle resident per set; per build in flight: keys and their copy 16 B,
+    # sort status 0.7 B, open subtrees <= 18 B, exchange 4 B per triangle.
+    need = 112 * (A.nF + B.nF) + 39 * (A.nF + B.nF) + 8 * (A.nE + B.nE)
+    if need > 0.97 * free0:
+        return {"workload": f"full intersection: {n} + {n} objects", "skipped":
+                f"needs about {need / 1e9:.0f} GB of device memory, {free0 / 1e9:.0f} GB free after generation"}
     stream = torch.cuda.Stream()
     sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
     with torch.cuda.stream(stream):
@@ -645,7 +654,10 @@ def run_intersection(args, n: int):
                         f"seed 2, {len(planted)} B objects planted inside A",
             "seconds": round(ms / 1e3, 5), "pairs": int(len(k)), "planted_found": int(found),
             "planted": len(planted), "triangles_per_set": [int(A.nF), int(B.nF)],
-            "edge_rays": int(A.nE + B.nE), "generation_s": round(gen_s, 1)}
+            "edge_rays": int(A.nE + B.nE), "generation_s": round(gen_s, 1),
+            "device_gb": {"inputs": round((total - free0) / 1e9, 1),
+                          "peak_in_use": round((total - torch.cuda.mem_get_info()[0]) / 1e9, 1),
+                          "total": round(total / 1e9, 1)}}
 
 
 def run_learned(args, full: bool):
