@@ -304,7 +304,7 @@ int rs_estimate_mlp(rs_mlp* mlp, const void* d_cellsA, const void* d_cellsB, int
  * library since load.  rs_profile_*: when enabled, device time of the main kernels is
  * accumulated with CUDA events on the launching stream; ids 0 edge join, 1 containment,
  * 2 point-in-mesh, 3 BVH build (whole), 4 pair finalisation, 5 estimator, 6 the build's
- * bottom-up tree kernel alone. */
+ * bottom-up tree kernel alone, 7 the learned estimator's GEMMs (with their split-K sums). */
 uint64_t rs_launch_count(void);
 int rs_profile_enable(int on);
 int rs_profile_reset(void);

@@ -28,7 +28,7 @@ inline void launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
 
 // Kernels whose device time the profiler accumulates (rs_profile_read ids).
 enum ProfId { P_EDGE_JOIN = 0, P_CONTAINMENT = 1, P_PIM = 2, P_BVH_BUILD = 3, P_FINALIZE = 4, P_ESTIMATE = 5,
-              P_BUILD_UP = 6, P_COUNT = 7 };
+              P_BUILD_UP = 6, P_GEMM = 7, P_COUNT = 8 };
 
 // Records an event pair around one launch when profiling is on; prof_collect()
 // (called after the stream has been synchronised) accumulates the elapsed time.

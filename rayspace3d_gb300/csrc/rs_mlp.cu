@@ -137,9 +137,204 @@ __global__ void __launch_bounds__(128) k_gemm(const __nv_bfloat16* __restrict__ 
             }
 }
 
+// ---------------------------------------------------------------------------------
+// Pipelined tensor-core GEMM for 16-byte-aligned operands: 128 x 128 x 64 CTA tiles, 8
+// warps of 64 x 32, three cp.async stages, fragments by ldmatrix (.trans for an operand
+// stored m- or n-contiguous), mma.sync m16n8k16 BF16 with FP32 accumulation.  A K-major
+// operand tile is kept as [row][k] (144-byte rows), an MN-major one as [k][row] (272-byte
+// rows); both paddings make the eight 16-byte rows of each ldmatrix fall in distinct banks.
+// SLAB (split K): split z writes its partial product to the z-th M x N slab of C.
+// ---------------------------------------------------------------------------------
+constexpr int TBM = 128, TBN = 128, TBK = 64, TST = 3, TTH = 256;
+constexpr int KM_LD = TBK + 8;    // bf16 per row of a K-major tile
+constexpr int MN_LD = TBM + 8;    // bf16 per row of an MN-major tile
+constexpr int TILE_ELEMS = TBM * KM_LD > TBK * MN_LD ? TBM * KM_LD : TBK * MN_LD;
+constexpr size_t kGemm2Smem = (size_t)2 * TST * TILE_ELEMS * sizeof(__nv_bfloat16);
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    const int bytes = valid ? 16 : 0;  // 0: the 16 bytes are zero-filled, nothing is read
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <bool TRANS>
+__device__ __forceinline__ void ldsm_x4(uint32_t* r, const void* smem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if (TRANS)
+        asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(sa));
+    else
+        asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(sa));
+}
+
+// One operand tile (128 rows x 64 k) of stage memory `t`: 1024 16-byte chunks, four per
+// thread.
+template <bool KM>
+__device__ __forceinline__ void load_tile2(__nv_bfloat16* t, const __nv_bfloat16* __restrict__ g, int ld, int row0,
+                                           int rows, int k0, int kend) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = threadIdx.x + q * TTH;
+        if (KM) {  // element (row, k) at g[row*ld + k]; chunk = 8 consecutive k
+            const int r = c >> 3, kk = (c & 7) * 8;
+            const bool ok = row0 + r < rows && k0 + kk < kend;
+            const __nv_bfloat16* src = ok ? g + (size_t)(row0 + r) * ld + (k0 + kk) : g;
+            cp_async16(t + r * KM_LD + kk, src, ok);
+        } else {   // element (row, k) at g[k*ld + row]; chunk = 8 consecutive rows
+            const int kk = c >> 4, r = (c & 15) * 8;
+            const bool ok = row0 + r < rows && k0 + kk < kend;
+            const __nv_bfloat16* src = ok ? g + (size_t)(k0 + kk) * ld + (row0 + r) : g;
+            cp_async16(t + kk * MN_LD + r, src, ok);
+        }
+    }
+}
+
+template <bool A_KM, bool B_KM, bool SLAB>
+__global__ void __launch_bounds__(TTH) k_gemm2(const __nv_bfloat16* __restrict__ A, int lda,
+                                               const __nv_bfloat16* __restrict__ B, int ldb, float* __restrict__ C,
+                                               int ldc, int M, int N, int K, int k_per_split) {
+    extern __shared__ __align__(16) __nv_bfloat16 smem[];
+    __nv_bfloat16* As = smem;                       // TST stages
+    __nv_bfloat16* Bs = smem + TST * TILE_ELEMS;    // TST stages
+    const int m0 = blockIdx.y * TBM, n0 = blockIdx.x * TBN;
+    const int kb = blockIdx.z * k_per_split, ke = min(K, kb + k_per_split);
+    const int nk = (ke - kb + TBK - 1) / TBK;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32;
+    float acc[4][4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.0f;
+    // Prologue: the first TST - 1 stages.
+#pragma unroll
+    for (int st = 0; st < TST - 1; ++st) {
+        if (st < nk) {
+            load_tile2<A_KM>(As + st * TILE_ELEMS, A, lda, m0, M, kb + st * TBK, ke);
+            load_tile2<B_KM>(Bs + st * TILE_ELEMS, B, ldb, n0, N, kb + st * TBK, ke);
+        }
+        cp_async_commit();
+    }
+    // Lane addresses inside a 16 x 16 fragment block (see the fragment layouts of
+    // mma.m16n8k16): A K-major (row, k), A MN-major (k, row), B K-major, B MN-major.
+    const int a_r = A_KM ? (lane & 15) : (((lane >> 3) & 1) * 8);
+    const int a_k = A_KM ? ((lane >> 4) * 8) : ((lane & 7) + ((lane >> 4) << 3));
+    const int b_r = B_KM ? ((lane & 7) + ((lane >> 4) << 3)) : ((lane >> 4) * 8);
+    const int b_k = B_KM ? (((lane >> 3) & 1) * 8) : (lane & 15);
+    for (int it = 0; it < nk; ++it) {
+        cp_async_wait<TST - 2>();
+        __syncthreads();
+        {   // refill the stage consumed TST - 1 iterations ago
+            const int nxt = it + TST - 1;
+            if (nxt < nk) {
+                load_tile2<A_KM>(As + (nxt % TST) * TILE_ELEMS, A, lda, m0, M, kb + nxt * TBK, ke);
+                load_tile2<B_KM>(Bs + (nxt % TST) * TILE_ELEMS, B, ldb, n0, N, kb + nxt * TBK, ke);
+            }
+            cp_async_commit();
+        }
+        const __nv_bfloat16* at = As + (it % TST) * TILE_ELEMS;
+        const __nv_bfloat16* bt = Bs + (it % TST) * TILE_ELEMS;
+#pragma unroll
+        for (int ks = 0; ks < TBK; ks += 16) {
+            uint32_t af[4][4], bfr[2][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = wm + 16 * i + a_r, k = ks + a_k;
+                ldsm_x4<!A_KM>(af[i], A_KM ? at + r * KM_LD + k : at + k * MN_LD + r);
+            }
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int r = wn + 16 * j + b_r, k = ks + b_k;
+                ldsm_x4<!B_KM>(bfr[j], B_KM ? bt + r * KM_LD + k : bt + k * MN_LD + r);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t bb[2] = {bfr[j >> 1][(j & 1) * 2], bfr[j >> 1][(j & 1) * 2 + 1]};
+                    mma_bf16(acc[i][j], af[i], bb);
+                }
+        }
+    }
+    cp_async_wait<0>();
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int r = m0 + wm + 16 * i + g + (e >= 2 ? 8 : 0);
+                const int c = n0 + wn + 8 * j + 2 * t + (e & 1);
+                // PARTIAL (split K): each split writes its own M x N slab of C.
+                if (r < M && c < N) C[(SLAB ? (size_t)blockIdx.z * M * ldc : 0) + (size_t)r * ldc + c] = acc[i][j][e];
+            }
+}
+
+// Sum of the split-K slabs: C[r][c] = sum_z W[z][r][c] (W rows of ldw).
+__global__ void k_splitk_sum(const float* __restrict__ W, int split, int M, int N, int ldw, float* __restrict__ C,
+                             int ldc) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)M * N) return;
+    const int r = (int)(i / N), c = (int)(i % N);
+    float sum = 0.0f;
+    for (int z = 0; z < split; ++z) sum += W[((size_t)z * M + r) * ldw + c];
+    C[(size_t)r * ldc + c] = sum;
+}
+
+// The pipelined kernel needs 16-byte chunks along each operand's contiguous dimension.
+template <bool KM>
+bool chunkable(const __nv_bfloat16* p, int ld, int rows, int K) {
+    if ((reinterpret_cast<uintptr_t>(p) & 15) || (ld % 8)) return false;
+    return KM ? (K % 8 == 0) : (rows % 8 == 0);
+}
+
 template <bool A_KM, bool B_KM>
 void gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc, int M, int N, int K,
           cudaStream_t s) {
+    if (chunkable<A_KM>(A, lda, M, K) && chunkable<B_KM>(B, ldb, N, K)) {
+        static bool attr_set[64] = {};  // the kernels' shared-memory opt-in, once per device
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+            cudaFuncSetAttribute(k_gemm2<A_KM, B_KM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kGemm2Smem);
+            cudaFuncSetAttribute(k_gemm2<A_KM, B_KM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kGemm2Smem);
+            attr_set[dev] = true;
+        }
+        const int tiles2 = ((M + TBM - 1) / TBM) * ((N + TBN - 1) / TBN);
+        int split2 = 1;
+        const int target2 = 2 * sm_count();
+        while (tiles2 * split2 < target2 && K / (split2 * 2) >= 4 * TBK) split2 *= 2;
+        int kps2 = (K + split2 - 1) / split2;
+        kps2 = (kps2 + TBK - 1) / TBK * TBK;
+        split2 = (K + kps2 - 1) / kps2;
+        const dim3 grid2((N + TBN - 1) / TBN, (M + TBM - 1) / TBM, split2);
+        float* ws = nullptr;
+        const int ptok = prof_begin(P_GEMM, s);
+        if (split2 > 1 && dmalloc((void**)&ws, (size_t)split2 * M * N * sizeof(float), s) == cudaSuccess) {
+            // Split K: each split writes its own slab of the workspace, then one pass sums them
+            // (in split order, so the result does not depend on scheduling).
+            launch(k_gemm2<A_KM, B_KM, true>, grid2, TTH, kGemm2Smem, s, A, lda, B, ldb, ws, N, M, N, K, kps2);
+            launch(k_splitk_sum, (unsigned)(((uint64_t)M * N + 255) / 256), 256, 0, s, (const float*)ws, split2, M, N,
+                   N, C, ldc);
+            cudaFreeAsync(ws, s);
+        } else if (split2 > 1) {
+            launch(k_gemm2<A_KM, B_KM, false>, dim3(grid2.x, grid2.y, 1), TTH, kGemm2Smem, s, A, lda, B, ldb, C, ldc,
+                   M, N, K, K);
+        } else {
+            launch(k_gemm2<A_KM, B_KM, false>, grid2, TTH, kGemm2Smem, s, A, lda, B, ldb, C, ldc, M, N, K, kps2);
+        }
+        prof_end(P_GEMM, s, ptok);
+        return;
+    }
     const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
     int split = 1;
     const int target = 2 * sm_count();
