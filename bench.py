@@ -197,9 +197,9 @@ def run_engine(args, rank, world, local):
             if ps is None:
                 ps = api.PairSet(size, pow2=True, stream=stream)
                 pairs_out[key] = ps
-            if edges_ready is not None:
-                stream.wait_event(edges_ready)
-            api.overlap_join(ba, bb, ps, stream=stream)
+            # End to end, the broad phase runs while the edge payloads are still in flight
+            # and each direction's rays wait for their own payload.
+            api.overlap_join(ba, bb, ps, stream=stream, edges_ready=edges_ready)
             keys = ps.finalize(order=1, stream=stream)
             ba.close()
             bb.close()
@@ -252,12 +252,13 @@ def run_engine(args, rank, world, local):
             dst.cells = torch.empty_like(src.cells)
 
         sc = torch.cuda.Stream(device=dev)
-        ev = {k: torch.cuda.Event() for k in ("A", "B", "cells", "edges")}
+        ev = {k: torch.cuda.Event() for k in ("A", "B", "cells", "edgesA", "edgesB")}
 
         def e2e_step():
             # All inputs go over one copy stream, in the order the step needs them: each
             # set's triangles (its build starts when they land), the grids (the estimate and
-            # the table sizing run while the edge payloads are still in flight), the edges.
+            # the table sizing run while the edge payloads are still in flight), A's edges,
+            # B's edges.
             sc.wait_stream(stream)
             with torch.cuda.stream(sc):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
@@ -270,11 +271,11 @@ def run_engine(args, rank, world, local):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
                     for d, h in zip(dst.edges, host[tag][3:8]):
                         d.copy_(h, non_blocking=True)
-                ev["edges"].record(sc)
+                    ev["edges" + tag].record(sc)
             sa.wait_event(ev["A"])
             sb.wait_event(ev["B"])
             stream.wait_event(ev["cells"])
-            k = step(ga2, gb2, after_copies=True, edges_ready=ev["edges"])
+            k = step(ga2, gb2, after_copies=True, edges_ready=(ev["edgesA"], ev["edgesB"]))
             out = k.cpu()
             return out
 

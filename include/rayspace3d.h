@@ -198,6 +198,18 @@ int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_ends
                     const int32_t* d_countsB, const int32_t* d_sourcesB, uint64_t nEB,
                     int direction, int with_containment, rs_pairset* ps, void* stream);
 
+/* rs_overlap_join whose edge payloads may still be in flight (no counterpart in the
+ * reference): the broad phase runs at once, each direction's edge rays wait on the stream
+ * for the caller's event (cudaEvent_t; nullable) marking its source payload as written --
+ * edges_a_ready for the A->B rays, edges_b_ready for B->A.  A host that copies the payloads
+ * in hides the broad phase, and the first direction, behind the copies. */
+int rs_overlap_join_after(const rs_bvh* A, const float* d_startsA, const float* d_endsA, const int32_t* d_offsetsA,
+                          const int32_t* d_countsA, const int32_t* d_sourcesA, uint64_t nEA,
+                          const rs_bvh* B, const float* d_startsB, const float* d_endsB, const int32_t* d_offsetsB,
+                          const int32_t* d_countsB, const int32_t* d_sourcesB, uint64_t nEB,
+                          int direction, int with_containment, rs_pairset* ps, void* edges_a_ready,
+                          void* edges_b_ready, void* stream);
+
 /* Broad phase of rs_overlap_join (no counterpart in the reference), on by default: each
  * object's box is tested against the other set's triangle boxes, both widened by more
  * than the edge payload's quantisation and the slab arithmetic's rounding; edges whose

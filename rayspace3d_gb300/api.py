@@ -228,12 +228,21 @@ def triangle_join(target: Bvh, source: DeviceGeometry, ps: PairSet, swap: bool =
 
 
 def overlap_join(A: Bvh, B: Bvh, ps: PairSet, direction: int = 0, with_containment: bool = False,
-                 stream=None) -> None:
-    """Both edge directions (and containment when asked) into ps, growing it on overflow."""
+                 stream=None, edges_ready=None) -> None:
+    """Both edge directions (and containment when asked) into ps, growing it on overflow.
+    edges_ready = (event for A's edges, event for B's edges) (torch.cuda.Event, either None):
+    the broad phase runs at once, each direction's rays wait for their event."""
     ea = A.geom.edge_ptrs()
     eb = B.geom.edge_ptrs()
-    _check(_lib.load().rs_overlap_join(A.handle, *ea, A.geom.nE, B.handle, *eb, B.geom.nE, int(direction),
-                                       int(with_containment), ps.handle, _stream(stream)), "rs_overlap_join")
+    L = _lib.load()
+    if edges_ready is None:
+        _check(L.rs_overlap_join(A.handle, *ea, A.geom.nE, B.handle, *eb, B.geom.nE, int(direction),
+                                 int(with_containment), ps.handle, _stream(stream)), "rs_overlap_join")
+        return
+    evs = [ctypes.c_void_p(e.cuda_event) if e is not None else None for e in edges_ready]
+    _check(L.rs_overlap_join_after(A.handle, *ea, A.geom.nE, B.handle, *eb, B.geom.nE, int(direction),
+                                   int(with_containment), ps.handle, evs[0], evs[1], _stream(stream)),
+           "rs_overlap_join_after")
 
 
 def keys_to_pairs(keys) -> np.ndarray:

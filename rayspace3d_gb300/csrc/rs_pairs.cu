@@ -178,11 +178,12 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
     return n > capacity ? RS_ERR_OUTPUT_OVERFLOW : RS_OK;
 }
 
-extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
-                               const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
-                               uint64_t nEA, const rs_bvh* B, const float* d_startsB, const float* d_endsB,
-                               const int32_t* d_offsetsB, const int32_t* d_countsB, const int32_t* d_sourcesB,
-                               uint64_t nEB, int direction, int with_containment, rs_pairset* ps, void* stream) {
+static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
+                             const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
+                             uint64_t nEA, const rs_bvh* B, const float* d_startsB, const float* d_endsB,
+                             const int32_t* d_offsetsB, const int32_t* d_countsB, const int32_t* d_sourcesB,
+                             uint64_t nEB, int direction, int with_containment, rs_pairset* ps, void* stream,
+                             cudaEvent_t edges_a_ready, cudaEvent_t edges_b_ready) {
     if (!A || !B || !ps || direction < 0 || direction > 2) return RS_ERR_INVALID;
     const bool a2b = direction == 0 || direction == 1;
     const bool b2a = direction == 0 || direction == 2;
@@ -218,8 +219,11 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
         // back to back and checked with one status read.
         cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
+        // Each direction reads its source edges only after the caller's event for them.
+        if (e == cudaSuccess && a2b && edges_a_ready) e = cudaStreamWaitEvent(s, edges_a_ready, 0);
         if (e == cudaSuccess && a2b)
             e = edge_join_async(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s, cullA);
+        if (e == cudaSuccess && b2a && edges_b_ready) e = cudaStreamWaitEvent(s, edges_b_ready, 0);
         if (e == cudaSuccess && b2a)
             e = edge_join_async(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, s, cullB);
         int st = table_status(ps, s, e);
@@ -243,6 +247,27 @@ extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const fl
     }
     release();
     return RS_ERR_TABLE_FULL;
+}
+
+extern "C" int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
+                               const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
+                               uint64_t nEA, const rs_bvh* B, const float* d_startsB, const float* d_endsB,
+                               const int32_t* d_offsetsB, const int32_t* d_countsB, const int32_t* d_sourcesB,
+                               uint64_t nEB, int direction, int with_containment, rs_pairset* ps, void* stream) {
+    return overlap_join_impl(A, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, B, d_startsB, d_endsB,
+                             d_offsetsB, d_countsB, d_sourcesB, nEB, direction, with_containment, ps, stream, nullptr,
+                             nullptr);
+}
+
+extern "C" int rs_overlap_join_after(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
+                                     const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
+                                     uint64_t nEA, const rs_bvh* B, const float* d_startsB, const float* d_endsB,
+                                     const int32_t* d_offsetsB, const int32_t* d_countsB,
+                                     const int32_t* d_sourcesB, uint64_t nEB, int direction, int with_containment,
+                                     rs_pairset* ps, void* edges_a_ready, void* edges_b_ready, void* stream) {
+    return overlap_join_impl(A, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, B, d_startsB, d_endsB,
+                             d_offsetsB, d_countsB, d_sourcesB, nEB, direction, with_containment, ps, stream,
+                             (cudaEvent_t)edges_a_ready, (cudaEvent_t)edges_b_ready);
 }
 
 extern "C" int rs_set_overlap_cull(int on) {

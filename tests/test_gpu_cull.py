@@ -75,3 +75,33 @@ def test_cull_budget_exhausted(cuda):
     big = synth.make_geometry((v * 9.0 + 10.0).astype(np.float32), f, np.zeros(len(f), np.int32))
     _check(big, small)
     _check(small, big)
+
+
+def test_overlap_join_after_events_matches(cuda):
+    """rs_overlap_join_after: the edge payloads are copied on another stream after the call
+    is queued; each direction's rays wait for their event.  Same pair set as the plain join."""
+    A, B = synth.overlap_workload(n_objects=300, level=2, world=30.0, seed=9)
+    da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+    ba, bb = api.Bvh(da), api.Bvh(db)
+    ps = api.PairSet(1 << 14)
+    api.overlap_join(ba, bb, ps)
+    want = np.sort(ps.finalize().cpu().numpy())
+    # fresh edge buffers written by a copy stream that first waits on a slow kernel
+    host = [[t.cpu().pin_memory() for t in g.edges] for g in (da, db)]
+    for g in (da, db):
+        g.edges = tuple(torch.zeros_like(t) for t in g.edges)
+    cs = torch.cuda.Stream()
+    evs = [torch.cuda.Event(), torch.cuda.Event()]
+    with torch.cuda.stream(cs):
+        torch.cuda._sleep(20_000_000)  # keep the copies behind the join's queueing
+        for k, g in enumerate((da, db)):
+            for d, h in zip(g.edges, host[k]):
+                d.copy_(h, non_blocking=True)
+            evs[k].record(cs)
+    ps2 = api.PairSet(1 << 14)
+    api.overlap_join(ba, bb, ps2, edges_ready=(evs[0], evs[1]))
+    got = np.sort(ps2.finalize().cpu().numpy())
+    np.testing.assert_array_equal(got, want)
+    assert len(got) > 0
+    ba.close()
+    bb.close()
