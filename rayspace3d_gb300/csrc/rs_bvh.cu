@@ -309,27 +309,39 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
     s_d[tid + 1] = (k < nG - 1) ? group_prefix(keys, k, G.L) : -1;
     if (tid == 0) s_d[0] = (bb > 0 && bb - 1 < nG - 1) ? group_prefix(keys, bb - 1, G.L) : -1;
     s_abs[tid] = 0;
+    s_state[tid] = 0;
     int l = k, r = k, self = 0;
     bool active = valid && nG > 1;  // a single group is the root's only child (k_one_group_root)
+    // Role of the owned subtree: -1 not yet decided, 0 right child (its state is published
+    // in shared memory, and stays until it is absorbed: a right child never merges), 1 left
+    // child (it merges with the subtree at thread r + 1 once that one is a complete right
+    // child).  A thread publishes only when its role is decided, so most threads stop
+    // writing after their first merges.
+    int role = -1;
     __syncthreads();
     for (int round = 0; round < kT; ++round) {
-        bool left_child = false;
-        if (active) {
+        if (active && role < 0) {
             const int dr = s_d[r - bb + 1], dl = s_d[l - bb];
-            left_child = (l == 0) ? true : (r == nG - 1) ? false : dr > dl;
-        }
-        s_r[tid] = r;
-        s_self[tid] = self;
+            const bool left_child = (l == 0) ? true : (r == nG - 1) ? false : dr > dl;
+            if (left_child) {
+                s_state[tid] = 3;
+                role = 1;
+            } else {
+                s_r[tid] = r;
+                s_self[tid] = self;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            s_box[q][tid] = lo[q];
-            s_box[3 + q][tid] = hi[q];
+                for (int q = 0; q < 3; ++q) {
+                    s_box[q][tid] = lo[q];
+                    s_box[3 + q][tid] = hi[q];
+                }
+                s_state[tid] = 1;
+                role = 0;
+            }
         }
-        s_state[tid] = (unsigned char)((active ? 1 : 0) | (left_child ? 2 : 0));
         __syncthreads();
         bool merged = false;
         const int sib = r + 1 - bb;
-        if (active && left_child && sib < kT && r + 1 < nG && s_state[sib] == 1) {
+        if (active && role == 1 && sib < kT && r + 1 < nG && s_state[sib] == 1) {
             const int p = r;
             const int o_r = s_r[sib];
             float olo[3], ohi[3];
@@ -352,16 +364,18 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
             self = p + 1;
             s_abs[sib] = 1;
             merged = true;
+            role = -1;
             if (l == 0 && r == nG - 1) {
                 const BNode nd = nodes[self];
                 nodes[0] = nd;
                 active = false;
+                s_state[tid] = 0;
             }
         }
         __syncthreads();
-        if (s_abs[tid]) {
+        if (active && role == 0 && s_abs[tid]) {
             active = false;
-            s_abs[tid] = 0;
+            s_state[tid] = 0;
         }
         if (!__syncthreads_or(merged)) break;
     }
