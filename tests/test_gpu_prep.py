@@ -209,3 +209,53 @@ def test_preprocess_refuses_other_loaders(cuda, tmp_path):
     r = subprocess.run([os.path.join(build.BIN, "preprocess_dataset"), "--dataset", str(obj)], capture_output=True,
                        text=True, timeout=120)
     assert r.returncode == 1 and "Could not determine loader" in r.stderr
+
+
+def test_extract_edges_capacity_overflow_reports_sizes(cuda):
+    import ctypes
+    from rayspace3d_gb300 import _lib
+    rng = np.random.default_rng(1)
+    g = synth.sphere_set(20, 1, 0.5, 1.0, 10.0, rng, edges=False)
+    want = synth.extract_edges(g.vertices, g.indices, g.tri2obj)
+    dV = torch.from_numpy(np.ascontiguousarray(g.vertices, np.float32)).cuda()
+    dI = torch.from_numpy(np.ascontiguousarray(g.indices, np.uint32).view(np.int32)).cuda()
+    dT = torch.from_numpy(np.ascontiguousarray(g.tri2obj, np.int32)).cuda()
+    cap = 10
+    bufs = [torch.zeros(cap * 3, dtype=torch.float32, device="cuda") for _ in range(2)] + \
+           [torch.zeros(cap, dtype=torch.int32, device="cuda") for _ in range(3)]
+    nE, nS = ctypes.c_uint64(), ctypes.c_uint64()
+    st = _lib.load().rs_extract_edges(dV.data_ptr(), len(g.vertices), dI.data_ptr(), len(g.indices), dT.data_ptr(),
+                                      *[b.data_ptr() for b in bufs], cap, ctypes.byref(nE), ctypes.byref(nS), None)
+    assert st == 4  # RS_ERR_OUTPUT_OVERFLOW
+    assert nE.value == len(want.starts) and nS.value == len(want.sources)
+    assert all(int(b.abs().sum().item()) == 0 for b in bufs)  # outputs untouched
+
+
+def test_grid_stats_without_triangles(cuda):
+    V = np.array([[0, 0, 0], [2, 3, 4], [1, 1, 1]], np.float32)
+    st, b, cells = _gpu_grid(V, np.zeros((0, 3), np.uint32), np.zeros(0, np.int32), 4, -1.0, n_obj=0)
+    assert st == 0
+    np.testing.assert_array_equal(b, np.array([0, 0, 0, 2, 3, 4], np.float32))
+    assert cells.view(np.uint8).sum() == 0
+
+
+def test_preprocess_shuffle_moves_objects_rigidly(cuda, tmp_path):
+    """--shuffle: one random translation per object (as the reference, not reproducible);
+    triangles and objects unchanged, each object's vertices moved by one vector in
+    [-15, 15]^3, edges and grid derived from the moved geometry."""
+    from rayspace3d_gb300 import formats
+    rng = np.random.default_rng(3)
+    g = synth.sphere_set(50, 1, 0.5, 1.0, 40.0, rng, edges=False)
+    src = tmp_path / "in.pre"
+    formats.write_pre(str(src), formats.Geometry(g.vertices, g.indices, g.tri2obj, total_triangles=len(g.indices)))
+    out, _, _ = _run_pre(tmp_path, src, "--shuffle")
+    h = formats.read_pre(str(tmp_path / "out.pre"))
+    np.testing.assert_array_equal(h.indices, g.indices)
+    np.testing.assert_array_equal(h.tri2obj, g.tri2obj)
+    d = h.vertices.astype(np.float64) - g.vertices.astype(np.float64)
+    for o in range(50):
+        vs = np.unique(g.indices[g.tri2obj == o])
+        assert np.all(np.abs(d[vs] - d[vs[0]]) < 1e-4) and np.all(np.abs(d[vs[0]]) <= 15.0 + 1e-4)
+    e = synth.extract_edges(h.vertices, h.indices, h.tri2obj)
+    np.testing.assert_array_equal(h.edges.offsets, e.offsets)
+    np.testing.assert_array_equal(h.edges.sources, e.sources)
