@@ -256,11 +256,6 @@ __global__ void k_gs_vbounds(const float* __restrict__ V, uint64_t nV, int* __re
     }
 }
 
-int bits_for(unsigned long long v) {
-    int b = 0;
-    while (b < 64 && (v >> b) != 0) ++b;
-    return b;
-}
 
 // Iteration order of a std::unordered_map<int, V> after operator[] on each key in turn:
 // the order in which the reference's pass 3 visits its objects.
@@ -273,19 +268,6 @@ std::vector<uint32_t> map_visit_order(const std::vector<uint32_t>& first_seen) {
     return out;
 }
 
-struct Scratch {
-    cudaStream_t s;
-    std::vector<void*> p;
-    template <class T>
-    cudaError_t get(T** out, size_t bytes) {
-        cudaError_t e = dmalloc((void**)out, bytes ? bytes : 16, s);
-        if (e == cudaSuccess) p.push_back(*out);
-        return e;
-    }
-    ~Scratch() {
-        for (void* q : p) cudaFreeAsync(q, s);
-    }
-};
 
 }  // namespace
 }  // namespace rs

@@ -18,6 +18,30 @@ inline cudaError_t dmalloc(T** p, size_t bytes, cudaStream_t s) {
     return dmalloc(reinterpret_cast<void**>(p), bytes, s);
 }
 
+// Pool allocations of one call, released (stream-ordered) when the scope ends.
+struct Scratch {
+    cudaStream_t s;
+    void* p[16] = {};
+    int n = 0;
+    template <class T>
+    cudaError_t get(T** out, size_t bytes) {
+        if (n == 16) return cudaErrorMemoryAllocation;
+        cudaError_t e = dmalloc((void**)out, bytes ? bytes : 16, s);
+        if (e == cudaSuccess) p[n++] = *out;
+        return e;
+    }
+    ~Scratch() {
+        for (int i = 0; i < n; ++i) cudaFreeAsync(p[i], s);
+    }
+};
+
+// Number of bits needed to write v (0 for 0).
+inline int bits_for(unsigned long long v) {
+    int b = 0;
+    while (b < 64 && (v >> b) != 0) ++b;
+    return b;
+}
+
 // Every kernel of the engine is launched through this wrapper so the number of
 // launches is observable (rs_launch_count).
 template <class... KArgs, class... Args>

@@ -191,27 +191,7 @@ __global__ void k_emit(const float* __restrict__ V, const uint32_t* __restrict__
     offsets[run] = (int32_t)kpos[j];
 }
 
-int bits_for(unsigned long long span) {
-    int b = 0;
-    while (b < 64 && (span >> b) != 0) ++b;
-    return b;
-}
 
-// Pool allocations released (stream-ordered) when the scope ends.
-struct Scratch {
-    cudaStream_t s;
-    void* p[8] = {};
-    int n = 0;
-    template <class T>
-    cudaError_t get(T** out, size_t bytes) {
-        cudaError_t e = dmalloc((void**)out, bytes ? bytes : 16, s);
-        if (e == cudaSuccess) p[n++] = *out;
-        return e;
-    }
-    ~Scratch() {
-        for (int i = 0; i < n; ++i) cudaFreeAsync(p[i], s);
-    }
-};
 
 }  // namespace
 }  // namespace rs
