@@ -259,3 +259,28 @@ def test_count_and_compact_hits_compat(cuda):
     L.compact_hits_gpu(d.data_ptr(), out.data_ptr(), n, ctypes.byref(h))
     assert h.value == int((rr[:, 1] != -1).sum())
     assert np.array_equal(out.cpu().numpy()[: h.value], rr[rr[:, 1] != -1])
+
+
+@pytest.mark.parametrize("leaf", [1, 3, 4, 8, 16])
+def test_overlap_join_leaf_sizes(cuda, leaf):
+    """Every leaf size builds a tree (groups of max(1, leaf / 2) triangles, leaves of up to
+    `leaf`) whose traversal gives the oracle's pair set, with and without the broad phase;
+    oblique point-in-mesh rays traverse the same tree."""
+    A, B = synth.overlap_workload(n_objects=300, level=2, world=22.0, seed=4)
+    want = bind.overlap_join(A, B)
+    da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+    ba, bb = api.Bvh(da, leaf_size=leaf), api.Bvh(db, leaf_size=leaf)
+    L = _lib.load()
+    for cull in (1, 0):
+        L.rs_set_overlap_cull(cull)
+        ps = api.PairSet(1 << 14)
+        api.overlap_join(ba, bb, ps)
+        got = np.sort(ps.finalize().cpu().numpy().astype(np.uint64))
+        np.testing.assert_array_equal(got, want)
+    L.rs_set_overlap_cull(1)
+    g, pts = synth.pim_workload(20_000, level=3, seed=5)
+    d = np.array([0.3, -0.5, 0.81], np.float64)
+    d = tuple(float(x) for x in (d / np.linalg.norm(d)).astype(np.float32))
+    _check_pim(g, pts, direction=d, leaf=leaf)
+    ba.close()
+    bb.close()
