@@ -363,9 +363,10 @@ def recheck(L, fn):
             "rate_per_test": (ex.value / tests.value) if tests.value else 0.0}
 
 
-def run_pim(args, local, n_points, direction, reps=20):
+def run_pim(args, local, n_points, direction, reps=20, filtered=False):
     """Point-in-mesh on one level-4 icosphere: kernel time (profiler), stream time and
-    end-to-end time with the points copied in from pinned host memory."""
+    end-to-end time with the points copied in from pinned host memory.  filtered: the
+    filter-refine variant (bounding-box mesh test first, raytracer_filter_refine)."""
     import ctypes
 
     import torch
@@ -381,14 +382,16 @@ def run_pim(args, local, n_points, direction, reps=20):
         obj = torch.empty(len(pts), dtype=torch.int32, device="cuda")
         inside = torch.empty(len(pts), dtype=torch.uint8, device="cuda")
         for _ in range(3):
-            api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside, stream=stream)
+            api.point_in_mesh(bvh, dp, direction=direction, filtered=filtered, out_obj=obj, out_inside=inside,
+                              stream=stream)
         torch.cuda.synchronize()
         L.rs_profile_reset()
         L.rs_profile_enable(1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(reps):
-            api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside, stream=stream)
+            api.point_in_mesh(bvh, dp, direction=direction, filtered=filtered, out_obj=obj, out_inside=inside,
+                              stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
         L.rs_profile_enable(0)
@@ -403,17 +406,18 @@ def run_pim(args, local, n_points, direction, reps=20):
         t0 = time.perf_counter()
         for _ in range(reps):
             dp.copy_(hp, non_blocking=True)
-            api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside, stream=stream)
+            api.point_in_mesh(bvh, dp, direction=direction, filtered=filtered, out_obj=obj, out_inside=inside,
+                              stream=stream)
             hin.copy_(inside, non_blocking=True)
         torch.cuda.synchronize()
         e2e = (time.perf_counter() - t0) / reps
-        rc = recheck(L, lambda: (api.point_in_mesh(bvh, dp, direction=direction, out_obj=obj, out_inside=inside,
-                                                   stream=stream), torch.cuda.synchronize()))
+        rc = recheck(L, lambda: (api.point_in_mesh(bvh, dp, direction=direction, filtered=filtered, out_obj=obj,
+                                                   out_inside=inside, stream=stream), torch.cuda.synchronize()))
     hbm, kind = peaks()
     nbytes = 13 * len(pts) + 12 * dg.nV + 16 * dg.nF
     axis = "xyz"[int(np.argmax(np.abs(direction)))]
     return {"workload": f"{len(pts)} points uniform in [-1.5,1.5]^3, level-4 icosphere (5120 triangles), "
-                        f"+{axis} rays, seed 0",
+                        f"+{axis} rays, seed 0" + (", bounding-box filter then refine" if filtered else ""),
             "mpts_s": round(len(pts) / (ms * 1e-3) / 1e6, 2), "ms": round(ms, 4),
             "kernel_ms": round(kavg, 4), "inside_frac": round(float((obj >= 0).float().mean().item()), 5),
             "e2e_mpts_s": round(len(pts) / e2e / 1e6, 2),
@@ -888,6 +892,7 @@ def main():
     if not args.no_pim:
         result["pim"] = run_pim(args, local, args.pim_points, (1.0, 0.0, 0.0))
         result["pim_z"] = run_pim(args, local, args.pim_points, (0.0, 0.0, 1.0))
+        result["pim_filtered"] = run_pim(args, local, args.pim_points, (0.0, 0.0, 1.0), filtered=True)
         if not args.no_variants:
             result["pim_100m"] = run_pim(args, local, 100_000_000, (1.0, 0.0, 0.0), reps=5)
     if not args.no_variants:
