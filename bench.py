@@ -428,8 +428,10 @@ def run_pim(args, local, n_points, direction, reps=20, filtered=False):
                          "algorithmic_bytes_per_launch": nbytes, "peak_source": kind + " hbm_gbs"}}
 
 
-def run_join_variant(args, world_size, steps=5):
-    """The overlap join at another world size (device-resident), pairs and recheck rate."""
+def run_join_variant(args, world_size, steps=5, filtered=False):
+    """The overlap join at another world size (device-resident), pairs and recheck rate.
+    filtered: the same join through rs_overlap_join_filtered (object-box filter, BVHs over
+    the overlapping objects' triangles only, built inside the call)."""
     import torch
     from rayspace3d_gb300 import _lib, api, synth
 
@@ -444,14 +446,17 @@ def run_join_variant(args, world_size, steps=5):
         sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
 
         def step():
-            sa.wait_stream(stream)
-            sb.wait_stream(stream)
-            ba, bb = api.Bvh(da, stream=sa, asynchronous=True), api.Bvh(db, stream=sb, asynchronous=True)
             est, _ = api.estimate_pairs(da, db, stream=stream)
             size = api.hash_size_pow2(est)
             ps = cache.get(size)
             if ps is None:
                 ps = cache[size] = api.PairSet(size, pow2=True, stream=stream)
+            if filtered:
+                api.overlap_join_filtered(da, db, ps, stream=stream)
+                return ps.finalize(order=1, stream=stream), est
+            sa.wait_stream(stream)
+            sb.wait_stream(stream)
+            ba, bb = api.Bvh(da, stream=sa, asynchronous=True), api.Bvh(db, stream=sb, asynchronous=True)
             api.overlap_join(ba, bb, ps, stream=stream)
             keys = ps.finalize(order=1, stream=stream)
             ba.close()
@@ -471,7 +476,7 @@ def run_join_variant(args, world_size, steps=5):
         rc = recheck(L, lambda: (step(), torch.cuda.synchronize()))
     n_pairs = int(keys.numel())
     return {"workload": f"overlap join: {args.objects} + {args.objects} level-2 icospheres, world {world_size:g}^3, "
-                        f"seed 1, {args.grid}^3 grid",
+                        f"seed 1, {args.grid}^3 grid" + (", object-filtered BVHs" if filtered else ""),
             "seconds": round(ms / 1e3, 6), "pairs": n_pairs, "estimated_pairs": int(est),
             "selectivity": n_pairs / float(args.objects) ** 2,
             "edge_rays_per_join": int(da.nE + db.nE), "recheck": rc}
@@ -897,6 +902,8 @@ def main():
             result["pim_100m"] = run_pim(args, local, 100_000_000, (1.0, 0.0, 0.0), reps=5)
     if not args.no_variants:
         result["join_w80"] = run_join_variant(args, 80.7)
+        result["join_filtered"] = run_join_variant(args, args.world, filtered=True)
+        result["join_w80_filtered"] = run_join_variant(args, 80.7, filtered=True)
         result["batch"] = run_batch(args, args.batch_full)
         result["learned"] = run_learned(args, args.learned_full)
         result["intersection"] = run_intersection(args, args.intersection_n)

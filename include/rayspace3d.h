@@ -210,6 +210,22 @@ int rs_overlap_join_after(const rs_bvh* A, const float* d_startsA, const float* 
                           int direction, int with_containment, rs_pairset* ps, void* edges_a_ready,
                           void* edges_b_ready, void* stream);
 
+/* Overlap (with_containment = 0) or full intersection join straight from two device
+ * geometries (no counterpart in the reference): every object's box is computed, objects
+ * whose widened box overlaps no widened object box of the other set are dropped, and each
+ * set's BVH (leaf_size as rs_bvh_build) is built over the triangles of its remaining
+ * objects only.  Same pair set as rs_bvh_build of both sets + rs_overlap_join, with the
+ * same table growth; the BVHs live only inside the call.  Sparse joins build and trace a
+ * small fraction of the data. */
+int rs_overlap_join_filtered(const float* d_VA, uint64_t nVA, const uint32_t* d_IA, uint64_t nFA,
+                             const int32_t* d_TA, const float* d_startsA, const float* d_endsA,
+                             const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
+                             uint64_t nEA, const float* d_VB, uint64_t nVB, const uint32_t* d_IB, uint64_t nFB,
+                             const int32_t* d_TB, const float* d_startsB, const float* d_endsB,
+                             const int32_t* d_offsetsB, const int32_t* d_countsB, const int32_t* d_sourcesB,
+                             uint64_t nEB, int direction, int with_containment, int leaf_size, rs_pairset* ps,
+                             void* stream);
+
 /* Broad phase of rs_overlap_join (no counterpart in the reference), on by default: each
  * object's box is tested against the other set's triangle boxes, both widened by more
  * than the edge payload's quantisation and the slab arithmetic's rounding; edges whose

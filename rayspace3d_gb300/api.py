@@ -245,6 +245,17 @@ def overlap_join(A: Bvh, B: Bvh, ps: PairSet, direction: int = 0, with_containme
            "rs_overlap_join_after")
 
 
+def overlap_join_filtered(A: DeviceGeometry, B: DeviceGeometry, ps: PairSet, direction: int = 0,
+                          with_containment: bool = False, leaf_size: int = 0, stream=None) -> None:
+    """The join of overlap_join from the two geometries directly, with the BVHs built over
+    the triangles of the objects whose boxes overlap the other set's (rs_overlap_join_filtered)."""
+    ea, eb = A.edge_ptrs(), B.edge_ptrs()
+    _check(_lib.load().rs_overlap_join_filtered(
+        _ptr(A.V), A.nV, _ptr(A.I), A.nF, _ptr(A.T), *ea, A.nE, _ptr(B.V), B.nV, _ptr(B.I), B.nF, _ptr(B.T), *eb,
+        B.nE, int(direction), int(with_containment), int(leaf_size), ps.handle, _stream(stream)),
+        "rs_overlap_join_filtered")
+
+
 def keys_to_pairs(keys) -> np.ndarray:
     """u64 keys (id1<<32 | id2) -> int32[n,2] (id1, id2)."""
     k = np.asarray(keys.cpu().numpy() if isinstance(keys, torch.Tensor) else keys).astype(np.uint64)

@@ -42,6 +42,8 @@ uint64_t next_pow2(uint64_t v) {
     return v + 1;
 }
 
+}  // namespace
+
 cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s) {
     if (ps->slots) cudaFreeAsync(ps->slots, s);
     ps->slots = nullptr;
@@ -49,8 +51,6 @@ cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s) {
     ps->max_probes = (unsigned)std::min<uint64_t>(capacity, 8192);
     return dmalloc((void**)&ps->slots, capacity * sizeof(unsigned long long), s);
 }
-
-}  // namespace
 }  // namespace rs
 
 using namespace rs;

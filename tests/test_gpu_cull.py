@@ -105,3 +105,41 @@ def test_overlap_join_after_events_matches(cuda):
     assert len(got) > 0
     ba.close()
     bb.close()
+
+
+@pytest.mark.parametrize("world,containment", [(30.0, False), (8.0, False), (400.0, False), (30.0, True)])
+def test_filtered_join_matches_full_join(cuda, world, containment):
+    """rs_overlap_join_filtered: BVHs over the objects whose boxes overlap the other set's
+    only; the pair set equals the join over full BVHs (and the oracle's)."""
+    A, B = synth.overlap_workload(n_objects=300, level=2, world=world, seed=12)
+    da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+    ba, bb = api.Bvh(da), api.Bvh(db)
+    ps = api.PairSet(1 << 12)
+    api.overlap_join(ba, bb, ps, with_containment=containment)
+    want = np.sort(ps.finalize().cpu().numpy())
+    for direction in (0, 1, 2):
+        ps2 = api.PairSet(1 << 8)  # small: exercises the table growth
+        api.overlap_join_filtered(da, db, ps2, direction=direction, with_containment=containment)
+        got = np.sort(ps2.finalize().cpu().numpy())
+        if direction == 0:
+            np.testing.assert_array_equal(got, want)
+        else:
+            ps3 = api.PairSet(1 << 12)
+            api.overlap_join(ba, bb, ps3, direction=direction, with_containment=containment)
+            np.testing.assert_array_equal(got, np.sort(ps3.finalize().cpu().numpy()))
+    if not containment and world == 30.0:
+        np.testing.assert_array_equal(want.astype(np.uint64), bind.overlap_join(A, B))
+    ba.close()
+    bb.close()
+
+
+def test_filtered_join_with_an_empty_set(cuda):
+    A, _ = synth.overlap_workload(n_objects=50, level=1, world=10.0, seed=2)
+    V, F = synth.cube_mesh((0, 0, 0), (1, 1, 1))
+    empty = synth.make_geometry(V, F[:0], np.zeros(0, np.int32), edges=False)
+    da, de = api.DeviceGeometry(A), api.DeviceGeometry(empty)
+    de.edges = (torch.zeros((0, 3), device="cuda"), torch.zeros((0, 3), device="cuda")) + tuple(
+        torch.zeros(0, dtype=torch.int32, device="cuda") for _ in range(3))
+    ps = api.PairSet(1 << 8)
+    api.overlap_join_filtered(da, de, ps, with_containment=True)
+    assert ps.finalize().numel() == 0
