@@ -36,7 +36,7 @@ void usage(const char* exe) {
               << std::endl;
     std::cout << "Options:" << std::endl;
     std::cout << "  --mode <wkt|mesh|dt>       Dataset loading mode (default: mesh)" << std::endl;
-    std::cout << "  --dataset <path>           Path to dataset (this build reads .pre geometry)" << std::endl;
+    std::cout << "  --dataset <path>           Path to dataset (a .pre file: its geometry is preprocessed again)" << std::endl;
     std::cout << "  --output-geometry <path>   Path to text file for geometry data output" << std::endl;
     std::cout << "  --output-timing <path>     Path to JSON file for preprocessing timing output" << std::endl;
     std::cout << "  --shuffle                  Randomly translate each loaded object" << std::endl;
@@ -144,7 +144,7 @@ int main(int argc, char** argv) {
     timer.start(modeStr == "wkt" ? "Loading WKT Dataset" : "Loading Dataset");
     if (lowerExt(datasetPath) != ".pre") {
         std::cerr << "Error: Could not determine loader for path: " << datasetPath
-                  << " (this build preprocesses .pre geometry; OBJ, DT and WKT loaders are not included)"
+                  << " (preprocess_dataset on the GPU reads .pre geometry; OBJ, DT and WKT loaders are not included)"
                   << std::endl;
         return 1;
     }
