@@ -31,6 +31,11 @@ def cuda_include() -> str:
     return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nv))), "include")
 
 
+def available() -> bool:
+    """True where the reference sources this recipe compiles are present."""
+    return os.path.isdir(REF)
+
+
 def build(force: bool = False) -> str:
     if not os.path.isdir(REF):
         raise RuntimeError("reference sources are not present on this machine")
