@@ -161,7 +161,12 @@ int rs_pairset_counters(const rs_pairset* ps, uint64_t* h_out8, void* stream);
  * order 0: ascending (id1,id2); order 1: ascending (id2,id1), the order of
  * raytracer_mesh_overlap's output, whose dedup sorts MeshQueryResult{id1,id2} reinterpreted
  * as a little-endian u64.  d_keys receives up to `capacity` keys (id1<<32 | id2) and
- * *h_count the total; RS_ERR_OUTPUT_OVERFLOW if it exceeds capacity. */
+ * *h_count the total; RS_ERR_OUTPUT_OVERFLOW if it exceeds capacity.  The function returns
+ * after d_keys is written, unless `order` carries RS_FINALIZE_NO_WAIT: then, for up to 4096
+ * keys that fit, it returns once the work is queued on `stream` (read d_keys in stream
+ * order).  The count comes from the table's last status read (the one every join entry
+ * point makes) when no launch has used the table since, else from a read of its own. */
+#define RS_FINALIZE_NO_WAIT 0x100
 int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, uint64_t capacity,
                         uint64_t* h_count, void* stream);
 

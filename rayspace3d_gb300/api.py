@@ -26,6 +26,9 @@ from .formats import Geometry, Grid
 _check = _lib.check
 
 
+RS_FINALIZE_NO_WAIT = 0x100  # rs_pairset_finalize: return once the small-table path is queued
+
+
 def _stream(stream: Optional[torch.cuda.Stream] = None) -> ctypes.c_void_p:
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
@@ -189,12 +192,15 @@ class PairSet:
         return cap.value, cnt.value
 
     def finalize(self, order: int = 0, stream=None) -> torch.Tensor:
-        """Sorted unique keys as an int64 tensor on the GPU (bit pattern of the u64 keys)."""
+        """Sorted unique keys as an int64 tensor on the GPU (bit pattern of the u64 keys),
+        written in the order of `stream` (the current stream waits for it when they differ)."""
         _, cnt = self.info(stream)
         out = torch.empty(max(cnt, 1), dtype=torch.int64, device="cuda")
         n = ctypes.c_uint64()
-        _check(_lib.load().rs_pairset_finalize(self.handle, int(order), _ptr(out), cnt, ctypes.byref(n),
-                                               _stream(stream)), "rs_pairset_finalize")
+        _check(_lib.load().rs_pairset_finalize(self.handle, int(order) | RS_FINALIZE_NO_WAIT, _ptr(out), cnt,
+                                               ctypes.byref(n), _stream(stream)), "rs_pairset_finalize")
+        if stream is not None and stream != torch.cuda.current_stream():
+            torch.cuda.current_stream().wait_stream(stream)
         return out[:n.value]
 
     def close(self):

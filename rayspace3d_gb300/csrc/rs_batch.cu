@@ -417,6 +417,7 @@ extern "C" int rs_batch_submit(rs_batch* b, void* stream) {
     for (const rs_batch_item& it : b->items) {
         const int u = bvh_use(effective(b, it.bvh), s);
         if (u != RS_OK) return u;
+        if (it.ps) it.ps->known_count = -1;  // a replayed graph inserts without table_view()
     }
     b->last_stream = s;
     if (!b->use_graph || s == nullptr) return to_status(enqueue(b, s));  // the legacy stream cannot be captured

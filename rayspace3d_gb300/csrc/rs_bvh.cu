@@ -159,14 +159,42 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
 
 // Keys of the triangles: the Morton code of the box centre quantised in the bounds of
 // all vertices, << 32 | triangle id.  Also flags out-of-range vertex indices.
+// Object boxes of the objects below min(largest id + 1, cap) set to empty (min +inf, max
+// -inf as ordered ints); the largest id comes from k_vertex_bounds.
+__global__ void k_obox_init(int* __restrict__ box, uint64_t cap, const int* __restrict__ max_obj) {
+    const uint64_t n = min((uint64_t)(max(*max_obj, -1) + 1), cap);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < 6 * n; i += (uint64_t)gridDim.x * blockDim.x)
+        box[i] = (i % 6) < 3 ? 0x7fffffff : (int)0x80000000;
+}
+
+// Morton key of each triangle's box centre (and, into obox, the box of each object below
+// obox_cap: triangles of one object are usually stored together, so the lanes of a warp
+// with equal objects reduce first and one of them does the atomics).
 __global__ void k_morton(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I, uint64_t nF,
-                         const int* __restrict__ bounds, uint64_t* __restrict__ keys,
-                         unsigned int* __restrict__ bad_index) {
+                         const int32_t* __restrict__ T, const int* __restrict__ bounds, uint64_t* __restrict__ keys,
+                         unsigned int* __restrict__ bad_index, int* __restrict__ obox, uint64_t obox_cap) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t < nF) {
         if (I[3 * t] >= nV || I[3 * t + 1] >= nV || I[3 * t + 2] >= nV) atomicOr(bad_index, 1u);
         float lo[3], hi[3];
         tri_box(V, nV, I, t, lo, hi);
+        if (obox) {
+            const int32_t o = T[t];
+            int v[6] = {flt_ord(lo[0]), flt_ord(lo[1]), flt_ord(lo[2]), flt_ord(hi[0]), flt_ord(hi[1]), flt_ord(hi[2])};
+            const unsigned int peers = __match_any_sync(__activemask(), o);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                v[k] = __reduce_min_sync(peers, v[k]);
+                v[3 + k] = __reduce_max_sync(peers, v[3 + k]);
+            }
+            if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && o >= 0 && (uint64_t)o < obox_cap) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    atomicMin(&obox[6 * (uint64_t)o + k], v[k]);
+                    atomicMax(&obox[6 * (uint64_t)o + 3 + k], v[3 + k]);
+                }
+            }
+        }
         uint32_t q[3];
         const float scale[3] = {2048.0f, 2048.0f, 1024.0f};
 #pragma unroll
@@ -546,6 +574,7 @@ static void bvh_free(rs_bvh* h) {
     pinned_slot_release(h->pending);
     if (h->nodes) cudaFree(h->nodes);
     if (h->tris) cudaFree(h->tris);
+    if (h->obox) cudaFree(h->obox);
     for (auto& g : h->cgrid) {
         if (g.start) cudaFree(g.start);
         if (g.list) cudaFree(g.list);
@@ -609,8 +638,14 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
         if (e == cudaSuccess) e = alloc(&open, (size_t)nG / 2 + kT, s);
         if (e == cudaSuccess) e = alloc(&n_open, 1, s);
         if (e != cudaSuccess) goto fail;
-        launch(k_morton, (n + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, nF, bounds, keys,
-               reinterpret_cast<unsigned int*>(bounds + 12));
+        // Object boxes for the broad phase of the joins, for up to min(nF, 2^24) objects
+        // (dense ids: every object has a triangle); more objects, and the joins compute them.
+        h->obox_cap = std::min<uint64_t>(nF, 1ull << 24);
+        e = alloc(&h->obox, 6 * h->obox_cap, s);
+        if (e != cudaSuccess) goto fail;
+        launch(k_obox_init, 2 * sm_count(), kT, 0, s, h->obox, h->obox_cap, (const int*)(bounds + 13));
+        launch(k_morton, (n + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, nF, d_tri2obj, (const int*)bounds,
+               keys, reinterpret_cast<unsigned int*>(bounds + 12), h->obox, h->obox_cap);
         e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32, reinterpret_cast<uint32_t*>(bounds + 12), 2u);
         if (e != cudaSuccess) goto fail;
         cudaMemsetAsync(xchg, 0xff, (size_t)std::max(nG - 1, 1) * sizeof(int), s);
@@ -644,8 +679,10 @@ fail:
     if (e != cudaSuccess) {
         if (h->nodes) cudaFreeAsync(h->nodes, s);
         if (h->tris) cudaFreeAsync(h->tris, s);
+        if (h->obox) cudaFreeAsync(h->obox, s);
         h->nodes = nullptr;
         h->tris = nullptr;
+        h->obox = nullptr;
         cudaStreamSynchronize(s);
         pinned_slot_release(slot);
         if (h->done) cudaEventDestroy(h->done);

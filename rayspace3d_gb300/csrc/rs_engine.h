@@ -37,6 +37,10 @@ struct rs_bvh {
     float vmax[3] = {0, 0, 0};
     // Largest object id + 1 over the triangles (0 when there are none).
     uint64_t n_obj = 0;
+    // Object boxes (ordered-int min xyz, max xyz per object) from the build's Morton
+    // pass, for the objects below obox_cap; valid when n_obj <= obox_cap.
+    int* obox = nullptr;
+    uint64_t obox_cap = 0;
     int device = 0;
     // Completion of the build, and its device result words until bvh_ready() has read
     // them (asynchronous builds); the fields above that come from them (vmin, vmax,
@@ -56,10 +60,14 @@ struct rs_pairset {
     unsigned long long* meta = nullptr;
     int track = 0;  // count slot accesses and contention
     int device = 0;
+    // meta[1] as last read by the host with status ok, while no launch has been given the
+    // table since (table_view() resets it); -1 when unknown.
+    long long known_count = -1;
 };
 
 namespace rs {
 constexpr int kMetaWords = 16;
+constexpr int kGatherWord = 10;  // meta word used as the finalize gather counter
 // Upper bound on the node visits of one traversal of a valid tree.
 inline uint32_t max_steps(const rs_bvh* b) { return (uint32_t)(2 * b->n_nodes + 8); }
 int to_status(cudaError_t e);

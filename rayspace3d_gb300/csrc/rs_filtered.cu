@@ -385,6 +385,7 @@ extern "C" int rs_overlap_join_filtered(const float* d_VA, uint64_t nVA, const u
     // 5. The join over the filtered BVHs, with the table growth of rs_overlap_join.
     const EdgeCull cullA{A.cand, A.n_obj}, cullB{B.cand, B.n_obj};
     for (int attempt = 0; attempt < 8; ++attempt) {
+        ps->known_count = -1;
         e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
         if (e == cudaSuccess && a2b && A.cand)

@@ -51,46 +51,62 @@ __global__ void __launch_bounds__(kT) k_tri_edge_join(const float* __restrict__ 
     triangle_edge_ray<kStack>(V, I, T, r, nodes, max_steps, tris, swap, table);
 }
 
-// Broad phase of one direction: the edges with at least one candidate source object
-// (k_cull_query) are appended to `live` (any order: the pair table deduplicates).  A
-// light kernel, so the dependent loads of many edges are in flight at once.
-__global__ void __launch_bounds__(256) k_edge_live(const int32_t* __restrict__ offsets,
-                                                   const int32_t* __restrict__ counts,
-                                                   const int32_t* __restrict__ sources, uint64_t nE,
-                                                   const uint8_t* __restrict__ cull, uint64_t n_cull,
-                                                   uint32_t* __restrict__ live, unsigned int* __restrict__ n_live) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+// The edges of one source set traced against the other set's BVH, with the source
+// objects' broad-phase flags and the list of live edges.
+struct EdgeJob {
+    const float* starts;
+    const float* ends;
+    const int32_t* offsets;
+    const int32_t* counts;
+    const int32_t* sources;
+    uint64_t nE;
+    const uint8_t* cull;  // flag per source object below n_cull
+    uint64_t n_cull;
+    uint32_t* live;
+    unsigned int* n_live;
+    const BNode* nodes;
+    uint32_t max_steps;
+    const float4* tris;
+    int swap;
+};
+
+// Broad phase: the edges with at least one candidate source object (k_cull_query) are
+// appended to their job's `live` list (any order: the pair table deduplicates).  A light
+// kernel, so the dependent loads of many edges are in flight at once.  Blocks below
+// blocks0 run job j0, the others j1.
+__global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsigned int blocks0) {
+    const bool second = blockIdx.x >= blocks0;
+    const EdgeJob& j = second ? j1 : j0;
+    const uint64_t i = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x;
     bool any = false;
-    if (i < nE) {
-        const int ns = counts[i];
-        const int32_t* sp = sources + offsets[i];
+    if (i < j.nE) {
+        const int ns = j.counts[i];
+        const int32_t* sp = j.sources + j.offsets[i];
         for (int q = 0; q < ns && !any; ++q) {
             const int32_t so = sp[q];
-            any = (so < 0 || (uint64_t)so >= n_cull) ? true : cull[so] != 0;
+            any = (so < 0 || (uint64_t)so >= j.n_cull) ? true : j.cull[so] != 0;
         }
     }
     const unsigned int m = __ballot_sync(0xffffffffu, any);
     if (!m) return;
     const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
     unsigned int base = 0;
-    if (lane == leader) base = atomicAdd(n_live, (unsigned int)__popc(m));
+    if (lane == leader) base = atomicAdd(j.n_live, (unsigned int)__popc(m));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (any) live[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    if (any) j.live[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
 }
 
-// Edge rays of the live list (grid-stride: the list length is only known on the device).
-__global__ void __launch_bounds__(kT) k_edge_join_live(const float* __restrict__ starts,
-                                                       const float* __restrict__ ends,
-                                                       const int32_t* __restrict__ offsets,
-                                                       const int32_t* __restrict__ counts,
-                                                       const int32_t* __restrict__ sources,
-                                                       const uint32_t* __restrict__ live,
-                                                       const unsigned int* __restrict__ n_live,
-                                                       const BNode* __restrict__ nodes, uint32_t max_steps,
-                                                       const float4* __restrict__ tris, int swap, PairTable table) {
-    const unsigned int n = *n_live;
-    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        edge_ray<kStack>(starts, ends, offsets, counts, sources, live[j], nodes, max_steps, tris, swap, table);
+// Edge rays of the live lists of j0 then j1 (grid-stride: the list lengths are only known
+// on the device; a null n_live is an empty list).
+__global__ void __launch_bounds__(kT) k_edge_join_live(EdgeJob j0, EdgeJob j1, PairTable table) {
+    const unsigned int n0 = j0.n_live ? *j0.n_live : 0u, n1 = j1.n_live ? *j1.n_live : 0u;
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n0 + n1; k += gridDim.x * blockDim.x) {
+        const bool b = k >= n0;
+        edge_ray<kStack>(b ? j1.starts : j0.starts, b ? j1.ends : j0.ends, b ? j1.offsets : j0.offsets,
+                         b ? j1.counts : j0.counts, b ? j1.sources : j0.sources, b ? j1.live[k - n0] : j0.live[k],
+                         b ? j1.nodes : j0.nodes, b ? j1.max_steps : j0.max_steps, b ? j1.tris : j0.tris,
+                         b ? j1.swap : j0.swap, table);
+    }
 }
 
 __global__ void k_first_tri_init(int32_t* __restrict__ first, uint64_t nObj) {
@@ -180,14 +196,31 @@ __device__ __forceinline__ bool cull_overlap(float l0, float l1, float l2, float
            l2 - m2 <= qhi[2] && h2 + m2 >= qlo[2];
 }
 
+// The objects of one set (their boxes) queried against the other set's BVH.
+struct CullJob {
+    const int* box;  // ordered-int min xyz, max xyz per object
+    uint64_t n_obj;
+    const BNode* nodes;
+    uint32_t max_steps;
+    const float4* tris;
+    uint8_t* cand;
+};
+
 // One thread per object of one set: does its widened box overlap any widened triangle
 // box of the other set's BVH?  cand[o] = 1 on the first overlap, or when the query runs
 // out of its node budget or stack; 0 otherwise.  Node boxes contain their triangles'
-// boxes and the widening grows with the box, so node culling is conservative.
-__global__ void k_cull_query(const int* __restrict__ box, uint64_t n_obj, const BNode* __restrict__ nodes,
-                             uint32_t max_steps, const float4* __restrict__ tris, uint8_t* __restrict__ cand) {
-    const uint64_t a = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (a >= n_obj) return;
+// boxes and the widening grows with the box, so node culling is conservative.  Blocks
+// below blocks0 run job j0, the others j1 (both directions of a join in one launch).
+__global__ void k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
+    const bool second = blockIdx.x >= blocks0;
+    const CullJob j = second ? j1 : j0;
+    const uint64_t a = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x;
+    if (a >= j.n_obj) return;
+    const int* __restrict__ box = j.box;
+    const BNode* __restrict__ nodes = j.nodes;
+    const float4* __restrict__ tris = j.tris;
+    uint8_t* __restrict__ cand = j.cand;
+    const uint32_t max_steps = j.max_steps;
     float qlo[3], qhi[3];
     bool empty = false;
 #pragma unroll
@@ -377,6 +410,7 @@ __global__ void __launch_bounds__(kT) k_containment(const float* __restrict__ V,
 int recheck_join(int op, unsigned long long* out) { return recheck_op(op, out); }
 
 PairTable table_view(rs_pairset* ps) {
+    ps->known_count = -1;  // a launch is about to insert
     PairTable t;
     t.slots = ps->slots;
     t.capacity = ps->capacity;
@@ -394,6 +428,8 @@ using namespace rs;
 
 namespace rs {
 // Launches one edge-ray direction without waiting for it (status lands in the table's meta word).
+cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream_t s);
+
 cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const float* d_ends,
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
                             int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull) {
@@ -406,51 +442,111 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
         prof_end(P_EDGE_JOIN, s, ptok);
         return cudaGetLastError();
     }
-    // Live edges first, then rays for them only.
+    EdgeJob job{d_starts, d_ends, d_offsets, d_counts, d_sources, nE, cull.cand, cull.n_obj, nullptr, nullptr,
+                (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap};
+    return edge_jobs_async(&job, 1, ps, s);
+}
+
+// Live edges first, then rays for them only: the live checks of all jobs in one launch,
+// their rays in another.  Each job's nE < 2^32 and its cull flags set.
+cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream_t s) {
     unsigned int* n_live = nullptr;
-    uint32_t* live = nullptr;
-    cudaError_t e = dmalloc((void**)&n_live, sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = dmalloc((void**)&live, nE * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(n_live, 0, sizeof(unsigned int), s);
-    if (e == cudaSuccess) {
+    cudaError_t e = dmalloc((void**)&n_live, 2 * sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(n_live, 0, 2 * sizeof(unsigned int), s);
+    uint64_t blocks[2] = {0, 0}, total_e = 0;
+    EdgeJob jobs[2] = {};
+    for (int d = 0; d < n_jobs && e == cudaSuccess; ++d) {
+        jobs[d] = job[d];
+        e = dmalloc((void**)&jobs[d].live, std::max<uint64_t>(jobs[d].nE, 1) * sizeof(uint32_t), s);
+        jobs[d].n_live = n_live + d;
+        blocks[d] = (jobs[d].nE + 255) / 256;
+        total_e += jobs[d].nE;
+    }
+    if (e == cudaSuccess && total_e) {
         const int ptok = prof_begin(P_EDGE_JOIN, s);
-        launch(k_edge_live, (unsigned)((nE + 255) / 256), 256, 0, s, d_offsets, d_counts, d_sources, nE,
-               (const uint8_t*)cull.cand, cull.n_obj, live, n_live);
-        launch(k_edge_join_live, (unsigned)std::min<uint64_t>(grid, 8ull * sm_count()), kT, 0, s, d_starts, d_ends,
-               d_offsets, d_counts, d_sources, (const uint32_t*)live, (const unsigned int*)n_live, target->nodes,
-               max_steps(target), target->tris, swap, table_view(ps));
+        launch(k_edge_live, (unsigned)(blocks[0] + blocks[1]), 256, 0, s, jobs[0], jobs[1], (unsigned)blocks[0]);
+        launch(k_edge_join_live, (unsigned)std::min<uint64_t>((total_e + kT - 1) / kT, 8ull * sm_count()), kT, 0, s,
+               jobs[0], jobs[1], table_view(ps));
         prof_end(P_EDGE_JOIN, s, ptok);
         e = cudaGetLastError();
     }
-    if (live) cudaFreeAsync(live, s);
+    for (int d = 0; d < n_jobs; ++d)
+        if (jobs[d].live) cudaFreeAsync(jobs[d].live, s);
     if (n_live) cudaFreeAsync(n_live, s);
     return e;
 }
 
-// Broad-phase flags of `src`'s objects against `other`'s BVH (one query per object).
-cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cudaStream_t s) {
-    int* box = nullptr;
-    cudaError_t e = dmalloc((void**)&box, 6 * src->n_obj * sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    launch(k_obj_box_init, (unsigned)((6 * src->n_obj + 255) / 256), 256, 0, s, box, src->n_obj);
-    launch(k_obj_boxes, (unsigned)((src->n_tris + 255) / 256), 256, 0, s, (const float4*)src->tris, src->n_tris,
-           box, src->n_obj);
-    launch(k_cull_query, (unsigned)((src->n_obj + kT - 1) / kT), kT, 0, s, (const int*)box, src->n_obj,
-           (const BNode*)other->nodes, max_steps(other), (const float4*)other->tris, cand);
-    e = cudaGetLastError();
-    cudaFreeAsync(box, s);
+// Both edge directions of a join with both broad-phase flag sets: A's edges against B's
+// BVH (swap 0) and B's edges against A's BVH (swap 1), rays of both in flight together.
+cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const float* endsA, const int32_t* offsetsA,
+                                 const int32_t* countsA, const int32_t* sourcesA, uint64_t nEA, const EdgeCull& cullA,
+                                 const rs_bvh* B, const float* startsB, const float* endsB, const int32_t* offsetsB,
+                                 const int32_t* countsB, const int32_t* sourcesB, uint64_t nEB, const EdgeCull& cullB,
+                                 rs_pairset* ps, cudaStream_t s) {
+    EdgeJob job[2];
+    int n = 0;
+    if (nEA && B->n_tris)
+        job[n++] = EdgeJob{startsA, endsA, offsetsA, countsA, sourcesA, nEA, cullA.cand, cullA.n_obj, nullptr, nullptr,
+                           (const BNode*)B->nodes, max_steps(B), (const float4*)B->tris, 0};
+    if (nEB && A->n_tris)
+        job[n++] = EdgeJob{startsB, endsB, offsetsB, countsB, sourcesB, nEB, cullB.cand, cullB.n_obj, nullptr, nullptr,
+                           (const BNode*)A->nodes, max_steps(A), (const float4*)A->tris, 1};
+    return n ? edge_jobs_async(job, n, ps, s) : cudaSuccess;
+}
+
+// Broad-phase flags of A's objects against B's BVH into candA and of B's objects against
+// A's BVH into candB (either null: that direction is skipped), one query per object, both
+// directions in one launch.  The object boxes are the build's (k_morton) when they cover
+// every object of the set, else computed here from its leaf triangles.
+cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, cudaStream_t s) {
+    const rs_bvh* src[2] = {A, B};
+    const rs_bvh* other[2] = {B, A};
+    uint8_t* cand[2] = {candA, candB};
+    int* tmp[2] = {nullptr, nullptr};
+    CullJob job[2] = {};
+    unsigned int blocks[2] = {0, 0};
+    cudaError_t e = cudaSuccess;
+    for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
+        const rs_bvh* h = src[d];
+        if (!cand[d] || h->n_obj == 0) continue;
+        const int* box = h->obox;
+        if (!box || h->n_obj > h->obox_cap) {
+            e = dmalloc((void**)&tmp[d], 6 * h->n_obj * sizeof(int), s);
+            if (e != cudaSuccess) break;
+            launch(k_obj_box_init, (unsigned)((6 * h->n_obj + 255) / 256), 256, 0, s, tmp[d], h->n_obj);
+            launch(k_obj_boxes, (unsigned)((h->n_tris + 255) / 256), 256, 0, s, (const float4*)h->tris, h->n_tris,
+                   tmp[d], h->n_obj);
+            box = tmp[d];
+        }
+        job[d] = CullJob{box, h->n_obj, (const BNode*)other[d]->nodes, max_steps(other[d]),
+                         (const float4*)other[d]->tris, cand[d]};
+        blocks[d] = (unsigned int)((h->n_obj + kT - 1) / kT);
+    }
+    if (e == cudaSuccess && blocks[0] + blocks[1] > 0)
+        launch(k_cull_query, blocks[0] + blocks[1], kT, 0, s, job[0], job[1], blocks[0]);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    for (int* p : tmp)
+        if (p) cudaFreeAsync(p, s);
     return e;
 }
 
+// Broad-phase flags of `src`'s objects against `other`'s BVH.
+cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cudaStream_t s) {
+    return cull_pair_async(src, other, cand, nullptr, s);
+}
+
 // Waits for the stream and turns the table's status bits into an rs_status.
+// The distinct-key count read with it is kept for rs_pairset_finalize/info.
 int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e) {
-    unsigned long long st = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ps->meta, sizeof(st), cudaMemcpyDeviceToHost, s);
+    unsigned long long m[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m, ps->meta, sizeof(m), cudaMemcpyDeviceToHost, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
     prof_collect();
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return to_status(e);
-    return status_from_bits((uint32_t)st);
+    const int st = status_from_bits((uint32_t)m[0]);
+    ps->known_count = st == RS_OK ? (long long)m[1] : -1;
+    return st;
 }
 }  // namespace rs
 

@@ -19,7 +19,12 @@ PairTable table_view(rs_pairset* ps);
 cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const float* d_ends,
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
                             int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull);
-cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cudaStream_t s);
+cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, cudaStream_t s);
+cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const float* endsA, const int32_t* offsetsA,
+                                 const int32_t* countsA, const int32_t* sourcesA, uint64_t nEA, const EdgeCull& cullA,
+                                 const rs_bvh* B, const float* startsB, const float* endsB, const int32_t* offsetsB,
+                                 const int32_t* countsB, const int32_t* sourcesB, uint64_t nEB, const EdgeCull& cullB,
+                                 rs_pairset* ps, cudaStream_t s);
 bool g_overlap_cull = true;
 int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e);
 
@@ -45,6 +50,7 @@ uint64_t next_pow2(uint64_t v) {
 }  // namespace
 
 cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s) {
+    ps->known_count = -1;
     if (ps->slots) cudaFreeAsync(ps->slots, s);
     ps->slots = nullptr;
     ps->capacity = capacity;
@@ -102,9 +108,11 @@ extern "C" int rs_pairset_create(uint64_t capacity, int pow2, rs_pairset** out, 
 extern "C" int rs_pairset_clear(rs_pairset* ps, void* stream) {
     if (!ps) return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
+    ps->known_count = -1;
     cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) ps->known_count = 0;
     return to_status(e);
 }
 
@@ -123,7 +131,9 @@ extern "C" int rs_pairset_destroy(rs_pairset* ps) {
 extern "C" int rs_pairset_info(const rs_pairset* ps, uint64_t* capacity, uint64_t* count, void* stream) {
     if (!ps) return RS_ERR_INVALID;
     if (capacity) *capacity = ps->capacity;
-    if (count) {
+    if (count && ps->known_count >= 0) {
+        *count = (uint64_t)ps->known_count;
+    } else if (count) {
         cudaStream_t s = (cudaStream_t)stream;
         unsigned long long c = 0;
         cudaError_t e = cudaMemcpyAsync(&c, ps->meta + 1, sizeof(c), cudaMemcpyDeviceToHost, s);
@@ -136,17 +146,39 @@ extern "C" int rs_pairset_info(const rs_pairset* ps, uint64_t* capacity, uint64_
 
 extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, uint64_t capacity,
                                    uint64_t* h_count, void* stream) {
+    const bool no_wait = (order & RS_FINALIZE_NO_WAIT) != 0;
+    order &= ~RS_FINALIZE_NO_WAIT;
     if (!ps || !h_count || (capacity && !d_keys)) return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     *h_count = 0;
-    unsigned long long meta[2] = {0, 0};
-    cudaError_t e = cudaMemcpyAsync(meta, ps->meta, sizeof(meta), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return to_status(e);
-    int st = status_from_bits((uint32_t)meta[0]);
-    if (st != RS_OK) return st;
-    const uint64_t n = meta[1];
+    cudaError_t e = cudaSuccess;
+    // The status and count: from the last read when no launch has touched the table since.
+    uint64_t n = 0;
+    if (ps->known_count >= 0) {
+        n = (uint64_t)ps->known_count;
+    } else {
+        unsigned long long meta[2] = {0, 0};
+        e = cudaMemcpyAsync(meta, ps->meta, sizeof(meta), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return to_status(e);
+        const int st = status_from_bits((uint32_t)meta[0]);
+        if (st != RS_OK) return st;
+        n = meta[1];
+        ps->known_count = (long long)n;
+    }
     if (n == 0) return RS_OK;
+    if (n <= kSmallTableSort && n <= capacity) {
+        // Gather and one-block sort straight into d_keys; nothing to read back.
+        const int ptok = prof_begin(P_FINALIZE, s);
+        e = table_keys_sorted_small(reinterpret_cast<const uint64_t*>(ps->slots), ps->capacity, kEmptyKey,
+                                    order == 1 ? 1 : 0, d_keys, n, ps->meta + kGatherWord, s);
+        prof_end(P_FINALIZE, s, ptok);
+        if (e == cudaSuccess && !no_wait) e = cudaStreamSynchronize(s);
+        if (!no_wait) prof_collect();
+        if (e != cudaSuccess) return to_status(e);
+        *h_count = n;
+        return RS_OK;
+    }
     uint64_t* tmp = nullptr;
     uint64_t* dcount = nullptr;
     const int ptok = prof_begin(P_FINALIZE, s);
@@ -201,8 +233,7 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
     EdgeCull cullA, cullB;
     if (g_overlap_cull && A->n_obj && B->n_obj && A->n_tris && B->n_tris) {
         cudaError_t e = dmalloc((void**)&cand, A->n_obj + B->n_obj, s);
-        if (e == cudaSuccess && a2b) e = cull_async(A, B, cand, s);
-        if (e == cudaSuccess && b2a) e = cull_async(B, A, cand + A->n_obj, s);
+        if (e == cudaSuccess) e = cull_pair_async(A, B, a2b ? cand : nullptr, b2a ? cand + A->n_obj : nullptr, s);
         if (e == cudaSuccess) {
             if (a2b) cullA = EdgeCull{cand, A->n_obj};
             if (b2a) cullB = EdgeCull{cand + A->n_obj, B->n_obj};
@@ -217,15 +248,25 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
         // Order of executeHashQuery (raytracer_intersection_estimated_main.cpp:107-158): overlap A->B,
         // overlap B->A, containment A->B, containment B->A.  The two edge directions are queued
         // back to back and checked with one status read.
+        ps->known_count = -1;
         cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
-        // Each direction reads its source edges only after the caller's event for them.
-        if (e == cudaSuccess && a2b && edges_a_ready) e = cudaStreamWaitEvent(s, edges_a_ready, 0);
-        if (e == cudaSuccess && a2b)
-            e = edge_join_async(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s, cullA);
-        if (e == cudaSuccess && b2a && edges_b_ready) e = cudaStreamWaitEvent(s, edges_b_ready, 0);
-        if (e == cudaSuccess && b2a)
-            e = edge_join_async(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, s, cullB);
+        // Both directions with their broad phase and no events: one live-edge launch and one
+        // ray launch for both.  Otherwise each direction reads its source edges only after
+        // the caller's event for them.
+        const bool together = a2b && b2a && !edges_a_ready && !edges_b_ready && cullA.cand && cullB.cand &&
+                              nEA <= 0xffffffffull && nEB <= 0xffffffffull;
+        if (e == cudaSuccess && together) {
+            e = edge_join_pair_async(A, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, cullA, B, d_startsB,
+                                     d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, cullB, ps, s);
+        } else {
+            if (e == cudaSuccess && a2b && edges_a_ready) e = cudaStreamWaitEvent(s, edges_a_ready, 0);
+            if (e == cudaSuccess && a2b)
+                e = edge_join_async(B, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s, cullA);
+            if (e == cudaSuccess && b2a && edges_b_ready) e = cudaStreamWaitEvent(s, edges_b_ready, 0);
+            if (e == cudaSuccess && b2a)
+                e = edge_join_async(A, d_startsB, d_endsB, d_offsetsB, d_countsB, d_sourcesB, nEB, 1, ps, s, cullB);
+        }
         int st = table_status(ps, s, e);
         if (with_containment) {
             if (st == RS_OK && a2b) st = rs_containment(B, A->V, A->nV, A->I, A->nF, A->t2o, 0, ps, stream);

@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kThreads) k_compact_write(const uint64_t* __re
 // Single-block bitonic sort of up to kSmallSort keys in shared memory.
 constexpr int kSmallSort = 4096;
 
-__global__ void __launch_bounds__(1024) k_sort_small(uint64_t* __restrict__ keys, int n) {
+__global__ void __launch_bounds__(1024) k_sort_small(uint64_t* __restrict__ keys, int n, int swap_out) {
     __shared__ uint64_t sh[kSmallSort];
     int m = 1;
     while (m < n) m <<= 1;
@@ -436,15 +436,49 @@ __global__ void __launch_bounds__(1024) k_sort_small(uint64_t* __restrict__ keys
             __syncthreads();
         }
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = sh[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint64_t k = sh[i];
+        keys[i] = swap_out ? (k << 32) | (k >> 32) : k;
+    }
+}
+
+// The keys of a hash table (slots not equal to `empty`) appended to out in any order,
+// halves swapped when swap; positions from a zeroed counter, those at or past n dropped.
+__global__ void k_table_gather(const uint64_t* __restrict__ slots, uint64_t capacity, uint64_t empty, int swap,
+                               uint64_t* __restrict__ out, uint64_t n, unsigned long long* __restrict__ counter) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < capacity; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        const uint64_t k = i < capacity ? slots[i] : empty;
+        const bool keep = k != empty;
+        const unsigned int m = __ballot_sync(0xffffffffu, keep);
+        if (!m) continue;
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        unsigned long long pos = 0;
+        if (lane == leader) pos = atomicAdd(counter, (unsigned long long)__popc(m));
+        pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(m & ((1u << lane) - 1u));
+        if (keep && pos < n) out[pos] = swap ? (k << 32) | (k >> 32) : k;
+    }
 }
 
 }  // namespace
 
+cudaError_t table_keys_sorted_small(const uint64_t* slots, uint64_t capacity, uint64_t empty, int swap, uint64_t* out,
+                                    uint64_t n, unsigned long long* counter, cudaStream_t s) {
+    if (n > (uint64_t)kSmallSort) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || n == 0) return e;
+    const uint64_t blocks = std::min<uint64_t>((capacity + 255) / 256, 4ull * sm_count());
+    launch(k_table_gather, (unsigned)std::max<uint64_t>(blocks, 1), 256, 0, s, slots, capacity, empty, swap, out, n,
+           counter);
+    launch(k_sort_small, 1, 1024, 0, s, out, (int)n, swap);
+    return cudaGetLastError();
+}
+
 cudaError_t sort_u64_any(uint64_t* keys, size_t n, cudaStream_t s) {
     if (n <= 1) return cudaSuccess;
     if (n <= (size_t)kSmallSort) {
-        launch(k_sort_small, 1, 1024, 0, s, keys, (int)n);
+        launch(k_sort_small, 1, 1024, 0, s, keys, (int)n, 0);
         return cudaGetLastError();
     }
     return radix_sort_u64(keys, nullptr, n, 64, s);

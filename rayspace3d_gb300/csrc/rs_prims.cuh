@@ -22,6 +22,14 @@ cudaError_t sort_error_clear(cudaStream_t s);
 // Full 64-bit ascending sort of keys: a single-block bitonic sort for small inputs,
 // the radix sort otherwise.
 cudaError_t sort_u64_any(uint64_t* keys, size_t n, cudaStream_t s);
+// Largest n of table_keys_sorted_small.
+constexpr uint64_t kSmallTableSort = 4096;
+// The n keys of a hash table (slots not equal to `empty`) into out[0..n), ascending by the
+// key with its halves swapped when swap (and written that way back), else by the key:
+// a gather kernel and a one-block sort, no host wait.  n <= kSmallTableSort; counter is
+// one device word of scratch.
+cudaError_t table_keys_sorted_small(const uint64_t* slots, uint64_t capacity, uint64_t empty, int swap, uint64_t* out,
+                                    uint64_t n, unsigned long long* counter, cudaStream_t s);
 
 // Exclusive prefix sums.  `total` (device, nullable) receives the sum of all inputs.
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* total, cudaStream_t s);

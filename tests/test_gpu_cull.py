@@ -2,6 +2,8 @@
 equal to the oracle's, on contact-heavy inputs (face-sharing and touching cubes, shared
 edges, objects that only touch within the edge payload's quantisation) and on a query that
 exhausts its node budget (one object whose box covers the whole other set)."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -142,4 +144,48 @@ def test_filtered_join_with_an_empty_set(cuda):
         torch.zeros(0, dtype=torch.int32, device="cuda") for _ in range(3))
     ps = api.PairSet(1 << 8)
     api.overlap_join_filtered(da, de, ps, with_containment=True)
+    assert ps.finalize().numel() == 0
+
+
+def test_cull_with_sparse_object_ids(cuda):
+    """Object ids far above the triangle count: the build's object boxes do not cover them,
+    so the broad phase computes the boxes itself; the pairs stay the oracle's."""
+    A, B = synth.overlap_workload(n_objects=150, level=1, world=10.0, seed=31)
+    A2 = synth.make_geometry(A.vertices, A.indices, A.tri2obj * 4001 + 3)
+    B2 = synth.make_geometry(B.vertices, B.indices, B.tri2obj * 7 + 1)
+    assert int(A2.tri2obj.max()) + 1 > len(A2.indices)
+    _check(A2, B2)
+    _check(B2, A2, containment=True)
+
+
+@pytest.mark.parametrize("n_objects, world", [(150, 10.0), (2500, 12.0)])
+def test_finalize_orders_and_count(cuda, n_objects, world):
+    """Both finalize paths (gather + one-block sort up to 4096 keys, radix sort above): the
+    keys ascending as (id1, id2) for order 0 and as (id2, id1) for order 1, the count from the
+    join's own status read, and the same result on a second call."""
+    A, B = synth.overlap_workload(n_objects=n_objects, level=1, world=world, seed=32)
+    want = bind.overlap_join(A, B)
+    ps = api.PairSet(1 << 16)
+    api.overlap_join(api.Bvh(api.DeviceGeometry(A)), api.Bvh(api.DeviceGeometry(B)), ps)
+    assert ps.info()[1] == len(want)
+    k0 = ps.finalize(order=0).cpu().numpy().astype(np.uint64)
+    np.testing.assert_array_equal(k0, want)
+    k1 = ps.finalize(order=1).cpu().numpy().astype(np.uint64)
+    swapped = (k1 << np.uint64(32)) | (k1 >> np.uint64(32))
+    assert np.all(swapped[1:] > swapped[:-1])
+    np.testing.assert_array_equal(np.sort(k1), want)
+    np.testing.assert_array_equal(ps.finalize(order=0).cpu().numpy().astype(np.uint64), want)
+    # through the C ABI with the default wait, and with too small an output buffer
+    L = _lib.load()
+    out = torch.empty(max(len(want), 1), dtype=torch.int64, device="cuda")
+    n = ctypes.c_uint64()
+    assert L.rs_pairset_finalize(ps.handle, 0, out.data_ptr(), len(want), ctypes.byref(n), None) == 0
+    assert n.value == len(want)
+    np.testing.assert_array_equal(out[:n.value].cpu().numpy().astype(np.uint64), want)
+    if len(want) > 1:
+        rc = L.rs_pairset_finalize(ps.handle, 0, out.data_ptr(), len(want) - 1, ctypes.byref(n), None)
+        assert rc == _lib.RS_ERR_OUTPUT_OVERFLOW and n.value == len(want)
+    assert (len(want) <= 4096) == (n_objects == 150)
+    ps.clear()
+    assert ps.info()[1] == 0
     assert ps.finalize().numel() == 0
