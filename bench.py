@@ -238,16 +238,24 @@ def run_engine(args, rank, world, local):
                 prof[name] = {"total_ms": ms.value, "launches": cnt.value, "avg_ms": ms.value / cnt.value}
 
         # End to end through the C ABI with host buffers.
+        # Per set: the triangles (vertices, indices, object ids), the edge payload, the grid.
         host = {}
+
+        def tri_tensors(g):
+            return [g.V, g.I, g.T]
+
         for tag, g in (("A", da), ("B", db)):
-            tensors = [g.V, g.I, g.T] + list(g.edges) + [g.cells]
-            host[tag] = [t.cpu().pin_memory() for t in tensors]
-        h2d = sum(t.numel() * t.element_size() for ts in host.values() for t in ts)
+            host[tag] = {"tri": [t.cpu().pin_memory() for t in tri_tensors(g)],
+                         "edges": [t.cpu().pin_memory() for t in g.edges],
+                         "cells": g.cells.cpu().pin_memory()}
+        h2d = sum(t.numel() * t.element_size() for hs in host.values()
+                  for t in hs["tri"] + hs["edges"] + [hs["cells"]])
         ga2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
         gb2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
         for dst, src in ((ga2, da), (gb2, db)):
             dst.__dict__.update(src.__dict__)
             dst.V, dst.I, dst.T = [torch.empty_like(t) for t in (src.V, src.I, src.T)]
+            dst.clusters = None  # the join builds over all triangles
             dst.edges = tuple(torch.empty_like(t) for t in src.edges)
             dst.cells = torch.empty_like(src.cells)
 
@@ -262,14 +270,14 @@ def run_engine(args, rank, world, local):
             sc.wait_stream(stream)
             with torch.cuda.stream(sc):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
-                    for d, h in zip([dst.V, dst.I, dst.T], host[tag][:3]):
+                    for d, h in zip(tri_tensors(dst), host[tag]["tri"]):
                         d.copy_(h, non_blocking=True)
                     ev[tag].record(sc)
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
-                    dst.cells.copy_(host[tag][-1], non_blocking=True)
+                    dst.cells.copy_(host[tag]["cells"], non_blocking=True)
                 ev["cells"].record(sc)
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
-                    for d, h in zip(dst.edges, host[tag][3:8]):
+                    for d, h in zip(dst.edges, host[tag]["edges"]):
                         d.copy_(h, non_blocking=True)
                     ev["edges" + tag].record(sc)
             sa.wait_event(ev["A"])

@@ -66,6 +66,17 @@ int rs_bvh_destroy(rs_bvh* bvh);
 int rs_bvh_build_async(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
                        const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream);
 int rs_bvh_wait(const rs_bvh* bvh);
+/* The same BVH contract built per cluster (no counterpart in the reference): the triangles
+ * come as n_clusters consecutive ranges, cluster c = [d_cluster_starts[c],
+ * d_cluster_starts[c+1]) (device array of n_clusters + 1 entries, first 0, last nF), each of
+ * 1..512 triangles, normally the runs of one object.  One block builds each cluster's tree
+ * in shared memory and a radix tree over the cluster boxes joins them: no sort over all
+ * triangles.  Query results are those of rs_bvh_build (the tree shape differs).  Cluster
+ * ranges that are empty, longer than 512 or not a partition of [0, nF) make the build fail
+ * with RS_ERR_INVALID.  asynchronous != 0: as rs_bvh_build_async. */
+int rs_bvh_build_clustered(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
+                           const int32_t* d_tri2obj, const uint32_t* d_cluster_starts, uint64_t n_clusters,
+                           int leaf_size, int asynchronous, rs_bvh** out, void* stream);
 /* Number of triangles, nodes, engine-owned device bytes, and the bounds of all vertices. */
 int rs_bvh_info(const rs_bvh* bvh, uint64_t* n_tri, uint64_t* n_nodes, uint64_t* bytes,
                 float* h_min3, float* h_max3);

@@ -37,6 +37,7 @@ SIGNATURES = {
     "rs_status_string": (ctypes.c_char_p, [I]),
     "rs_bvh_build": (I, [P, U64, P, U64, P, I, PP, P]),
     "rs_bvh_build_async": (I, [P, U64, P, U64, P, I, PP, P]),
+    "rs_bvh_build_clustered": (I, [P, U64, P, U64, P, P, U64, I, I, PP, P]),
     "rs_bvh_wait": (I, [P]),
     "rs_bvh_destroy": (I, [P]),
     "rs_bvh_info": (I, [P, PU64, PU64, PU64, P, P]),
