@@ -12,6 +12,8 @@
 #include <algorithm>
 #include <climits>
 
+#include <mutex>
+
 #include "rs_engine.h"
 #include "rs_prims.cuh"
 #include "rs_query_core.cuh"
@@ -96,17 +98,32 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
     if (any) j.live[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
 }
 
-// Edge rays of the live lists of j0 then j1 (grid-stride: the list lengths are only known
-// on the device; a null n_live is an empty list).
-__global__ void __launch_bounds__(kT) k_edge_join_live(EdgeJob j0, EdgeJob j1, PairTable table) {
-    const unsigned int n0 = j0.n_live ? *j0.n_live : 0u, n1 = j1.n_live ? *j1.n_live : 0u;
-    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n0 + n1; k += gridDim.x * blockDim.x) {
-        const bool b = k >= n0;
-        edge_ray<kStack>(b ? j1.starts : j0.starts, b ? j1.ends : j0.ends, b ? j1.offsets : j0.offsets,
-                         b ? j1.counts : j0.counts, b ? j1.sources : j0.sources, b ? j1.live[k - n0] : j0.live[k],
-                         b ? j1.nodes : j0.nodes, b ? j1.max_steps : j0.max_steps, b ? j1.tris : j0.tris,
-                         b ? j1.swap : j0.swap, table);
-    }
+// Edge rays of one live list (grid-stride: the list length is only known on the device).
+__global__ void __launch_bounds__(kT) k_edge_join_live(const float* __restrict__ starts,
+                                                       const float* __restrict__ ends,
+                                                       const int32_t* __restrict__ offsets,
+                                                       const int32_t* __restrict__ counts,
+                                                       const int32_t* __restrict__ sources,
+                                                       const uint32_t* __restrict__ live,
+                                                       const unsigned int* __restrict__ n_live,
+                                                       const BNode* __restrict__ nodes, uint32_t max_steps,
+                                                       const float4* __restrict__ tris, int swap, PairTable table) {
+    const unsigned int n = *n_live;
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        edge_ray<kStack>(starts, ends, offsets, counts, sources, live[j], nodes, max_steps, tris, swap, table);
+}
+
+// A stream per device for the second direction's rays, forked from and joined back into
+// the join's stream.
+cudaStream_t ray_side_stream() {
+    static cudaStream_t st[64] = {};
+    static std::mutex mu;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> g(mu);
+    if (!st[dev] && cudaStreamCreateWithFlags(&st[dev], cudaStreamNonBlocking) != cudaSuccess) st[dev] = nullptr;
+    return st[dev];
 }
 
 __global__ void k_first_tri_init(int32_t* __restrict__ first, uint64_t nObj) {
@@ -465,10 +482,32 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
     if (e == cudaSuccess && total_e) {
         const int ptok = prof_begin(P_EDGE_JOIN, s);
         launch(k_edge_live, (unsigned)(blocks[0] + blocks[1]), 256, 0, s, jobs[0], jobs[1], (unsigned)blocks[0]);
-        launch(k_edge_join_live, (unsigned)std::min<uint64_t>((total_e + kT - 1) / kT, 8ull * sm_count()), kT, 0, s,
-               jobs[0], jobs[1], table_view(ps));
+        // The rays of the second job on a side stream, concurrent with the first's: each
+        // list's rays are latency-bound chains when the lists are short, and a full list
+        // keeps the GPU busy either way.
+        const PairTable table = table_view(ps);
+        cudaStream_t side = n_jobs == 2 ? ray_side_stream() : nullptr;
+        cudaEvent_t fork = nullptr, joined = nullptr;
+        if (side && (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess ||
+                     cudaEventCreateWithFlags(&joined, cudaEventDisableTiming) != cudaSuccess ||
+                     cudaEventRecord(fork, s) != cudaSuccess || cudaStreamWaitEvent(side, fork, 0) != cudaSuccess)) {
+            cudaGetLastError();
+            side = nullptr;  // both on s
+        }
+        for (int d = 0; d < n_jobs; ++d) {
+            const EdgeJob& j = jobs[d];
+            launch(k_edge_join_live, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 8ull * sm_count()), kT, 0,
+                   d == 1 && side ? side : s, j.starts, j.ends, j.offsets, j.counts, j.sources, (const uint32_t*)j.live,
+                   (const unsigned int*)j.n_live, j.nodes, j.max_steps, j.tris, j.swap, table);
+        }
+        if (side) {
+            e = cudaEventRecord(joined, side);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(s, joined, 0);
+        }
+        if (fork) cudaEventDestroy(fork);
+        if (joined) cudaEventDestroy(joined);
         prof_end(P_EDGE_JOIN, s, ptok);
-        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaGetLastError();
     }
     for (int d = 0; d < n_jobs; ++d)
         if (jobs[d].live) cudaFreeAsync(jobs[d].live, s);
