@@ -503,6 +503,7 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
         if (side) {
             e = cudaEventRecord(joined, side);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(s, joined, 0);
+            if (e != cudaSuccess) cudaStreamSynchronize(side);  // the lists are freed on s below
         }
         if (fork) cudaEventDestroy(fork);
         if (joined) cudaEventDestroy(joined);

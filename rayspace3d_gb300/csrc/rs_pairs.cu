@@ -251,9 +251,9 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
         ps->known_count = -1;
         cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
-        // Both directions with their broad phase and no events: one live-edge launch and one
-        // ray launch for both.  Otherwise each direction reads its source edges only after
-        // the caller's event for them.
+        // Both directions with their broad phase and no events: one live-edge launch for both,
+        // and the two directions' rays concurrently.  Otherwise each direction reads its
+        // source edges only after the caller's event for them.
         const bool together = a2b && b2a && !edges_a_ready && !edges_b_ready && cullA.cand && cullB.cand &&
                               nEA <= 0xffffffffull && nEB <= 0xffffffffull;
         if (e == cudaSuccess && together) {
