@@ -22,6 +22,7 @@ to seconds per full join.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import os
 import statistics
@@ -103,17 +104,26 @@ class Clocks:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.f, stderr=subprocess.DEVNULL)
+            atexit.register(self.__exit__, None, None, None)  # never outlive the bench
+            # Sampling is live once the first line is written (nvidia-smi takes a moment to start).
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+                self.f.flush()
+                if os.path.getsize(self.path) > 0:
+                    break
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
     def __exit__(self, *a):
-        if self.proc is not None:
+        if self.proc is not None and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+        if getattr(self, "f", None) is not None and not self.f.closed:
             self.f.close()
 
     def summary(self):
@@ -205,6 +215,10 @@ def run_engine(args, rank, world, local):
             bb.close()
             return keys
 
+        # Clocks are sampled from before the warm-up steps until after the end-to-end steps:
+        # the timed region alone (K joins of about a millisecond) is shorter than the sampling
+        # period.
+        clk = Clocks(local).__enter__()
         for _ in range(args.warmup):
             keys = step(da, db)
         torch.cuda.synchronize()
@@ -218,12 +232,11 @@ def run_engine(args, rank, world, local):
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
-        with Clocks(local) as clk:
-            ev0.record(stream)
-            for _ in range(args.steps):
-                keys = step(da, db)
-            ev1.record(stream)
-            torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            keys = step(da, db)
+        ev1.record(stream)
+        torch.cuda.synchronize()
         launches = L.rs_launch_count() - launches0
         L.rs_profile_enable(0)
         dev_ms = ev0.elapsed_time(ev1) / args.steps
@@ -299,6 +312,7 @@ def run_engine(args, rank, world, local):
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.steps
         d2h = int(out.numel() * out.element_size())
+        clk.__exit__(None, None, None)
 
     # Parity spot check of this run's output against the previous device-resident result.
     assert int(out.numel()) == n_pairs
@@ -353,7 +367,7 @@ def run_engine(args, rank, world, local):
                     for k, v in prof.items()},
         "roofline": roof,
         "roofline_edge_rays": roof_edges,
-        "clocks": clk.summary(),
+        "clocks": dict(clk.summary(), window="warm-up, timed and end-to-end joins"),
     }
     return result, A, B
 
