@@ -362,6 +362,9 @@ def run_engine(args, rank, world, local):
                    "parallelism": f"independent joins per rank x{world}"},
         "e2e": {"value": round(e2e_s, 6), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
+        # The workload's second metric: edge rays of both directions (2 x edges per set) per
+        # second of join; the broad phase traces only the live ones.
+        "edge_rays_mrays_s": round((da.nE + db.nE) / (dev_ms * 1e-3) / 1e6, 1),
         "recheck": rc,
         "kernels": {k: {kk: round(vv, 5) if isinstance(vv, float) else vv for kk, vv in v.items()}
                     for k, v in prof.items()},
