@@ -59,9 +59,8 @@ def cluster_starts(tri2obj: np.ndarray, max_size: int = MAX_CLUSTER) -> Optional
 
 
 class DeviceGeometry:
-    """One .pre geometry set resident on the GPU (vertices, indices, tri2obj, edges, grid,
-    and the cluster starts of the clustered BVH build when every object's triangles are
-    stored together, at most 512 of them)."""
+    """One .pre geometry set resident on the GPU (vertices, indices, tri2obj, edges, grid;
+    the cluster starts of the clustered BVH build on first use)."""
 
     def __init__(self, g: Geometry, device: str = "cuda"):
         self.host = g
@@ -71,8 +70,6 @@ class DeviceGeometry:
         self.T = torch.from_numpy(np.ascontiguousarray(g.tri2obj, np.int32)).to(dev)
         self.nV = int(len(g.vertices))
         self.nF = int(len(g.indices))
-        cs = cluster_starts(g.tri2obj)
-        self.clusters = None if cs is None else torch.from_numpy(cs.view(np.int32)).to(dev)
         self.edges = None
         if g.edges is not None and len(g.edges.starts):
             e = g.edges
@@ -101,8 +98,22 @@ class DeviceGeometry:
         self.edges = tuple(t.contiguous() for t in edges) if edges is not None else None
         self.nE = int(self.edges[0].shape[0]) if self.edges is not None else 0
         self.cells = cells
-        self.clusters = None
+        self._clusters = None
         return self
+
+    @property
+    def clusters(self) -> Optional[torch.Tensor]:
+        """Cluster starts for rs_bvh_build_clustered (uint32 bits in an int32 tensor on the
+        geometry's device), computed from the host object ids on first use; None when the
+        objects are not stored together in runs of at most 512 triangles."""
+        if not hasattr(self, "_clusters"):
+            cs = cluster_starts(self.host.tri2obj) if getattr(self, "host", None) is not None else None
+            self._clusters = None if cs is None else torch.from_numpy(cs.view(np.int32)).to(self.V.device)
+        return self._clusters
+
+    @clusters.setter
+    def clusters(self, value: Optional[torch.Tensor]) -> None:
+        self._clusters = value
 
     def edge_ptrs(self):
         if self.edges is None:

@@ -50,3 +50,23 @@ def test_clock_summary(tmp_path, monkeypatch):
     assert got == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "samples": 3, "reasons": ["sw_power_cap"]}
     c.proc = None
     assert c.summary()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_device_geometry_clusters_on_first_use():
+    """The cluster starts are computed from the host object ids when first asked for, can be
+    overridden (a copy that builds over all triangles), and are absent for wrapped tensors
+    and for objects over 512 triangles (on the CPU device: no GPU needed)."""
+    import torch
+    A, _ = synth.overlap_workload(n_objects=20, level=1, world=50.0, seed=2)
+    g = api.DeviceGeometry(A, device="cpu")
+    assert "_clusters" not in g.__dict__
+    cs = g.clusters
+    assert cs.dtype == torch.int32 and int(cs[-1]) == len(A.indices) and cs.shape[0] == 21
+    copy = api.DeviceGeometry.__new__(api.DeviceGeometry)
+    copy.__dict__.update(g.__dict__)
+    copy.clusters = None
+    assert copy.clusters is None and g.clusters is cs
+    assert api.DeviceGeometry.from_tensors(g.V, g.I, g.T).clusters is None
+    v, f = synth.icosphere(3)
+    big = synth.make_geometry(v.astype(np.float32), f, np.zeros(len(f), np.int32), edges=False)
+    assert api.DeviceGeometry(big, device="cpu").clusters is None
