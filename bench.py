@@ -16,8 +16,11 @@ Secondary (reported in `pim`): point-in-mesh parity of 1,000,000 points uniform 
 `--impl reference` times the reference algorithm on the host cores instead: the
 reference's OptiX build cannot run on this machine (no OptiX SDK, and the GPU has no
 RT cores), so the arm runs the project's CPU port of the same parity / edge-ray tests
-(oracle/) with all host threads on a bounded sample of the same workload, extrapolated
-to seconds per full join.
+(oracle/) with all host threads: each step is one whole join (both CPU BVH builds and
+every edge ray of both directions), timed, with the GPU arm's warm-up and step counts.
+
+Every line carries `parity`: its result compared with the oracle's on the same inputs,
+outside the timed region.
 """
 from __future__ import annotations
 
@@ -371,6 +374,7 @@ def run_engine(args, rank, world, local):
         "roofline": roof,
         "roofline_edge_rays": roof_edges,
         "clocks": dict(clk.summary(), window="warm-up, timed and end-to-end joins"),
+        "_keys": out.numpy().view(np.uint64),
     }
     return result, A, B
 
@@ -390,7 +394,7 @@ def recheck(L, fn):
             "rate_per_test": (ex.value / tests.value) if tests.value else 0.0}
 
 
-def run_pim(args, local, n_points, direction, reps=20, filtered=False):
+def run_pim(args, local, n_points, direction, reps=20, filtered=False, cpu=False):
     """Point-in-mesh on one level-4 icosphere: kernel time (profiler), stream time and
     end-to-end time with the points copied in from pinned host memory.  filtered: the
     filter-refine variant (bounding-box mesh test first, raytracer_filter_refine)."""
@@ -443,7 +447,17 @@ def run_pim(args, local, n_points, direction, reps=20, filtered=False):
     hbm, kind = peaks()
     nbytes = 13 * len(pts) + 12 * dg.nV + 16 * dg.nF
     axis = "xyz"[int(np.argmax(np.abs(direction)))]
-    return {"workload": f"{len(pts)} points uniform in [-1.5,1.5]^3, level-4 icosphere (5120 triangles), "
+    extra = {}
+    if cpu:
+        # Parity of this run's objects against the oracle, and the oracle's own rate on
+        # the host cores over the same points (the CPU baseline).
+        got = obj.cpu().numpy()
+        t_cpu, want = cpu_pim(g, pts, direction, filtered)
+        extra["parity"] = parity_of(got, want, f"object id of all {len(pts)} points")
+        extra["cpu_baseline"] = {"value": round(len(pts) / t_cpu / 1e6, 2), "unit": "Mpts/s", "cores": os.cpu_count(),
+                                 "kind": "port", "sample": f"all {len(pts)} points, one pass"}
+    return {**extra,
+            "workload": f"{len(pts)} points uniform in [-1.5,1.5]^3, level-4 icosphere (5120 triangles), "
                         f"+{axis} rays, seed 0" + (", bounding-box filter then refine" if filtered else ""),
             "mpts_s": round(len(pts) / (ms * 1e-3) / 1e6, 2), "ms": round(ms, 4),
             "kernel_ms": round(kavg, 4), "inside_frac": round(float((obj >= 0).float().mean().item()), 5),
@@ -455,7 +469,7 @@ def run_pim(args, local, n_points, direction, reps=20, filtered=False):
                          "algorithmic_bytes_per_launch": nbytes, "peak_source": kind + " hbm_gbs"}}
 
 
-def run_join_variant(args, world_size, steps=5, filtered=False):
+def run_join_variant(args, world_size, steps=5, filtered=False, cpu=False):
     """The overlap join at another world size (device-resident), pairs and recheck rate.
     filtered: the same join through rs_overlap_join_filtered (object-box filter, BVHs over
     the overlapping objects' triangles only, built inside the call)."""
@@ -493,20 +507,52 @@ def run_join_variant(args, world_size, steps=5, filtered=False):
         for _ in range(3):
             keys, est = step()
         torch.cuda.synchronize()
+        L.rs_profile_reset()
+        L.rs_profile_enable(1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
             keys, est = step()
         e1.record(stream)
         torch.cuda.synchronize()
+        L.rs_profile_enable(0)
         ms = e0.elapsed_time(e1) / steps
+        prof = {}
+        for kid, name in ((0, "edge_rays"), (6, "build_up")):
+            import ctypes
+            kms, cnt = ctypes.c_double(), ctypes.c_uint64()
+            L.rs_profile_read(kid, ctypes.byref(kms), ctypes.byref(cnt))
+            if cnt.value:
+                prof[name] = {"avg_ms": round(kms.value / cnt.value, 5), "launches": cnt.value}
         rc = recheck(L, lambda: (step(), torch.cuda.synchronize()))
     n_pairs = int(keys.numel())
-    return {"workload": f"overlap join: {args.objects} + {args.objects} level-2 icospheres, world {world_size:g}^3, "
-                        f"seed 1, {args.grid}^3 grid" + (", object-filtered BVHs" if filtered else ""),
-            "seconds": round(ms / 1e3, 6), "pairs": n_pairs, "estimated_pairs": int(est),
-            "selectivity": n_pairs / float(args.objects) ** 2,
-            "edge_rays_per_join": int(da.nE + db.nE), "recheck": rc}
+    out = {"workload": f"overlap join: {args.objects} + {args.objects} level-2 icospheres, world {world_size:g}^3, "
+                       f"seed 1, {args.grid}^3 grid" + (", object-filtered BVHs" if filtered else ""),
+           "seconds": round(ms / 1e3, 6), "pairs": n_pairs, "estimated_pairs": int(est),
+           "selectivity": n_pairs / float(args.objects) ** 2,
+           "edge_rays_per_join": int(da.nE + db.nE), "recheck": rc, "kernels": prof}
+    p = prof.get("edge_rays")
+    if p and not filtered:
+        # The edge rays of one join (broad-phase live check, binning, fast and deferred ray
+        # kernels of both directions; one timed interval per join) against the bytes every
+        # edge's ray needs: each direction's source payload and target geometry once, 8 B per
+        # pair.  This is the join's dominant interval at this selectivity.
+        hbm, kind = peaks()
+        nbytes = join_bytes(da, db) + join_bytes(db, da) + 8.0 * n_pairs
+        ach = nbytes / (p["avg_ms"] * 1e-3) / 1e9
+        out["roofline"] = {"bound": "hbm", "kernel": "edge rays of both directions (k_edge_live .. k_edge_long)",
+                           "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 5),
+                           "algorithmic_bytes_per_launch": int(nbytes), "avg_launch_ms": p["avg_ms"],
+                           "peak_source": kind + " hbm_gbs", "traffic": None}
+    if cpu:
+        t_cpu, want = cpu_join(A, B)
+        out["parity"] = parity_of(keys.cpu().numpy().view(np.uint64), key_order1(want),
+                                  "sorted pair list (raytracer_mesh_overlap order)")
+        if not filtered:
+            out["cpu_baseline"] = {"value": round(t_cpu, 4), "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                                   "sample": f"one whole join: {len(A.edges.starts)} + {len(B.edges.starts)} edge rays "
+                                             f"and both CPU BVH builds"}
+    return out
 
 
 def run_batch(args, full: bool):
@@ -861,33 +907,40 @@ def combine_ranks(result: dict, world: int, device) -> dict:
     return result
 
 
-def cpu_join_sample(A, B, frac=0.02, threads=None):
-    """Oracle overlap join on a bounded sample of both edge sets, extrapolated to one
-    full join: 2 x CPU BVH build + (sampled traversal time / frac)."""
+def cpu_join(A, B, threads=None):
+    """One whole oracle overlap join on the host cores, timed: the CPU BVH of each set and
+    every edge ray of both directions (the reference's hit rule).  Returns (seconds, keys)."""
     from oracle import bind
-    from rayspace3d_gb300.formats import Edges
     threads = threads or os.cpu_count()
-
-    def sub(e, f):
-        n = max(1, int(len(e.starts) * f))
-        return Edges(e.starts[:n], e.ends[:n], e.offsets[:n], e.counts[:n], e.sources), n
-
-    ea, na = sub(A.edges, frac)
-    eb, nb = sub(B.edges, frac)
-    empty = Edges(A.edges.starts[:0], A.edges.ends[:0], A.edges.offsets[:0], A.edges.counts[:0], A.edges.sources)
     t0 = time.perf_counter()
-    bind.edge_join(empty, B.vertices, B.indices, B.tri2obj, threads=threads)
-    bind.edge_join(empty, A.vertices, A.indices, A.tri2obj, threads=threads)
-    t_build = time.perf_counter() - t0
+    keys = bind.overlap_join(A, B, threads=threads)
+    return time.perf_counter() - t0, keys
+
+
+def cpu_pim(g, pts, direction, filtered=False, threads=None):
+    """The oracle's point-in-mesh over the points on the host cores, timed (seconds, objects)."""
+    from oracle import bind
+    threads = threads or os.cpu_count()
     t0 = time.perf_counter()
-    bind.edge_join(ea, B.vertices, B.indices, B.tri2obj, threads=threads)
-    bind.edge_join(eb, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads)
-    t_sample = time.perf_counter() - t0
-    t_trav = max(t_sample - t_build, 0.0)
-    full = t_build + t_trav * (len(A.edges.starts) + len(B.edges.starts)) / float(na + nb)
-    return full, {"cores": threads, "sample": f"{na}+{nb} of {len(A.edges.starts)}+{len(B.edges.starts)} edges "
-                                              f"({frac:.0%}) plus both CPU BVH builds, extrapolated to one join",
-                  "sample_seconds": round(t_build + t_sample, 3)}
+    out = bind.pim(g.vertices, g.indices, g.tri2obj, pts, direction=direction, filtered=filtered, threads=threads)
+    return time.perf_counter() - t0, out
+
+
+def key_order1(keys):
+    """Sorted u64 keys (id1 << 32 | id2) reordered by (id2, id1), raytracer_mesh_overlap's order."""
+    keys = np.asarray(keys, dtype=np.uint64)
+    return keys[np.lexsort((keys >> np.uint64(32), keys & np.uint64(0xffffffff)))]
+
+
+def parity_of(got, want, what):
+    got = np.asarray(got)
+    want = np.asarray(want)
+    if got.shape != want.shape:
+        mism = int(abs(len(got) - len(want)) + np.count_nonzero(got[:min(len(got), len(want))] !=
+                                                                want[:min(len(got), len(want))]))
+    else:
+        mism = int(np.count_nonzero(got != want))
+    return {"against": "oracle", "checked": what, "mismatches": mism}
 
 
 def main():
@@ -898,20 +951,20 @@ def main():
         if rank != 0:
             return
         A, B = make_workload(args)
-        vals = []
-        meta = None
-        steps = max(1, min(args.steps, 3))
-        for _ in range(steps):
-            v, meta = cpu_join_sample(A, B, frac=0.01)
-            vals.append(v)
+        threads = os.cpu_count()
+        for _ in range(args.warmup):
+            cpu_join(A, B, threads)
+        vals = [cpu_join(A, B, threads)[0] for _ in range(args.steps)]
         v = statistics.median(vals)
+        sample = (f"whole joins: {len(A.edges.starts)} + {len(B.edges.starts)} edge rays and both CPU BVH builds "
+                  f"per step, median of {args.steps} after {args.warmup} warm-up")
         line = {"impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": world,
-                "steps": steps, "warmup": 0, "ms_per_step": round(v * 1e3, 3), "higher_is_better": False,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v * 1e3, 3),
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded icospheres)",
                 "config": {"workload": WORKLOAD, "objects_per_set": args.objects, "world": args.world},
-                "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": meta["cores"], "kind": "port",
-                                 "sample": meta["sample"]},
+                "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": sample},
                 "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "reference OptiX build unavailable on this box (no OptiX SDK; GB300 has no RT cores); "
                         "CPU port of the same exact tests on all host threads"}
@@ -921,24 +974,32 @@ def main():
         import torch.distributed as dist
         dist.init_process_group(backend="nccl")
     result, A, B = run_engine(args, rank, world, local)
+    cpu = rank == 0 and not args.no_cpu_baseline
     if not args.no_pim:
-        result["pim"] = run_pim(args, local, args.pim_points, (1.0, 0.0, 0.0))
-        result["pim_z"] = run_pim(args, local, args.pim_points, (0.0, 0.0, 1.0))
-        result["pim_filtered"] = run_pim(args, local, args.pim_points, (0.0, 0.0, 1.0), filtered=True)
+        result["pim"] = run_pim(args, local, args.pim_points, (1.0, 0.0, 0.0), cpu=cpu)
+        result["pim_z"] = run_pim(args, local, args.pim_points, (0.0, 0.0, 1.0), cpu=cpu)
+        result["pim_filtered"] = run_pim(args, local, args.pim_points, (0.0, 0.0, 1.0), filtered=True, cpu=cpu)
         if not args.no_variants:
-            result["pim_100m"] = run_pim(args, local, 100_000_000, (1.0, 0.0, 0.0), reps=5)
+            result["pim_100m"] = run_pim(args, local, 100_000_000, (1.0, 0.0, 0.0), reps=5, cpu=cpu)
     if not args.no_variants:
-        result["join_w80"] = run_join_variant(args, 80.7)
-        result["join_filtered"] = run_join_variant(args, args.world, filtered=True)
-        result["join_w80_filtered"] = run_join_variant(args, 80.7, filtered=True)
+        result["join_w80"] = run_join_variant(args, 80.7, cpu=cpu)
+        result["join_filtered"] = run_join_variant(args, args.world, filtered=True, cpu=cpu)
+        result["join_w80_filtered"] = run_join_variant(args, 80.7, filtered=True, cpu=cpu)
         result["batch"] = run_batch(args, args.batch_full)
         result["learned"] = run_learned(args, args.learned_full)
         result["intersection"] = run_intersection(args, args.intersection_n)
         result["prep"] = run_prep(A, cpu=(rank == 0 and not args.no_cpu_baseline))
-    if rank == 0 and not args.no_cpu_baseline:
-        v, meta = cpu_join_sample(A, B, frac=0.01)
-        result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": meta["cores"], "kind": "port",
-                                  "sample": meta["sample"]}
+    if rank == 0:
+        # Parity of the headline join, and its CPU baseline: the oracle's whole join, timed.
+        v, want = cpu_join(A, B)
+        result["parity"] = parity_of(result.pop("_keys"), key_order1(want),
+                                     "sorted pair list of the end-to-end join (raytracer_mesh_overlap order)")
+        if not args.no_cpu_baseline:
+            result["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                      "sample": f"one whole join: {len(A.edges.starts)} + {len(B.edges.starts)} edge "
+                                                f"rays and both CPU BVH builds (not extrapolated)"}
+    else:
+        result.pop("_keys", None)
     if world > 1:
         combine_ranks(result, world, "cuda")
     if rank == 0:

@@ -84,7 +84,9 @@ int rs_bvh_info(const rs_bvh* bvh, uint64_t* n_tri, uint64_t* n_nodes, uint64_t*
 /* Point-in-mesh parity (replaces __raygen__rg, query/src/cuda/raytracing.cu:9-78, launched by
  * RayLauncher::launch, query/src/raytracing/RayLauncher.cpp:44-58).  One ray per point along
  * (dx,dy,dz) (the reference uses +Z); hits are ordered by distance and counted with the
- * reference's advance rule t_min = t + 1e-6.  d_obj[i] = object of the first counted hit
+ * reference's advance rule t_min = t + 1e-6; as in the reference's 10000-iteration loop, a
+ * hit at a t where t + 1e-6 rounds to t (t >= 32) makes the count 10000, and no count
+ * exceeds 10000.  d_obj[i] = object of the first counted hit
  * when the count is odd, else -1 (RayResult.polygon_index); d_inside[i] = count & 1.
  * Either output may be NULL.  d_points: float32[n*3]. */
 int rs_pim(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
@@ -97,16 +99,17 @@ int rs_pim_filtered(const rs_bvh* bvh, const float* d_points, uint64_t n, float 
                     int32_t* d_obj, uint8_t* d_inside, void* stream);
 
 /* Point-in-mesh without any device allocation (no counterpart in the reference).
- * For callers that cannot allocate device memory while they query: code running while
- * another framework captures the stream into a CUDA graph, services whose allocator has
- * reserved the whole GPU, or loops that cannot afford an allocation's implicit
- * synchronisation.  Same results as rs_pim / rs_pim_filtered (filtered != 0).  Per-call
+ * For callers that cannot allocate device memory while they query: services whose own
+ * allocator has reserved the whole GPU (a memory pool sized to the device leaves nothing
+ * for cudaMalloc or a second pool), and hosts with a fixed device-memory budget checked
+ * per request.  Same results as rs_pim / rs_pim_filtered (filtered != 0).  Per-call
  * scratch comes from a fixed 4 MiB array inside the library that every GPU which loads
  * it holds until the process exits; n above 1,048,576 points returns RS_ERR_TOO_LARGE.
  * The first call on a device looks the array up (cudaGetSymbolAddress); make that first
- * call before any stream capture.  All calls share the one array, so calls whose work
- * overlaps on the GPU (other streams or threads) race: serialise them.  It uses an
- * axis-aligned column grid only if an earlier rs_pim built it, never building one. */
+ * call before any stream capture.  The call waits for `stream` and returns once the
+ * results are written.  All calls share the one array, so calls whose work overlaps on
+ * the GPU (other streams or threads) race: serialise them.  It uses an axis-aligned
+ * column grid only if an earlier rs_pim built it, never building one. */
 int rs_pim_noalloc(const rs_bvh* bvh, const float* d_points, uint64_t n, float dx, float dy, float dz,
                    int32_t* d_obj, uint8_t* d_inside, int filtered, void* stream);
 
@@ -130,8 +133,9 @@ int rs_pairset_info(const rs_pairset* ps, uint64_t* capacity, uint64_t* count, v
 /* Edge-ray overlap of one direction (replaces __raygen__mesh_overlap_edges,
  * query/src/cuda/mesh_overlap_edges.cu:183-216, and __raygen__mesh_overlap,
  * mesh_intersection.cu:288-334).  Each unique source edge is traced as the segment
- * t in [1e-6, |e-s| + 1e-6] along normalize(e-s) against `target`; every crossed target
- * object o and every source object k of the edge insert (k,o), or (o,k) when swap != 0.
+ * t in [1e-6, |e-s| + 1e-6] along normalize(e-s) against `target`; the target object o of
+ * every crossing the table's hit rule takes (rs_pairset_set_edge_rule) and every source
+ * object k of the edge insert (k,o), or (o,k) when swap != 0.
  * Edge arrays are the .pre v2 edge payload on the device (float32[nE*3] starts/ends,
  * int32 offsets/counts[nE], int32 sources[]). */
 int rs_edge_join(const rs_bvh* target, const float* d_starts, const float* d_ends,
@@ -161,11 +165,23 @@ int rs_containment_tracked(const rs_bvh* target, const float* d_src_vertices, ui
 
 /* Query counters of a table (mesh_overlap_edges.cu:83-96 hash contention tracking and the
  * profiling counters of mesh_intersection.h:7-22), collected while tracking is on:
- * [0] slot accesses, [1] contended probes, [2] edge rays traced, [3] edge-ray crossings,
- * [4] containment rays, [5] containment crossings, [6] distinct containment targets, [7] 0.
- * Counters reset with rs_pairset_clear. */
+ * [0] slot accesses, [1] contended probes, [2] edge rays traced, [3] edge-ray hits taken
+ * (overlap_hits_total), [4] containment rays, [5] containment crossings, [6] distinct
+ * containment targets, [7] 0.  Counters reset with rs_pairset_clear. */
 int rs_pairset_set_tracking(rs_pairset* ps, int on);
 int rs_pairset_counters(const rs_pairset* ps, uint64_t* h_out8, void* stream);
+
+/* Hit rule of the edge rays inserting into this table (the iteration cap and t_min step of
+ * the reference's edge loops).  Each edge's crossings are taken in (distance, triangle id)
+ * order as repeated closest-hit traces would return them: the first at t >= 1e-6, each next
+ * at t >= the previous t + 1e-6 (t + 2e-4 when that float sum does not exceed t), at most
+ * max_hits of them (max_hits <= 0 means 100); crossings skipped by the step, or beyond the
+ * cap, add no pair.  Default (100, 0): trace_edge_multi_hits_edges of raytracer_mesh_overlap
+ * and the estimated joins (query/src/cuda/mesh_overlap_edges.cu:106-178), with max_hits =
+ * --overlap-max-iterations for raytracer_intersection_estimated (mesh_intersection.cu:16-91).
+ * next_float != 0: the next t_min is the next float after t, the rule of raytracer_containment's
+ * edge check (mesh_containment.cu:99-170, used there with max_hits = 256). */
+int rs_pairset_set_edge_rule(rs_pairset* ps, int max_hits, int next_float);
 
 /* Sorted unique keys of a table (replaces compact_hash_table_pairs + the sort/unique of
  * merge_and_deduplicate_pairs_gpu, query/src/cuda/mesh_query_deduplication.cu:56-144).
@@ -190,6 +206,13 @@ int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, uint64_t ca
  * {avgSizeA, avgVolRatioA, avgSizeB, avgVolRatioB} as the reference host code computes them. */
 int rs_estimate_grid(const void* d_cellsA, const void* d_cellsB, uint64_t ncells, float cell_volume,
                      float epsilon, float gamma, double* h_raw, float* h_means4, void* stream);
+
+/* The per-cell estimates that rs_estimate_grid sums (estimateSelectivityKernel's result
+ * buffer, query/src/cuda/estimated_overlap.cu:8-41): d_values[i] =
+ * TA*TB*min(1, (SA+SB+eps)^3/cellVolume * sqrt(RA*RB)^gamma), 0 where either TouchCount is 0,
+ * in the reference kernel's float operation order.  d_values: float32[ncells] on the device. */
+int rs_estimate_grid_cells(const void* d_cellsA, const void* d_cellsB, uint64_t ncells, float cell_volume,
+                           float epsilon, float gamma, float* d_values, void* stream);
 
 /* Estimated pairs from the raw sum, as raytracer_overlap_estimated_main.cpp:275-291 does:
  * alpha = max(1, ((sA*cbrt(rA)) + (sB*cbrt(rB)))^3 / cellVolume), est = (int64)((float)raw/alpha);
@@ -340,6 +363,16 @@ int rs_mlp_gradients(rs_mlp* mlp, const float* d_X, const float* d_target, int B
 /* One Adam step (beta 0.9/0.999, eps 1e-8) on a minibatch. */
 int rs_mlp_train_step(rs_mlp* mlp, const float* d_X, const float* d_target, int B, float lr, float* h_loss,
                       void* stream);
+/* GEMM path of the MLP: 0 (default) runs the products whose operands are both K-major -- the
+ * forward pass -- on the tcgen05 tensor cores (TMA-fed shared memory, tensor-memory
+ * accumulators) and the rest on mma.sync tiles; 1 runs every product on mma.sync.  Calls
+ * return RS_ERR_ITER_LIMIT if a tcgen05 kernel's bounded wait ran out. */
+int rs_mlp_set_gemm(int mode);
+/* The MLP's GEMM alone: C[m][n] = sum_k A[m][k] B[n][k] (BF16 row-major A [M][lda], B [N][ldb],
+ * FP32 C [M][ldc], all on the device); mode 0 tcgen05 (RS_ERR_INVALID unless N % 256 == 0,
+ * K % 64 == 0, 16-byte aligned operands and lda, ldb multiples of 8), mode 1 mma.sync. */
+int rs_mlp_gemm(const void* d_A, int lda, const void* d_B, int ldb, float* d_C, int ldc, int M, int N, int K,
+                int mode, void* stream);
 /* Estimated pair count of two grids (expm1 of the prediction, rounded; h_log1p nullable). */
 int rs_estimate_mlp(rs_mlp* mlp, const void* d_cellsA, const void* d_cellsB, int resolution, int64_t* h_estimate,
                     double* h_log1p, void* stream);
@@ -350,6 +383,9 @@ int rs_estimate_mlp(rs_mlp* mlp, const void* d_cellsA, const void* d_cellsB, int
  * 2 point-in-mesh, 3 BVH build (whole), 4 pair finalisation, 5 estimator, 6 the build's
  * bottom-up tree kernel alone, 7 the learned estimator's GEMMs (with their split-K sums). */
 uint64_t rs_launch_count(void);
+/* Device allocations the library has requested from its stream-ordered memory pool since
+ * it was loaded (diagnostics; no counterpart in the reference). */
+uint64_t rs_alloc_count(void);
 int rs_profile_enable(int on);
 int rs_profile_reset(void);
 int rs_profile_read(int kernel, double* total_ms, uint64_t* launches);
@@ -383,15 +419,31 @@ int compact_hash_table_pairs(const unsigned long long* d_hash_table, unsigned lo
 int count_hits_gpu(const void* d_results, int num_results);
 void compact_hits_gpu(const void* d_input, void* d_output, int num_results, int* h_num_hits);
 
-/* query/src/cuda/estimated_overlap.h:6-13 and estimated_intersection.h: host GridCell arrays,
- * returns the raw float estimate (-1.0f if device memory cannot be allocated). */
-float estimateOverlapSelectivity(const void* h_gridA, const void* h_gridB, int numCells, float cellVolume,
-                                 float epsilon, float gamma);
-float estimateIntersectionSelectivity(const void* h_gridA, const void* h_gridB, int numCells, float cellVolume,
+/* The estimators of query/src/cuda/estimated_overlap.h:6-13 and estimated_intersection.h:6-13
+ * with C linkage (no counterpart in the reference, for C and FFI callers): host GridCell
+ * arrays (16 B records), returns the raw estimate (-1.0f if device memory cannot be
+ * allocated).  The raw sum is accumulated in double in a fixed order and rounded to float
+ * once; the reference's thrust::reduce sums the per-cell floats in float in its own order,
+ * so the two can differ in the last bits of the float. */
+float rs_estimate_overlap_selectivity(const void* h_gridA, const void* h_gridB, int numCells, float cellVolume,
                                       float epsilon, float gamma);
+float rs_estimate_intersection_selectivity(const void* h_gridA, const void* h_gridB, int numCells,
+                                           float cellVolume, float epsilon, float gamma);
 
 #ifdef __cplusplus
 }
+
+/* The same two estimators with the reference's exact C++ declarations
+ * (query/src/cuda/estimated_overlap.h:6-13, estimated_intersection.h:6-13; GridCell as
+ * common/include/GridCell.h:5-10 defines it), so the reference's mains
+ * (raytracer_overlap_estimated_main.cpp:266, raytracer_overlap_direct_estimation_main.cpp:384)
+ * link against this library unchanged.  Include either this header or the reference's
+ * estimated_*.h in one translation unit, not both (both give default arguments). */
+struct GridCell;
+float estimateOverlapSelectivity(const GridCell* h_gridA, const GridCell* h_gridB, int numCells, float cellVolume,
+                                 float epsilon = 0.001f, float gamma = 0.8f);
+float estimateIntersectionSelectivity(const GridCell* h_gridA, const GridCell* h_gridB, int numCells,
+                                      float cellVolume, float epsilon = 0.001f, float gamma = 0.8f);
 #endif
 
 #endif /* RAYSPACE3D_H */

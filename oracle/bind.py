@@ -44,7 +44,7 @@ def lib():
         L.orc_pim.argtypes = [P, U64, P, U64, P, P, U64, F, F, F, P, I, I]
         L.orc_pim_filtered.argtypes = L.orc_pim.argtypes
         L.orc_edge_join.argtypes = [P, P, P, P, P, U64, P, U64, P, U64, P, I,
-                                    ctypes.POINTER(ctypes.POINTER(U64)), ctypes.POINTER(U64), I, I]
+                                    ctypes.POINTER(ctypes.POINTER(U64)), ctypes.POINTER(U64), I, I, I, I]
         L.orc_containment.argtypes = [P, U64, P, U64, P, P, U64, P, U64, P, I,
                                       ctypes.POINTER(ctypes.POINTER(U64)), ctypes.POINTER(U64), I, I]
         L.orc_containment_diag.argtypes = [P, U64, P, U64, P, P, U64, P, U64, P, P, U64,
@@ -57,6 +57,7 @@ def lib():
         L.orc_orient.argtypes = [P, P, P, P]
         L.orc_perturbed_sign.argtypes = [P, P, P, P]
         L.orc_free.argtypes = [P]
+        L.orc_segment_hits.argtypes = [P, P, P, U64, P, U64, P, P, P, U64, ctypes.POINTER(U64)]
         L.orc_box_mesh.argtypes = [P, U64, P, P]
         PF, PI = ctypes.POINTER(ctypes.POINTER(F)), ctypes.POINTER(ctypes.POINTER(ctypes.c_int32))
         L.orc_extract_edges.argtypes = [P, U64, P, U64, P, PF, PF, PI, PI, PI, ctypes.POINTER(U64),
@@ -91,16 +92,31 @@ def _take_keys(kp, nk):
     return out
 
 
-def edge_join(edges, V, I, T, swap=False, threads=None, use_bvh=True):
-    """Sorted unique pair keys (id1<<32|id2) of one edge-ray direction."""
+def edge_join(edges, V, I, T, swap=False, threads=None, use_bvh=True, max_hits=100, next_float=False):
+    """Sorted unique pair keys (id1<<32|id2) of one edge-ray direction, each edge's crossings
+    taken by the reference's edge loop (at most max_hits; t_min + 1e-6, or the next float)."""
     s, e = _c(edges.starts, np.float32), _c(edges.ends, np.float32)
     off, cnt, src = _c(edges.offsets, np.int32), _c(edges.counts, np.int32), _c(edges.sources, np.int32)
     V, I, T = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32)
     kp = ctypes.POINTER(ctypes.c_uint64)()
     nk = ctypes.c_uint64()
     lib().orc_edge_join(_p(s), _p(e), _p(off), _p(cnt), _p(src), len(s), _p(V), len(V), _p(I), len(I), _p(T),
-                        int(swap), ctypes.byref(kp), ctypes.byref(nk), threads or os.cpu_count(), int(use_bvh))
+                        int(swap), ctypes.byref(kp), ctypes.byref(nk), threads or os.cpu_count(), int(use_bvh),
+                        int(max_hits), int(next_float))
     return _take_keys(kp, nk)
+
+
+def segment_hits(start, end, V, I, T, cap=4096):
+    """(t float32[], triangle uint64[]) of every crossing of one segment, unsorted."""
+    st, en = _c(start, np.float32), _c(end, np.float32)
+    V, I, T = _c(V, np.float32), _c(I, np.uint32), _c(T, np.int32)
+    t = np.zeros(cap, np.float32)
+    tri = np.zeros(cap, np.uint64)
+    n = ctypes.c_uint64()
+    lib().orc_segment_hits(_p(st), _p(en), _p(V), len(V), _p(I), len(I), _p(T), _p(t), _p(tri), cap, ctypes.byref(n))
+    k = int(n.value)
+    assert k <= cap, "more crossings than cap"
+    return t[:k], tri[:k]
 
 
 def containment(src_geom, V, I, T, swap=False, threads=None, use_bvh=True):
@@ -132,16 +148,18 @@ def containment_diag(src_geom, V, I, T, threads=None):
     return cand[:n_obj], _take_keys(kp, nk), hits
 
 
-def overlap_join(A, B, threads=None, use_bvh=True):
+def overlap_join(A, B, threads=None, use_bvh=True, max_hits=100, next_float=False):
     """Union of both edge directions: A-edges into B, B-edges into A (swapped)."""
-    k1 = edge_join(A.edges, B.vertices, B.indices, B.tri2obj, swap=False, threads=threads, use_bvh=use_bvh)
-    k2 = edge_join(B.edges, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh)
+    k1 = edge_join(A.edges, B.vertices, B.indices, B.tri2obj, swap=False, threads=threads, use_bvh=use_bvh,
+                   max_hits=max_hits, next_float=next_float)
+    k2 = edge_join(B.edges, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh,
+                   max_hits=max_hits, next_float=next_float)
     return np.union1d(k1, k2).astype(np.uint64)
 
 
-def intersection_join(A, B, threads=None, use_bvh=True):
+def intersection_join(A, B, threads=None, use_bvh=True, max_hits=100):
     """Overlap of both directions plus containment of both directions (sorted unique)."""
-    parts = [overlap_join(A, B, threads, use_bvh),
+    parts = [overlap_join(A, B, threads, use_bvh, max_hits=max_hits),
              containment(A, B.vertices, B.indices, B.tri2obj, swap=False, threads=threads, use_bvh=use_bvh),
              containment(B, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh)]
     return np.unique(np.concatenate(parts)).astype(np.uint64)
@@ -186,7 +204,7 @@ def box_mesh(V):
 def containment_strict(A, B, threads=None, use_bvh=True):
     """raytracer_containment: B objects inside A objects (B->A containment rays, as (a, b))
     whose pair is not an overlap pair.  Returns (strict containment keys, overlap keys)."""
-    overlap = overlap_join(A, B, threads, use_bvh)
+    overlap = overlap_join(A, B, threads, use_bvh, max_hits=256, next_float=True)  # mesh_containment.cu:99-170
     inside = containment(B, A.vertices, A.indices, A.tri2obj, swap=True, threads=threads, use_bvh=use_bvh)
     return np.setdiff1d(inside, overlap).astype(np.uint64), overlap
 

@@ -487,29 +487,60 @@ static void parallel_for(uint64_t n, int nthreads, F fn) {
     for (auto& th : pool) th.join();
 }
 
-// Point-in-mesh parity: hits sorted by (t, triangle id), counted greedily with
-// the reference's advance rule t_min = t + 1e-6 (raytracing.cu:23-60); a
-// threshold that fails to advance moves to the next float instead of
-// re-counting the same hit.
-static int32_t pim_one(const Mesh& m, const CpuBvh* bvh, const float p[3], const float d[3], std::vector<Hit>& hits) {
-    const float eps = 1e-6f, tmax = 1e16f;
-    Ray r = make_ray(p, d, eps, tmax);
-    collect_hits(m, bvh, r, hits);
+static void sort_hits(std::vector<Hit>& hits) {
     std::sort(hits.begin(), hits.end(), [](const Hit& x, const Hit& y) {
         return x.t < y.t || (x.t == y.t && x.tri < y.tri);
     });
+}
+
+// Point-in-mesh parity (raytracing.cu:22-77): the loop traces from t_min + 1e-6, counts
+// the closest hit and sets t_min = t, at most 10000 times.  On the hits sorted by
+// (t, triangle id) that is a greedy walk.  When t + 1e-6 rounds back to t, every
+// remaining trace finds that hit again, so the count ends at the cap (10000).
+static int32_t pim_one(const Mesh& m, const CpuBvh* bvh, const float p[3], const float d[3], std::vector<Hit>& hits) {
+    const float eps = 1e-6f, tmax = 1e16f;
+    const uint64_t max_iters = 10000;
+    Ray r = make_ray(p, d, eps, tmax);
+    collect_hits(m, bvh, r, hits);
+    sort_hits(hits);
     float thr = eps;
     uint64_t count = 0, first = 0;
     for (const Hit& h : hits) {
+        if (count == max_iters) break;
         if (h.t >= thr && h.t < tmax) {
             if (count == 0) first = h.tri;
             ++count;
-            float nt = h.t + eps;
-            if (!(nt > h.t)) nt = std::nextafter(h.t, INFINITY);
+            const float nt = h.t + eps;
+            if (!(nt > h.t)) count = max_iters;
             thr = nt;
         }
     }
     return (count & 1) ? m.t2o[first] : -1;
+}
+
+// Edge-ray hit sequence of trace_edge_multi_hits_edges (mesh_overlap_edges.cu:106-178;
+// the same loop in mesh_intersection.cu:16-91 and mesh_overlap.cu:13-70): closest-hit
+// traces over [t_min, len + 1e-6], t_min = 1e-6 first and t + 1e-6 after a hit at t
+// (t + 2e-4 when the float sum does not exceed t), at most max_hits traces.  next_float:
+// the edge check of mesh_containment.cu:99-170, where t_min moves to the next float after
+// t.  Takes the sorted hits the traces would return; a step that cannot advance ends the
+// walk (the remaining traces return the same hit).
+static void edge_walk(const std::vector<Hit>& sorted, int max_hits, int next_float, std::vector<uint64_t>& taken) {
+    taken.clear();
+    float thr = 1e-6f;
+    for (const Hit& h : sorted) {
+        if ((int)taken.size() >= max_hits) break;
+        if (!(h.t >= thr)) continue;
+        taken.push_back(h.tri);
+        if (next_float) {
+            thr = std::nextafter(h.t, INFINITY);
+        } else {
+            float nt = h.t + 1e-6f;
+            if (!(nt > h.t)) nt = h.t + 2e-4f;
+            if (!(nt > h.t)) break;
+            thr = nt;
+        }
+    }
 }
 
 static void box_mesh(const Mesh& m, std::vector<float>& bv, std::vector<uint32_t>& bi, std::vector<int32_t>& bo) {
@@ -583,7 +614,9 @@ int orc_pim_filtered(const float* V, uint64_t nV, const uint32_t* I, uint64_t nF
 int orc_edge_join(const float* starts, const float* ends, const int32_t* offsets, const int32_t* counts,
                   const int32_t* sources, uint64_t nE,
                   const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* tri2obj,
-                  int swap, uint64_t** keys, uint64_t* nkeys, int nthreads, int use_bvh) {
+                  int swap, uint64_t** keys, uint64_t* nkeys, int nthreads, int use_bvh, int max_hits,
+                  int next_float) {
+    if (max_hits <= 0) max_hits = 100;  // mesh_intersection.cu:25-28
     Mesh m{V, nV, I, nF, tri2obj};
     CpuBvh bvh;
     if (use_bvh) build_bvh(m, bvh);
@@ -591,7 +624,7 @@ int orc_edge_join(const float* starts, const float* ends, const int32_t* offsets
     std::vector<uint64_t> all;
     std::mutex mu;
     parallel_for(nE, nt, [&](uint64_t b, uint64_t e) {
-        std::vector<uint64_t> mine;
+        std::vector<uint64_t> mine, taken;
         std::vector<Hit> hits;
         for (uint64_t i = b; i < e; ++i) {
             const float* s = starts + 3 * i;
@@ -603,8 +636,10 @@ int orc_edge_join(const float* starts, const float* ends, const int32_t* offsets
             const float d[3] = {dxe / len, dye / len, dze / len};
             Ray r = make_ray(s, d, 1e-6f, len + 1e-6f);
             collect_hits(m, use_bvh ? &bvh : nullptr, r, hits);
-            for (const Hit& h : hits) {
-                uint32_t tgt = (uint32_t)m.t2o[h.tri];
+            sort_hits(hits);
+            edge_walk(hits, max_hits, next_float, taken);
+            for (uint64_t tri : taken) {
+                uint32_t tgt = (uint32_t)m.t2o[tri];
                 for (int32_t k = 0; k < counts[i]; ++k) {
                     uint32_t src = (uint32_t)sources[offsets[i] + k];
                     uint64_t key = swap ? (((uint64_t)tgt << 32) | src) : (((uint64_t)src << 32) | tgt);
@@ -622,6 +657,29 @@ int orc_edge_join(const float* starts, const float* ends, const int32_t* offsets
     *nkeys = all.size();
     *keys = (uint64_t*)std::malloc(sizeof(uint64_t) * (all.size() ? all.size() : 1));
     if (!all.empty()) std::memcpy(*keys, all.data(), sizeof(uint64_t) * all.size());
+    return 0;
+}
+
+// Every crossing of the segment start -> end with t in [1e-6, len + 1e-6], testing every
+// triangle (no BVH), unsorted: the hits a trace of mesh_overlap_edges.cu:135-145 chooses
+// from.  Writes up to cap of them; *n receives the total.
+int orc_segment_hits(const float* start, const float* end, const float* V, uint64_t nV, const uint32_t* I,
+                     uint64_t nF, const int32_t* tri2obj, float* out_t, uint64_t* out_tri, uint64_t cap,
+                     uint64_t* n) {
+    Mesh m{V, nV, I, nF, tri2obj};
+    float dxe = end[0] - start[0], dye = end[1] - start[1], dze = end[2] - start[2];
+    float len = std::sqrt((dxe * dxe + dye * dye) + dze * dze);
+    *n = 0;
+    if (len < 1e-6f) return 0;
+    const float d[3] = {dxe / len, dye / len, dze / len};
+    Ray r = make_ray(start, d, 1e-6f, len + 1e-6f);
+    std::vector<Hit> hits;
+    collect_hits(m, nullptr, r, hits);
+    *n = hits.size();
+    for (uint64_t k = 0; k < hits.size() && k < cap; ++k) {
+        out_t[k] = hits[k].t;
+        out_tri[k] = hits[k].tri;
+    }
     return 0;
 }
 

@@ -43,12 +43,21 @@ int orc_pim_filtered(const float* V, uint64_t nV, const uint32_t* I, uint64_t nF
                      int32_t* out_obj, int nthreads, int use_bvh);
 
 /* Edge-ray overlap of one direction: the edges of the source set against the
- * triangles of the target set.  Returns sorted unique keys (id1<<32 | id2) in a
- * malloc'd buffer (*keys, *nkeys); free with orc_free.  swap=1 emits (target,source). */
+ * triangles of the target set, each edge's crossings taken by the reference's edge loop
+ * (at most max_hits, <= 0 meaning 100; t_min stepped by 1e-6, or to the next float when
+ * next_float).  Returns sorted unique keys (id1<<32 | id2) in a malloc'd buffer (*keys,
+ * *nkeys); free with orc_free.  swap=1 emits (target,source). */
 int orc_edge_join(const float* starts, const float* ends, const int32_t* offsets, const int32_t* counts,
                   const int32_t* sources, uint64_t nE,
                   const float* V, uint64_t nV, const uint32_t* I, uint64_t nF, const int32_t* tri2obj,
-                  int swap, uint64_t** keys, uint64_t* nkeys, int nthreads, int use_bvh);
+                  int swap, uint64_t** keys, uint64_t* nkeys, int nthreads, int use_bvh, int max_hits,
+                  int next_float);
+
+/* Every crossing of the segment start -> end with t in [1e-6, len + 1e-6] (all triangles
+ * tested, unsorted): up to cap (t, triangle) pairs; *n receives the total. */
+int orc_segment_hits(const float* start, const float* end, const float* V, uint64_t nV, const uint32_t* I,
+                     uint64_t nF, const int32_t* tri2obj, float* out_t, uint64_t* out_tri, uint64_t cap,
+                     uint64_t* n);
 
 /* Containment fallback of one direction: one +Z ray per source object from the
  * first vertex of its lowest-index triangle, parity per target object. */

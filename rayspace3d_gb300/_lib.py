@@ -54,8 +54,10 @@ SIGNATURES = {
     "rs_pairset_finalize": (I, [P, I, P, U64, PU64, P]),
     "rs_containment_tracked": (I, [P, P, U64, P, U64, P, I, P, I, P, P, P, U64, P]),
     "rs_pairset_set_tracking": (I, [P, I]),
+    "rs_pairset_set_edge_rule": (I, [P, I, I]),
     "rs_pairset_counters": (I, [P, PU64, P]),
     "rs_estimate_grid": (I, [P, P, U64, F, F, F, ctypes.POINTER(ctypes.c_double), P, P]),
+    "rs_estimate_grid_cells": (I, [P, P, U64, F, F, F, P, P]),
     "rs_estimate_pairs_from_raw": (I64, [ctypes.c_double, P, F, I]),
     "rs_hash_size_pow2": (U64, [I64]),
     "rs_hash_size_odd": (U64, [I64, F]),
@@ -64,6 +66,7 @@ SIGNATURES = {
     "rs_overlap_join_filtered": (I, [P, U64, P, U64, P, P, P, P, P, P, U64, P, U64, P, U64, P, P, P, P, P, P, U64,
                                      I, I, I, P, P]),
     "rs_launch_count": (U64, []),
+    "rs_alloc_count": (U64, []),
     "rs_profile_enable": (I, [I]),
     "rs_profile_reset": (I, []),
     "rs_profile_read": (I, [I, ctypes.POINTER(ctypes.c_double), PU64]),
@@ -78,6 +81,8 @@ SIGNATURES = {
     "rs_mlp_get_params": (I, [P, ctypes.POINTER(F), ctypes.POINTER(F)]),
     "rs_mlp_set_params": (I, [P, ctypes.POINTER(F)]),
     "rs_mlp_features": (I, [P, P, I, P, P]),
+    "rs_mlp_gemm": (I, [P, I, P, I, P, I, I, I, I, I, P]),
+    "rs_mlp_set_gemm": (I, [I]),
     "rs_mlp_forward": (I, [P, P, I, P, P]),
     "rs_mlp_gradients": (I, [P, P, P, I, ctypes.POINTER(F), P]),
     "rs_mlp_train_step": (I, [P, P, P, I, F, ctypes.POINTER(F), P]),
@@ -98,8 +103,8 @@ SIGNATURES = {
     "compact_hash_table_pairs": (I, [P, ctypes.c_ulonglong, P, I]),
     "count_hits_gpu": (I, [P, I]),
     "compact_hits_gpu": (None, [P, P, I, ctypes.POINTER(ctypes.c_int)]),
-    "estimateOverlapSelectivity": (F, [P, P, I, F, F, F]),
-    "estimateIntersectionSelectivity": (F, [P, P, I, F, F, F]),
+    "rs_estimate_overlap_selectivity": (F, [P, P, I, F, F, F]),
+    "rs_estimate_intersection_selectivity": (F, [P, P, I, F, F, F]),
 }
 
 _lib = None

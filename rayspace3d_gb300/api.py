@@ -120,6 +120,12 @@ class DeviceGeometry:
             raise ValueError("geometry has no precomputed edge payload")
         return [t.data_ptr() for t in self.edges]
 
+    def host_tri2obj(self) -> np.ndarray:
+        """The object id of every triangle on the host."""
+        if getattr(self, "host", None) is not None:
+            return np.asarray(self.host.tri2obj)
+        return self.T.cpu().numpy()
+
 
 class Bvh:
     """Engine-owned BVH over a DeviceGeometry (which must stay alive)."""
@@ -228,6 +234,13 @@ class PairSet:
     def clear(self, stream=None):
         _check(_lib.load().rs_pairset_clear(self.handle, _stream(stream)), "rs_pairset_clear")
 
+    def set_edge_rule(self, max_hits: int = 100, next_float: bool = False):
+        """Hit rule of the edge rays inserting into this table (rs_pairset_set_edge_rule):
+        at most max_hits crossings per edge, the next searched from t + 1e-6, or from the
+        next float after t when next_float."""
+        _check(_lib.load().rs_pairset_set_edge_rule(self.handle, int(max_hits), int(next_float)),
+               "rs_pairset_set_edge_rule")
+
     def info(self, stream=None):
         cap, cnt = ctypes.c_uint64(), ctypes.c_uint64()
         _check(_lib.load().rs_pairset_info(self.handle, ctypes.byref(cap), ctypes.byref(cnt), _stream(stream)),
@@ -292,6 +305,29 @@ def overlap_join(A: Bvh, B: Bvh, ps: PairSet, direction: int = 0, with_containme
     _check(L.rs_overlap_join_after(A.handle, *ea, A.geom.nE, B.handle, *eb, B.geom.nE, int(direction),
                                    int(with_containment), ps.handle, evs[0], evs[1], _stream(stream)),
            "rs_overlap_join_after")
+
+
+def overlap_join_edges(A: Bvh, edges_a, B: Bvh, edges_b, ps: PairSet, stream=None) -> None:
+    """rs_overlap_join (both directions, broad phase, table growth) with explicit edge
+    payloads: edges_a = (starts, ends, offsets, counts, sources) device tensors of edges of
+    A's objects -- any contiguous range of A's payload, its sources array whole -- traced
+    against B, and edges_b likewise against A."""
+    def ptrs(e):
+        return [t.data_ptr() for t in e], int(e[0].shape[0])
+    pa, na = ptrs(edges_a)
+    pb, nb = ptrs(edges_b)
+    _check(_lib.load().rs_overlap_join(A.handle, *pa, na, B.handle, *pb, nb, 0, 0, ps.handle, _stream(stream)),
+           "rs_overlap_join")
+
+
+def containment_range(target: Bvh, source: DeviceGeometry, tri_lo: int, tri_hi: int, ps: PairSet,
+                      swap: bool = False, stream=None) -> None:
+    """Containment rays of the source objects whose triangles are [tri_lo, tri_hi) (each
+    object's triangles stored together, all of them inside the range)."""
+    I = source.I[tri_lo:tri_hi]
+    T = source.T[tri_lo:tri_hi]
+    _check(_lib.load().rs_containment(target.handle, _ptr(source.V), source.nV, _ptr(I), int(tri_hi - tri_lo),
+                                      _ptr(T), int(swap), ps.handle, _stream(stream)), "rs_containment")
 
 
 def overlap_join_filtered(A: DeviceGeometry, B: DeviceGeometry, ps: PairSet, direction: int = 0,

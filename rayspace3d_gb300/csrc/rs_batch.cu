@@ -8,8 +8,9 @@
 // counter and trace its rays with the same per-ray bodies as the single-query kernels
 // (rs_query_core.cuh), so queries of very uneven sizes share the GPU without a launch
 // or a tail per query.  Axis-aligned point-in-mesh queries read the handle's column
-// grid (built at the first submit), others traverse the BVH.  Points whose rays cross more than 8 triangles go to one
-// overflow list that a second launch resolves exactly.  The launches of an unchanged
+// grid (built at the first submit), others traverse the BVH.  Points whose rays cross
+// more than 8 triangles, and edges with more than 4 crossings or a deep traversal, go to
+// one overflow list that a second launch resolves exactly.  The launches of an unchanged
 // batch are captured once as a CUDA graph and replayed.  rs_batch_autotune times the
 // batch over BVH leaf sizes, chunk sizes and traversal stack depths and keeps the best.
 #include <algorithm>
@@ -25,7 +26,7 @@ namespace rs {
 namespace {
 
 constexpr int kBT = 128;                      // threads per CTA of the persistent kernel
-constexpr uint64_t kOverflowCap = 1ull << 22;  // points queued for the exact fallback per submit
+constexpr uint64_t kOverflowCap = 1ull << 22;  // rays queued for the exact fallback per submit
 
 struct BatchQuery {
     const BNode* nodes;
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(kBT) k_batch(const BatchQuery* __restrict__ q,
                                                int chunk, unsigned long long* __restrict__ next,
                                                uint2* __restrict__ ovf, unsigned long long* __restrict__ ovf_count) {
     __shared__ GridWarpSlots slots[kBT / 32];
+    __shared__ EdgeSmem<kBT, STACK> esm;  // edge rays' stacks and crossings, one column per thread
     const int lane = threadIdx.x & 31;
     GridWarpSlots& sl = slots[threadIdx.x >> 5];
     for (;;) {
@@ -123,8 +125,13 @@ __global__ void __launch_bounds__(kBT) k_batch(const BatchQuery* __restrict__ q,
         }
         for (uint64_t i = r0 + lane; i < r1; i += 32) {
             if (Q.kind == 1) {
-                edge_ray<STACK>(Q.starts, Q.ends, Q.offsets, Q.counts, Q.sources, i, Q.nodes, Q.max_steps, Q.tris,
-                                Q.swap, Q.table);
+                const EdgePayload p{Q.starts, Q.ends, Q.offsets, Q.counts, Q.sources};
+                if (!edge_ray_fast<STACK>(esm.column(threadIdx.x), p, i, Q.nodes, Q.max_steps, Q.tris, Q.swap,
+                                          Q.table)) {
+                    const unsigned long long slot = atomicAdd(ovf_count, 1ull);
+                    if (slot < kOverflowCap) ovf[slot] = make_uint2((uint32_t)qi, (uint32_t)i);
+                    else atomicOr(Q.status, ST_HIT_OVERFLOW);
+                }
             } else if (Q.axis == 0) {
                 batch_pim_ray<0, STACK>(Q, qi, i, ovf, ovf_count);
             } else if (Q.axis == 1) {
@@ -148,6 +155,11 @@ __global__ void __launch_bounds__(kBT) k_batch_fallback(const BatchQuery* __rest
         const uint2 item = ovf[e];
         const BatchQuery& Q = q[item.x];
         const uint64_t i = item.y;
+        if (Q.kind == 1) {
+            edge_ray_long(EdgePayload{Q.starts, Q.ends, Q.offsets, Q.counts, Q.sources}, i, Q.nodes, Q.max_steps,
+                          Q.tris, Q.swap, Q.table);
+            continue;
+        }
         const Ray r = make_ray(Q.pts[3 * i], Q.pts[3 * i + 1], Q.pts[3 * i + 2], Q.dx, Q.dy, Q.dz, kEps, kTmax);
         if (Q.axis == 0) pim_fallback_ray<0, STACK>(Q.nodes, Q.max_steps, Q.tris, r, Q.status, Q.obj, Q.in, i);
         else if (Q.axis == 1) pim_fallback_ray<1, STACK>(Q.nodes, Q.max_steps, Q.tris, r, Q.status, Q.obj, Q.in, i);
@@ -277,7 +289,7 @@ int commit(rs_batch* b, cudaStream_t s) {
     cudaError_t e = cudaMalloc((void**)&b->d_q, std::max(nq, 1) * sizeof(BatchQuery));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_status, std::max(nq, 1) * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_counters, 2 * sizeof(unsigned long long));
-    if (e == cudaSuccess && any_pim) e = cudaMalloc((void**)&b->d_ovf, kOverflowCap * sizeof(uint2));
+    if (e == cudaSuccess && nq) e = cudaMalloc((void**)&b->d_ovf, kOverflowCap * sizeof(uint2));
     for (int i = 0; i < nq && e == cudaSuccess; ++i) {
         const rs_batch_item& it = b->items[i];
         hq[i].status = it.kind == 1 ? hq[i].table.status : b->d_status + i;
@@ -299,10 +311,9 @@ int commit(rs_batch* b, cudaStream_t s) {
 // One fallback thread per possible overflow entry, up to the list's capacity (the count
 // is only known on the device; threads past it return at once).
 unsigned fallback_grid(const rs_batch* b) {
-    uint64_t pim = 0;
-    for (const rs_batch_item& it : b->items)
-        if (it.kind == 0) pim += it.n;
-    return (unsigned)std::max<uint64_t>(1, (std::min(pim, kOverflowCap) + kBT - 1) / kBT);
+    uint64_t rays = 0;
+    for (const rs_batch_item& it : b->items) rays += it.n;
+    return (unsigned)std::max<uint64_t>(1, (std::min(rays, kOverflowCap) + kBT - 1) / kBT);
 }
 
 // The launches of one submit: counters, per-query statuses, outputs of queries against

@@ -164,12 +164,33 @@ static float estimate_host_grids(const void* hA, const void* hB, int numCells, f
     return st == RS_OK ? (float)sums[0] : -1.0f;
 }
 
-extern "C" float estimateOverlapSelectivity(const void* h_gridA, const void* h_gridB, int numCells, float cellVolume,
-                                            float epsilon, float gamma) {
+extern "C" float rs_estimate_overlap_selectivity(const void* h_gridA, const void* h_gridB, int numCells,
+                                                 float cellVolume, float epsilon, float gamma) {
     return estimate_host_grids(h_gridA, h_gridB, numCells, cellVolume, epsilon, gamma);
 }
 
-extern "C" float estimateIntersectionSelectivity(const void* h_gridA, const void* h_gridB, int numCells,
-                                                 float cellVolume, float epsilon, float gamma) {
+extern "C" float rs_estimate_intersection_selectivity(const void* h_gridA, const void* h_gridB, int numCells,
+                                                      float cellVolume, float epsilon, float gamma) {
+    return estimate_host_grids(h_gridA, h_gridB, numCells, cellVolume, epsilon, gamma);
+}
+
+// The reference's own declarations (estimated_overlap.h:6-13, estimated_intersection.h:6-13)
+// have C++ linkage and take the GridCell of common/include/GridCell.h:5-10; this struct has
+// that name and layout, so these definitions carry the symbols the reference's mains link to.
+struct GridCell {
+    uint32_t CenterCount;
+    uint32_t TouchCount;
+    float AvgSizeMean;
+    float VolRatio;
+};
+static_assert(sizeof(GridCell) == 16, "GridCell is 16 bytes");
+
+float estimateOverlapSelectivity(const GridCell* h_gridA, const GridCell* h_gridB, int numCells, float cellVolume,
+                                 float epsilon, float gamma) {
+    return estimate_host_grids(h_gridA, h_gridB, numCells, cellVolume, epsilon, gamma);
+}
+
+float estimateIntersectionSelectivity(const GridCell* h_gridA, const GridCell* h_gridB, int numCells,
+                                      float cellVolume, float epsilon, float gamma) {
     return estimate_host_grids(h_gridA, h_gridB, numCells, cellVolume, epsilon, gamma);
 }

@@ -319,10 +319,21 @@ __device__ __forceinline__ int orient_sign(const float* d, const float* o, const
     return orient_exact(d[0], d[1], d[2], o[0], o[1], o[2], a[0], a[1], a[2], b[0], b[1], b[2]);
 }
 
+// Perturbation axes of a direction: kz = the dominant axis of d (ties keep z, then x),
+// kx = kz+1, ky = kz+2 (mod 3).  Written without indexing d by a variable.
+__device__ __forceinline__ void perturb_axes(const float* d, int& kx, int& ky) {
+    const float ax = fabsf(d[0]), ay = fabsf(d[1]), az = fabsf(d[2]);
+    int kz = 2;
+    float best = az;
+    if (ax > best) { kz = 0; best = ax; }
+    if (ay > best) kz = 1;
+    kx = kz == 2 ? 0 : kz + 1;
+    ky = kz == 0 ? 2 : (kz == 1 ? 0 : 1);
+}
+
 // Edge sign of (a,b) for the perturbed origin (see file header).
 template <int AXIS>
-__device__ __forceinline__ int perturbed_sign(const float* d, const float* o, const float* a, const float* b,
-                                              int kx, int ky) {
+__device__ __forceinline__ int perturbed_sign(const float* d, const float* o, const float* a, const float* b) {
     int s = orient_sign<AXIS>(d, o, a, b);
     if (s) return s;
     if (AXIS >= 0) {
@@ -334,6 +345,8 @@ __device__ __forceinline__ int perturbed_sign(const float* d, const float* o, co
         if (b[kxa] != a[kxa]) return b[kxa] > a[kxa] ? 1 : -1;
         return 0;
     }
+    int kx, ky;
+    perturb_axes(d, kx, ky);
     s = -axis_det_exact(kx, d[0], d[1], d[2], a[0], a[1], a[2], b[0], b[1], b[2]);
     if (s) return s;
     return -axis_det_exact(ky, d[0], d[1], d[2], a[0], a[1], a[2], b[0], b[1], b[2]);
@@ -342,10 +355,10 @@ __device__ __forceinline__ int perturbed_sign(const float* d, const float* o, co
 // ---------------------------------------------------------------------------
 // Rays and the slab rule.
 // ---------------------------------------------------------------------------
+// A ray: origin, direction, 1/direction per axis (0 for an axis the direction does not
+// move along: d == 0, or 1/d overflows), and the accepted t range.
 struct Ray {
     float o[3], d[3], inv[3];
-    int zero[3];
-    int kx, ky;
     float tmin, tmax;
 };
 
@@ -356,23 +369,12 @@ __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, 
     r.d[0] = dx; r.d[1] = dy; r.d[2] = dz;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        r.zero[k] = 0;
         r.inv[k] = 0.0f;
-        if (r.d[k] == 0.0f) {
-            r.zero[k] = 1;
-        } else {
-            r.inv[k] = __fdiv_rn(1.0f, r.d[k]);
-            if (isinf(r.inv[k])) r.zero[k] = 1;
+        if (r.d[k] != 0.0f) {
+            const float inv = __fdiv_rn(1.0f, r.d[k]);
+            if (!isinf(inv)) r.inv[k] = inv;
         }
     }
-    // Dominant axis (ties keep z, then x): written without indexing r.d by a variable.
-    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
-    int kz = 2;
-    float best = az;
-    if (ax > best) { kz = 0; best = ax; }
-    if (ay > best) kz = 1;
-    r.kx = kz == 2 ? 0 : kz + 1;
-    r.ky = kz == 0 ? 2 : (kz == 1 ? 0 : 1);
     r.tmin = tmin;
     r.tmax = tmax;
     return r;
@@ -385,7 +387,7 @@ __device__ __forceinline__ bool slab(const Ray& r, const float* lo, const float*
                                      float& enter, float& exit) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const bool zero = (AXIS >= 0) ? (k != AXIS) : (r.zero[k] != 0);
+        const bool zero = (AXIS >= 0) ? (k != AXIS) : (r.inv[k] == 0.0f);
         if (zero) {
             if (r.o[k] < lo[k] || r.o[k] > hi[k]) return false;
             continue;
@@ -421,10 +423,10 @@ __device__ __forceinline__ bool hit_triangle(const Ray& r, const float* a, const
     if (!slab<AXIS>(r, lo, hi, -INFINITY, INFINITY, en, ex)) return false;
     // Cheap reject before the sign tests: the clamped t lies in [en, ex].
     if (ex < r.tmin || en > r.tmax) return false;
-    const int s0 = perturbed_sign<AXIS>(r.d, r.o, a, b, r.kx, r.ky);
+    const int s0 = perturbed_sign<AXIS>(r.d, r.o, a, b);
     if (s0 == 0) return false;
-    if (perturbed_sign<AXIS>(r.d, r.o, b, c, r.kx, r.ky) != s0) return false;
-    if (perturbed_sign<AXIS>(r.d, r.o, c, a, r.kx, r.ky) != s0) return false;
+    if (perturbed_sign<AXIS>(r.d, r.o, b, c) != s0) return false;
+    if (perturbed_sign<AXIS>(r.d, r.o, c, a) != s0) return false;
     const float e1x = __fsub_rn(b[0], a[0]), e1y = __fsub_rn(b[1], a[1]), e1z = __fsub_rn(b[2], a[2]);
     const float e2x = __fsub_rn(c[0], a[0]), e2y = __fsub_rn(c[1], a[1]), e2z = __fsub_rn(c[2], a[2]);
     const float nx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
@@ -536,6 +538,11 @@ struct PairTable {
     unsigned int* status;         // OR of ST_* bits
     unsigned long long* count;    // number of distinct keys inserted
     unsigned long long* stats;    // nullable: [0] slot accesses, [1] contended probes (--track-hash-contention)
+    // Hit rule of the edge rays that insert into the table: at most max_hits hits per
+    // edge, the next hit searched from t + 1e-6 (next_float == 0) or from the next float
+    // after t (next_float != 0).
+    int max_hits;
+    int next_float;
 };
 
 __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long long key) {

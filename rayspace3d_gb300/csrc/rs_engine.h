@@ -60,6 +60,10 @@ struct rs_pairset {
     unsigned long long* meta = nullptr;
     int track = 0;  // count slot accesses and contention
     int device = 0;
+    // Edge-ray hit rule (rs_pairset_set_edge_rule): the reference's kMaxIterations and
+    // advance step of the overlap loop.
+    int edge_max_hits = 100;
+    int edge_next_float = 0;
     // meta[1] as last read by the host with status ok, while no launch has been given the
     // table since (table_view() resets it); -1 when unknown.
     long long known_count = -1;

@@ -69,6 +69,19 @@ __global__ void __launch_bounds__(kT) k_estimate(const uint4* __restrict__ A, co
     if (threadIdx.x < kSums) part[blockIdx.x * kSums + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// Per-cell estimates only (rs_estimate_grid_cells): the values estimateSelectivityKernel
+// writes to its result buffer (estimated_overlap.cu:8-41).
+__global__ void __launch_bounds__(kT) k_estimate_cells(const uint4* __restrict__ A, const uint4* __restrict__ B,
+                                                       uint64_t n, float cell_volume, float eps, float gamma,
+                                                       float* __restrict__ out) {
+    const uint64_t i = blockIdx.x * (uint64_t)kT + threadIdx.x;
+    if (i >= n) return;
+    const uint4 ra = __ldg(&A[i]), rb = __ldg(&B[i]);
+    const Cell a{ra.x, ra.y, __uint_as_float(ra.z), __uint_as_float(ra.w)};
+    const Cell b{rb.x, rb.y, __uint_as_float(rb.z), __uint_as_float(rb.w)};
+    out[i] = cell_estimate(a, b, cell_volume, eps, gamma);
+}
+
 // Fixed-order reduction of the per-block partials: thread t sums blocks t, t+256, ...
 // in order, then a fixed shared-memory tree combines the 256 thread sums.
 __global__ void __launch_bounds__(256) k_estimate_final(const double* __restrict__ part, double* __restrict__ out) {
@@ -135,6 +148,19 @@ extern "C" int rs_estimate_grid(const void* d_cellsA, const void* d_cellsB, uint
         h_means4[3] = sums[6] > 0 ? (float)(sums[5] / sums[6]) : 1.0f;
     }
     return RS_OK;
+}
+
+extern "C" int rs_estimate_grid_cells(const void* d_cellsA, const void* d_cellsB, uint64_t ncells, float cell_volume,
+                                      float epsilon, float gamma, float* d_values, void* stream) {
+    if (ncells && (!d_cellsA || !d_cellsB || !d_values)) return RS_ERR_INVALID;
+    if (ncells == 0) return RS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    launch(k_estimate_cells, (unsigned)((ncells + kT - 1) / kT), kT, 0, s, reinterpret_cast<const uint4*>(d_cellsA),
+           reinterpret_cast<const uint4*>(d_cellsB), ncells, cell_volume, epsilon, gamma, d_values);
+    cudaError_t e = cudaGetLastError();
+    const cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    return to_status(e);
 }
 
 extern "C" int64_t rs_estimate_pairs_from_raw(double raw, const float* m, float cell_volume, int alpha_correction) {

@@ -4,9 +4,12 @@
 // (query/src/cuda/mesh_overlap_edges.cu:106-216) and __raygen__mesh_overlap
 // (mesh_intersection.cu:16-91,288-334): one thread per unique edge traces the
 // segment once (the reference re-traces per hit and, in the intersection variant,
-// per source object) and inserts (source, target) pairs straight into the pair
-// table.  Containment replaces __raygen__mesh_containment_anyhit +
-// __anyhit__ah_containment (mesh_intersection_anyhit.cu:46-240): one +Z ray per
+// per source object), takes its crossings with the reference's hit rule and inserts
+// (source, target) pairs straight into the pair table.  The edges a broad phase keeps
+// are binned by the Morton cell of their midpoint first, so the 32 rays of a warp
+// start close together and descend the same subtrees.  Containment replaces
+// __raygen__mesh_containment_anyhit + __anyhit__ah_containment
+// (mesh_intersection_anyhit.cu:46-240): one +Z ray per
 // source object, parity per target object kept in registers instead of a
 // 256-slot global scratch per object.
 #include <algorithm>
@@ -23,26 +26,52 @@ namespace {
 
 constexpr int kT = 128;
 constexpr int kTargets = 32;
+constexpr int kFastStack = 32;  // shared-memory stack entries per lane of the edge-ray kernels
+constexpr int kCellBits = 5;    // 32^3 Morton cells order the live edges
+constexpr int kCells = 1 << (3 * kCellBits);
+// Jobs with more edges than this are traced in live-list order (no binning): the cell
+// ranks and the ordered list would cost 8 more bytes per edge.
+constexpr uint64_t kBinMaxEdges = 1ull << 27;
 
-__global__ void __launch_bounds__(kT) k_edge_join(const float* __restrict__ starts, const float* __restrict__ ends,
-                                                  const int32_t* __restrict__ offsets,
-                                                  const int32_t* __restrict__ counts,
-                                                  const int32_t* __restrict__ sources, uint64_t nE,
+// Fast path over the edges order[0..*n_order) of a payload of n_direct edges (or over all
+// of them when order is null); the edges it defers go to deferred[0..*n_def).
+__global__ void __launch_bounds__(kT) k_edge_rays(EdgePayload p, const uint32_t* __restrict__ order,
+                                                  const unsigned int* __restrict__ n_order, uint64_t n_direct,
+                                                  const BNode* __restrict__ nodes, uint32_t max_steps,
+                                                  const float4* __restrict__ tris, int swap, PairTable table,
+                                                  uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def) {
+    __shared__ EdgeSmem<kT, kFastStack> sm;
+    const EdgeColumn col = sm.column(threadIdx.x);
+    const uint64_t n = order ? (uint64_t)*n_order : n_direct;
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t e = order ? order[j] : (uint32_t)j;
+        if (e >= n_direct) continue;  // never, for a list of this payload's edges
+        if (!edge_ray_fast<kFastStack>(col, p, e, nodes, max_steps, tris, swap, table))
+            deferred[atomicAdd(n_def, 1u)] = e;
+    }
+}
+
+// Long path over the deferred edges.
+__global__ void __launch_bounds__(kT) k_edge_long(EdgePayload p, const uint32_t* __restrict__ deferred,
+                                                  const unsigned int* __restrict__ n_def,
                                                   const BNode* __restrict__ nodes, uint32_t max_steps,
                                                   const float4* __restrict__ tris, int swap, PairTable table) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= nE) return;
-    edge_ray<kStack>(starts, ends, offsets, counts, sources, i, nodes, max_steps, tris, swap, table);
+    const unsigned int n = *n_def;
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        edge_ray_long(p, deferred[j], nodes, max_steps, tris, swap, table);
 }
 
 // Legacy per-triangle overlap (mesh_overlap.cu:126-179): record r = 3 t + e is edge e of
-// source triangle t.  Triangles with an index >= nV set *bad and are skipped.
+// source triangle t.  Triangles with an index >= nV set *bad and are skipped.  Records the
+// fast path defers go to deferred (when given; else they run the long path here).
 __global__ void __launch_bounds__(kT) k_tri_edge_join(const float* __restrict__ V, uint64_t nV,
                                                       const uint32_t* __restrict__ I,
                                                       const int32_t* __restrict__ T, uint64_t m,
                                                       const BNode* __restrict__ nodes, uint32_t max_steps,
                                                       const float4* __restrict__ tris, int swap, PairTable table,
-                                                      unsigned int* __restrict__ bad) {
+                                                      unsigned int* __restrict__ bad, uint32_t* __restrict__ deferred,
+                                                      unsigned int* __restrict__ n_def) {
+    __shared__ EdgeSmem<kT, kFastStack> sm;
     const uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (r >= m) return;
     const uint64_t t = r / 3;
@@ -50,40 +79,87 @@ __global__ void __launch_bounds__(kT) k_tri_edge_join(const float* __restrict__ 
         if (r % 3 == 0) atomicOr(bad, 1u);
         return;
     }
-    triangle_edge_ray<kStack>(V, I, T, r, nodes, max_steps, tris, swap, table);
+    Ray ray;
+    if (!triangle_edge_of(V, I, r, ray)) return;
+    if (deferred) {
+        if (!segment_fast<kFastStack>(sm.column(threadIdx.x), ray, T + t, 1, nodes, max_steps, tris, swap, table))
+            deferred[atomicAdd(n_def, 1u)] = (uint32_t)r;
+    } else {
+        segment_long(ray, T + t, 1, nodes, max_steps, tris, swap, table);
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_tri_edge_long(const float* __restrict__ V, const uint32_t* __restrict__ I,
+                                                      const int32_t* __restrict__ T,
+                                                      const uint32_t* __restrict__ deferred,
+                                                      const unsigned int* __restrict__ n_def,
+                                                      const BNode* __restrict__ nodes, uint32_t max_steps,
+                                                      const float4* __restrict__ tris, int swap, PairTable table) {
+    const unsigned int n = *n_def;
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint64_t r = deferred[j];
+        Ray ray;
+        if (triangle_edge_of(V, I, r, ray)) segment_long(ray, T + r / 3, 1, nodes, max_steps, tris, swap, table);
+    }
 }
 
 // The edges of one source set traced against the other set's BVH, with the source
-// objects' broad-phase flags and the list of live edges.
+// objects' broad-phase flags and the job's work lists.
 struct EdgeJob {
-    const float* starts;
-    const float* ends;
-    const int32_t* offsets;
-    const int32_t* counts;
-    const int32_t* sources;
+    EdgePayload p;
     uint64_t nE;
     const uint8_t* cull;  // flag per source object below n_cull
     uint64_t n_cull;
-    uint32_t* live;
+    uint32_t* live;       // live edges, in arrival order
+    uint32_t* rank;       // rank of each live edge within its cell; then the deferred edges
+    uint32_t* order;      // live edges by cell (binned jobs)
+    uint32_t* cells;      // kCells counts, then their exclusive prefix sums (binned jobs)
     unsigned int* n_live;
+    unsigned int* n_def;
     const BNode* nodes;
     uint32_t max_steps;
     const float4* tris;
     int swap;
 };
 
+__device__ __forceinline__ uint32_t spread5(uint32_t v) {  // 5 bits -> every third bit
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// Morton cell (32^3 over the target BVH's root box) of edge i's midpoint.  Written with
+// rounded intrinsics so every kernel that calls it computes the same cell.
+__device__ __forceinline__ uint32_t edge_cell(const EdgeJob& j, uint64_t i) {
+    const float4 na = __ldg(&j.nodes[0].a), nb = __ldg(&j.nodes[0].b), nc = __ldg(&j.nodes[0].c);
+    const float lo[3] = {fminf(na.x, nb.z), fminf(na.y, nb.w), fminf(na.z, nc.x)};
+    const float hi[3] = {fmaxf(na.w, nc.y), fmaxf(nb.x, nc.z), fmaxf(nb.y, nc.w)};
+    uint32_t code = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float m = __fmul_rn(__fadd_rn(j.p.starts[3 * i + k], j.p.ends[3 * i + k]), 0.5f);
+        const float ext = __fsub_rn(hi[k], lo[k]);
+        float q = ext > 0.0f ? __fmul_rn(__fdiv_rn(__fsub_rn(m, lo[k]), ext), (float)(1 << kCellBits)) : 0.0f;
+        q = fminf(fmaxf(q, 0.0f), (float)((1 << kCellBits) - 1));
+        code |= spread5((uint32_t)q) << k;
+    }
+    return code;
+}
+
 // Broad phase: the edges with at least one candidate source object (k_cull_query) are
-// appended to their job's `live` list (any order: the pair table deduplicates).  A light
-// kernel, so the dependent loads of many edges are in flight at once.  Blocks below
-// blocks0 run job j0, the others j1.
+// appended to their job's `live` list; in binned jobs each also takes a rank within its
+// cell (one warp-aggregated atomic per cell and warp).  A light kernel, so the dependent
+// loads of many edges are in flight at once.  Blocks below blocks0 run job j0, the
+// others j1.
 __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsigned int blocks0) {
     const bool second = blockIdx.x >= blocks0;
     const EdgeJob& j = second ? j1 : j0;
     const uint64_t i = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x;
     bool any = false;
     if (i < j.nE) {
-        const int ns = j.counts[i];
-        const int32_t* sp = j.sources + j.offsets[i];
+        const int ns = j.p.counts[i];
+        const int32_t* sp = j.p.sources + j.p.offsets[i];
         for (int q = 0; q < ns && !any; ++q) {
             const int32_t so = sp[q];
             any = (so < 0 || (uint64_t)so >= j.n_cull) ? true : j.cull[so] != 0;
@@ -92,25 +168,80 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
     const unsigned int m = __ballot_sync(0xffffffffu, any);
     if (!m) return;
     const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    const unsigned int below = (1u << lane) - 1u;
     unsigned int base = 0;
     if (lane == leader) base = atomicAdd(j.n_live, (unsigned int)__popc(m));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (any) j.live[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    if (!any) return;
+    const unsigned int pos = base + __popc(m & below);
+    j.live[pos] = (uint32_t)i;
+    if (j.order) {
+        const uint32_t cell = edge_cell(j, i);
+        const unsigned int peers = __match_any_sync(m, cell);
+        const int first = __ffs(peers) - 1;
+        unsigned int r0 = 0;
+        if (lane == first) r0 = atomicAdd(&j.cells[cell], (unsigned int)__popc(peers));
+        r0 = __shfl_sync(peers, r0, first);
+        j.rank[pos] = r0 + __popc(peers & below);
+    }
 }
 
-// Edge rays of one live list (grid-stride: the list length is only known on the device).
-__global__ void __launch_bounds__(kT) k_edge_join_live(const float* __restrict__ starts,
-                                                       const float* __restrict__ ends,
-                                                       const int32_t* __restrict__ offsets,
-                                                       const int32_t* __restrict__ counts,
-                                                       const int32_t* __restrict__ sources,
-                                                       const uint32_t* __restrict__ live,
-                                                       const unsigned int* __restrict__ n_live,
-                                                       const BNode* __restrict__ nodes, uint32_t max_steps,
-                                                       const float4* __restrict__ tris, int swap, PairTable table) {
-    const unsigned int n = *n_live;
-    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        edge_ray<kStack>(starts, ends, offsets, counts, sources, live[j], nodes, max_steps, tris, swap, table);
+// Exclusive prefix sums of the kCells cell counts of each binned job, in place (one block
+// of 1024 threads per job, 32 cells per thread).
+__global__ void __launch_bounds__(1024) k_cell_scan(uint32_t* c0, uint32_t* c1) {
+    __shared__ uint32_t warp_sum[32];
+    uint32_t* c = blockIdx.x ? c1 : c0;
+    if (!c) return;
+    constexpr int kPer = kCells / 1024;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    uint32_t v[kPer];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        v[k] = c[t * kPer + k];
+        sum += v[k];
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_sum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t x = warp_sum[lane], xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, xi, o);
+            if (lane >= o) xi += y;
+        }
+        warp_sum[lane] = xi - x;
+    }
+    __syncthreads();
+    uint32_t run = warp_sum[w] + inc - sum;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        c[t * kPer + k] = run;
+        run += v[k];
+    }
+}
+
+// Live edges of the binned jobs into cell order.  Blocks below blocks0 run j0, the others
+// j1, each job's blocks striding over its live list.
+__global__ void __launch_bounds__(256) k_edge_order(EdgeJob j0, EdgeJob j1, unsigned int blocks0,
+                                                    unsigned int blocks1) {
+    const bool second = blockIdx.x >= blocks0;
+    const EdgeJob& j = second ? j1 : j0;
+    if (!j.order) return;
+    const unsigned int nb = second ? blocks1 : blocks0;
+    const unsigned int n = *j.n_live;
+    for (unsigned int k = (blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x; k < n;
+         k += nb * blockDim.x) {
+        const uint32_t e = j.live[k];
+        const uint32_t pos = j.cells[edge_cell(j, e)] + j.rank[k];
+        if (pos < n) j.order[pos] = e;  // always: the cell is recomputed with the same arithmetic
+    }
 }
 
 // A stream per device for the second direction's rays, forked from and joined back into
@@ -436,6 +567,8 @@ PairTable table_view(rs_pairset* ps) {
     t.status = reinterpret_cast<unsigned int*>(ps->meta);
     t.count = ps->meta + 1;
     t.stats = ps->track ? ps->meta + 2 : nullptr;
+    t.max_hits = ps->edge_max_hits;
+    t.next_float = ps->edge_next_float;
     return t;
 }
 
@@ -447,41 +580,99 @@ namespace rs {
 // Launches one edge-ray direction without waiting for it (status lands in the table's meta word).
 cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream_t s);
 
+// Every edge of a payload, in payload order (no broad phase), in chunks of 2^31 edges so
+// that edge ids fit the 32-bit deferred list (a chunk's payload pointers are offset; the
+// offsets still index the whole sources array).
+static cudaError_t edge_all_async(const rs_bvh* target, EdgePayload p, uint64_t nE, int swap, rs_pairset* ps,
+                                  cudaStream_t s) {
+    constexpr uint64_t kChunk = 1ull << 31;
+    const uint64_t cap = std::min(nE, kChunk);
+    uint32_t* deferred = nullptr;
+    unsigned int* n_def = nullptr;
+    cudaError_t e = dmalloc((void**)&deferred, std::max<uint64_t>(cap, 1) * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&n_def, sizeof(unsigned int), s);
+    const PairTable table = table_view(ps);
+    const int ptok = prof_begin(P_EDGE_JOIN, s);
+    for (uint64_t base = 0; base < nE && e == cudaSuccess; base += kChunk) {
+        const uint64_t n = std::min(kChunk, nE - base);
+        const EdgePayload q{p.starts + 3 * base, p.ends + 3 * base, p.offsets + base, p.counts + base, p.sources};
+        e = cudaMemsetAsync(n_def, 0, sizeof(unsigned int), s);
+        if (e != cudaSuccess) break;
+        const unsigned grid = (unsigned)std::min<uint64_t>((n + kT - 1) / kT, 8ull * sm_count());
+        launch(k_edge_rays, grid, kT, 0, s, q, (const uint32_t*)nullptr, (const unsigned int*)nullptr, n,
+               (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table, deferred,
+               n_def);
+        launch(k_edge_long, (unsigned)std::min<uint64_t>((n + kT - 1) / kT, 2ull * sm_count()), kT, 0, s, q,
+               (const uint32_t*)deferred, (const unsigned int*)n_def, (const BNode*)target->nodes, max_steps(target),
+               (const float4*)target->tris, swap, table);
+        e = cudaGetLastError();
+    }
+    prof_end(P_EDGE_JOIN, s, ptok);
+    if (deferred) cudaFreeAsync(deferred, s);
+    if (n_def) cudaFreeAsync(n_def, s);
+    return e;
+}
+
 cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const float* d_ends,
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
                             int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull) {
     if (nE == 0 || target->n_tris == 0) return cudaSuccess;
-    const unsigned grid = (unsigned)((nE + kT - 1) / kT);
-    if (!cull.cand || nE > 0xffffffffull) {
-        const int ptok = prof_begin(P_EDGE_JOIN, s);
-        launch(k_edge_join, grid, kT, 0, s, d_starts, d_ends, d_offsets, d_counts, d_sources, nE, target->nodes,
-               max_steps(target), target->tris, swap, table_view(ps));
-        prof_end(P_EDGE_JOIN, s, ptok);
-        return cudaGetLastError();
-    }
-    EdgeJob job{d_starts, d_ends, d_offsets, d_counts, d_sources, nE, cull.cand, cull.n_obj, nullptr, nullptr,
-                (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap};
+    const EdgePayload p{d_starts, d_ends, d_offsets, d_counts, d_sources};
+    if (!cull.cand || nE > 0xffffffffull) return edge_all_async(target, p, nE, swap, ps, s);
+    EdgeJob job{};
+    job.p = p;
+    job.nE = nE;
+    job.cull = cull.cand;
+    job.n_cull = cull.n_obj;
+    job.nodes = (const BNode*)target->nodes;
+    job.max_steps = max_steps(target);
+    job.tris = (const float4*)target->tris;
+    job.swap = swap;
     return edge_jobs_async(&job, 1, ps, s);
 }
 
 // Live edges first, then rays for them only: the live checks of all jobs in one launch,
-// their rays in another.  Each job's nE < 2^32 and its cull flags set.
+// the binning of their live edges by cell in two more, then each job's rays (the second
+// job's on a side stream) and its deferred edges.  Each job's nE < 2^32 and its cull flags
+// set.
 cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream_t s) {
-    unsigned int* n_live = nullptr;
-    cudaError_t e = dmalloc((void**)&n_live, 2 * sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(n_live, 0, 2 * sizeof(unsigned int), s);
-    uint64_t blocks[2] = {0, 0}, total_e = 0;
+    // One zeroed block: n_live[2], n_def[2], then the cell counts of the binned jobs.
+    uint32_t* zeroed = nullptr;
     EdgeJob jobs[2] = {};
-    for (int d = 0; d < n_jobs && e == cudaSuccess; ++d) {
+    uint64_t blocks[2] = {0, 0}, total_e = 0;
+    int n_bin = 0;
+    for (int d = 0; d < n_jobs; ++d) {
         jobs[d] = job[d];
-        e = dmalloc((void**)&jobs[d].live, std::max<uint64_t>(jobs[d].nE, 1) * sizeof(uint32_t), s);
-        jobs[d].n_live = n_live + d;
-        blocks[d] = (jobs[d].nE + 255) / 256;
-        total_e += jobs[d].nE;
+        if (jobs[d].nE <= kBinMaxEdges) ++n_bin;
+    }
+    const size_t zbytes = (4 + (size_t)n_bin * kCells) * sizeof(uint32_t);
+    cudaError_t e = dmalloc((void**)&zeroed, zbytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(zeroed, 0, zbytes, s);
+    uint32_t* next_cells = zeroed + 4;
+    for (int d = 0; d < n_jobs && e == cudaSuccess; ++d) {
+        EdgeJob& j = jobs[d];
+        const size_t bytes = std::max<uint64_t>(j.nE, 1) * sizeof(uint32_t);
+        j.n_live = zeroed + d;
+        j.n_def = zeroed + 2 + d;
+        e = dmalloc((void**)&j.live, bytes, s);
+        if (e == cudaSuccess) e = dmalloc((void**)&j.rank, bytes, s);
+        if (e == cudaSuccess && j.nE <= kBinMaxEdges) {
+            e = dmalloc((void**)&j.order, bytes, s);
+            j.cells = next_cells;
+            next_cells += kCells;
+        }
+        blocks[d] = (j.nE + 255) / 256;
+        total_e += j.nE;
     }
     if (e == cudaSuccess && total_e) {
         const int ptok = prof_begin(P_EDGE_JOIN, s);
         launch(k_edge_live, (unsigned)(blocks[0] + blocks[1]), 256, 0, s, jobs[0], jobs[1], (unsigned)blocks[0]);
+        if (n_bin) {
+            launch(k_cell_scan, 2, 1024, 0, s, jobs[0].cells, n_jobs > 1 ? jobs[1].cells : (uint32_t*)nullptr);
+            const unsigned ob0 = (unsigned)std::min<uint64_t>(std::max<uint64_t>(blocks[0], 1), 4ull * sm_count());
+            const unsigned ob1 = (unsigned)std::min<uint64_t>(blocks[1], 4ull * sm_count());
+            launch(k_edge_order, ob0 + ob1, 256, 0, s, jobs[0], jobs[1], ob0, ob1);
+        }
         // The rays of the second job on a side stream, concurrent with the first's: each
         // list's rays are latency-bound chains when the lists are short, and a full list
         // keeps the GPU busy either way.
@@ -496,9 +687,12 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
         }
         for (int d = 0; d < n_jobs; ++d) {
             const EdgeJob& j = jobs[d];
-            launch(k_edge_join_live, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 8ull * sm_count()), kT, 0,
-                   d == 1 && side ? side : s, j.starts, j.ends, j.offsets, j.counts, j.sources, (const uint32_t*)j.live,
-                   (const unsigned int*)j.n_live, j.nodes, j.max_steps, j.tris, j.swap, table);
+            cudaStream_t st = d == 1 && side ? side : s;
+            launch(k_edge_rays, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 8ull * sm_count()), kT, 0, st, j.p,
+                   (const uint32_t*)(j.order ? j.order : j.live), (const unsigned int*)j.n_live, j.nE, j.nodes,
+                   j.max_steps, j.tris, j.swap, table, j.rank, j.n_def);
+            launch(k_edge_long, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 2ull * sm_count()), kT, 0, st, j.p,
+                   (const uint32_t*)j.rank, (const unsigned int*)j.n_def, j.nodes, j.max_steps, j.tris, j.swap, table);
         }
         if (side) {
             e = cudaEventRecord(joined, side);
@@ -510,9 +704,12 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
         prof_end(P_EDGE_JOIN, s, ptok);
         if (e == cudaSuccess) e = cudaGetLastError();
     }
-    for (int d = 0; d < n_jobs; ++d)
+    for (int d = 0; d < n_jobs; ++d) {
         if (jobs[d].live) cudaFreeAsync(jobs[d].live, s);
-    if (n_live) cudaFreeAsync(n_live, s);
+        if (jobs[d].rank) cudaFreeAsync(jobs[d].rank, s);
+        if (jobs[d].order) cudaFreeAsync(jobs[d].order, s);
+    }
+    if (zeroed) cudaFreeAsync(zeroed, s);
     return e;
 }
 
@@ -523,14 +720,21 @@ cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const fl
                                  const rs_bvh* B, const float* startsB, const float* endsB, const int32_t* offsetsB,
                                  const int32_t* countsB, const int32_t* sourcesB, uint64_t nEB, const EdgeCull& cullB,
                                  rs_pairset* ps, cudaStream_t s) {
-    EdgeJob job[2];
+    EdgeJob job[2] = {};
     int n = 0;
-    if (nEA && B->n_tris)
-        job[n++] = EdgeJob{startsA, endsA, offsetsA, countsA, sourcesA, nEA, cullA.cand, cullA.n_obj, nullptr, nullptr,
-                           (const BNode*)B->nodes, max_steps(B), (const float4*)B->tris, 0};
-    if (nEB && A->n_tris)
-        job[n++] = EdgeJob{startsB, endsB, offsetsB, countsB, sourcesB, nEB, cullB.cand, cullB.n_obj, nullptr, nullptr,
-                           (const BNode*)A->nodes, max_steps(A), (const float4*)A->tris, 1};
+    auto add = [&](const rs_bvh* target, EdgePayload p, uint64_t nE, const EdgeCull& c, int swap) {
+        EdgeJob& j = job[n++];
+        j.p = p;
+        j.nE = nE;
+        j.cull = c.cand;
+        j.n_cull = c.n_obj;
+        j.nodes = (const BNode*)target->nodes;
+        j.max_steps = max_steps(target);
+        j.tris = (const float4*)target->tris;
+        j.swap = swap;
+    };
+    if (nEA && B->n_tris) add(B, EdgePayload{startsA, endsA, offsetsA, countsA, sourcesA}, nEA, cullA, 0);
+    if (nEB && A->n_tris) add(A, EdgePayload{startsB, endsB, offsetsB, countsB, sourcesB}, nEB, cullB, 1);
     return n ? edge_jobs_async(job, n, ps, s) : cudaSuccess;
 }
 
@@ -611,19 +815,30 @@ extern "C" int rs_triangle_join(const rs_bvh* target, const float* d_vertices, u
     cudaStream_t s = (cudaStream_t)stream;
     const int st = bvh_use(target, s);
     if (st != RS_OK) return st;
-    unsigned int* bad = nullptr;
+    // bad flag and deferred count in one zeroed pair; records as 32-bit ids when they fit
+    // (else every record runs the long path in the first kernel).
+    unsigned int* flags = nullptr;
+    uint32_t* deferred = nullptr;
     unsigned int hbad = 0;
-    cudaError_t e = dmalloc((void**)&bad, sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s);
+    cudaError_t e = dmalloc((void**)&flags, 2 * sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned int), s);
+    if (e == cudaSuccess && m <= 0xffffffffull) e = dmalloc((void**)&deferred, m * sizeof(uint32_t), s);
     if (e == cudaSuccess) {
+        const PairTable table = table_view(ps);
         const int ptok = prof_begin(P_EDGE_JOIN, s);
         launch(k_tri_edge_join, (unsigned)((m + kT - 1) / kT), kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, m,
-               target->nodes, max_steps(target), target->tris, swap, table_view(ps), bad);
+               (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table, flags,
+               deferred, flags + 1);
+        if (deferred)
+            launch(k_tri_edge_long, (unsigned)std::min<uint64_t>((m + kT - 1) / kT, 2ull * sm_count()), kT, 0, s,
+                   d_vertices, d_indices, d_tri2obj, (const uint32_t*)deferred, (const unsigned int*)(flags + 1),
+                   (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table);
         prof_end(P_EDGE_JOIN, s, ptok);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
-    if (bad) cudaFreeAsync(bad, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, flags, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    if (flags) cudaFreeAsync(flags, s);
+    if (deferred) cudaFreeAsync(deferred, s);
     const int r = table_status(ps, s, e);
     if (r == RS_OK && hbad) return RS_ERR_INVALID;
     return r;

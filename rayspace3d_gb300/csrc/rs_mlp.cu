@@ -10,10 +10,12 @@
 // GridCell carries CenterCount where a triangle count might be wanted; the features use
 // the four fields the .pre file has.
 //
-// GEMMs: BF16 operands, FP32 accumulation, mma.sync m16n8k16 tensor-core tiles of
-// 64x64x32 per CTA (four warps of 32x32), operands staged through shared memory, split
-// over K with FP32 atomics when M x N alone cannot fill the GPU.  Weights keep an FP32
-// master copy (Adam) and a BF16 copy that the GEMMs read.
+// GEMMs: BF16 operands, FP32 accumulation.  Products whose operands are both K-major (the
+// forward pass: features x W1^T, hidden x W2^T) run on tcgen05 with TMA-fed shared memory
+// and tensor-memory accumulators (rs_umma.cu); the backward products, whose operands are
+// stored M- or N-contiguous, run on mma.sync tiles (128x128x64, ldmatrix, cp.async stages).
+// rs_mlp_set_gemm(1) sends every product to mma.sync (the tests compare the two paths).
+// Weights keep an FP32 master copy (Adam) and a BF16 copy that the GEMMs read.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -24,7 +26,17 @@
 #include "rs_prims.cuh"
 
 namespace rs {
+// The tcgen05 GEMM (rs_umma.cu).
+bool umma_gemm_fits(const void* A, int lda, const void* B, int ldb, int M, int N, int K);
+cudaError_t umma_gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc, int M,
+                      int N, int K, cudaStream_t s);
+cudaError_t umma_error_take(unsigned int* h_word, cudaStream_t s);
+
 namespace {
+
+// 0: K-major x K-major products on tcgen05 where the shapes allow, the rest on mma.sync;
+// 1: every product on mma.sync (rs_mlp_set_gemm).
+int g_gemm_mode = 0;
 
 constexpr int kIn = 32768;
 constexpr int kHid = 512;
@@ -298,6 +310,9 @@ bool chunkable(const __nv_bfloat16* p, int ld, int rows, int K) {
 template <bool A_KM, bool B_KM>
 void gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc, int M, int N, int K,
           cudaStream_t s) {
+    if (A_KM && B_KM && g_gemm_mode == 0 && umma_gemm_fits(A, lda, B, ldb, M, N, K) &&
+        umma_gemm(A, lda, B, ldb, C, ldc, M, N, K, s) == cudaSuccess)
+        return;
     if (chunkable<A_KM>(A, lda, M, K) && chunkable<B_KM>(B, ldb, N, K)) {
         static bool attr_set[64] = {};  // the kernels' shared-memory opt-in, once per device
         int dev = 0;
@@ -682,13 +697,58 @@ extern "C" int rs_mlp_features(const void* d_cellsA, const void* d_cellsB, int r
     return to_status(cudaGetLastError());
 }
 
+// Status of a finished call: a CUDA error, or RS_ERR_ITER_LIMIT when a tcgen05 GEMM wait ran
+// out (its products are then incomplete).
+static int mlp_status(cudaError_t e, cudaStream_t s) {
+    if (e != cudaSuccess) return to_status(e);
+    if (g_gemm_mode != 0) return RS_OK;
+    unsigned int w = 0;
+    e = umma_error_take(&w, s);
+    if (e != cudaSuccess) return to_status(e);
+    return w ? RS_ERR_ITER_LIMIT : RS_OK;
+}
+
+extern "C" int rs_mlp_set_gemm(int mode) {
+    if (mode != 0 && mode != 1) return RS_ERR_INVALID;
+    g_gemm_mode = mode;
+    return RS_OK;
+}
+
+extern "C" int rs_mlp_gemm(const void* d_A, int lda, const void* d_B, int ldb, float* d_C, int ldc, int M, int N,
+                           int K, int mode, void* stream) {
+    if (!d_A || !d_B || !d_C || M <= 0 || N <= 0 || K <= 0 || (mode != 0 && mode != 1)) return RS_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const __nv_bfloat16* A = static_cast<const __nv_bfloat16*>(d_A);
+    const __nv_bfloat16* B = static_cast<const __nv_bfloat16*>(d_B);
+    cudaError_t e;
+    if (mode == 0) {
+        if (!umma_gemm_fits(A, lda, B, ldb, M, N, K)) return RS_ERR_INVALID;
+        e = umma_gemm(A, lda, B, ldb, d_C, ldc, M, N, K, s);
+    } else {
+        const int saved = g_gemm_mode;
+        g_gemm_mode = 1;
+        gemm<true, true>(A, lda, B, ldb, d_C, ldc, M, N, K, s);
+        g_gemm_mode = saved;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return to_status(e);
+    if (mode == 0) {
+        unsigned int w = 0;
+        e = umma_error_take(&w, s);
+        if (e != cudaSuccess) return to_status(e);
+        if (w) return RS_ERR_ITER_LIMIT;
+    }
+    return RS_OK;
+}
+
 extern "C" int rs_mlp_forward(rs_mlp* h, const float* d_X, int B, float* d_y, void* stream) {
     if (!h || !d_X || B <= 0) return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = forward(h, d_X, B, s);
     if (e == cudaSuccess && d_y) e = cudaMemcpyAsync(d_y, h->y, B * 4, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return to_status(e);
+    return mlp_status(e, s);
 }
 
 extern "C" int rs_mlp_gradients(rs_mlp* h, const float* d_X, const float* d_target, int B, float* h_loss,
@@ -699,7 +759,7 @@ extern "C" int rs_mlp_gradients(rs_mlp* h, const float* d_X, const float* d_targ
     if (e == cudaSuccess) e = backward(h, d_target, B, s);
     if (e == cudaSuccess && h_loss) e = cudaMemcpyAsync(h_loss, h->loss, 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return to_status(e);
+    return mlp_status(e, s);
 }
 
 extern "C" int rs_mlp_train_step(rs_mlp* h, const float* d_X, const float* d_target, int B, float lr, float* h_loss,
@@ -717,7 +777,7 @@ extern "C" int rs_mlp_train_step(rs_mlp* h, const float* d_X, const float* d_tar
     e = cudaGetLastError();
     if (e == cudaSuccess && h_loss) e = cudaMemcpyAsync(h_loss, h->loss, 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return to_status(e);
+    return mlp_status(e, s);
 }
 
 extern "C" int rs_estimate_mlp(rs_mlp* h, const void* d_cellsA, const void* d_cellsB, int resolution,
@@ -730,7 +790,8 @@ extern "C" int rs_estimate_mlp(rs_mlp* h, const void* d_cellsA, const void* d_ce
     float y = 0.0f;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&y, h->y, 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return to_status(e);
+    st = mlp_status(e, s);
+    if (st != RS_OK) return st;
     const double v = std::expm1((double)y);
     *h_estimate = v > 0.0 ? (int64_t)std::llround(v) : 0;
     if (h_log1p) *h_log1p = (double)y;

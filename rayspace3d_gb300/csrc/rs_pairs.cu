@@ -322,6 +322,14 @@ extern "C" int rs_pairset_set_tracking(rs_pairset* ps, int on) {
     return RS_OK;
 }
 
+extern "C" int rs_pairset_set_edge_rule(rs_pairset* ps, int max_hits, int next_float) {
+    if (!ps) return RS_ERR_INVALID;
+    ps->edge_max_hits = max_hits > 0 ? max_hits : 100;  // mesh_intersection.cu:25-28
+    ps->edge_next_float = next_float != 0;
+    ps->known_count = -1;
+    return RS_OK;
+}
+
 extern "C" int rs_pairset_counters(const rs_pairset* ps, uint64_t* h_out8, void* stream) {
     if (!ps || !h_out8) return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;

@@ -409,11 +409,10 @@ int recheck_pim(int op, unsigned long long* out) { return recheck_op(op, out); }
 // ---------------------------------------------------------------------------
 // Point-in-mesh without device allocation.
 //
-// Callers that cannot allocate device memory on their query path -- code that runs
-// while another framework captures the stream into a CUDA graph, services with a
-// fixed device-memory budget whose allocator already owns the GPU, or real-time
-// loops where an allocation's implicit synchronisation is not acceptable -- use
-// rs_pim_noalloc.  Its per-call scratch (status word, overflow count, the twelve
+// Callers that cannot allocate device memory on their query path -- services whose
+// own allocator has reserved the whole GPU, or hosts with a fixed device-memory budget
+// checked per request -- use rs_pim_noalloc.  It waits for the stream and returns once
+// the results are written.  Its per-call scratch (status word, overflow count, the twelve
 // filter-box triangles and the list of points with more than kHits crossings) lives
 // in the fixed array below instead of coming from an allocator.  Host code may not
 // use the array's name as a device address, so its address is looked up with

@@ -1,4 +1,5 @@
 // rs_profile.cu -- launch counter and the opt-in per-kernel event profiler.
+#include <atomic>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -10,7 +11,12 @@ namespace rs {
 
 std::atomic<uint64_t> g_launches{0};
 
+// Device allocations requested through dmalloc since the library was loaded
+// (rs_alloc_count).
+static std::atomic<uint64_t> g_alloc_count{0};
+
 cudaError_t dmalloc(void** p, size_t bytes, cudaStream_t s) {
+    g_alloc_count.fetch_add(1, std::memory_order_relaxed);
     static std::mutex mu;
     static cudaMemPool_t pools[64] = {};
     int dev = 0;
@@ -126,6 +132,8 @@ void prof_collect() {
 }  // namespace rs
 
 extern "C" uint64_t rs_launch_count(void) { return rs::g_launches.load(); }
+
+extern "C" uint64_t rs_alloc_count(void) { return rs::g_alloc_count.load(); }
 
 extern "C" int rs_profile_enable(int on) {
     std::lock_guard<std::mutex> g(rs::g_mu);

@@ -21,21 +21,54 @@ __device__ __forceinline__ bool hit_less(float t0, uint32_t i0, float t1, uint32
     return t0 < t1 || (t0 == t1 && i0 < i1);
 }
 
+// Iteration cap of the parity loop (raytracing.cu:26).
+constexpr uint32_t kPimMaxIters = 10000;
+
 // Advance rule of raytracing.cu:23-60 on hits sorted by (t, id): a hit counts when
-// t >= threshold; the next threshold is t + 1e-6, or the next float when that does
-// not advance.
+// t >= threshold; the next threshold is t + 1e-6.  When t + 1e-6 rounds back to t
+// (t >= 32) the reference's next trace starts at t and finds that hit again on every
+// remaining iteration, so the count ends at the 10000-iteration cap; the count is
+// capped there in any case.
 struct Chain {
     float thr = kEps;
     uint32_t count = 0;
     int32_t first_obj = -1;
     __device__ __forceinline__ void step(float t, int32_t obj) {
-        if (t >= thr && t < kTmax) {
+        if (count < kPimMaxIters && t >= thr && t < kTmax) {
             if (count == 0) first_obj = obj;
             ++count;
-            float nt = __fadd_rn(t, kEps);
-            if (!(nt > t)) nt = nextafterf(t, INFINITY);
+            const float nt = __fadd_rn(t, kEps);
+            if (!(nt > t)) count = kPimMaxIters;
             thr = nt;
         }
+    }
+};
+
+// Hit sequence of the edge loops (mesh_overlap_edges.cu:106-178, mesh_intersection.cu:16-91,
+// mesh_overlap.cu:13-70): repeated closest-hit traces over [t_min, len + 1e-6] with t_min
+// starting at 1e-6 and moving to t + 1e-6 after each hit (t + 2e-4 when that does not
+// advance), at most max_hits traces.  On hits sorted by (t, id) that is a greedy walk:
+// a hit is taken when t >= t_min.  When neither step advances, every later trace finds the
+// same hit again, which adds no pair, so the walk stops.  next_float selects the strict
+// containment join's edge loop (mesh_containment.cu:99-170): t_min moves to the next float
+// after t, so every distinct distance is taken once.
+struct EdgeWalk {
+    float thr = kEps;
+    int n = 0;
+    bool done = false;
+    __device__ __forceinline__ bool take(float t, int max_hits, int next_float) {
+        if (done || !(t >= thr)) return false;
+        if (++n >= max_hits) done = true;
+        float nt;
+        if (next_float) {
+            nt = nextafterf(t, INFINITY);
+        } else {
+            nt = __fadd_rn(t, kEps);
+            if (!(nt > t)) nt = __fadd_rn(t, 2e-4f);
+            if (!(nt > t)) done = true;
+        }
+        thr = nt;
+        return true;
     }
 };
 
@@ -61,7 +94,7 @@ struct HitList {
         ++n;
     }
     // Odd-even transposition sort of all kHits slots (empty slots sort last).
-    __device__ __forceinline__ Chain finish() {
+    __device__ __forceinline__ void sort() {
 #pragma unroll
         for (int j = 0; j < kHits; ++j)
             if (j >= n) {
@@ -80,6 +113,9 @@ struct HitList {
                 }
             }
         }
+    }
+    __device__ __forceinline__ Chain finish() {
+        sort();
         Chain c;
 #pragma unroll
         for (int j = 0; j < kHits; ++j)
@@ -287,7 +323,7 @@ __device__ __forceinline__ void pim_fallback_ray(const BNode* __restrict__ nodes
     uint32_t pid = 0;
     bool have_prev = false;
     int it = 0;
-    for (; it < kFallbackIters; ++it) {
+    for (; it < kFallbackIters && ch.count < kPimMaxIters; ++it) {
         float bt = INFINITY;
         uint32_t bid = 0xffffffffu;
         int32_t bobj = -1;
@@ -323,24 +359,77 @@ __device__ __forceinline__ void pim_fallback_ray(const BNode* __restrict__ nodes
     write_result(ch, i, out_obj, out_in);
 }
 
-// Edge ray i of mesh_overlap_edges.cu:106-216: every target object crossed with t in
-// [1e-6, len + 1e-6] is paired with every source object of the edge.
-// The segment (sx,sy,sz) -> (ex,ey,ez) with its nsrc source objects src[0..nsrc).
-template <int STACK>
-__device__ __forceinline__ void segment_ray(float sx, float sy, float sz, float ex, float ey, float ez,
-                                            const int32_t* __restrict__ src, int nsrc,
-                                            const BNode* __restrict__ nodes, uint32_t max_steps,
-                                            const float4* __restrict__ tris, int swap, const PairTable& table) {
-    // distance3f / normalize3f of mesh_overlap_edges.cu:47-60 as individually rounded operations.
+// ---------------------------------------------------------------------------
+// Edge rays.  The fast path traces an edge once with its stack and its crossings
+// (up to kEdgeHits) in a column of shared memory; an edge with more crossings, or a
+// traversal deeper than the fast stack, is deferred untouched to the long path, which
+// runs the reference's trace loop literally.
+// ---------------------------------------------------------------------------
+constexpr int kEdgeHits = 4;
+
+// One thread's shared-memory column: element k of an array at base[k * stride].
+struct EdgeColumn {
+    int* stack;
+    float* t;
+    uint32_t* id;
+    int32_t* obj;
+    int stride;
+};
+
+// Shared-memory block of the fast path for T threads and a STACK-entry stack.
+template <int T, int STACK>
+struct EdgeSmem {
+    int stack[STACK][T];
+    float t[kEdgeHits][T];
+    uint32_t id[kEdgeHits][T];
+    int32_t obj[kEdgeHits][T];
+    __device__ __forceinline__ EdgeColumn column(int tid) {
+        return EdgeColumn{&stack[0][tid], &t[0][tid], &id[0][tid], &obj[0][tid], T};
+    }
+};
+
+// The segment's ray as distance3f / normalize3f of mesh_overlap_edges.cu:47-60 compute it,
+// one rounded operation at a time; false for edges shorter than 1e-6 (never traced).
+__device__ __forceinline__ bool segment_ray_of(float sx, float sy, float sz, float ex, float ey, float ez, Ray& r) {
     const float dx = __fsub_rn(ex, sx), dy = __fsub_rn(ey, sy), dz = __fsub_rn(ez, sz);
     const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-    if (len < 1e-6f) return;
-    const Ray r = make_ray(sx, sy, sz, __fdiv_rn(dx, len), __fdiv_rn(dy, len), __fdiv_rn(dz, len), 1e-6f,
-                           __fadd_rn(len, 1e-6f));
-    int32_t last[4] = {INT_MIN, INT_MIN, INT_MIN, INT_MIN};
-    int lp = 0;
-    unsigned int crossings = 0, tests = 0;
-    const bool ok = traverse<-1, STACK>(nodes, max_steps, r, [&](int first, int cnt) {
+    if (len < 1e-6f) return false;
+    r = make_ray(sx, sy, sz, __fdiv_rn(dx, len), __fdiv_rn(dy, len), __fdiv_rn(dz, len), 1e-6f, __fadd_rn(len, 1e-6f));
+    return true;
+}
+
+// (source, target) -- (target, source) when swap -- for every source object of the edge.
+__device__ __forceinline__ void insert_sources(const PairTable& table, const int32_t* __restrict__ src, int nsrc,
+                                               int32_t obj, int swap) {
+    for (int q = 0; q < nsrc; ++q) {
+        const uint32_t sobj = (uint32_t)src[q];
+        const unsigned long long key = swap ? (((unsigned long long)(uint32_t)obj << 32) | sobj)
+                                            : (((unsigned long long)sobj << 32) | (uint32_t)obj);
+        table_insert(table, key);
+    }
+}
+
+__device__ __forceinline__ void count_edge(const PairTable& table, int taken) {
+    if (table.stats) {
+        atomicAdd(&table.stats[2], 1ull);
+        if (taken) atomicAdd(&table.stats[3], (unsigned long long)taken);
+    }
+}
+
+// Edge ray of mesh_overlap_edges.cu:106-216, fast path: one traversal over
+// t in [1e-6, len + 1e-6] with the stack and crossings in the thread's shared-memory
+// column; the crossings, sorted by (t, triangle id), are walked with the table's hit rule
+// (EdgeWalk) and every target object of a hit taken is paired with every source object.
+// Returns false, having inserted nothing, when the edge has more than kEdgeHits crossings
+// or the traversal ran out of stack or steps: the caller then defers it to segment_long.
+template <int STACK>
+__device__ __forceinline__ bool segment_fast(const EdgeColumn& col, const Ray& r, const int32_t* __restrict__ src,
+                                             int nsrc, const BNode* __restrict__ nodes, uint32_t max_steps,
+                                             const float4* __restrict__ tris, int swap, const PairTable& table) {
+    const int S = col.stride;
+    int n = 0;
+    unsigned int tests = 0;
+    const bool ok = traverse_with<-1, STACK>(col.stack, S, nodes, max_steps, r, [&](int first, int cnt) {
         tests += (unsigned int)cnt;
         for (int k = first; k < first + cnt; ++k) {
             float a[3], b[3], c[3];
@@ -349,49 +438,121 @@ __device__ __forceinline__ void segment_ray(float sx, float sy, float sz, float 
             load_tri(tris, k, a, b, c, tid, obj);
             float t;
             if (!hit_triangle<-1>(r, a, b, c, t)) continue;
-            ++crossings;
-            if (obj == last[0] || obj == last[1] || obj == last[2] || obj == last[3]) continue;
-            last[lp] = obj;
-            lp = (lp + 1) & 3;
-            for (int q = 0; q < nsrc; ++q) {
-                const uint32_t sobj = (uint32_t)src[q];
-                const unsigned long long key = swap ? (((unsigned long long)(uint32_t)obj << 32) | sobj)
-                                                    : (((unsigned long long)sobj << 32) | (uint32_t)obj);
-                table_insert(table, key);
+            if (n < kEdgeHits) {
+                // Insertion into the sorted column.
+                int j = n;
+                while (j > 0 && hit_less(t, tid, col.t[(j - 1) * S], col.id[(j - 1) * S])) {
+                    col.t[j * S] = col.t[(j - 1) * S];
+                    col.id[j * S] = col.id[(j - 1) * S];
+                    col.obj[j * S] = col.obj[(j - 1) * S];
+                    --j;
+                }
+                col.t[j * S] = t;
+                col.id[j * S] = tid;
+                col.obj[j * S] = obj;
             }
+            ++n;
         }
     });
-    if (!ok) atomicOr(table.status, ST_STACK_OVERFLOW);
     add_tests(tests);
-    if (table.stats) {
-        atomicAdd(&table.stats[2], 1ull);
-        if (crossings) atomicAdd(&table.stats[3], (unsigned long long)crossings);
+    if (!ok || n > kEdgeHits) return false;
+    EdgeWalk w;
+    int32_t last = INT_MIN;
+    for (int j = 0; j < n; ++j) {
+        if (!w.take(col.t[j * S], table.max_hits, table.next_float)) continue;
+        const int32_t obj = col.obj[j * S];
+        if (obj == last) continue;
+        last = obj;
+        insert_sources(table, src, nsrc, obj, swap);
     }
+    count_edge(table, w.n);
+    return true;
 }
 
-template <int STACK>
-__device__ __forceinline__ void edge_ray(const float* __restrict__ starts, const float* __restrict__ ends,
-                                         const int32_t* __restrict__ offsets, const int32_t* __restrict__ counts,
-                                         const int32_t* __restrict__ sources, uint64_t i,
-                                         const BNode* __restrict__ nodes, uint32_t max_steps,
-                                         const float4* __restrict__ tris, int swap, const PairTable& table) {
-    segment_ray<STACK>(starts[3 * i], starts[3 * i + 1], starts[3 * i + 2], ends[3 * i], ends[3 * i + 1],
-                       ends[3 * i + 2], sources + offsets[i], counts[i], nodes, max_steps, tris, swap, table);
+// Long path: the reference's loop itself.  Each round traverses [t_min, len + 1e-6] for
+// the smallest (t, id) and the walk takes it; every round takes a hit beyond the
+// previous one, so the rounds end.  Stack of kStack entries per thread.
+__device__ __forceinline__ void segment_long(Ray r, const int32_t* __restrict__ src, int nsrc,
+                                             const BNode* __restrict__ nodes, uint32_t max_steps,
+                                             const float4* __restrict__ tris, int swap, const PairTable& table) {
+    EdgeWalk w;
+    int32_t last = INT_MIN;
+    while (!w.done) {
+        r.tmin = w.thr;
+        float bt = INFINITY;
+        uint32_t bid = 0xffffffffu;
+        int32_t bobj = -1;
+        bool found = false;
+        const bool ok = traverse<-1, kStack>(nodes, max_steps, r, [&](int first, int cnt) {
+            for (int k = first; k < first + cnt; ++k) {
+                float a[3], b[3], c[3];
+                uint32_t tid;
+                int32_t obj;
+                load_tri(tris, k, a, b, c, tid, obj);
+                float t;
+                if (!hit_triangle<-1>(r, a, b, c, t)) continue;
+                if (!found || hit_less(t, tid, bt, bid)) {
+                    found = true;
+                    bt = t;
+                    bid = tid;
+                    bobj = obj;
+                }
+            }
+        });
+        if (!ok) {
+            atomicOr(table.status, ST_STACK_OVERFLOW);
+            break;
+        }
+        if (!found) break;
+        w.take(bt, table.max_hits, table.next_float);
+        if (bobj != last) {
+            last = bobj;
+            insert_sources(table, src, nsrc, bobj, swap);
+        }
+    }
+    count_edge(table, w.n);
 }
 
-// Edge e of triangle t of a source mesh, in the triangle's own orientation (v0v1, v1v2,
-// v2v0), with the triangle's object as its one source: the legacy per-triangle overlap
-// (mesh_overlap.cu:126-179), which traces shared edges once per triangle.
+// Edge i of a .pre edge payload (starts/ends float3, offsets/counts into sources).
+struct EdgePayload {
+    const float* starts;
+    const float* ends;
+    const int32_t* offsets;
+    const int32_t* counts;
+    const int32_t* sources;
+};
+
 template <int STACK>
-__device__ __forceinline__ void triangle_edge_ray(const float* __restrict__ V, const uint32_t* __restrict__ I,
-                                                  const int32_t* __restrict__ T, uint64_t r,
-                                                  const BNode* __restrict__ nodes, uint32_t max_steps,
-                                                  const float4* __restrict__ tris, int swap, const PairTable& table) {
+__device__ __forceinline__ bool edge_ray_fast(const EdgeColumn& col, const EdgePayload& p, uint64_t i,
+                                              const BNode* __restrict__ nodes, uint32_t max_steps,
+                                              const float4* __restrict__ tris, int swap, const PairTable& table) {
+    Ray r;
+    if (!segment_ray_of(p.starts[3 * i], p.starts[3 * i + 1], p.starts[3 * i + 2], p.ends[3 * i], p.ends[3 * i + 1],
+                        p.ends[3 * i + 2], r))
+        return true;
+    return segment_fast<STACK>(col, r, p.sources + p.offsets[i], p.counts[i], nodes, max_steps, tris, swap, table);
+}
+
+__device__ __forceinline__ void edge_ray_long(const EdgePayload& p, uint64_t i, const BNode* __restrict__ nodes,
+                                              uint32_t max_steps, const float4* __restrict__ tris, int swap,
+                                              const PairTable& table) {
+    Ray r;
+    if (!segment_ray_of(p.starts[3 * i], p.starts[3 * i + 1], p.starts[3 * i + 2], p.ends[3 * i], p.ends[3 * i + 1],
+                        p.ends[3 * i + 2], r))
+        return;
+    segment_long(r, p.sources + p.offsets[i], p.counts[i], nodes, max_steps, tris, swap, table);
+}
+
+// Record r = 3 t + e: edge e of triangle t of a source mesh, in the triangle's own
+// orientation (v0v1, v1v2, v2v0), with the triangle's object as its one source -- the
+// legacy per-triangle overlap (mesh_overlap.cu:126-179), which traces shared edges once
+// per triangle.
+__device__ __forceinline__ bool triangle_edge_of(const float* __restrict__ V, const uint32_t* __restrict__ I,
+                                                 uint64_t r, Ray& ray) {
     const uint64_t t = r / 3;
     const int e = (int)(r % 3);
     const uint64_t a = I[3 * t + e], b = I[3 * t + (e == 2 ? 0 : e + 1)];
-    segment_ray<STACK>(V[3 * a], V[3 * a + 1], V[3 * a + 2], V[3 * b], V[3 * b + 1], V[3 * b + 2], T + t, 1, nodes,
-                       max_steps, tris, swap, table);
+    return segment_ray_of(V[3 * a], V[3 * a + 1], V[3 * a + 2], V[3 * b], V[3 * b + 1], V[3 * b + 2], ray);
 }
 
 }  // namespace

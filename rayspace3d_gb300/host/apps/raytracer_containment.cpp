@@ -135,6 +135,9 @@ int main(int argc, char* argv[]) {
     dB.uploadEdges(gB);
     rs_pairset *psO = nullptr, *psC = nullptr;
     check(rs_pairset_create(1 << 20, 1, &psO, nullptr), "rs_pairset_create");
+    // __raygen__check_edges (mesh_containment.cu:99-170): t_min moves to the next float after
+    // each hit, at most 256 traces per edge.
+    check(rs_pairset_set_edge_rule(psO, 256, 1), "rs_pairset_set_edge_rule");
     check(rs_pairset_create(1 << 20, 1, &psC, nullptr), "rs_pairset_create");
     timer.next("Warmup");
     if (opt.warmupRuns > 0) {

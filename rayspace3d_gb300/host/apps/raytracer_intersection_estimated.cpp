@@ -3,10 +3,13 @@
 // `raytracer_intersection_estimated` (query/src/applications/raytracer_intersection_estimated_main.cpp:212-760):
 // same flags, phases, manual measurements, counters, intersection_pairs.csv
 // (a_object_id,b_object_id; here sorted by (a, b)), intersection_pair_hits.csv and
-// intersection_containment_tracking.csv.  --containment-max-iterations and
-// --use-anyhit-containment are accepted; the engine's containment ray always collects
-// every crossing in one traversal (the any-hit path), so the tracking CSV reports one
-// iteration per ray.
+// intersection_containment_tracking.csv.  --overlap-max-iterations caps the hits each
+// edge ray takes (rs_pairset_set_edge_rule), as in trace_edge_multi_hits
+// (mesh_intersection.cu:16-91).  --containment-max-iterations and --use-anyhit-containment
+// are accepted: the reference always runs the any-hit containment path
+// (useAnyhitContainment is never false, raytracer_intersection_estimated_main.cpp:227,280),
+// which ignores the iteration cap, and the engine's containment ray likewise collects every
+// crossing in one traversal, so the tracking CSV reports one iteration per ray.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -39,8 +42,9 @@ int main(int argc, char* argv[]) {
                    {"--epsilon <float>", "Estimation epsilon (default: 0.001)"},
                    {"--estimate-only", "Run only selectivity estimation"},
                    {"--query-direction <both|mesh1_to_mesh2|mesh2_to_mesh1>", "Control query direction (default: both)"},
-                   {"--overlap-max-iterations <int>", "Accepted (the engine traces every crossing)"},
-                   {"--containment-max-iterations <int>", "Accepted (the engine traces every crossing)"},
+                   {"--overlap-max-iterations <int>", "Overlap ray iteration cap (default: 100)"},
+                   {"--containment-max-iterations <int>",
+                    "Accepted (the any-hit containment path, always on, has no iteration cap)"},
                    {"--use-anyhit-containment", "Accepted (the engine's containment is the any-hit path)"},
                    {"--hash-load-factor <float>", "Hash load factor in (0,1] (default: 0.5)"},
                    {"--enable-profiling-stats", "Enable device-side profiling counters"},
@@ -161,6 +165,7 @@ int main(int argc, char* argv[]) {
     rs_pairset* ps = nullptr;
     check(rs_pairset_create(tableSize, 0, &ps, nullptr), "rs_pairset_create");
     rs_pairset_set_tracking(ps, profiling ? 1 : 0);
+    check(rs_pairset_set_edge_rule(ps, overlapMax, 0), "rs_pairset_set_edge_rule");
     // Per-source tracking buffers (PairHitTracking.h: 256 targets per source).
     constexpr int kMaxTargets = 256;
     int32_t maxObj1 = -1, maxObj2 = -1;
@@ -219,6 +224,7 @@ int main(int argc, char* argv[]) {
             rs_pairset_destroy(ps);
             check(rs_pairset_create(cap * 4 + 1, 0, &ps, nullptr), "rs_pairset_create");
             rs_pairset_set_tracking(ps, profiling ? 1 : 0);
+            check(rs_pairset_set_edge_rule(ps, overlapMax, 0), "rs_pairset_set_edge_rule");
             std::cout << "Pair table full: growing it to " << (cap * 4 + 1) << " slots and rerunning" << std::endl;
             continue;
         }

@@ -407,6 +407,19 @@ def cube_mesh(lo, hi) -> Tuple[np.ndarray, np.ndarray]:
     return V, _CUBE_F.copy()
 
 
+def box_set(boxes, edges: bool = True, grid_resolution: int = 0) -> Geometry:
+    """One object per axis-aligned box (lo, hi), in the given order (grid statistics over the
+    vertices' bounds when grid_resolution > 0)."""
+    Vs, Is, Ts = [], [], []
+    for k, (lo, hi) in enumerate(boxes):
+        V, F = cube_mesh(lo, hi)
+        Is.append(F + 8 * k)
+        Vs.append(V)
+        Ts.append(np.full(len(F), k, np.int32))
+    return make_geometry(np.concatenate(Vs), np.concatenate(Is), np.concatenate(Ts), edges=edges,
+                         grid_resolution=grid_resolution)
+
+
 def cube_grid(nx: int, ny: int, nz: int, size: float = 1.0, origin=(0.0, 0.0, 0.0), edges: bool = True,
               grid_resolution: int = 0) -> Geometry:
     """nx*ny*nz unit cubes that share faces with their neighbours, one object each."""

@@ -225,7 +225,7 @@ def test_estimator_matches_oracle(cuda):
     cv = api.cell_volume(A.grid)
     ca = np.ascontiguousarray(A.grid.cells)
     cb = np.ascontiguousarray(B.grid.cells)
-    f = _lib.load().estimateOverlapSelectivity(ca.ctypes.data, cb.ctypes.data, len(ca), cv, 0.001, 0.8)
+    f = _lib.load().rs_estimate_overlap_selectivity(ca.ctypes.data, cb.ctypes.data, len(ca), cv, 0.001, 0.8)
     assert f == pytest.approx(want_raw, rel=1e-5)
 
 
