@@ -66,17 +66,6 @@ int rs_bvh_destroy(rs_bvh* bvh);
 int rs_bvh_build_async(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
                        const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream);
 int rs_bvh_wait(const rs_bvh* bvh);
-/* The same BVH contract built per cluster (no counterpart in the reference): the triangles
- * come as n_clusters consecutive ranges, cluster c = [d_cluster_starts[c],
- * d_cluster_starts[c+1]) (device array of n_clusters + 1 entries, first 0, last nF), each of
- * 1..512 triangles, normally the runs of one object.  One block builds each cluster's tree
- * in shared memory and a radix tree over the cluster boxes joins them: no sort over all
- * triangles.  Query results are those of rs_bvh_build (the tree shape differs).  Cluster
- * ranges that are empty, longer than 512 or not a partition of [0, nF) make the build fail
- * with RS_ERR_INVALID.  asynchronous != 0: as rs_bvh_build_async. */
-int rs_bvh_build_clustered(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
-                           const int32_t* d_tri2obj, const uint32_t* d_cluster_starts, uint64_t n_clusters,
-                           int leaf_size, int asynchronous, rs_bvh** out, void* stream);
 /* Number of triangles, nodes, engine-owned device bytes, and the bounds of all vertices. */
 int rs_bvh_info(const rs_bvh* bvh, uint64_t* n_tri, uint64_t* n_nodes, uint64_t* bytes,
                 float* h_min3, float* h_max3);
@@ -373,6 +362,15 @@ int rs_mlp_set_gemm(int mode);
  * K % 64 == 0, 16-byte aligned operands and lda, ldb multiples of 8), mode 1 mma.sync. */
 int rs_mlp_gemm(const void* d_A, int lda, const void* d_B, int ldb, float* d_C, int ldc, int M, int N, int K,
                 int mode, void* stream);
+/* Decoupled weight decay of W1, W2 and W3 in rs_mlp_train_step (default 0; no counterpart
+ * in the reference). */
+int rs_mlp_set_weight_decay(rs_mlp* mlp, float weight_decay);
+/* Grid-estimator prior (no counterpart in the reference): with on != 0, rs_estimate_mlp
+ * adds the network's output to log1p(grid estimate) of the same two grids (rs_estimate_grid
+ * with cell_volume, epsilon, gamma, then rs_estimate_pairs_from_raw with alpha_correction),
+ * so the network is trained on the correction of the grid estimator rather than on the
+ * count itself.  Off by default. */
+int rs_mlp_set_prior(rs_mlp* mlp, int on, float cell_volume, float epsilon, float gamma, int alpha_correction);
 /* Estimated pair count of two grids (expm1 of the prediction, rounded; h_log1p nullable). */
 int rs_estimate_mlp(rs_mlp* mlp, const void* d_cellsA, const void* d_cellsB, int resolution, int64_t* h_estimate,
                     double* h_log1p, void* stream);

@@ -37,7 +37,6 @@ SIGNATURES = {
     "rs_status_string": (ctypes.c_char_p, [I]),
     "rs_bvh_build": (I, [P, U64, P, U64, P, I, PP, P]),
     "rs_bvh_build_async": (I, [P, U64, P, U64, P, I, PP, P]),
-    "rs_bvh_build_clustered": (I, [P, U64, P, U64, P, P, U64, I, I, PP, P]),
     "rs_bvh_wait": (I, [P]),
     "rs_bvh_destroy": (I, [P]),
     "rs_bvh_info": (I, [P, PU64, PU64, PU64, P, P]),
@@ -82,6 +81,8 @@ SIGNATURES = {
     "rs_mlp_set_params": (I, [P, ctypes.POINTER(F)]),
     "rs_mlp_features": (I, [P, P, I, P, P]),
     "rs_mlp_gemm": (I, [P, I, P, I, P, I, I, I, I, I, P]),
+    "rs_mlp_set_weight_decay": (I, [P, F]),
+    "rs_mlp_set_prior": (I, [P, I, F, F, F, I]),
     "rs_mlp_set_gemm": (I, [I]),
     "rs_mlp_forward": (I, [P, P, I, P, P]),
     "rs_mlp_gradients": (I, [P, P, P, I, ctypes.POINTER(F), P]),

@@ -44,23 +44,8 @@ def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
     return t.data_ptr()
 
 
-MAX_CLUSTER = 512  # largest cluster of rs_bvh_build_clustered
-
-
-def cluster_starts(tri2obj: np.ndarray, max_size: int = MAX_CLUSTER) -> Optional[np.ndarray]:
-    """Starts of the runs of equal object ids (n_runs + 1 entries, last = number of
-    triangles) when every run has at most max_size triangles, else None."""
-    t = np.asarray(tri2obj)
-    if len(t) == 0:
-        return None
-    heads = np.flatnonzero(np.concatenate(([True], t[1:] != t[:-1])))
-    starts = np.concatenate((heads, [len(t)])).astype(np.uint32)
-    return starts if int(np.diff(starts).max()) <= max_size else None
-
-
 class DeviceGeometry:
-    """One .pre geometry set resident on the GPU (vertices, indices, tri2obj, edges, grid;
-    the cluster starts of the clustered BVH build on first use)."""
+    """One .pre geometry set resident on the GPU (vertices, indices, tri2obj, edges, grid)."""
 
     def __init__(self, g: Geometry, device: str = "cuda"):
         self.host = g
@@ -98,22 +83,7 @@ class DeviceGeometry:
         self.edges = tuple(t.contiguous() for t in edges) if edges is not None else None
         self.nE = int(self.edges[0].shape[0]) if self.edges is not None else 0
         self.cells = cells
-        self._clusters = None
         return self
-
-    @property
-    def clusters(self) -> Optional[torch.Tensor]:
-        """Cluster starts for rs_bvh_build_clustered (uint32 bits in an int32 tensor on the
-        geometry's device), computed from the host object ids on first use; None when the
-        objects are not stored together in runs of at most 512 triangles."""
-        if not hasattr(self, "_clusters"):
-            cs = cluster_starts(self.host.tri2obj) if getattr(self, "host", None) is not None else None
-            self._clusters = None if cs is None else torch.from_numpy(cs.view(np.int32)).to(self.V.device)
-        return self._clusters
-
-    @clusters.setter
-    def clusters(self, value: Optional[torch.Tensor]) -> None:
-        self._clusters = value
 
     def edge_ptrs(self):
         if self.edges is None:
@@ -130,28 +100,16 @@ class DeviceGeometry:
 class Bvh:
     """Engine-owned BVH over a DeviceGeometry (which must stay alive)."""
 
-    def __init__(self, geom: DeviceGeometry, leaf_size: int = 0, stream=None, asynchronous: bool = False,
-                 clustered: bool = False):
+    def __init__(self, geom: DeviceGeometry, leaf_size: int = 0, stream=None, asynchronous: bool = False):
         """asynchronous=True queues the build on `stream` and returns at once (rs_bvh_build_async);
-        queries are ordered after it, wait() reports its status.  clustered=True builds per
-        cluster (rs_bvh_build_clustered) with the geometry's cluster starts; the build over all
-        triangles is the default, being the faster of the two on GB300 so far."""
+        queries are ordered after it, wait() reports its status."""
         self.geom = geom
         h = ctypes.c_void_p()
         L = _lib.load()
-        cs = getattr(geom, "clusters", None)
-        if clustered:
-            if cs is None:
-                raise ValueError("geometry has no cluster starts (objects not stored together or over 512 triangles)")
-            _check(L.rs_bvh_build_clustered(_ptr(geom.V), geom.nV, _ptr(geom.I), geom.nF, _ptr(geom.T), _ptr(cs),
-                                            int(cs.shape[0]) - 1, leaf_size, int(asynchronous), ctypes.byref(h),
-                                            _stream(stream)), "rs_bvh_build_clustered")
-        else:
-            fn = L.rs_bvh_build_async if asynchronous else L.rs_bvh_build
-            _check(fn(_ptr(geom.V), geom.nV, _ptr(geom.I), geom.nF, _ptr(geom.T), leaf_size, ctypes.byref(h),
-                      _stream(stream)), "rs_bvh_build")
+        fn = L.rs_bvh_build_async if asynchronous else L.rs_bvh_build
+        _check(fn(_ptr(geom.V), geom.nV, _ptr(geom.I), geom.nF, _ptr(geom.T), leaf_size, ctypes.byref(h),
+                  _stream(stream)), "rs_bvh_build")
         self.handle = h
-        self.clustered = bool(clustered)
 
     def wait(self):
         _check(_lib.load().rs_bvh_wait(self.handle), "rs_bvh_wait")

@@ -503,359 +503,6 @@ __global__ void k_empty_root(BNode* nodes) {
     nodes[0] = nd;
 }
 
-// ---- Clustered build -----------------------------------------------------------------
-// The triangles come in clusters, consecutive ranges [starts[c], starts[c+1]) of 1..kCluster
-// triangles (the runs of one object).  One block builds a cluster's tree in shared memory:
-// Morton codes of the triangle box centres in the cluster's box, a bitonic sort, the Karras
-// radix tree over the sorted codes (Karras 2012, "Maximizing Parallelism in the Construction
-// of BVHs, Octrees, and k-d Trees"), and the boxes bottom-up, each split's box computed by
-// whichever of its children arrives second.  A second radix tree over the clusters (Morton
-// codes of their box centres in the bounds of all vertices) joins the cluster trees.  Node
-// slots: top split p at slot p (the root at 0), split k of cluster c at n_c - 1 + starts[c]
-// + k; a subtree of <= leaf triangles is entered as a leaf by its parent and gets no slot.
-constexpr int kCluster = 512;
-constexpr int kCT = 128;
-
-// Length of the common prefix of keys a and b of a sorted array of n distinct keys, -1 when
-// b is outside [0, n).
-__device__ __forceinline__ int key_delta(const uint64_t* keys, int n, int a, int b) {
-    return (b < 0 || b >= n) ? -1 : __clzll((long long)(keys[a] ^ keys[b]));
-}
-
-// Karras' split k of n sorted distinct keys: its key range [*lo, *hi] and its children, a
-// split index >= 0 or ~(leaf position) for a single key.
-__device__ __forceinline__ void karras_split(const uint64_t* keys, int n, int k, int* lo, int* hi, int* left,
-                                             int* right) {
-    const int d = key_delta(keys, n, k, k + 1) > key_delta(keys, n, k, k - 1) ? 1 : -1;
-    const int dmin = key_delta(keys, n, k, k - d);
-    int lmax = 2;
-    while (key_delta(keys, n, k, k + lmax * d) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (key_delta(keys, n, k, k + (l + t) * d) > dmin) l += t;
-    const int j = k + l * d;
-    const int dnode = key_delta(keys, n, k, j);
-    int sp = 0, t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (key_delta(keys, n, k, k + (sp + t) * d) > dnode) sp += t;
-    } while (t > 1);
-    const int g = k + sp * d + min(d, 0);
-    *lo = min(k, j);
-    *hi = max(k, j);
-    *left = *lo == g ? ~g : g;
-    *right = *hi == g + 1 ? ~(g + 1) : g + 1;
-}
-
-__device__ __forceinline__ uint32_t morton_key32(const float c[3], const float lo[3], const float hi[3], const float scale[3]) {
-    uint32_t q[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float ext = hi[k] - lo[k];
-        float u = ext > 0.0f ? (c[k] - lo[k]) / ext : 0.0f;
-        u = fminf(fmaxf(u, 0.0f), 1.0f);
-        q[k] = (uint32_t)fminf(u * scale[k], scale[k] - 1.0f);
-    }
-    return ((q[0] >> 10) << 31) | ((q[1] >> 10) << 30) | (spread10(q[0]) << 2) | (spread10(q[1]) << 1) |
-           spread10(q[2]);
-}
-
-// One block per cluster.  Writes the cluster's leaf triangles (sorted order, at its own
-// range of tris), its splits larger than `leaf`, its object boxes (into obox, as k_morton),
-// and its record: box, entry (leaf range or root slot) and key (Morton code of the box
-// centre << 32 | c).  A cluster range that is empty, too long or not a partition of [0, nF)
-// sets flags bit 0 and writes nothing.
-__global__ void __launch_bounds__(kCT) k_cluster_build(const float* __restrict__ V, uint64_t nV,
-                                                      const uint32_t* __restrict__ I, const int32_t* __restrict__ T,
-                                                      const uint32_t* __restrict__ starts, int n_c, int nF, int leaf,
-                                                      const int* __restrict__ bounds, unsigned int* __restrict__ flags,
-                                                      int* __restrict__ obox, uint64_t obox_cap,
-                                                      float4* __restrict__ tris, BNode* __restrict__ nodes,
-                                                      float* __restrict__ cbox, int2* __restrict__ centry,
-                                                      uint64_t* __restrict__ ckey) {
-    __shared__ uint64_t s_key[kCluster];
-    __shared__ float s_box[6][kCluster];   // triangle boxes, by position in the cluster's range
-    __shared__ float s_nbox[6][kCluster];  // split boxes
-    __shared__ short s_l[kCluster], s_r[kCluster], s_lo[kCluster], s_hi[kCluster];
-    __shared__ short s_par[2 * kCluster];  // parent split of split k at [k], of sorted leaf i at [kCluster + i]
-    __shared__ int s_cnt[kCluster];
-    __shared__ int s_red[6];
-    const int c = blockIdx.x, tid = threadIdx.x;
-    const uint32_t s = starts[c], e = starts[c + 1];
-    const bool ok = e > s && e - s <= (uint32_t)kCluster && e <= (uint32_t)nF && (c > 0 || s == 0) &&
-                    (c < n_c - 1 || e == (uint32_t)nF);
-    if (!ok) {  // the same for every thread of the block; an empty record keeps k_top_* in bounds
-        if (tid == 0) {
-            atomicOr(flags, 1u);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                cbox[6 * (uint64_t)c + k] = INFINITY;
-                cbox[6 * (uint64_t)c + 3 + k] = -INFINITY;
-            }
-            centry[c] = make_int2(0, 0);
-            ckey[c] = (uint64_t)(uint32_t)c;
-        }
-        return;
-    }
-    const int n = (int)(e - s);
-    if (tid < 6) s_red[tid] = tid < 3 ? 0x7fffffff : (int)0x80000000;
-    __syncthreads();
-    const float inf = INFINITY;
-    float clo[3] = {inf, inf, inf}, chi[3] = {-inf, -inf, -inf};
-    for (int b0 = 0; b0 < n; b0 += kCT) {
-        const int i = b0 + tid;
-        if (i < n) {
-            const uint64_t t = s + (uint64_t)i;
-            if (I[3 * t] >= nV || I[3 * t + 1] >= nV || I[3 * t + 2] >= nV) atomicOr(flags, 1u);
-            float lo[3], hi[3];
-            tri_box(V, nV, I, t, lo, hi);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                s_box[k][i] = lo[k];
-                s_box[3 + k][i] = hi[k];
-                clo[k] = fminf(clo[k], lo[k]);
-                chi[k] = fmaxf(chi[k], hi[k]);
-            }
-            if (obox) {
-                const int32_t o = T[t];
-                int v[6] = {flt_ord(lo[0]), flt_ord(lo[1]), flt_ord(lo[2]), flt_ord(hi[0]), flt_ord(hi[1]),
-                            flt_ord(hi[2])};
-                const unsigned int peers = __match_any_sync(__activemask(), o);
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    v[k] = __reduce_min_sync(peers, v[k]);
-                    v[3 + k] = __reduce_max_sync(peers, v[3 + k]);
-                }
-                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && o >= 0 && (uint64_t)o < obox_cap) {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        atomicMin(&obox[6 * (uint64_t)o + k], v[k]);
-                        atomicMax(&obox[6 * (uint64_t)o + 3 + k], v[3 + k]);
-                    }
-                }
-            }
-        }
-    }
-    {
-        int v[6] = {flt_ord(clo[0]), flt_ord(clo[1]), flt_ord(clo[2]), flt_ord(chi[0]), flt_ord(chi[1]),
-                    flt_ord(chi[2])};
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            v[k] = __reduce_min_sync(0xffffffffu, v[k]);
-            v[3 + k] = __reduce_max_sync(0xffffffffu, v[3 + k]);
-        }
-        if ((tid & 31) == 0) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                atomicMin(&s_red[k], v[k]);
-                atomicMax(&s_red[3 + k], v[3 + k]);
-            }
-        }
-    }
-    __syncthreads();
-    float cl[3], ch[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        cl[k] = ord_flt(s_red[k]);
-        ch[k] = ord_flt(s_red[3 + k]);
-    }
-    // Keys: 30-bit Morton code in the cluster box << 9 | position (distinct), padded to m.
-    int m = 1;
-    while (m < n) m <<= 1;
-    const float lscale[3] = {1024.0f, 1024.0f, 1024.0f};
-    for (int i = tid; i < m; i += kCT) {
-        uint64_t key = ~0ull;
-        if (i < n) {
-            const float cc[3] = {0.5f * s_box[0][i] + 0.5f * s_box[3][i], 0.5f * s_box[1][i] + 0.5f * s_box[4][i],
-                                 0.5f * s_box[2][i] + 0.5f * s_box[5][i]};
-            key = ((uint64_t)(morton_key32(cc, cl, ch, lscale) & 0x3fffffffu) << 9) | (uint64_t)i;
-        }
-        s_key[i] = key;
-    }
-    __syncthreads();
-    for (int k = 2; k <= m; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < m; i += kCT) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const uint64_t a = s_key[i], b = s_key[ixj];
-                    if ((a > b) == ((i & k) == 0)) {
-                        s_key[i] = b;
-                        s_key[ixj] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    // Radix tree over the n sorted keys.
-    for (int k = tid; k < n - 1; k += kCT) {
-        int lo, hi, left, right;
-        karras_split(s_key, n, k, &lo, &hi, &left, &right);
-        s_lo[k] = (short)lo;
-        s_hi[k] = (short)hi;
-        s_l[k] = (short)left;
-        s_r[k] = (short)right;
-        s_par[left < 0 ? kCluster + ~left : left] = (short)k;
-        s_par[right < 0 ? kCluster + ~right : right] = (short)k;
-        s_cnt[k] = 0;
-    }
-    if (tid == 0) {
-        s_par[0] = -1;  // split 0 is the root
-        if (n == 1) s_par[kCluster] = -1;
-    }
-    __syncthreads();
-    // Boxes bottom-up: the second child to arrive at a split computes its box.
-    volatile float* nb = &s_nbox[0][0];
-    for (int i = tid; i < n; i += kCT) {
-        int p = s_par[kCluster + i];
-        while (p >= 0) {
-            __threadfence_block();
-            if (atomicAdd(&s_cnt[p], 1) == 0) break;
-            __threadfence_block();
-            float lo[3], hi[3];
-#pragma unroll
-            for (int side = 0; side < 2; ++side) {
-                const int chd = side == 0 ? s_l[p] : s_r[p];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    float a, b;
-                    if (chd < 0) {
-                        const int li = (int)(s_key[~chd] & 511u);
-                        a = s_box[k][li];
-                        b = s_box[3 + k][li];
-                    } else {
-                        a = nb[k * kCluster + chd];
-                        b = nb[(3 + k) * kCluster + chd];
-                    }
-                    lo[k] = side == 0 ? a : fminf(lo[k], a);
-                    hi[k] = side == 0 ? b : fmaxf(hi[k], b);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                nb[k * kCluster + p] = lo[k];
-                nb[(3 + k) * kCluster + p] = hi[k];
-            }
-            p = s_par[p];
-        }
-    }
-    __syncthreads();
-    // Leaf triangles in sorted order.
-    const uint64_t last = nV - 1;
-    for (int i = tid; i < n; i += kCT) {
-        const uint64_t t = s + (s_key[i] & 511u);
-        const uint64_t i0 = min((uint64_t)I[3 * t], last), i1 = min((uint64_t)I[3 * t + 1], last),
-                       i2 = min((uint64_t)I[3 * t + 2], last);
-        const uint64_t j = s + (uint64_t)i;
-        tris[3 * j] = make_float4(V[3 * i0], V[3 * i0 + 1], V[3 * i0 + 2], __uint_as_float((uint32_t)t));
-        tris[3 * j + 1] = make_float4(V[3 * i1], V[3 * i1 + 1], V[3 * i1 + 2], __int_as_float(T[t]));
-        tris[3 * j + 2] = make_float4(V[3 * i2], V[3 * i2 + 1], V[3 * i2 + 2], 0.0f);
-    }
-    // Splits larger than a leaf.
-    const int base = n_c - 1 + (int)s;
-    for (int k = tid; k < n - 1; k += kCT) {
-        if (s_hi[k] - s_lo[k] + 1 <= leaf) continue;
-        float lo[2][3], hi[2][3];
-        int idx[2], cnt[2];
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const int chd = side == 0 ? s_l[k] : s_r[k];
-            const int a = chd < 0 ? ~chd : s_lo[chd], b = chd < 0 ? ~chd : s_hi[chd];
-            const bool is_leaf = b - a + 1 <= leaf;
-            idx[side] = is_leaf ? (int)s + a : base + chd;
-            cnt[side] = is_leaf ? b - a + 1 : 0;
-            const int li = chd < 0 ? (int)(s_key[~chd] & 511u) : 0;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                lo[side][q] = chd < 0 ? s_box[q][li] : s_nbox[q][chd];
-                hi[side][q] = chd < 0 ? s_box[3 + q][li] : s_nbox[3 + q][chd];
-            }
-        }
-        store_node(nodes + base + k, lo[0], hi[0], idx[0], cnt[0], lo[1], hi[1], idx[1], cnt[1]);
-    }
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            cbox[6 * (uint64_t)c + k] = cl[k];
-            cbox[6 * (uint64_t)c + 3 + k] = ch[k];
-        }
-        centry[c] = n <= leaf ? make_int2((int)s, n) : make_int2(base, 0);
-        float vlo[3], vhi[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            vlo[k] = ord_flt(bounds[6 + k]);
-            vhi[k] = ord_flt(bounds[9 + k]);
-        }
-        const float cc[3] = {0.5f * cl[0] + 0.5f * ch[0], 0.5f * cl[1] + 0.5f * ch[1], 0.5f * cl[2] + 0.5f * ch[2]};
-        const float gscale[3] = {2048.0f, 2048.0f, 1024.0f};
-        ckey[c] = ((uint64_t)morton_key32(cc, vlo, vhi, gscale) << 32) | (uint32_t)c;
-    }
-}
-
-// Top radix tree over the n_c sorted cluster keys: children and parents of each split.
-__global__ void k_top_splits(const uint64_t* __restrict__ keys, int n_c, int2* __restrict__ child,
-                             int* __restrict__ par, int* __restrict__ leaf_par) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_c - 1) return;
-    int lo, hi, left, right;
-    karras_split(keys, n_c, k, &lo, &hi, &left, &right);
-    child[k] = make_int2(left, right);
-    if (left < 0) leaf_par[~left] = k; else par[left] = k;
-    if (right < 0) leaf_par[~right] = k; else par[right] = k;
-    if (k == 0) par[0] = -1;
-}
-
-// Boxes and nodes of the top splits, bottom-up from the clusters: the second child to
-// arrive at a split writes it (slot = split index) and walks on.
-__global__ void k_top_nodes(const uint64_t* __restrict__ keys, int n_c, const int2* __restrict__ child,
-                            const int* __restrict__ par, const int* __restrict__ leaf_par,
-                            const float* __restrict__ cbox, const int2* __restrict__ centry,
-                            float* __restrict__ tbox, unsigned int* __restrict__ arrived, BNode* __restrict__ nodes) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n_c) return;
-    int p = leaf_par[q];
-    while (p >= 0) {
-        __threadfence();
-        if (atomicAdd(&arrived[p], 1u) == 0) break;
-        __threadfence();
-        const int2 ch = child[p];
-        float lo[2][3], hi[2][3];
-        int idx[2], cnt[2];
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const int chd = side == 0 ? ch.x : ch.y;
-            if (chd < 0) {
-                // The low word is a cluster index; the clamp only matters after a failed sort.
-                const uint32_t cl = min((uint32_t)(keys[~chd] & 0xffffffffull), (uint32_t)(n_c - 1));
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    lo[side][k] = cbox[6 * (uint64_t)cl + k];
-                    hi[side][k] = cbox[6 * (uint64_t)cl + 3 + k];
-                }
-                const int2 en = centry[cl];
-                idx[side] = en.x;
-                cnt[side] = en.y;
-            } else {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    lo[side][k] = __ldcg(&tbox[6 * (uint64_t)chd + k]);
-                    hi[side][k] = __ldcg(&tbox[6 * (uint64_t)chd + 3 + k]);
-                }
-                idx[side] = chd;
-                cnt[side] = 0;
-            }
-        }
-        store_node(nodes + p, lo[0], hi[0], idx[0], cnt[0], lo[1], hi[1], idx[1], cnt[1]);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            tbox[6 * (uint64_t)p + k] = fminf(lo[0][k], lo[1][k]);
-            tbox[6 * (uint64_t)p + 3 + k] = fmaxf(hi[0][k], hi[1][k]);
-        }
-        p = par[p];
-    }
-}
-
 template <class T>
 cudaError_t alloc(T** p, size_t count, cudaStream_t s) {
     return dmalloc((void**)p, (count ? count : 1) * sizeof(T), s);
@@ -937,11 +584,8 @@ static void bvh_free(rs_bvh* h) {
     delete h;
 }
 
-// d_cstarts (n_c + 1 cluster starts) selects the clustered build, else the LBVH over all
-// triangles.
 static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
-                      const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, cudaStream_t s, bool async,
-                      const uint32_t* d_cstarts = nullptr, uint64_t n_c = 0) {
+                      const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, cudaStream_t s, bool async) {
 
     if (!out) return RS_ERR_INVALID;
     *out = nullptr;
@@ -952,9 +596,6 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     // trace fastest on dense joins (4 doubles the edge-ray time at selectivity 1e-4).
     if (leaf_size == 0) leaf_size = 2;
     if (leaf_size < 1 || leaf_size > 16) return RS_ERR_INVALID;
-    if (d_cstarts && nF && (n_c == 0 || n_c > nF || n_c >= (1ull << 30) || n_c - 1 + nF >= 0x7fffffffull))
-        return RS_ERR_INVALID;  // node slots are int32
-    if (nF == 0) d_cstarts = nullptr;
     rs_bvh* h = new rs_bvh();
     h->V = d_vertices;
     h->nV = nV;
@@ -969,15 +610,6 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     int* xchg = nullptr;
     OpenTree* open = nullptr;
     unsigned int* n_open = nullptr;
-    float* cbox = nullptr;  // clustered build: cluster records and the top tree
-    int2* centry = nullptr;
-    uint64_t* ckey = nullptr;
-    int2* tchild = nullptr;
-    int* tpar = nullptr;
-    int* tleaf = nullptr;
-    float* tbox = nullptr;
-    unsigned int* tarrived = nullptr;
-    const int nc = (int)n_c;
     cudaError_t e = cudaSuccess;
     int* slot = nullptr;
     const int grid = 4 * sm_count();
@@ -985,10 +617,7 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     // subtrees of <= leaf_size triangles become leaves.
     const int group = std::max(1, leaf_size / 2);
     const int nG = (n + group - 1) / group;
-    if (d_cstarts)
-        h->n_nodes = std::max<uint64_t>(n_c - 1 + nF, 1);  // top splits, then each cluster's
-    else
-        h->n_nodes = nG >= 2 ? (uint64_t)nG : 1;  // slot 0 = root, slot p+1 = split p
+    h->n_nodes = nG >= 2 ? (uint64_t)nG : 1;  // slot 0 = root, slot p+1 = split p
     h->n_tris = (uint64_t)n;
     const int ptok = prof_begin(P_BVH_BUILD, s);
     e = alloc(&h->nodes, h->n_nodes, s);
@@ -1001,35 +630,6 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     if (nV || nF) launch(k_vertex_bounds, grid, kT, 0, s, d_vertices, nV, d_tri2obj, nF, bounds, bounds + 13);
     if (n == 0) {
         launch(k_empty_root, 1, 1, 0, s, h->nodes);
-    } else if (d_cstarts) {
-        h->obox_cap = std::min<uint64_t>(nF, 1ull << 24);
-        e = alloc(&h->obox, 6 * h->obox_cap, s);
-        if (e == cudaSuccess) e = alloc(&cbox, 6 * (size_t)nc, s);
-        if (e == cudaSuccess) e = alloc(&centry, nc, s);
-        if (e == cudaSuccess) e = alloc(&ckey, nc, s);
-        if (e != cudaSuccess) goto fail;
-        launch(k_obox_init, 2 * sm_count(), kT, 0, s, h->obox, h->obox_cap, (const int*)(bounds + 13));
-        const int ctok = prof_begin(P_BUILD_UP, s);
-        launch(k_cluster_build, nc, kCT, 0, s, d_vertices, nV, d_indices, d_tri2obj, d_cstarts, nc, n, leaf_size,
-               (const int*)bounds, reinterpret_cast<unsigned int*>(bounds + 12), h->obox, h->obox_cap, h->tris,
-               h->nodes, cbox, centry, ckey);
-        prof_end(P_BUILD_UP, s, ctok);
-        if (nc >= 2) {
-            e = radix_sort_u64(ckey, nullptr, (size_t)nc, 64, s, 32, reinterpret_cast<uint32_t*>(bounds + 12), 2u);
-            if (e == cudaSuccess) e = alloc(&tchild, nc - 1, s);
-            if (e == cudaSuccess) e = alloc(&tpar, nc - 1, s);
-            if (e == cudaSuccess) e = alloc(&tleaf, nc, s);
-            if (e == cudaSuccess) e = alloc(&tbox, 6 * (size_t)(nc - 1), s);
-            if (e == cudaSuccess) e = alloc(&tarrived, nc - 1, s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(tarrived, 0, (size_t)(nc - 1) * sizeof(unsigned int), s);
-            if (e != cudaSuccess) goto fail;
-            launch(k_top_splits, (nc - 1 + kT - 1) / kT, kT, 0, s, (const uint64_t*)ckey, nc, tchild, tpar, tleaf);
-            launch(k_top_nodes, (nc + kT - 1) / kT, kT, 0, s, (const uint64_t*)ckey, nc, (const int2*)tchild,
-                   (const int*)tpar, (const int*)tleaf, (const float*)cbox, (const int2*)centry, tbox, tarrived,
-                   h->nodes);
-        } else if (n <= leaf_size) {
-            launch(k_one_group_root, 1, 1, 0, s, (const float4*)h->tris, n, h->nodes);
-        }
     } else {
         const Groups G{n, group, leaf_size};
         e = alloc(&keys, n, s);
@@ -1072,9 +672,6 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
 fail:
-    for (void* p : {(void*)cbox, (void*)centry, (void*)ckey, (void*)tchild, (void*)tpar, (void*)tleaf, (void*)tbox,
-                    (void*)tarrived})
-        if (p) cudaFreeAsync(p, s);
     if (keys) cudaFreeAsync(keys, s);
     if (xchg) cudaFreeAsync(xchg, s);
     if (open) cudaFreeAsync(open, s);
@@ -1116,14 +713,6 @@ extern "C" int rs_bvh_build(const float* d_vertices, uint64_t nV, const uint32_t
 extern "C" int rs_bvh_build_async(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
                                   const int32_t* d_tri2obj, int leaf_size, rs_bvh** out, void* stream) {
     return rs::build_impl(d_vertices, nV, d_indices, nF, d_tri2obj, leaf_size, out, (cudaStream_t)stream, true);
-}
-
-extern "C" int rs_bvh_build_clustered(const float* d_vertices, uint64_t nV, const uint32_t* d_indices, uint64_t nF,
-                                      const int32_t* d_tri2obj, const uint32_t* d_cluster_starts, uint64_t n_clusters,
-                                      int leaf_size, int asynchronous, rs_bvh** out, void* stream) {
-    if (nF && !d_cluster_starts) return RS_ERR_INVALID;
-    return rs::build_impl(d_vertices, nV, d_indices, nF, d_tri2obj, leaf_size, out, (cudaStream_t)stream,
-                          asynchronous != 0, d_cluster_starts, n_clusters);
 }
 
 extern "C" int rs_bvh_wait(const rs_bvh* bvh) {

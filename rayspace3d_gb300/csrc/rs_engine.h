@@ -82,10 +82,18 @@ int bvh_use(const rs_bvh* h, cudaStream_t s);
 // Builds the column grid of +e_axis rays for the handle if it does not exist yet.
 int ensure_grid(const rs_bvh* h, int axis, cudaStream_t s);
 // Broad-phase flags for one edge direction: cand[o] != 0 for source objects o that may
-// have a partner; no culling when cand is null.
+// have a partner; no culling when cand is null.  With partner lists (part != null):
+// cand[o] = the number of partner objects of the other set (0..kPartners) listed in
+// part[o * kPartners ...], or kCandAll when they were not all collected; pbox holds the
+// other set's object boxes (ordered-int min xyz, max xyz), n_pbox of them.
+constexpr int kPartners = 8;
+constexpr uint8_t kCandAll = 255;
 struct EdgeCull {
     const uint8_t* cand = nullptr;
     uint64_t n_obj = 0;
+    const int32_t* part = nullptr;
+    const int* pbox = nullptr;
+    uint64_t n_pbox = 0;
 };
 
 // Recheck statistics of the translation units that run hit tests (see rs_device.cuh).

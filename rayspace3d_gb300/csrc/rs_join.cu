@@ -32,17 +32,23 @@ constexpr int kCells = 1 << (3 * kCellBits);
 // Jobs with more edges than this are traced in live-list order (no binning): the cell
 // ranks and the ordered list would cost 8 more bytes per edge.
 constexpr uint64_t kBinMaxEdges = 1ull << 27;
+// Fewer live edges than this are traced in live-list order: the scan and the scatter would
+// cost more than the coherence saves.
+constexpr unsigned int kBinMinLive = 1u << 16;
 
 // Fast path over the edges order[0..*n_order) of a payload of n_direct edges (or over all
 // of them when order is null); the edges it defers go to deferred[0..*n_def).
 __global__ void __launch_bounds__(kT) k_edge_rays(EdgePayload p, const uint32_t* __restrict__ order,
+                                                  const uint32_t* __restrict__ live,
                                                   const unsigned int* __restrict__ n_order, uint64_t n_direct,
                                                   const BNode* __restrict__ nodes, uint32_t max_steps,
                                                   const float4* __restrict__ tris, int swap, PairTable table,
                                                   uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def) {
     __shared__ EdgeSmem<kT, kFastStack> sm;
     const EdgeColumn col = sm.column(threadIdx.x);
-    const uint64_t n = order ? (uint64_t)*n_order : n_direct;
+    const uint64_t n = live ? (uint64_t)*n_order : n_direct;
+    // The cell-ordered list when the job was binned and is long enough, else the live list.
+    if (live) order = (order && n >= kBinMinLive) ? order : live;
     for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t e = order ? order[j] : (uint32_t)j;
         if (e >= n_direct) continue;  // never, for a list of this payload's edges
@@ -103,13 +109,56 @@ __global__ void __launch_bounds__(kT) k_tri_edge_long(const float* __restrict__ 
     }
 }
 
+// Broad-phase widening (the broad phase below says why it covers every hit).
+constexpr float kCullAbs = 1e-4f;
+constexpr float kCullRel = 4e-6f;
+
+__device__ __forceinline__ float cull_margin(float l, float h) {
+    return kCullRel * (fmaxf(fabsf(l), fabsf(h)) + (h - l));
+}
+
+__device__ __forceinline__ int f2ord(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+// The box of edge i's segment widened like a broad-phase query box: kCullAbs plus the
+// relative margin of the box, per axis.
+__device__ __forceinline__ void edge_query_box(const EdgePayload& p, uint64_t i, float* qlo, float* qhi) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a = p.starts[3 * i + k], b = p.ends[3 * i + k];
+        const float l = fminf(a, b), h = fmaxf(a, b);
+        const float m = kCullAbs + cull_margin(l, h);
+        qlo[k] = l - m;
+        qhi[k] = h + m;
+    }
+}
+
+// An object box (ordered ints, min xyz then max xyz) widened by its margin overlaps the
+// (already widened) query box.
+__device__ __forceinline__ bool box_overlaps(const int* __restrict__ ob, const float* qlo, const float* qhi) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float l = ord2f(__ldg(&ob[k])), h = ord2f(__ldg(&ob[3 + k]));
+        const float m = cull_margin(l, h);
+        ok = ok && (l - m <= qhi[k]) && (h + m >= qlo[k]);
+    }
+    return ok;
+}
+
 // The edges of one source set traced against the other set's BVH, with the source
 // objects' broad-phase flags and the job's work lists.
 struct EdgeJob {
     EdgePayload p;
     uint64_t nE;
-    const uint8_t* cull;  // flag per source object below n_cull
+    const uint8_t* cull;  // flag (or partner count) per source object below n_cull
     uint64_t n_cull;
+    const int32_t* part;  // partner lists (nullable), as EdgeCull
+    const int* pbox;      // the target set's object boxes
+    uint64_t n_pbox;
     uint32_t* live;       // live edges, in arrival order
     uint32_t* rank;       // rank of each live edge within its cell; then the deferred edges
     uint32_t* order;      // live edges by cell (binned jobs)
@@ -160,9 +209,30 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
     if (i < j.nE) {
         const int ns = j.p.counts[i];
         const int32_t* sp = j.p.sources + j.p.offsets[i];
+        float qlo[3], qhi[3];
+        bool have_box = false;
         for (int q = 0; q < ns && !any; ++q) {
             const int32_t so = sp[q];
-            any = (so < 0 || (uint64_t)so >= j.n_cull) ? true : j.cull[so] != 0;
+            if (so < 0 || (uint64_t)so >= j.n_cull) {
+                any = true;
+                break;
+            }
+            const uint8_t c = j.cull[so];
+            if (c == 0) continue;
+            if (!j.part || c == kCandAll) {
+                any = true;
+                break;
+            }
+            // The edge is live when its own widened box reaches a partner's widened box.
+            if (!have_box) {
+                edge_query_box(j.p, i, qlo, qhi);
+                have_box = true;
+            }
+            const int32_t* pl = j.part + (uint64_t)so * kPartners;
+            for (int k = 0; k < (int)c && !any; ++k) {
+                const int32_t b = pl[k];
+                any = b < 0 || (uint64_t)b >= j.n_pbox || box_overlaps(j.pbox + 6 * (uint64_t)b, qlo, qhi);
+            }
         }
     }
     const unsigned int m = __ballot_sync(0xffffffffu, any);
@@ -188,10 +258,11 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
 
 // Exclusive prefix sums of the kCells cell counts of each binned job, in place (one block
 // of 1024 threads per job, 32 cells per thread).
-__global__ void __launch_bounds__(1024) k_cell_scan(uint32_t* c0, uint32_t* c1) {
+__global__ void __launch_bounds__(1024) k_cell_scan(uint32_t* c0, uint32_t* c1, const unsigned int* __restrict__ n0,
+                                                   const unsigned int* __restrict__ n1) {
     __shared__ uint32_t warp_sum[32];
     uint32_t* c = blockIdx.x ? c1 : c0;
-    if (!c) return;
+    if (!c || *(blockIdx.x ? n1 : n0) < kBinMinLive) return;
     constexpr int kPer = kCells / 1024;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     uint32_t v[kPer];
@@ -236,6 +307,7 @@ __global__ void __launch_bounds__(256) k_edge_order(EdgeJob j0, EdgeJob j1, unsi
     if (!j.order) return;
     const unsigned int nb = second ? blocks1 : blocks0;
     const unsigned int n = *j.n_live;
+    if (n < kBinMinLive) return;
     for (unsigned int k = (blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x; k < n;
          k += nb * blockDim.x) {
         const uint32_t e = j.live[k];
@@ -292,20 +364,13 @@ __global__ void k_max_obj(const int32_t* __restrict__ t2o, uint64_t nF, int* __r
 // of the other set cannot be the source of a pair, so its edges are not traced.  Each
 // set's flags come from its own objects' queries against the other set's BVH.
 
-constexpr float kCullAbs = 1e-4f;
-constexpr float kCullRel = 4e-6f;
-constexpr int kCullBudget = 256;  // BVH nodes one object's query may visit before giving up
+constexpr int kCullBudget = 256;      // BVH nodes a flag-only query may visit before giving up
+constexpr int kPartnerBudget = 2048;  // the same for a query that collects partner objects
 
 __global__ void k_obj_box_init(int* __restrict__ box, uint64_t n_obj) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i < 6 * n_obj) box[i] = (i % 6) < 3 ? 0x7fffffff : (int)0x80000000;
 }
-
-__device__ __forceinline__ int f2ord(float f) {
-    const int i = __float_as_int(f);
-    return i >= 0 ? i : i ^ 0x7fffffff;
-}
-__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
 // Object boxes from the leaf-ordered triangles (consecutive leaves mostly share an
 // object, so lanes with equal objects reduce first and one lane updates the box).
@@ -332,10 +397,6 @@ __global__ void k_obj_boxes(const float4* __restrict__ tris, uint64_t n, int* __
     }
 }
 
-__device__ __forceinline__ float cull_margin(float l, float h) {
-    return kCullRel * (fmaxf(fabsf(l), fabsf(h)) + (h - l));
-}
-
 // [l, h] widened by its margin overlaps the (already widened) query box.
 __device__ __forceinline__ bool cull_overlap(float l0, float l1, float l2, float h0, float h1, float h2,
                                              const float* qlo, const float* qhi) {
@@ -352,13 +413,17 @@ struct CullJob {
     uint32_t max_steps;
     const float4* tris;
     uint8_t* cand;
+    int32_t* part;  // nullable: partner lists (kPartners per object)
 };
 
 // One thread per object of one set: does its widened box overlap any widened triangle
-// box of the other set's BVH?  cand[o] = 1 on the first overlap, or when the query runs
-// out of its node budget or stack; 0 otherwise.  Node boxes contain their triangles'
-// boxes and the widening grows with the box, so node culling is conservative.  Blocks
-// below blocks0 run job j0, the others j1 (both directions of a join in one launch).
+// box of the other set's BVH?  Flag mode (part == null): cand[o] = 1 on the first overlap,
+// or when the query runs out of its node budget or stack; 0 otherwise.  Partner mode: the
+// distinct objects of the overlapping triangles go to part[o * kPartners ...] and cand[o] =
+// their number, or kCandAll when there are more than kPartners or the query ran out (the
+// triangles of objects already listed are not tested again).  Node boxes contain their
+// triangles' boxes and the widening grows with the box, so node culling is conservative.
+// Blocks below blocks0 run job j0, the others j1 (both directions of a join in one launch).
 __global__ void k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
     const bool second = blockIdx.x >= blocks0;
     const CullJob j = second ? j1 : j0;
@@ -369,6 +434,7 @@ __global__ void k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
     const float4* __restrict__ tris = j.tris;
     uint8_t* __restrict__ cand = j.cand;
     const uint32_t max_steps = j.max_steps;
+    const bool collect = j.part != nullptr;
     float qlo[3], qhi[3];
     bool empty = false;
 #pragma unroll
@@ -383,12 +449,15 @@ __global__ void k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
         cand[a] = 0;
         return;
     }
+    int32_t pl[kPartners];
+    int np = 0;
+    bool stop = false, all = false;  // all: flag 1 (flag mode) or kCandAll (partner mode)
+    const uint32_t budget = collect ? (uint32_t)kPartnerBudget : (uint32_t)kCullBudget;
     int stack[kStack];
     int sp = 0, node = 0;
-    uint8_t result = 0;
     for (uint32_t step = 0;; ++step) {
-        if (step > max_steps || step > (uint32_t)kCullBudget) {
-            result = 1;
+        if (step > max_steps || step > budget) {
+            all = true;
             break;
         }
         const float4 na = __ldg(&nodes[node].a), nb = __ldg(&nodes[node].b), nc = __ldg(&nodes[node].c);
@@ -396,27 +465,41 @@ __global__ void k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
         bool h0 = cull_overlap(na.x, na.y, na.z, na.w, nb.x, nb.y, qlo, qhi);
         bool h1 = cull_overlap(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, qlo, qhi);
 #pragma unroll 1
-        for (int side = 0; side < 2 && !result; ++side) {
+        for (int side = 0; side < 2 && !stop; ++side) {
             const bool h = side == 0 ? h0 : h1;
             const int first = side == 0 ? nd.x : nd.z, cnt = side == 0 ? nd.y : nd.w;
             if (!h || cnt == 0) continue;
             for (int k = first; k < first + cnt; ++k) {
-                const float4 p = __ldg(&tris[3 * (size_t)k]), q = __ldg(&tris[3 * (size_t)k + 1]),
-                             r = __ldg(&tris[3 * (size_t)k + 2]);
-                if (cull_overlap(fminf(fminf(p.x, q.x), r.x), fminf(fminf(p.y, q.y), r.y),
-                                 fminf(fminf(p.z, q.z), r.z), fmaxf(fmaxf(p.x, q.x), r.x),
-                                 fmaxf(fmaxf(p.y, q.y), r.y), fmaxf(fmaxf(p.z, q.z), r.z), qlo, qhi)) {
-                    result = 1;
+                const float4 q = __ldg(&tris[3 * (size_t)k + 1]);
+                const int32_t pobj = __float_as_int(q.w);
+                if (collect) {
+                    bool known = false;
+#pragma unroll
+                    for (int t = 0; t < kPartners; ++t) known |= (t < np && pl[t] == pobj);
+                    if (known) continue;
+                }
+                const float4 p = __ldg(&tris[3 * (size_t)k]), r = __ldg(&tris[3 * (size_t)k + 2]);
+                if (!cull_overlap(fminf(fminf(p.x, q.x), r.x), fminf(fminf(p.y, q.y), r.y),
+                                  fminf(fminf(p.z, q.z), r.z), fmaxf(fmaxf(p.x, q.x), r.x),
+                                  fmaxf(fmaxf(p.y, q.y), r.y), fmaxf(fmaxf(p.z, q.z), r.z), qlo, qhi))
+                    continue;
+                if (!collect || np == kPartners) {
+                    all = true;
+                    stop = true;
                     break;
                 }
+#pragma unroll
+                for (int t = 0; t < kPartners; ++t)
+                    if (t == np) pl[t] = pobj;
+                ++np;
             }
         }
-        if (result) break;
+        if (stop) break;
         if (nd.y > 0) h0 = false;
         if (nd.w > 0) h1 = false;
         if (h0 && h1) {
             if (sp == kStack) {
-                result = 1;
+                all = true;
                 break;
             }
             stack[sp++] = nd.z;
@@ -430,7 +513,16 @@ __global__ void k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
             node = stack[--sp];
         }
     }
-    cand[a] = result;
+    if (!collect) {
+        cand[a] = all ? 1 : 0;
+        return;
+    }
+    cand[a] = all ? kCandAll : (uint8_t)np;
+    if (!all) {
+#pragma unroll
+        for (int t = 0; t < kPartners; ++t)
+            if (t < np) j.part[a * kPartners + t] = pl[t];
+    }
 }
 
 // Optional per-source outputs of the containment pass (the reference's pair-hit and
@@ -599,7 +691,8 @@ static cudaError_t edge_all_async(const rs_bvh* target, EdgePayload p, uint64_t 
         e = cudaMemsetAsync(n_def, 0, sizeof(unsigned int), s);
         if (e != cudaSuccess) break;
         const unsigned grid = (unsigned)std::min<uint64_t>((n + kT - 1) / kT, 8ull * sm_count());
-        launch(k_edge_rays, grid, kT, 0, s, q, (const uint32_t*)nullptr, (const unsigned int*)nullptr, n,
+        launch(k_edge_rays, grid, kT, 0, s, q, (const uint32_t*)nullptr, (const uint32_t*)nullptr,
+               (const unsigned int*)nullptr, n,
                (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table, deferred,
                n_def);
         launch(k_edge_long, (unsigned)std::min<uint64_t>((n + kT - 1) / kT, 2ull * sm_count()), kT, 0, s, q,
@@ -624,6 +717,9 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
     job.nE = nE;
     job.cull = cull.cand;
     job.n_cull = cull.n_obj;
+    job.part = cull.part;
+    job.pbox = cull.pbox;
+    job.n_pbox = cull.n_pbox;
     job.nodes = (const BNode*)target->nodes;
     job.max_steps = max_steps(target);
     job.tris = (const float4*)target->tris;
@@ -668,7 +764,9 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
         const int ptok = prof_begin(P_EDGE_JOIN, s);
         launch(k_edge_live, (unsigned)(blocks[0] + blocks[1]), 256, 0, s, jobs[0], jobs[1], (unsigned)blocks[0]);
         if (n_bin) {
-            launch(k_cell_scan, 2, 1024, 0, s, jobs[0].cells, n_jobs > 1 ? jobs[1].cells : (uint32_t*)nullptr);
+            launch(k_cell_scan, 2, 1024, 0, s, jobs[0].cells, n_jobs > 1 ? jobs[1].cells : (uint32_t*)nullptr,
+                   (const unsigned int*)jobs[0].n_live,
+                   (const unsigned int*)(n_jobs > 1 ? jobs[1].n_live : jobs[0].n_live));
             const unsigned ob0 = (unsigned)std::min<uint64_t>(std::max<uint64_t>(blocks[0], 1), 4ull * sm_count());
             const unsigned ob1 = (unsigned)std::min<uint64_t>(blocks[1], 4ull * sm_count());
             launch(k_edge_order, ob0 + ob1, 256, 0, s, jobs[0], jobs[1], ob0, ob1);
@@ -689,7 +787,7 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
             const EdgeJob& j = jobs[d];
             cudaStream_t st = d == 1 && side ? side : s;
             launch(k_edge_rays, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 8ull * sm_count()), kT, 0, st, j.p,
-                   (const uint32_t*)(j.order ? j.order : j.live), (const unsigned int*)j.n_live, j.nE, j.nodes,
+                   (const uint32_t*)j.order, (const uint32_t*)j.live, (const unsigned int*)j.n_live, j.nE, j.nodes,
                    j.max_steps, j.tris, j.swap, table, j.rank, j.n_def);
             launch(k_edge_long, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 2ull * sm_count()), kT, 0, st, j.p,
                    (const uint32_t*)j.rank, (const unsigned int*)j.n_def, j.nodes, j.max_steps, j.tris, j.swap, table);
@@ -728,6 +826,9 @@ cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const fl
         j.nE = nE;
         j.cull = c.cand;
         j.n_cull = c.n_obj;
+        j.part = c.part;
+        j.pbox = c.pbox;
+        j.n_pbox = c.n_pbox;
         j.nodes = (const BNode*)target->nodes;
         j.max_steps = max_steps(target);
         j.tris = (const float4*)target->tris;
@@ -738,21 +839,27 @@ cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const fl
     return n ? edge_jobs_async(job, n, ps, s) : cudaSuccess;
 }
 
-// Broad-phase flags of A's objects against B's BVH into candA and of B's objects against
-// A's BVH into candB (either null: that direction is skipped), one query per object, both
-// directions in one launch.  The object boxes are the build's (k_morton) when they cover
-// every object of the set, else computed here from its leaf triangles.
-cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, cudaStream_t s) {
+// Broad phase of both directions in one launch: set d's objects (A for d = 0, B for d = 1)
+// are queried against the other set's BVH when cand[d] is given (either null: that
+// direction is skipped), in partner mode when part[d] is given too.  Object boxes come from
+// the build (k_morton) when they cover the set, else from its leaf triangles into
+// temporaries.  With boxes_out, both sets' boxes are made and returned (the partner filter
+// of the edge rays reads them) and the temporaries go to tmps_out, for the caller to free
+// after those rays; otherwise they are freed here.
+cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, int32_t* partA,
+                      int32_t* partB, const int** boxes_out, int** tmps_out, cudaStream_t s) {
     const rs_bvh* src[2] = {A, B};
     const rs_bvh* other[2] = {B, A};
     uint8_t* cand[2] = {candA, candB};
+    int32_t* part[2] = {partA, partB};
     int* tmp[2] = {nullptr, nullptr};
+    const int* boxes[2] = {nullptr, nullptr};
     CullJob job[2] = {};
     unsigned int blocks[2] = {0, 0};
     cudaError_t e = cudaSuccess;
     for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
         const rs_bvh* h = src[d];
-        if (!cand[d] || h->n_obj == 0) continue;
+        if ((!cand[d] && !boxes_out) || h->n_obj == 0) continue;
         const int* box = h->obox;
         if (!box || h->n_obj > h->obox_cap) {
             e = dmalloc((void**)&tmp[d], 6 * h->n_obj * sizeof(int), s);
@@ -762,16 +869,34 @@ cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, ui
                    tmp[d], h->n_obj);
             box = tmp[d];
         }
-        job[d] = CullJob{box, h->n_obj, (const BNode*)other[d]->nodes, max_steps(other[d]),
-                         (const float4*)other[d]->tris, cand[d]};
+        boxes[d] = box;
+    }
+    for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
+        const rs_bvh* h = src[d];
+        if (!cand[d] || h->n_obj == 0) continue;
+        job[d] = CullJob{boxes[d], h->n_obj, (const BNode*)other[d]->nodes, max_steps(other[d]),
+                         (const float4*)other[d]->tris, cand[d], part[d]};
         blocks[d] = (unsigned int)((h->n_obj + kT - 1) / kT);
     }
     if (e == cudaSuccess && blocks[0] + blocks[1] > 0)
         launch(k_cull_query, blocks[0] + blocks[1], kT, 0, s, job[0], job[1], blocks[0]);
     if (e == cudaSuccess) e = cudaGetLastError();
-    for (int* p : tmp)
-        if (p) cudaFreeAsync(p, s);
+    if (boxes_out && e == cudaSuccess) {
+        boxes_out[0] = boxes[0];
+        boxes_out[1] = boxes[1];
+        tmps_out[0] = tmp[0];
+        tmps_out[1] = tmp[1];
+    } else {
+        for (int* p : tmp)
+            if (p) cudaFreeAsync(p, s);
+    }
     return e;
+}
+
+// Broad-phase flags of A's objects against B's BVH into candA and of B's objects against
+// A's BVH into candB (either null: that direction is skipped), both in one launch.
+cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, cudaStream_t s) {
+    return cull_impl(A, B, candA, candB, nullptr, nullptr, nullptr, nullptr, s);
 }
 
 // Broad-phase flags of `src`'s objects against `other`'s BVH.

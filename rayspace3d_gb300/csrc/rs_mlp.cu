@@ -469,7 +469,7 @@ __global__ void k_relu_back(float* __restrict__ d, const float* __restrict__ h, 
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, uint64_t n, float lr, float b1, float b2, float eps, float c1, float c2,
                        __nv_bfloat16* __restrict__ w1h, uint64_t n_w1, __nv_bfloat16* __restrict__ w2h,
-                       uint64_t w2_off, uint64_t n_w2) {
+                       uint64_t w2_off, uint64_t n_w2, float wd, uint64_t w3_off, uint64_t n_w3) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float gi = g[i];
@@ -477,7 +477,10 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
     m[i] = mi;
     v[i] = vi;
-    const float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    // Decoupled weight decay (Loshchilov & Hutter 2019) on the weight matrices only.
+    const bool weight = i < n_w1 || (i >= w2_off && i < w2_off + n_w2) || (i >= w3_off && i < w3_off + n_w3);
+    const float p0 = weight ? p[i] * (1.0f - lr * wd) : p[i];
+    const float pi = p0 - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
     p[i] = pi;
     if (i < n_w1) w1h[i] = __float2bfloat16_rn(pi);
     else if (i >= w2_off && i < w2_off + n_w2) w2h[i - w2_off] = __float2bfloat16_rn(pi);
@@ -542,6 +545,13 @@ struct rs_mlp {
     float *h1 = nullptr, *h2 = nullptr, *y = nullptr, *dy = nullptr, *d2 = nullptr, *d1 = nullptr, *loss = nullptr;
     float* feat = nullptr;  // one feature vector for rs_estimate_mlp
     int device = 0;
+    // Decoupled weight decay of W1, W2, W3 (rs_mlp_set_weight_decay).
+    float weight_decay = 0.0f;
+    // Grid-estimator prior (rs_mlp_set_prior): the network's output is a correction added
+    // to log1p of the grid estimate of the same two grids, in rs_estimate_mlp.
+    int prior = 0;
+    float prior_cell_volume = 0.0f, prior_eps = 0.001f, prior_gamma = 0.8f;
+    int prior_alpha = 1;
 };
 
 namespace {
@@ -773,7 +783,7 @@ extern "C" int rs_mlp_train_step(rs_mlp* h, const float* d_X, const float* d_tar
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.0f - std::pow(b1, (float)h->step), c2 = 1.0f - std::pow(b2, (float)h->step);
     launch(k_adam, blocks(kParams), 256, 0, s, h->p, (const float*)h->g, h->m, h->v, kParams, lr, b1, b2, 1e-8f, c1,
-           c2, h->w1h, oB1, h->w2h, oW2, (uint64_t)kHid * kHid);
+           c2, h->w1h, oB1, h->w2h, oW2, (uint64_t)kHid * kHid, h->weight_decay, oW3, (uint64_t)kHid);
     e = cudaGetLastError();
     if (e == cudaSuccess && h_loss) e = cudaMemcpyAsync(h_loss, h->loss, 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -792,8 +802,38 @@ extern "C" int rs_estimate_mlp(rs_mlp* h, const void* d_cellsA, const void* d_ce
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     st = mlp_status(e, s);
     if (st != RS_OK) return st;
-    const double v = std::expm1((double)y);
+    double base = 0.0;
+    if (h->prior) {
+        // The grid estimator's count on the same grids (rs_estimate_grid and
+        // rs_estimate_pairs_from_raw), the prior the network corrects.
+        double raw = 0.0;
+        float means[4];
+        const uint64_t ncells = (uint64_t)resolution * resolution * resolution;
+        st = rs_estimate_grid(d_cellsA, d_cellsB, ncells, h->prior_cell_volume, h->prior_eps, h->prior_gamma, &raw,
+                              means, stream);
+        if (st != RS_OK) return st;
+        const int64_t g = rs_estimate_pairs_from_raw(raw, means, h->prior_cell_volume, h->prior_alpha);
+        base = std::log1p((double)std::max<int64_t>(g, 0));
+    }
+    const double v = std::expm1((double)y + base);
     *h_estimate = v > 0.0 ? (int64_t)std::llround(v) : 0;
-    if (h_log1p) *h_log1p = (double)y;
+    if (h_log1p) *h_log1p = (double)y + base;
+    return RS_OK;
+}
+
+extern "C" int rs_mlp_set_weight_decay(rs_mlp* h, float weight_decay) {
+    if (!h || !(weight_decay >= 0.0f)) return RS_ERR_INVALID;
+    h->weight_decay = weight_decay;
+    return RS_OK;
+}
+
+extern "C" int rs_mlp_set_prior(rs_mlp* h, int on, float cell_volume, float epsilon, float gamma,
+                                int alpha_correction) {
+    if (!h || (on && !(cell_volume > 0.0f))) return RS_ERR_INVALID;
+    h->prior = on != 0;
+    h->prior_cell_volume = cell_volume;
+    h->prior_eps = epsilon;
+    h->prior_gamma = gamma;
+    h->prior_alpha = alpha_correction != 0;
     return RS_OK;
 }

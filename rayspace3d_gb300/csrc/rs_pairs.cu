@@ -20,6 +20,8 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
                             int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull);
 cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, cudaStream_t s);
+cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, int32_t* partA,
+                      int32_t* partB, const int** boxes_out, int** tmps_out, cudaStream_t s);
 cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const float* endsA, const int32_t* offsetsA,
                                  const int32_t* countsA, const int32_t* sourcesA, uint64_t nEA, const EdgeCull& cullA,
                                  const rs_bvh* B, const float* startsB, const float* endsB, const int32_t* offsetsB,
@@ -228,21 +230,33 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
         if (st != RS_OK) return st;
     }
     // Broad phase once per call (it does not depend on the table, so reruns after growth
-    // reuse it): object boxes of each set against the other set's triangle boxes.
+    // reuse it): object boxes of each set against the other set's triangle boxes, listing
+    // each object's partner objects, so that only edges whose own box reaches a partner's
+    // box are traced.
     uint8_t* cand = nullptr;  // [A objects | B objects]
+    int32_t* part = nullptr;  // kPartners per object, same order
+    const int* boxes[2] = {nullptr, nullptr};
+    int* tmps[2] = {nullptr, nullptr};
     EdgeCull cullA, cullB;
     if (g_overlap_cull && A->n_obj && B->n_obj && A->n_tris && B->n_tris) {
-        cudaError_t e = dmalloc((void**)&cand, A->n_obj + B->n_obj, s);
-        if (e == cudaSuccess) e = cull_pair_async(A, B, a2b ? cand : nullptr, b2a ? cand + A->n_obj : nullptr, s);
+        const uint64_t n_obj = A->n_obj + B->n_obj;
+        cudaError_t e = dmalloc((void**)&cand, n_obj, s);
+        if (e == cudaSuccess) e = dmalloc((void**)&part, n_obj * kPartners * sizeof(int32_t), s);
+        if (e == cudaSuccess)
+            e = cull_impl(A, B, a2b ? cand : nullptr, b2a ? cand + A->n_obj : nullptr, part,
+                          part + A->n_obj * kPartners, boxes, tmps, s);
         if (e == cudaSuccess) {
-            if (a2b) cullA = EdgeCull{cand, A->n_obj};
-            if (b2a) cullB = EdgeCull{cand + A->n_obj, B->n_obj};
+            if (a2b) cullA = EdgeCull{cand, A->n_obj, part, boxes[1], B->n_obj};
+            if (b2a) cullB = EdgeCull{cand + A->n_obj, B->n_obj, part + A->n_obj * kPartners, boxes[0], A->n_obj};
         } else {
             cudaGetLastError();  // culling is an optimisation: run without it
         }
     }
     auto release = [&]() {
         if (cand) cudaFreeAsync(cand, s);
+        if (part) cudaFreeAsync(part, s);
+        for (int* p : tmps)
+            if (p) cudaFreeAsync(p, s);
     };
     for (int attempt = 0; attempt < 8; ++attempt) {
         // Order of executeHashQuery (raytracer_intersection_estimated_main.cpp:107-158): overlap A->B,

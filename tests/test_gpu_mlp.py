@@ -65,16 +65,15 @@ def test_forward_and_gradients_match_oracle(cuda):
     m.close()
 
 
-def test_training_and_gain_over_grid_estimator(cuda):
-    """A short training run on engine-labelled dataset pairs: the loss falls, and on the
-    pairs it saw the network's log1p error is below the grid estimator's."""
+def test_training_fits_and_estimate_entry_point(cuda):
+    """A short training run of the plain network (no prior, no weight decay, no
+    augmentation) on engine-labelled dataset pairs: the loss falls by 10x, and
+    rs_estimate_mlp agrees with the forward pass."""
     samples = [learned.make_sample(500 + i, 500, 4000) for i in range(40)]
     assert all(s.pairs >= 0 for s in samples)
-    m, losses = learned.train(samples, epochs=120, batch=16, lr=1e-3, seed=1)
+    m, losses = learned.train(samples, epochs=120, batch=16, lr=1e-3, seed=1, prior=False, weight_decay=0.0,
+                              augment=False)
     assert losses[-1] < 0.1 * losses[0]
-    ev = learned.evaluate(m, samples)
-    assert ev["mlp_abs_log1p_error"] < ev["grid_abs_log1p_error"]
-    # the estimate entry point agrees with the forward pass
     L = _lib.load()
     s = samples[0]
     y = m.forward(s.features[None].contiguous()).item()
@@ -87,4 +86,28 @@ def test_training_and_gain_over_grid_estimator(cuda):
                              None) == 0
     assert abs(lg.value - y) < 1e-4 * max(1.0, abs(y))
     assert est.value == max(0, int(round(np.expm1(lg.value))))
+    m.close()
+
+
+def test_held_out_gain_over_grid_estimator(cuda):
+    """What the network gains on dataset pairs it never saw: trained (grid-estimate prior,
+    weight decay, symmetry augmentation, early stopping on a validation split) on 160
+    engine-labelled pairs, its mean |log1p error| on 40 held-out pairs is below the grid
+    estimator's, and rs_estimate_mlp with the prior returns the grid estimate corrected by
+    the network."""
+    samples = [learned.make_sample(7000 + i, 500, 4000) for i in range(200)]
+    train, test = samples[:160], samples[160:]
+    m, _ = learned.train(train, epochs=60, batch=32, lr=1e-3, seed=2, prior=True, weight_decay=1e-2,
+                         val_frac=0.15)
+    ev = learned.evaluate(m, test)
+    assert ev["mlp_abs_log1p_error"] < ev["grid_abs_log1p_error"], ev
+    L = _lib.load()
+    seed = 7000 + 160
+    A, na, B, nb = learned.dataset_pair(seed, 500, 4000)
+    ca, cb = learned.grid_cells(A, na), learned.grid_cells(B, nb)
+    est, lg = ctypes.c_int64(), ctypes.c_double()
+    assert L.rs_estimate_mlp(m.h, ca.data_ptr(), cb.data_ptr(), learned.RES, ctypes.byref(est), ctypes.byref(lg),
+                             None) == 0
+    want = learned.predict(m, [test[0]])[0]
+    assert abs(lg.value - np.log1p(want)) < 1e-4 * max(1.0, abs(lg.value))
     m.close()
