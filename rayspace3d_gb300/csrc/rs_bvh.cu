@@ -40,20 +40,37 @@ __global__ void k_init_bounds(int* b) {
     if (threadIdx.x < 12) b[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0x7fffffff : (int)0x80000000;
 }
 
-__device__ __forceinline__ void block_minmax_atomic(float mn[3], float mx[3], int* out) {
+// Block-wide min/max of the three components (and the largest object id), then one atomic
+// per value and block: same-address atomics from every warp of the grid would serialise in
+// one L2 slice.  Called by every thread of the block.
+__device__ __forceinline__ void block_minmax_atomic(float mn[3], float mx[3], int mo, int* out, int* max_obj) {
+    __shared__ int s_v[32][7];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    int v[7];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
-        }
+        v[k] = __reduce_min_sync(0xffffffffu, flt_ord(mn[k]));
+        v[3 + k] = __reduce_max_sync(0xffffffffu, flt_ord(mx[k]));
     }
-    if ((threadIdx.x & 31) == 0) {
+    v[6] = __reduce_max_sync(0xffffffffu, mo);
+    if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            atomicMin(&out[k], flt_ord(mn[k]));
-            atomicMax(&out[3 + k], flt_ord(mx[k]));
+        for (int k = 0; k < 7; ++k) s_v[w][k] = v[k];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const int x = lane < nw ? s_v[lane][k] : s_v[0][k];
+            v[k] = (k < 3) ? __reduce_min_sync(0xffffffffu, x) : __reduce_max_sync(0xffffffffu, x);
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&out[k], v[k]);
+                atomicMax(&out[3 + k], v[3 + k]);
+            }
+            if (v[6] >= 0) atomicMax(max_obj, v[6]);
         }
     }
 }
@@ -110,7 +127,6 @@ __global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, const 
         done = 4 * n4;
     }
     for (uint64_t f = done + tid; f < nf; f += stride) fold_component(mn, mx, (int)(f % 3), V[f]);
-    block_minmax_atomic(mn, mx, bounds + 6);
     int mo = -1;
     if ((reinterpret_cast<uintptr_t>(t2o) & 15u) == 0) {
         const int4* T4 = reinterpret_cast<const int4*>(t2o);
@@ -129,8 +145,7 @@ __global__ void k_vertex_bounds(const float* __restrict__ V, uint64_t nV, const 
     } else {
         for (uint64_t q = tid; q < nF; q += stride) mo = max(mo, t2o[q]);
     }
-    mo = __reduce_max_sync(0xffffffffu, mo);
-    if ((threadIdx.x & 31) == 0 && mo >= 0) atomicMax(max_obj, mo);
+    block_minmax_atomic(mn, mx, mo, bounds + 6, max_obj);
 }
 
 // Indices are clamped so a malformed index buffer cannot read out of bounds; the
@@ -348,7 +363,14 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
     // writing after their first merges.
     int role = -1;
     __syncthreads();
+    // Two barriers per round: (1) a right child absorbed in the previous round's merge phase
+    // retires, and threads without a role publish one; (2) left children merge with their
+    // complete right siblings, and the round's barrier also tells whether anything merged.
     for (int round = 0; round < kT; ++round) {
+        if (active && role == 0 && s_abs[tid]) {
+            active = false;
+            s_state[tid] = 0;
+        }
         if (active && role < 0) {
             const int dr = s_d[r - bb + 1], dl = s_d[l - bb];
             const bool left_child = (l == 0) ? true : (r == nG - 1) ? false : dr > dl;
@@ -400,11 +422,6 @@ __global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, ui
                 active = false;
                 s_state[tid] = 0;
             }
-        }
-        __syncthreads();
-        if (active && role == 0 && s_abs[tid]) {
-            active = false;
-            s_state[tid] = 0;
         }
         if (!__syncthreads_or(merged)) break;
     }
