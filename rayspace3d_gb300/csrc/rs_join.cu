@@ -364,8 +364,6 @@ __global__ void k_max_obj(const int32_t* __restrict__ t2o, uint64_t nF, int* __r
 // of the other set cannot be the source of a pair, so its edges are not traced.  Each
 // set's flags come from its own objects' queries against the other set's BVH.
 
-constexpr int kCullBudget = 256;      // BVH nodes a flag-only query may visit before giving up
-constexpr int kPartnerBudget = 2048;  // the same for a query that collects partner objects
 
 __global__ void k_obj_box_init(int* __restrict__ box, uint64_t n_obj) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -416,112 +414,145 @@ struct CullJob {
     int32_t* part;  // nullable: partner lists (kPartners per object)
 };
 
-// One thread per object of one set: does its widened box overlap any widened triangle
-// box of the other set's BVH?  Flag mode (part == null): cand[o] = 1 on the first overlap,
-// or when the query runs out of its node budget or stack; 0 otherwise.  Partner mode: the
+// One warp per object of one set: does its widened box overlap any widened triangle box
+// of the other set's BVH?  Flag mode (part == null): cand[o] = 1 on the first overlap, or
+// when the query runs out of its node budget or stack; 0 otherwise.  Partner mode: the
 // distinct objects of the overlapping triangles go to part[o * kPartners ...] and cand[o] =
-// their number, or kCandAll when there are more than kPartners or the query ran out (the
-// triangles of objects already listed are not tested again).  Node boxes contain their
-// triangles' boxes and the widening grows with the box, so node culling is conservative.
-// Blocks below blocks0 run job j0, the others j1 (both directions of a join in one launch).
-__global__ void k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
+// their number, or kCandAll when there are more than kPartners or the query ran out.  Node
+// boxes contain their triangles' boxes and the widening grows with the box, so node
+// culling is conservative.
+//
+// The 32 lanes walk the tree together: each step pops up to 32 nodes from the warp's
+// shared-memory stack (one per lane), tests both children of each, tests the triangles of
+// the leaves hit, and pushes the inner children hit (ballot prefix sums give the slots).
+// Partners found in a step are deduplicated across lanes with ballots and appended to a
+// list every lane holds.  A query's latency is therefore its depth plus its node count
+// over 32, not its node count.  Blocks below blocks0 run job j0, the others j1 (both
+// directions of a join in one launch).
+constexpr int kCullWarps = 4;             // warps (objects) per block
+constexpr int kCullStack = 256;           // entries of a warp's stack
+constexpr uint32_t kFlagBudget = 1024;    // node visits of a flag-mode query
+constexpr uint32_t kPartnerBudget = 8192; // node visits of a partner-mode query
+
+__global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
+    __shared__ int s_stack[kCullWarps][kCullStack];
     const bool second = blockIdx.x >= blocks0;
     const CullJob j = second ? j1 : j0;
-    const uint64_t a = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x;
-    if (a >= j.n_obj) return;
-    const int* __restrict__ box = j.box;
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const uint64_t a = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * kCullWarps + wi;
+    if (a >= j.n_obj) return;  // warp-uniform
+    int* stack = s_stack[wi];
+    const bool collect = j.part != nullptr;
     const BNode* __restrict__ nodes = j.nodes;
     const float4* __restrict__ tris = j.tris;
-    uint8_t* __restrict__ cand = j.cand;
-    const uint32_t max_steps = j.max_steps;
-    const bool collect = j.part != nullptr;
     float qlo[3], qhi[3];
     bool empty = false;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float l = ord2f(box[6 * a + c]), h = ord2f(box[6 * a + 3 + c]);
+        const float l = ord2f(j.box[6 * a + c]), h = ord2f(j.box[6 * a + 3 + c]);
         empty |= !(l <= h);
         const float m = kCullAbs + cull_margin(l, h);
         qlo[c] = l - m;
         qhi[c] = h + m;
     }
     if (empty) {  // no triangle of this object, hence no edges
-        cand[a] = 0;
+        if (lane == 0) j.cand[a] = 0;
         return;
     }
-    int32_t pl[kPartners];
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t budget = min(j.max_steps, collect ? kPartnerBudget : kFlagBudget);
+    int32_t pl[kPartners];  // the partner list, the same in every lane
     int np = 0;
-    bool stop = false, all = false;  // all: flag 1 (flag mode) or kCandAll (partner mode)
-    const uint32_t budget = collect ? (uint32_t)kPartnerBudget : (uint32_t)kCullBudget;
-    int stack[kStack];
-    int sp = 0, node = 0;
-    for (uint32_t step = 0;; ++step) {
-        if (step > max_steps || step > budget) {
+    bool all = false;  // flag 1 (flag mode) or kCandAll (partner mode)
+    if (lane == 0) stack[0] = 0;
+    __syncwarp();
+    int sp = 1;
+    uint32_t visits = 0;
+    while (sp > 0 && !all) {
+        const int take = min(sp, 32);
+        const int node = lane < take ? stack[sp - take + lane] : -1;
+        __syncwarp();
+        sp -= take;
+        visits += (uint32_t)take;
+        if (visits > budget) {
             all = true;
             break;
         }
-        const float4 na = __ldg(&nodes[node].a), nb = __ldg(&nodes[node].b), nc = __ldg(&nodes[node].c);
-        const int4 nd = __ldg(&nodes[node].d);
-        bool h0 = cull_overlap(na.x, na.y, na.z, na.w, nb.x, nb.y, qlo, qhi);
-        bool h1 = cull_overlap(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, qlo, qhi);
-#pragma unroll 1
-        for (int side = 0; side < 2 && !stop; ++side) {
-            const bool h = side == 0 ? h0 : h1;
-            const int first = side == 0 ? nd.x : nd.z, cnt = side == 0 ? nd.y : nd.w;
-            if (!h || cnt == 0) continue;
-            for (int k = first; k < first + cnt; ++k) {
-                const float4 q = __ldg(&tris[3 * (size_t)k + 1]);
-                const int32_t pobj = __float_as_int(q.w);
-                if (collect) {
+        bool h[2] = {false, false};
+        int first[2] = {0, 0}, cnt[2] = {0, 0};
+        if (node >= 0) {
+            const float4 na = __ldg(&nodes[node].a), nb = __ldg(&nodes[node].b), nc = __ldg(&nodes[node].c);
+            const int4 nd = __ldg(&nodes[node].d);
+            h[0] = cull_overlap(na.x, na.y, na.z, na.w, nb.x, nb.y, qlo, qhi);
+            h[1] = cull_overlap(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, qlo, qhi);
+            first[0] = nd.x;
+            cnt[0] = nd.y;
+            first[1] = nd.z;
+            cnt[1] = nd.w;
+        }
+        // Leaves hit: their triangles, one per lane and round, in warp-uniform rounds.
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const int mine = (h[side] && cnt[side] > 0) ? cnt[side] : 0;
+            const int rounds = __reduce_max_sync(0xffffffffu, mine);
+            for (int k = 0; k < rounds && !all; ++k) {
+                bool found = false;
+                int32_t pobj = 0;
+                if (k < mine) {
+                    const int t = first[side] + k;
+                    const float4 q = __ldg(&tris[3 * (size_t)t + 1]);
+                    pobj = __float_as_int(q.w);
                     bool known = false;
 #pragma unroll
-                    for (int t = 0; t < kPartners; ++t) known |= (t < np && pl[t] == pobj);
-                    if (known) continue;
+                    for (int u = 0; u < kPartners; ++u) known |= (u < np && pl[u] == pobj);
+                    if (!known) {
+                        const float4 p = __ldg(&tris[3 * (size_t)t]), r = __ldg(&tris[3 * (size_t)t + 2]);
+                        found = cull_overlap(fminf(fminf(p.x, q.x), r.x), fminf(fminf(p.y, q.y), r.y),
+                                             fminf(fminf(p.z, q.z), r.z), fmaxf(fmaxf(p.x, q.x), r.x),
+                                             fmaxf(fmaxf(p.y, q.y), r.y), fmaxf(fmaxf(p.z, q.z), r.z), qlo, qhi);
+                    }
                 }
-                const float4 p = __ldg(&tris[3 * (size_t)k]), r = __ldg(&tris[3 * (size_t)k + 2]);
-                if (!cull_overlap(fminf(fminf(p.x, q.x), r.x), fminf(fminf(p.y, q.y), r.y),
-                                  fminf(fminf(p.z, q.z), r.z), fmaxf(fmaxf(p.x, q.x), r.x),
-                                  fmaxf(fmaxf(p.y, q.y), r.y), fmaxf(fmaxf(p.z, q.z), r.z), qlo, qhi))
-                    continue;
-                if (!collect || np == kPartners) {
-                    all = true;
-                    stop = true;
-                    break;
-                }
+                unsigned m = __ballot_sync(0xffffffffu, found);
+                if (m && !collect) all = true;
+                while (m && !all) {
+                    const int32_t o = __shfl_sync(0xffffffffu, pobj, __ffs(m) - 1);
+                    if (np == kPartners) {
+                        all = true;
+                        break;
+                    }
 #pragma unroll
-                for (int t = 0; t < kPartners; ++t)
-                    if (t == np) pl[t] = pobj;
-                ++np;
+                    for (int u = 0; u < kPartners; ++u)
+                        if (u == np) pl[u] = o;
+                    ++np;
+                    m &= ~__ballot_sync(0xffffffffu, found && pobj == o);
+                }
             }
         }
-        if (stop) break;
-        if (nd.y > 0) h0 = false;
-        if (nd.w > 0) h1 = false;
-        if (h0 && h1) {
-            if (sp == kStack) {
-                all = true;
-                break;
-            }
-            stack[sp++] = nd.z;
-            node = nd.x;
-        } else if (h0) {
-            node = nd.x;
-        } else if (h1) {
-            node = nd.z;
-        } else {
-            if (sp == 0) break;
-            node = stack[--sp];
+        if (all) break;
+        // Inner children hit go on the stack.
+        const bool p0 = h[0] && cnt[0] == 0, p1 = h[1] && cnt[1] == 0;
+        const unsigned b0 = __ballot_sync(0xffffffffu, p0), b1 = __ballot_sync(0xffffffffu, p1);
+        const int total = __popc(b0) + __popc(b1);
+        if (sp + total > kCullStack) {
+            all = true;
+            break;
         }
+        int pos = sp + __popc(b0 & lt) + __popc(b1 & lt);
+        if (p0) stack[pos++] = first[0];
+        if (p1) stack[pos] = first[1];
+        __syncwarp();
+        sp += total;
     }
+    if (lane != 0) return;
     if (!collect) {
-        cand[a] = all ? 1 : 0;
+        j.cand[a] = all ? 1 : 0;
         return;
     }
-    cand[a] = all ? kCandAll : (uint8_t)np;
+    j.cand[a] = all ? kCandAll : (uint8_t)np;
     if (!all) {
 #pragma unroll
-        for (int t = 0; t < kPartners; ++t)
-            if (t < np) j.part[a * kPartners + t] = pl[t];
+        for (int u = 0; u < kPartners; ++u)
+            if (u < np) j.part[a * kPartners + u] = pl[u];
     }
 }
 
@@ -876,10 +907,10 @@ cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t*
         if (!cand[d] || h->n_obj == 0) continue;
         job[d] = CullJob{boxes[d], h->n_obj, (const BNode*)other[d]->nodes, max_steps(other[d]),
                          (const float4*)other[d]->tris, cand[d], part[d]};
-        blocks[d] = (unsigned int)((h->n_obj + kT - 1) / kT);
+        blocks[d] = (unsigned int)((h->n_obj + kCullWarps - 1) / kCullWarps);
     }
     if (e == cudaSuccess && blocks[0] + blocks[1] > 0)
-        launch(k_cull_query, blocks[0] + blocks[1], kT, 0, s, job[0], job[1], blocks[0]);
+        launch(k_cull_query, blocks[0] + blocks[1], 32 * kCullWarps, 0, s, job[0], job[1], blocks[0]);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (boxes_out && e == cudaSuccess) {
         boxes_out[0] = boxes[0];

@@ -469,20 +469,33 @@ __device__ __forceinline__ bool segment_fast(const EdgeColumn& col, const Ray& r
     return true;
 }
 
-// Long path: the reference's loop itself.  Each round traverses [t_min, len + 1e-6] for
-// the smallest (t, id) and the walk takes it; every round takes a hit beyond the
-// previous one, so the rounds end.  Stack of kStack entries per thread.
+// Long path, in the reference loop's order: the crossings in [t_min, len + 1e-6] are
+// walked in (t, triangle id) order with the table's hit rule, kLongChunk at a time.  Each
+// pass traverses once and keeps the kLongChunk smallest crossings beyond the last one
+// walked (the ray's tmax shrinks to the largest kept one once the chunk is full, so the
+// pass visits little beyond it); the walk then takes them, and a full chunk starts the
+// next pass after its last crossing.  A crossing's t does not depend on tmin or tmax (the
+// node and triangle slab tests only accept or reject), so the passes see exactly the
+// crossings the reference's one-hit-per-trace loop sees, in the same order, while an
+// edge with h crossings costs about h / kLongChunk traversals instead of h.
+constexpr int kLongChunk = 16;
+
 __device__ __forceinline__ void segment_long(Ray r, const int32_t* __restrict__ src, int nsrc,
                                              const BNode* __restrict__ nodes, uint32_t max_steps,
                                              const float4* __restrict__ tris, int swap, const PairTable& table) {
     EdgeWalk w;
     int32_t last = INT_MIN;
+    const float tmax0 = r.tmax;
+    bool cursor = false;  // (ct, cid): the last crossing of the previous pass
+    float ct = 0.0f;
+    uint32_t cid = 0;
     while (!w.done) {
         r.tmin = w.thr;
-        float bt = INFINITY;
-        uint32_t bid = 0xffffffffu;
-        int32_t bobj = -1;
-        bool found = false;
+        r.tmax = tmax0;
+        float lt[kLongChunk];
+        uint32_t lid[kLongChunk];
+        int32_t lobj[kLongChunk];
+        int n = 0;
         const bool ok = traverse<-1, kStack>(nodes, max_steps, r, [&](int first, int cnt) {
             for (int k = first; k < first + cnt; ++k) {
                 float a[3], b[3], c[3];
@@ -491,24 +504,36 @@ __device__ __forceinline__ void segment_long(Ray r, const int32_t* __restrict__ 
                 load_tri(tris, k, a, b, c, tid, obj);
                 float t;
                 if (!hit_triangle<-1>(r, a, b, c, t)) continue;
-                if (!found || hit_less(t, tid, bt, bid)) {
-                    found = true;
-                    bt = t;
-                    bid = tid;
-                    bobj = obj;
+                if (cursor && !hit_less(ct, cid, t, tid)) continue;  // walked in an earlier pass
+                if (n == kLongChunk && !hit_less(t, tid, lt[kLongChunk - 1], lid[kLongChunk - 1])) continue;
+                int j = n < kLongChunk ? n++ : kLongChunk - 1;
+                while (j > 0 && hit_less(t, tid, lt[j - 1], lid[j - 1])) {
+                    lt[j] = lt[j - 1];
+                    lid[j] = lid[j - 1];
+                    lobj[j] = lobj[j - 1];
+                    --j;
                 }
+                lt[j] = t;
+                lid[j] = tid;
+                lobj[j] = obj;
+                if (n == kLongChunk) r.tmax = lt[kLongChunk - 1];
             }
         });
         if (!ok) {
             atomicOr(table.status, ST_STACK_OVERFLOW);
             break;
         }
-        if (!found) break;
-        w.take(bt, table.max_hits, table.next_float);
-        if (bobj != last) {
-            last = bobj;
-            insert_sources(table, src, nsrc, bobj, swap);
+        for (int j = 0; j < n && !w.done; ++j) {
+            if (!w.take(lt[j], table.max_hits, table.next_float)) continue;
+            if (lobj[j] != last) {
+                last = lobj[j];
+                insert_sources(table, src, nsrc, last, swap);
+            }
         }
+        if (n < kLongChunk) break;
+        cursor = true;
+        ct = lt[kLongChunk - 1];
+        cid = lid[kLongChunk - 1];
     }
     count_edge(table, w.n);
 }
