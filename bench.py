@@ -768,35 +768,47 @@ def run_learned(args, full: bool):
     train_s = time.perf_counter() - t0
     ev_test = learned.evaluate(m, test)
     ev_train = learned.evaluate(m, train)
-    # Forward-pass throughput on a 256-row batch (2 * (32768*512 + 512*512 + 512) flop/row).
-    B = 256
-    X = torch.rand((B, learned.N_FEAT), device="cuda")
-    for _ in range(3):
-        m.forward(X)
-    torch.cuda.synchronize()
-    reps = 20
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
-        m.forward(X)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    flop = 2.0 * B * (32768 * 512 + 512 * 512 + 512)
-    tflops = flop / (ms * 1e-3) / 1e12
-    # The GEMMs alone (device time of the two GEMM launches per forward and their split-K
-    # sums, CUDA events on the launching stream): the tensor-bound part of the pass.
+    # Forward-pass throughput (2 * (32768*512 + 512*512 + 512) flop per row) and the two
+    # GEMMs alone (device time of the GEMM launches and their split-K sums, CUDA events on the
+    # launching stream).  At 256 rows the first GEMM streams W1 (32 MB) for 8.6 GFLOP, below
+    # the machine balance: bound by HBM.  At 4096 rows (a whole evaluation set per pass) it
+    # is bound by the tensor cores.
     L0 = _lib.load()
-    L0.rs_profile_reset()
-    L0.rs_profile_enable(1)
-    for _ in range(reps):
-        m.forward(X)
-    torch.cuda.synchronize()
-    gms, gcnt = ctypes.c_double(), ctypes.c_uint64()
-    L0.rs_profile_read(7, ctypes.byref(gms), ctypes.byref(gcnt))
-    L0.rs_profile_enable(0)
-    gemm_ms = gms.value / reps if gcnt.value else None
+
+    def forward_rates(B, reps=20):
+        X = torch.rand((B, learned.N_FEAT), device="cuda")
+        for _ in range(3):
+            m.forward(X)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            m.forward(X)
+        e1.record()
+        torch.cuda.synchronize()
+        fms = e0.elapsed_time(e1) / reps
+        L0.rs_profile_reset()
+        L0.rs_profile_enable(1)
+        for _ in range(reps):
+            m.forward(X)
+        torch.cuda.synchronize()
+        gms, gcnt = ctypes.c_double(), ctypes.c_uint64()
+        L0.rs_profile_read(7, ctypes.byref(gms), ctypes.byref(gcnt))
+        L0.rs_profile_enable(0)
+        g = gms.value / reps if gcnt.value else None
+        del X
+        return fms, g
+
+    B = 256
+    ms, gemm_ms = forward_rates(B)
+    tflops = 2.0 * B * (32768 * 512 + 512 * 512 + 512) / (ms * 1e-3) / 1e12
     gemm_tflops = (2.0 * B * (32768 * 512 + 512 * 512)) / (gemm_ms * 1e-3) / 1e12 if gemm_ms else None
+    # Bytes the 256-row GEMMs must move: X (BF16) and W1 once, W2, the split-K workspace is
+    # not counted.
+    gemm_bytes = 2.0 * (B * 32768 + 512 * 32768 + 512 * 512 + B * 512)
+    BL = 4096
+    ms_l, gemm_ms_l = forward_rates(BL, reps=10)
+    gemm_tflops_l = (2.0 * BL * (32768 * 512 + 512 * 512)) / (gemm_ms_l * 1e-3) / 1e12 if gemm_ms_l else None
     peak = None
     try:
         with open(MEASURED_PEAKS) as f:
@@ -846,11 +858,18 @@ def run_learned(args, full: bool):
             "estimator_ms": {"mlp": round(mlp_ms, 3), "grid": round(grid_ms, 3)},
             "roofline": {"bound": "tensor", "kernel": "k_umma_gemm (tcgen05.mma bf16 into tensor memory, TMA "
                                                           "128B-swizzled operands, split K) + its split sums, the "
-                                                          "forward pass's two GEMMs at B=256",
-                         "achieved": round(gemm_tflops, 2) if gemm_tflops else None, "peak": peak, "unit": "TFLOP/s",
-                         "frac": round(gemm_tflops / peak, 5) if gemm_tflops else None,
-                         "gemm_ms": round(gemm_ms, 4) if gemm_ms else None,
-                         "forward_pass": {"ms": round(ms, 4), "tflops": round(tflops, 2)}}}
+                                                          f"forward pass's two GEMMs at B={BL}",
+                         "achieved": round(gemm_tflops_l, 2) if gemm_tflops_l else None, "peak": peak,
+                         "unit": "TFLOP/s", "frac": round(gemm_tflops_l / peak, 5) if gemm_tflops_l else None,
+                         "gemm_ms": round(gemm_ms_l, 4) if gemm_ms_l else None,
+                         "forward_pass": {"rows": BL, "ms": round(ms_l, 4)}},
+            "roofline_b256": {"bound": "hbm", "kernel": "the same two GEMMs at B=256 (streaming W1)",
+                              "achieved": round(gemm_bytes / (gemm_ms * 1e-3) / 1e9, 2) if gemm_ms else None,
+                              "peak": peaks()[0], "unit": "GB/s",
+                              "frac": round(gemm_bytes / (gemm_ms * 1e-3) / 1e9 / peaks()[0], 5) if gemm_ms else None,
+                              "gemm_ms": round(gemm_ms, 4) if gemm_ms else None,
+                              "tflops": round(gemm_tflops, 2) if gemm_tflops else None,
+                              "forward_pass": {"rows": B, "ms": round(ms, 4), "tflops": round(tflops, 2)}}}
 
 
 def run_prep(A, cpu: bool = True):

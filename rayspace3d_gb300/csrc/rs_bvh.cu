@@ -312,7 +312,9 @@ struct OpenTree {
 // thread r+1 and merges when that thread holds a complete subtree that chose the same
 // split.  The rounds end when no merge happens; the subtrees still open go to
 // k_build_cross.  Node slot p+1 holds split p, slot 0 the root.
-__global__ void __launch_bounds__(kT) k_build_up(const float* __restrict__ V, uint64_t nV,
+// Six blocks per SM (40 registers): the merge rounds stall on barriers, and more resident
+// blocks hide them; eight (32 registers) spill and run slower.
+__global__ void __launch_bounds__(kT, 6) k_build_up(const float* __restrict__ V, uint64_t nV,
                                                  const uint32_t* __restrict__ I, const int32_t* __restrict__ t2o,
                                                  const uint64_t* __restrict__ keys, Groups G, int nG,
                                                  float4* __restrict__ tris, BNode* __restrict__ nodes,

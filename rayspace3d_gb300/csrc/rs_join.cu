@@ -414,35 +414,19 @@ struct CullJob {
     int32_t* part;  // nullable: partner lists (kPartners per object)
 };
 
-// One warp per object of one set: does its widened box overlap any widened triangle box
-// of the other set's BVH?  Flag mode (part == null): cand[o] = 1 on the first overlap, or
-// when the query runs out of its node budget or stack; 0 otherwise.  Partner mode: the
-// distinct objects of the overlapping triangles go to part[o * kPartners ...] and cand[o] =
-// their number, or kCandAll when there are more than kPartners or the query ran out.  Node
-// boxes contain their triangles' boxes and the widening grows with the box, so node
-// culling is conservative.
-//
-// The 32 lanes walk the tree together: each step pops up to 32 nodes from the warp's
-// shared-memory stack (one per lane), tests both children of each, tests the triangles of
-// the leaves hit, and pushes the inner children hit (ballot prefix sums give the slots).
-// Partners found in a step are deduplicated across lanes with ballots and appended to a
-// list every lane holds.  A query's latency is therefore its depth plus its node count
-// over 32, not its node count.  Blocks below blocks0 run job j0, the others j1 (both
-// directions of a join in one launch).
-constexpr int kCullWarps = 4;             // warps (objects) per block
-constexpr int kCullStack = 256;           // entries of a warp's stack
-constexpr uint32_t kFlagBudget = 1024;    // node visits of a flag-mode query
-constexpr uint32_t kPartnerBudget = 8192; // node visits of a partner-mode query
+// Flag pass, one thread per object of one set: does its widened box overlap any widened
+// triangle box of the other set's BVH?  cand[o] = 1 on the first overlap, or when the query
+// runs out of its node budget or stack; 0 otherwise.  Node boxes contain their triangles'
+// boxes and the widening grows with the box, so node culling is conservative.  Most
+// objects of a sparse join overlap nothing, and a lone thread answers that in one descent.
+// Blocks below blocks0 run job j0, the others j1 (both directions of a join in one launch).
+constexpr uint32_t kFlagBudget = 256;  // node visits of a flag query
 
-__global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
-    __shared__ int s_stack[kCullWarps][kCullStack];
+__global__ void __launch_bounds__(kT) k_cull_flag(CullJob j0, CullJob j1, unsigned int blocks0) {
     const bool second = blockIdx.x >= blocks0;
     const CullJob j = second ? j1 : j0;
-    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-    const uint64_t a = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * kCullWarps + wi;
-    if (a >= j.n_obj) return;  // warp-uniform
-    int* stack = s_stack[wi];
-    const bool collect = j.part != nullptr;
+    const uint64_t a = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x;
+    if (a >= j.n_obj) return;
     const BNode* __restrict__ nodes = j.nodes;
     const float4* __restrict__ tris = j.tris;
     float qlo[3], qhi[3];
@@ -456,11 +440,102 @@ __global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, Cull
         qhi[c] = h + m;
     }
     if (empty) {  // no triangle of this object, hence no edges
+        j.cand[a] = 0;
+        return;
+    }
+    int stack[kStack];
+    int sp = 0, node = 0;
+    uint8_t result = 0;
+    const uint32_t budget = min(j.max_steps, kFlagBudget);
+    for (uint32_t step = 0;; ++step) {
+        if (step > budget) {
+            result = 1;
+            break;
+        }
+        const float4 na = __ldg(&nodes[node].a), nb = __ldg(&nodes[node].b), nc = __ldg(&nodes[node].c);
+        const int4 nd = __ldg(&nodes[node].d);
+        bool h0 = cull_overlap(na.x, na.y, na.z, na.w, nb.x, nb.y, qlo, qhi);
+        bool h1 = cull_overlap(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, qlo, qhi);
+#pragma unroll 1
+        for (int side = 0; side < 2 && !result; ++side) {
+            const bool h = side == 0 ? h0 : h1;
+            const int first = side == 0 ? nd.x : nd.z, cnt = side == 0 ? nd.y : nd.w;
+            if (!h || cnt == 0) continue;
+            for (int k = first; k < first + cnt; ++k) {
+                const float4 p = __ldg(&tris[3 * (size_t)k]), q = __ldg(&tris[3 * (size_t)k + 1]),
+                             r = __ldg(&tris[3 * (size_t)k + 2]);
+                if (cull_overlap(fminf(fminf(p.x, q.x), r.x), fminf(fminf(p.y, q.y), r.y),
+                                 fminf(fminf(p.z, q.z), r.z), fmaxf(fmaxf(p.x, q.x), r.x),
+                                 fmaxf(fmaxf(p.y, q.y), r.y), fmaxf(fmaxf(p.z, q.z), r.z), qlo, qhi)) {
+                    result = 1;
+                    break;
+                }
+            }
+        }
+        if (result) break;
+        if (nd.y > 0) h0 = false;
+        if (nd.w > 0) h1 = false;
+        if (h0 && h1) {
+            if (sp == kStack) {
+                result = 1;
+                break;
+            }
+            stack[sp++] = nd.z;
+            node = nd.x;
+        } else if (h0) {
+            node = nd.x;
+        } else if (h1) {
+            node = nd.z;
+        } else {
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    j.cand[a] = result;
+}
+
+// Partner pass, one warp per object that the flag pass marked (the others keep cand 0):
+// the distinct objects of the other set's triangles whose widened boxes overlap the
+// object's widened box go to part[o * kPartners ...] and cand[o] = their number, or
+// kCandAll when there are more than kPartners or the query ran out of its budget or stack.
+//
+// The 32 lanes walk the tree together: each step pops up to 32 nodes from the warp's
+// shared-memory stack (one per lane), tests both children of each, tests the triangles of
+// the leaves hit, and pushes the inner children hit (ballot prefix sums give the slots).
+// Partners found in a step are deduplicated across lanes with ballots and appended to a
+// list every lane holds.  A query's latency is therefore its depth plus its node count
+// over 32, not its node count.  Blocks below blocks0 run job j0, the others j1 (both
+// directions of a join in one launch).
+constexpr int kCullWarps = 4;             // warps (objects) per block
+constexpr int kCullStack = 256;           // entries of a warp's stack
+constexpr uint32_t kPartnerBudget = 8192;  // node visits of a partner query
+
+__global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, CullJob j1, unsigned int blocks0) {
+    __shared__ int s_stack[kCullWarps][kCullStack];
+    const bool second = blockIdx.x >= blocks0;
+    const CullJob j = second ? j1 : j0;
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const uint64_t a = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * kCullWarps + wi;
+    if (a >= j.n_obj || j.cand[a] == 0) return;  // warp-uniform
+    int* stack = s_stack[wi];
+    const BNode* __restrict__ nodes = j.nodes;
+    const float4* __restrict__ tris = j.tris;
+    float qlo[3], qhi[3];
+    bool empty = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float l = ord2f(j.box[6 * a + c]), h = ord2f(j.box[6 * a + 3 + c]);
+        empty |= !(l <= h);
+        const float m = kCullAbs + cull_margin(l, h);
+        qlo[c] = l - m;
+        qhi[c] = h + m;
+    }
+    if (empty) {  // never: the flag pass gave such an object cand 0
         if (lane == 0) j.cand[a] = 0;
         return;
     }
     const unsigned lt = (1u << lane) - 1u;
-    const uint32_t budget = min(j.max_steps, collect ? kPartnerBudget : kFlagBudget);
+    const uint32_t budget = min(j.max_steps, kPartnerBudget);
     int32_t pl[kPartners];  // the partner list, the same in every lane
     int np = 0;
     bool all = false;  // flag 1 (flag mode) or kCandAll (partner mode)
@@ -513,7 +588,6 @@ __global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, Cull
                     }
                 }
                 unsigned m = __ballot_sync(0xffffffffu, found);
-                if (m && !collect) all = true;
                 while (m && !all) {
                     const int32_t o = __shfl_sync(0xffffffffu, pobj, __ffs(m) - 1);
                     if (np == kPartners) {
@@ -544,10 +618,6 @@ __global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, Cull
         sp += total;
     }
     if (lane != 0) return;
-    if (!collect) {
-        j.cand[a] = all ? 1 : 0;
-        return;
-    }
     j.cand[a] = all ? kCandAll : (uint8_t)np;
     if (!all) {
 #pragma unroll
@@ -902,15 +972,20 @@ cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t*
         }
         boxes[d] = box;
     }
+    unsigned int wblocks[2] = {0, 0};
     for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
         const rs_bvh* h = src[d];
         if (!cand[d] || h->n_obj == 0) continue;
         job[d] = CullJob{boxes[d], h->n_obj, (const BNode*)other[d]->nodes, max_steps(other[d]),
                          (const float4*)other[d]->tris, cand[d], part[d]};
-        blocks[d] = (unsigned int)((h->n_obj + kCullWarps - 1) / kCullWarps);
+        blocks[d] = (unsigned int)((h->n_obj + kT - 1) / kT);
+        if (part[d]) wblocks[d] = (unsigned int)((h->n_obj + kCullWarps - 1) / kCullWarps);
     }
     if (e == cudaSuccess && blocks[0] + blocks[1] > 0)
-        launch(k_cull_query, blocks[0] + blocks[1], 32 * kCullWarps, 0, s, job[0], job[1], blocks[0]);
+        launch(k_cull_flag, blocks[0] + blocks[1], kT, 0, s, job[0], job[1], blocks[0]);
+    // The partner pass of a direction without partner lists has no blocks.
+    if (e == cudaSuccess && wblocks[0] + wblocks[1] > 0)
+        launch(k_cull_query, wblocks[0] + wblocks[1], 32 * kCullWarps, 0, s, job[0], job[1], wblocks[0]);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (boxes_out && e == cudaSuccess) {
         boxes_out[0] = boxes[0];

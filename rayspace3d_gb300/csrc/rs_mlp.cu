@@ -371,9 +371,22 @@ void gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, floa
 // ---------------------------------------------------------------------------------
 // Elementwise and reduction kernels.
 // ---------------------------------------------------------------------------------
+// Four elements per thread: one 16-byte load and one 8-byte store when both arrays are
+// aligned for them, element by element otherwise (and for the tail).
 __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, uint64_t n) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i < n) y[i] = __float2bfloat16_rn(x[i]);
+    const uint64_t i = 4 * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    const bool vec = ((reinterpret_cast<uintptr_t>(x) & 15) == 0) && ((reinterpret_cast<uintptr_t>(y) & 7) == 0);
+    if (vec && i + 4 <= n) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(x + i));
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+        uint2 w;
+        w.x = *reinterpret_cast<const uint32_t*>(&lo);
+        w.y = *reinterpret_cast<const uint32_t*>(&hi);
+        *reinterpret_cast<uint2*>(y + i) = w;
+    } else {
+        for (uint64_t k = i; k < n && k < i + 4; ++k) y[k] = __float2bfloat16_rn(x[k]);
+    }
 }
 
 // h = relu(h + bias) in place (rows x cols), with a BF16 copy.
@@ -597,7 +610,7 @@ unsigned blocks(uint64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 cudaError_t forward(rs_mlp* h, const float* X, int B, cudaStream_t s) {
     cudaError_t e = ensure_acts(h, B);
     if (e != cudaSuccess) return e;
-    launch(k_to_bf16, blocks((uint64_t)B * kIn), 256, 0, s, X, h->xh, (uint64_t)B * kIn);
+    launch(k_to_bf16, blocks(((uint64_t)B * kIn + 3) / 4), 256, 0, s, X, h->xh, (uint64_t)B * kIn);
     gemm<true, true>(h->xh, kIn, h->w1h, kIn, h->h1, kHid, B, kHid, kIn, s);
     launch(k_bias_relu, blocks((uint64_t)B * kHid), 256, 0, s, h->h1, (const float*)(h->p + oB1), h->h1h, B, kHid);
     gemm<true, true>(h->h1h, kHid, h->w2h, kHid, h->h2, kHid, B, kHid, kHid, s);
@@ -659,8 +672,8 @@ extern "C" int rs_mlp_create(uint64_t seed, rs_mlp** out) {
     launch(k_init, blocks((uint64_t)kHid * kHid + kHid), 256, 0, nullptr, h->p + oW2, (uint64_t)kHid * kHid + kHid, s2,
            seed * 4 + 3);
     launch(k_init, blocks(kHid + 1), 256, 0, nullptr, h->p + oW3, (uint64_t)kHid + 1, s2, seed * 4 + 4);
-    launch(k_to_bf16, blocks(oB1), 256, 0, nullptr, (const float*)(h->p + oW1), h->w1h, oB1);
-    launch(k_to_bf16, blocks((uint64_t)kHid * kHid), 256, 0, nullptr, (const float*)(h->p + oW2), h->w2h,
+    launch(k_to_bf16, blocks((oB1 + 3) / 4), 256, 0, nullptr, (const float*)(h->p + oW1), h->w1h, oB1);
+    launch(k_to_bf16, blocks(((uint64_t)kHid * kHid + 3) / 4), 256, 0, nullptr, (const float*)(h->p + oW2), h->w2h,
            (uint64_t)kHid * kHid);
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return to_status(e);
@@ -692,8 +705,8 @@ extern "C" int rs_mlp_set_params(rs_mlp* h, const float* h_params) {
     if (!h || !h_params) return RS_ERR_INVALID;
     cudaError_t e = cudaMemcpy(h->p, h_params, kParams * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return to_status(e);
-    launch(k_to_bf16, blocks(oB1), 256, 0, nullptr, (const float*)(h->p + oW1), h->w1h, oB1);
-    launch(k_to_bf16, blocks((uint64_t)kHid * kHid), 256, 0, nullptr, (const float*)(h->p + oW2), h->w2h,
+    launch(k_to_bf16, blocks((oB1 + 3) / 4), 256, 0, nullptr, (const float*)(h->p + oW1), h->w1h, oB1);
+    launch(k_to_bf16, blocks(((uint64_t)kHid * kHid + 3) / 4), 256, 0, nullptr, (const float*)(h->p + oW2), h->w2h,
            (uint64_t)kHid * kHid);
     return to_status(cudaDeviceSynchronize());
 }

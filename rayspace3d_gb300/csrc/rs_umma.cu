@@ -154,42 +154,51 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ CU
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t taddr = s_tmem;
 
+    // The producer and issuer roles belong to whole warps: lane 0 works, lanes 1-31 wait at
+    // the warp's reconvergence point instead of polling `done` in a branch that would share
+    // the warp's issue slots with lane 0's loop.
     int issued_tma = 0;  // k-blocks whose copies the producer issued
-    if (warp == 0 && lane == 0 && nkb > 0) {
-        // Producer: stage s = i % kStages, round r = i / kStages; a round r >= 1 waits for the
-        // products of round r - 1 to release the stage.
-        for (int i = 0; i < nkb; ++i) {
-            const int s = i % kStages, r = i / kStages;
-            if (r > 0 && !mbar_wait(&empty[s], (uint32_t)((r - 1) & 1))) {
-                atomicOr(err, 1u);
-                atomicExch(&s_abort, 1);
-                break;
+    if (warp == 0 && nkb > 0) {
+        if (lane == 0) {
+            // Producer: stage s = i % kStages, round r = i / kStages; a round r >= 1 waits for the
+            // products of round r - 1 to release the stage.
+            for (int i = 0; i < nkb; ++i) {
+                const int s = i % kStages, r = i / kStages;
+                if (r > 0 && !mbar_wait(&empty[s], (uint32_t)((r - 1) & 1))) {
+                    atomicOr(err, 1u);
+                    atomicExch(&s_abort, 1);
+                    break;
+                }
+                if (*(volatile int*)&s_abort) break;
+                uint8_t* a = smem + (size_t)s * kStageBytes;
+                mbar_expect_tx(&full[s], kStageBytes);
+                tma_load_2d(a, &tmA, &full[s], (kb0 + i) * UK, m0);
+                tma_load_2d(a + kATile, &tmB, &full[s], (kb0 + i) * UK, n0);
+                issued_tma = i + 1;
             }
-            if (*(volatile int*)&s_abort) break;
-            uint8_t* a = smem + (size_t)s * kStageBytes;
-            mbar_expect_tx(&full[s], kStageBytes);
-            tma_load_2d(a, &tmA, &full[s], (kb0 + i) * UK, m0);
-            tma_load_2d(a + kATile, &tmB, &full[s], (kb0 + i) * UK, n0);
-            issued_tma = i + 1;
         }
-    } else if (warp == 1 && lane == 0 && nkb > 0) {
-        // Issuer: four K=16 products per k-block; the commit frees the stage once they finish.
-        for (int i = 0; i < nkb; ++i) {
-            const int s = i % kStages, r = i / kStages;
-            if (!mbar_wait(&full[s], (uint32_t)(r & 1))) {
-                atomicOr(err, 1u);
-                atomicExch(&s_abort, 1);
-                break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a = smem_u32(smem + (size_t)s * kStageBytes);
-            const uint64_t da = tile_desc(a), db = tile_desc(a + kATile);
+        __syncwarp();
+    } else if (warp == 1 && nkb > 0) {
+        if (lane == 0) {
+            // Issuer: four K=16 products per k-block; the commit frees the stage once they finish.
+            for (int i = 0; i < nkb; ++i) {
+                const int s = i % kStages, r = i / kStages;
+                if (!mbar_wait(&full[s], (uint32_t)(r & 1))) {
+                    atomicOr(err, 1u);
+                    atomicExch(&s_abort, 1);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a = smem_u32(smem + (size_t)s * kStageBytes);
+                const uint64_t da = tile_desc(a), db = tile_desc(a + kATile);
 #pragma unroll
-            for (int j = 0; j < UK / 16; ++j)  // 16 BF16 = 32 bytes = 2 in the address field
-                umma_bf16(taddr, da + 2 * j, db + 2 * j, (i > 0 || j > 0) ? 1u : 0u);
-            umma_commit(&empty[s]);
+                for (int j = 0; j < UK / 16; ++j)  // 16 BF16 = 32 bytes = 2 in the address field
+                    umma_bf16(taddr, da + 2 * j, db + 2 * j, (i > 0 || j > 0) ? 1u : 0u);
+                umma_commit(&empty[s]);
+            }
+            umma_commit(&done);  // arrives when every product issued above has finished
         }
-        umma_commit(&done);  // arrives when every product issued above has finished
+        __syncwarp();
     }
     // Every thread waits for the last products (the issuer commits `done` even after an
     // abort, covering whatever it issued).
