@@ -446,6 +446,206 @@ __global__ void __launch_bounds__(kT, 6) k_build_up(const float* __restrict__ V,
     o.self = self;
 }
 
+// Bottom-up-free construction of the radix tree over the leaf groups of one block of kTB
+// groups (the tree Karras' top-down construction gives: Karras 2012, "Maximizing
+// Parallelism in the Construction of BVHs, Octrees, and k-d Trees"), fused with the
+// emission of the leaf-ordered triangles.  Split p (between groups p and p+1) has the
+// prefix length d(p) of their keys; the subtree of split p covers the groups [l, r]
+// bounded by the nearest splits on either side with a smaller d (the prefix length
+// strictly decreases at a subtree's boundary, and its minimum inside is unique).  A
+// subtree [l, r] is the left child of split r when d(r) > d(l-1), else the right child of
+// split l-1 (Apetrei 2014).  So every subtree -- the thread's own leaf group and its own
+// split -- finds its range, its parent and its box by itself: ranges by binary lifting
+// over a shared-memory sparse table of the block's d values (min over 2^k consecutive
+// splits), boxes by a query of a shared-memory pyramid of the groups' boxes (aligned
+// unions of 2^k groups).  It then writes its box and entry into its half of its parent's
+// slot (a parent of <= leaf triangles becomes a leaf of its own parent and gets no slot;
+// the root's children write slot 0).  No merge rounds: ten barriers per block in all.
+// A subtree whose parent's range leaves the block is handed to k_build_cross; a subtree
+// whose own range leaves the block is built there.  Node slot p+1 holds split p.
+constexpr int kTB = 256;   // groups per block
+constexpr int kLogTB = 8;  // log2(kTB)
+
+// Nearest index j < from (j >= 0) with t[0][j] < v, by binary lifting; -1 when none.
+__device__ __forceinline__ int nearest_left(const signed char (*t)[kTB + 1], int from, int v) {
+    int pos = from;
+#pragma unroll
+    for (int lv = kLogTB; lv >= 0; --lv)
+        if (pos - (1 << lv) >= 0 && t[lv][pos - (1 << lv)] >= v) pos -= 1 << lv;
+    return pos - 1;
+}
+
+// Nearest index j > from (j <= kTB) with t[0][j] < v; -1 when none.
+__device__ __forceinline__ int nearest_right(const signed char (*t)[kTB + 1], int from, int v) {
+    int pos = from + 1;
+#pragma unroll
+    for (int lv = kLogTB; lv >= 0; --lv)
+        if (pos + (1 << lv) - 1 <= kTB && t[lv][pos] >= v) pos += 1 << lv;
+    return pos <= kTB ? pos : -1;
+}
+
+__global__ void __launch_bounds__(kTB) k_build_tree(const float* __restrict__ V, uint64_t nV,
+                                                    const uint32_t* __restrict__ I, const int32_t* __restrict__ t2o,
+                                                    const uint64_t* __restrict__ keys, Groups G, int nG,
+                                                    float4* __restrict__ tris, BNode* __restrict__ nodes,
+                                                    OpenTree* __restrict__ open, unsigned int* __restrict__ n_open) {
+    // s_t[lv][j]: min of d over splits bb-1+j .. bb-1+j+2^lv-1 (-1 where no split exists).
+    __shared__ signed char s_t[kLogTB + 1][kTB + 1];
+    // Box pyramid: level lv holds kTB >> lv unions of 2^lv groups at offset 2kTB - (2kTB >> lv).
+    __shared__ float s_b[6][2 * kTB];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int bb = blockIdx.x * kTB;
+    const int g = bb + tid;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (g < nG) {
+        const int j0 = g * G.L, j1 = min(G.n, j0 + G.L);
+        const uint64_t last = nV - 1;
+        for (int j = j0; j < j1; ++j) {
+            // The low word is a triangle id; the clamp only matters after a failed sort.
+            const uint32_t t = min((uint32_t)(__ldg(&keys[j]) & 0xffffffffull), (uint32_t)(G.n - 1));
+            const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last),
+                           i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
+                           i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
+            float a[3], b[3], c[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                a[q] = V[3 * i0 + q];
+                b[q] = V[3 * i1 + q];
+                c[q] = V[3 * i2 + q];
+                lo[q] = fminf(lo[q], fminf(fminf(a[q], b[q]), c[q]));
+                hi[q] = fmaxf(hi[q], fmaxf(fmaxf(a[q], b[q]), c[q]));
+            }
+            tris[3 * (uint64_t)j] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
+            tris[3 * (uint64_t)j + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
+            tris[3 * (uint64_t)j + 2] = make_float4(c[0], c[1], c[2], 0.0f);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        s_b[q][tid] = lo[q];
+        s_b[3 + q][tid] = hi[q];
+    }
+    s_t[0][tid + 1] = (signed char)((g < nG - 1) ? group_prefix(keys, g, G.L) : -1);
+    if (tid == 0) s_t[0][0] = (signed char)((bb > 0 && bb - 1 < nG - 1) ? group_prefix(keys, bb - 1, G.L) : -1);
+    __syncthreads();
+#pragma unroll 1
+    for (int lv = 1; lv <= kLogTB; ++lv) {
+        const int h = 1 << (lv - 1);
+        if (tid + (1 << lv) - 1 <= kTB) s_t[lv][tid] = min(s_t[lv - 1][tid], s_t[lv - 1][tid + h]);
+        const int n_lv = kTB >> lv;
+        if (tid < n_lv) {
+            const int src = 2 * kTB - (2 * kTB >> (lv - 1)), dst = 2 * kTB - (2 * kTB >> lv);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                s_b[q][dst + tid] = fminf(s_b[q][src + 2 * tid], s_b[q][src + 2 * tid + 1]);
+                s_b[3 + q][dst + tid] = fmaxf(s_b[3 + q][src + 2 * tid], s_b[3 + q][src + 2 * tid + 1]);
+            }
+        }
+        __syncthreads();
+    }
+    // The thread's two subtrees: its leaf group (k = 0) and its split (k = 1).
+    bool emit[2] = {false, false};
+    OpenTree ot[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        int l, r, self = 0;
+        float blo[3], bhi[3];
+        if (k == 0) {
+            if (g >= nG) continue;
+            l = r = g;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                blo[q] = lo[q];
+                bhi[q] = hi[q];
+            }
+        } else {
+            // Split g exists inside the block (the block's last split leaves the block).
+            if (g >= nG - 1 || tid >= kTB - 1) continue;
+            const int v = s_t[0][tid + 1];
+            const int jl = nearest_left(s_t, tid + 1, v);
+            const int jr = nearest_right(s_t, tid + 1, v);
+            if (jl < 0 || jr < 0) continue;  // the range leaves the block
+            l = bb + jl;
+            r = bb - 1 + jr;
+            self = g + 1;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                blo[q] = INFINITY;
+                bhi[q] = -INFINITY;
+            }
+            int x = l - bb, y = r - bb + 1, off = 0, n_lv = kTB;
+            while (x < y) {
+                if (x & 1) {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        blo[q] = fminf(blo[q], s_b[q][off + x]);
+                        bhi[q] = fmaxf(bhi[q], s_b[3 + q][off + x]);
+                    }
+                    ++x;
+                }
+                if (y & 1) {
+                    --y;
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        blo[q] = fminf(blo[q], s_b[q][off + y]);
+                        bhi[q] = fmaxf(bhi[q], s_b[3 + q][off + y]);
+                    }
+                }
+                x >>= 1;
+                y >>= 1;
+                off += n_lv;
+                n_lv >>= 1;
+            }
+        }
+        // The parent: split r (this is its left child) when d(r) > d(l-1), else split l-1.
+        const int dl = s_t[0][l - bb], dr = s_t[0][r - bb + 1];
+        if (dl < 0 && dr < 0) continue;  // the root: nothing above it
+        const bool left = dr > dl;
+        int pl, pr, jp;
+        bool inside;
+        if (left) {
+            jp = r - bb + 1;  // index of split r
+            pl = l;
+            const int j = jp < kTB ? nearest_right(s_t, jp, dr) : -1;
+            inside = j >= 0;
+            pr = bb - 1 + j;
+        } else {
+            jp = l - bb;  // index of split l-1
+            pr = r;
+            const int j = jp > 0 ? nearest_left(s_t, jp, dl) : -1;
+            inside = j >= 0;
+            pl = bb + j;
+        }
+        if (!inside) {
+            emit[k] = true;
+            OpenTree& o = ot[k];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                o.lo[q] = blo[q];
+                o.hi[q] = bhi[q];
+            }
+            o.l = l;
+            o.r = r;
+            o.self = self;
+            continue;
+        }
+        const bool root = pl == 0 && pr == nG - 1;
+        if (!root && G.tris(pl, pr) <= G.leaf) continue;  // the parent is a leaf of its own parent
+        const int p = bb - 1 + jp;
+        store_half(nodes + (root ? 0 : p + 1), left ? 0 : 1, blo, bhi, G.idx(l, r, self), G.cnt(l, r));
+    }
+    // Open subtrees are packed densely for k_build_cross.
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const unsigned m = __ballot_sync(0xffffffffu, emit[k]);
+        if (!m) continue;
+        unsigned int slot = 0;
+        if (lane == __ffs(m) - 1) slot = atomicAdd(n_open, (unsigned int)__popc(m));
+        slot = __shfl_sync(0xffffffffu, slot, __ffs(m) - 1) + __popc(m & ((1u << lane) - 1u));
+        if (emit[k]) open[slot] = ot[k];
+    }
+}
+
 // Cross-block merges, one open subtree per thread: at split p the child writes its box and
 // entry into its half of node slot p+1, then exchanges its outer range bound in xchg[p]
 // with acquire-release semantics; the first arrival stops, the second reads its sibling's
@@ -671,7 +871,7 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
         cudaMemsetAsync(xchg, 0xff, (size_t)std::max(nG - 1, 1) * sizeof(int), s);
         cudaMemsetAsync(n_open, 0, sizeof(unsigned int), s);
         const int utok = prof_begin(P_BUILD_UP, s);
-        launch(k_build_up, (nG + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys,
+        launch(k_build_tree, (nG + kTB - 1) / kTB, kTB, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys,
                G, nG, h->tris, h->nodes, open, n_open);
         prof_end(P_BUILD_UP, s, utok);
         if (nG == 1)

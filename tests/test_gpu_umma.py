@@ -26,7 +26,7 @@ def _gemm(A, B, mode):
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 256, 64), (1, 256, 128), (37, 512, 512), (256, 512, 32768), (300, 256, 1024),
-                                   (1024, 512, 4096)])
+                                   (1024, 512, 4096), (4096, 512, 32768)])
 def test_umma_gemm_matches_fp32_matmul(cuda, M, N, K):
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N + K)
     A = (torch.rand(M, K, device="cuda", generator=g) * 4 - 2).to(torch.bfloat16)
