@@ -321,9 +321,9 @@ def run_engine(args, rank, world, local):
     with torch.cuda.stream(stream):
         rc = recheck(L, lambda: (step(da, db), torch.cuda.synchronize()))
 
-    # Roofline of the join's dominant kernel by the launch list, k_build_up (the bottom-up
-    # tree of each BVH build; two launches per join, one per set, on two concurrent
-    # streams).  Algorithmic bytes per launch: the set's triangles read once (12 B per
+    # Roofline of the join's dominant kernel by the launch list, k_build_tree (the triangles
+    # in leaf order and the tree of each BVH build; two launches per join, one per set, on
+    # two concurrent streams).  Algorithmic bytes per launch: the set's triangles read once (12 B per
     # vertex, 16 B index triple and object id per triangle), the sorted 8 B keys, the 48 B
     # leaf-ordered triangles written, and 64 B for each tree node over more than
     # leaf_size triangles (at least nF / leaf_size - 1 of them).
@@ -334,10 +334,10 @@ def run_engine(args, rank, world, local):
         leaf = 2
         per_launch = sum(12.0 * g.nV + (16.0 + 8.0 + 48.0) * g.nF + 64.0 * (g.nF / leaf - 1) for g in (da, db)) / 2.0
         achieved = per_launch / (p["avg_ms"] * 1e-3) / 1e9
-        roof = {"bound": "hbm", "kernel": "k_build_up", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+        roof = {"bound": "hbm", "kernel": "k_build_tree", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 5), "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
                 "algorithmic_bytes_per_launch": int(per_launch), "avg_launch_ms": round(p["avg_ms"], 4),
-                "traffic": profiled_traffic("k_build_up", args.objects)}
+                "traffic": profiled_traffic("k_build_tree", args.objects)}
     # The edge rays of one join (the live-edge check of both directions in one launch, then
     # each direction's rays for its live edges, the two directions concurrently; one timed
     # interval per join), against the bytes they would move if every edge were traced: each

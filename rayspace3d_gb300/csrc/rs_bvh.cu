@@ -8,11 +8,11 @@
 //      vertex bounds) << 32 | triangle id, unique by construction;
 //   3. stable radix sort of the 32 Morton bits only (4 passes; ids stay ascending
 //      within equal codes);
-//   4. groups of leaf_size / 2 consecutive sorted triangles; a bottom-up pass
-//      (k_build_up) writes the triangles in leaf order (3 x float4 each), builds the
-//      binary radix tree over the groups' keys agglomeratively and refits its boxes on
-//      the way up, emitting 64-byte nodes in which subtrees of <= leaf_size triangles
-//      become leaves, as far as one block of groups reaches;
+//   4. groups of leaf_size / 2 consecutive sorted triangles; k_build_tree writes the
+//      triangles in leaf order (3 x float4 each) and, per block of 256 groups, every
+//      subtree of the binary radix tree over the groups' keys that lies in the block,
+//      each from shared-memory range tables (64-byte nodes; subtrees of <= leaf_size
+//      triangles become leaves);
 //   5. k_build_cross joins the subtrees left open across blocks.
 #include <algorithm>
 #include <cstdio>
@@ -290,161 +290,11 @@ struct Groups {
     }
 };
 
-// A subtree left open by k_build_up: box, group range, node slot.
+// A subtree left open by k_build_tree: box, group range, node slot.
 struct OpenTree {
     float lo[3], hi[3];
     int l, r, self;
 };
-
-// Bottom-up construction of the binary radix tree over the leaf groups, fused with the
-// emission of the leaf-ordered triangles and the box refit (agglomerative LBVH, Apetrei
-// 2014, "Fast and Simple Agglomerative LBVH Construction").  Its leaves are groups of L
-// consecutive sorted triangles (group g = sorted triangles [gL, gL+L)), ordered by the
-// key of their first triangle; the tree is the radix tree of those group keys, the same
-// tree Karras' top-down construction gives, and subtrees of <= leaf triangles are
-// entered as leaves by their parents.  Thread k owns group k and starts with
-// the subtree [k, k].  A subtree [l, r] joins the neighbouring split whose keys share the
-// longer prefix: split r (it is the left child) or split l-1 (the right child); a split
-// with no neighbour on one side takes the other.
-//
-// Merges inside the block run in lock-step rounds through shared memory: a subtree is
-// owned by the thread of its leftmost group, so a left child finds its right sibling at
-// thread r+1 and merges when that thread holds a complete subtree that chose the same
-// split.  The rounds end when no merge happens; the subtrees still open go to
-// k_build_cross.  Node slot p+1 holds split p, slot 0 the root.
-// Six blocks per SM (40 registers): the merge rounds stall on barriers, and more resident
-// blocks hide them; eight (32 registers) spill and run slower.
-__global__ void __launch_bounds__(kT, 6) k_build_up(const float* __restrict__ V, uint64_t nV,
-                                                 const uint32_t* __restrict__ I, const int32_t* __restrict__ t2o,
-                                                 const uint64_t* __restrict__ keys, Groups G, int nG,
-                                                 float4* __restrict__ tris, BNode* __restrict__ nodes,
-                                                 OpenTree* __restrict__ open, unsigned int* __restrict__ n_open) {
-    __shared__ int s_d[kT + 1];  // split prefixes of splits bb-1 .. bb+kT-1
-    __shared__ int s_r[kT], s_self[kT];
-    __shared__ float s_box[6][kT];
-    __shared__ unsigned char s_state[kT];  // bit 0: open subtree, bit 1: left child
-    __shared__ unsigned char s_abs[kT];
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int bb = blockIdx.x * kT;
-    const int k = bb + tid;
-    const bool valid = k < nG;
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    if (valid) {
-        const int j0 = k * G.L, j1 = min(G.n, j0 + G.L);
-        const uint64_t last = nV - 1;
-        for (int j = j0; j < j1; ++j) {
-            // The low word is a triangle id; the clamp only matters after a failed sort.
-            const uint32_t t = min((uint32_t)(__ldg(&keys[j]) & 0xffffffffull), (uint32_t)(G.n - 1));
-            const uint64_t i0 = min((uint64_t)I[3 * (uint64_t)t], last),
-                           i1 = min((uint64_t)I[3 * (uint64_t)t + 1], last),
-                           i2 = min((uint64_t)I[3 * (uint64_t)t + 2], last);
-            float a[3], b[3], c[3];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                a[q] = V[3 * i0 + q];
-                b[q] = V[3 * i1 + q];
-                c[q] = V[3 * i2 + q];
-                lo[q] = fminf(lo[q], fminf(fminf(a[q], b[q]), c[q]));
-                hi[q] = fmaxf(hi[q], fmaxf(fmaxf(a[q], b[q]), c[q]));
-            }
-            tris[3 * (uint64_t)j] = make_float4(a[0], a[1], a[2], __uint_as_float(t));
-            tris[3 * (uint64_t)j + 1] = make_float4(b[0], b[1], b[2], __int_as_float(t2o[t]));
-            tris[3 * (uint64_t)j + 2] = make_float4(c[0], c[1], c[2], 0.0f);
-        }
-    }
-    s_d[tid + 1] = (k < nG - 1) ? group_prefix(keys, k, G.L) : -1;
-    if (tid == 0) s_d[0] = (bb > 0 && bb - 1 < nG - 1) ? group_prefix(keys, bb - 1, G.L) : -1;
-    s_abs[tid] = 0;
-    s_state[tid] = 0;
-    int l = k, r = k, self = 0;
-    bool active = valid && nG > 1;  // a single group is the root's only child (k_one_group_root)
-    // Role of the owned subtree: -1 not yet decided, 0 right child (its state is published
-    // in shared memory, and stays until it is absorbed: a right child never merges), 1 left
-    // child (it merges with the subtree at thread r + 1 once that one is a complete right
-    // child).  A thread publishes only when its role is decided, so most threads stop
-    // writing after their first merges.
-    int role = -1;
-    __syncthreads();
-    // Two barriers per round: (1) a right child absorbed in the previous round's merge phase
-    // retires, and threads without a role publish one; (2) left children merge with their
-    // complete right siblings, and the round's barrier also tells whether anything merged.
-    for (int round = 0; round < kT; ++round) {
-        if (active && role == 0 && s_abs[tid]) {
-            active = false;
-            s_state[tid] = 0;
-        }
-        if (active && role < 0) {
-            const int dr = s_d[r - bb + 1], dl = s_d[l - bb];
-            const bool left_child = (l == 0) ? true : (r == nG - 1) ? false : dr > dl;
-            if (left_child) {
-                s_state[tid] = 3;
-                role = 1;
-            } else {
-                s_r[tid] = r;
-                s_self[tid] = self;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    s_box[q][tid] = lo[q];
-                    s_box[3 + q][tid] = hi[q];
-                }
-                s_state[tid] = 1;
-                role = 0;
-            }
-        }
-        __syncthreads();
-        bool merged = false;
-        const int sib = r + 1 - bb;
-        if (active && role == 1 && sib < kT && r + 1 < nG && s_state[sib] == 1) {
-            const int p = r;
-            const int o_r = s_r[sib];
-            float olo[3], ohi[3];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                olo[q] = s_box[q][sib];
-                ohi[q] = s_box[3 + q][sib];
-            }
-            // A node of <= leaf triangles is entered as a leaf by its parent, so its slot is
-            // only written when it is larger (or the root).
-            if (G.tris(l, o_r) > G.leaf || (l == 0 && o_r == nG - 1))
-                store_node(nodes + (p + 1), lo, hi, G.idx(l, r, self), G.cnt(l, r), olo, ohi,
-                           G.idx(r + 1, o_r, s_self[sib]), G.cnt(r + 1, o_r));
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                lo[q] = fminf(lo[q], olo[q]);
-                hi[q] = fmaxf(hi[q], ohi[q]);
-            }
-            r = o_r;
-            self = p + 1;
-            s_abs[sib] = 1;
-            merged = true;
-            role = -1;
-            if (l == 0 && r == nG - 1) {
-                const BNode nd = nodes[self];
-                nodes[0] = nd;
-                active = false;
-                s_state[tid] = 0;
-            }
-        }
-        if (!__syncthreads_or(merged)) break;
-    }
-    // Open subtrees are packed densely for k_build_cross, so that its latency-bound walks
-    // do not hold this kernel's blocks.
-    const unsigned m = __ballot_sync(0xffffffffu, active);
-    if (!m) return;
-    unsigned int slot = 0;
-    if (lane == __ffs(m) - 1) slot = atomicAdd(n_open, (unsigned int)__popc(m));
-    slot = __shfl_sync(0xffffffffu, slot, __ffs(m) - 1) + __popc(m & ((1u << lane) - 1u));
-    if (!active) return;
-    OpenTree& o = open[slot];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        o.lo[q] = lo[q];
-        o.hi[q] = hi[q];
-    }
-    o.l = l;
-    o.r = r;
-    o.self = self;
-}
 
 // Bottom-up-free construction of the radix tree over the leaf groups of one block of kTB
 // groups (the tree Karras' top-down construction gives: Karras 2012, "Maximizing

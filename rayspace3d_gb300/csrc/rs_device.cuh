@@ -459,8 +459,10 @@ constexpr int kStack = 64;
 // for it.  The stack lives at stack[sp * stride] (a thread-private array, or a column
 // of a shared-memory array).  A valid tree visits each node at most once, so
 // `max_steps` (the node count) bounds the loop even if the node array were corrupt.
-// Returns false on stack overflow or an exhausted step budget.
-template <int AXIS, int STACK = kStack, class F>
+// Returns false on stack overflow or an exhausted step budget.  ORDERED visits first the
+// child the ray enters first, for callers that shrink r.tmax as hits come in: the far
+// child's subtree is then mostly rejected by the shrunken range when it is popped.
+template <int AXIS, int STACK = kStack, bool ORDERED = false, class F>
 __device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNode* __restrict__ nodes,
                                               uint32_t max_steps, const Ray& r, F&& on_leaf) {
     int sp = 0;
@@ -473,16 +475,17 @@ __device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNod
         const int4 nd = __ldg(&nodes[node].d);
         const float lo0[3] = {na.x, na.y, na.z}, hi0[3] = {na.w, nb.x, nb.y};
         const float lo1[3] = {nb.z, nb.w, nc.x}, hi1[3] = {nc.y, nc.z, nc.w};
-        float e, x;
-        bool h0 = slab<AXIS>(r, lo0, hi0, r.tmin, r.tmax, e, x);
-        bool h1 = slab<AXIS>(r, lo1, hi1, r.tmin, r.tmax, e, x);
+        float e0, x0, e1, x1;
+        bool h0 = slab<AXIS>(r, lo0, hi0, r.tmin, r.tmax, e0, x0);
+        bool h1 = slab<AXIS>(r, lo1, hi1, r.tmin, r.tmax, e1, x1);
         if (h0 && nd.y > 0) { on_leaf(nd.x, nd.y); h0 = false; }
         if (h1 && nd.w > 0) { on_leaf(nd.z, nd.w); h1 = false; }
         if (h0 && h1) {
             if (sp == STACK) return false;
-            stack[sp * stride] = nd.z;
+            const bool first1 = ORDERED && e1 < e0;
+            stack[sp * stride] = first1 ? nd.x : nd.z;
             ++sp;
-            node = nd.x;
+            node = first1 ? nd.z : nd.x;
         } else if (h0) {
             node = nd.x;
         } else if (h1) {
@@ -496,11 +499,11 @@ __device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNod
     return true;
 }
 
-template <int AXIS, int STACK = kStack, class F>
+template <int AXIS, int STACK = kStack, bool ORDERED = false, class F>
 __device__ __forceinline__ bool traverse(const BNode* __restrict__ nodes, uint32_t max_steps, const Ray& r,
                                          F&& on_leaf) {
     int stack[STACK];
-    return traverse_with<AXIS, STACK>(stack, 1, nodes, max_steps, r, on_leaf);
+    return traverse_with<AXIS, STACK, ORDERED>(stack, 1, nodes, max_steps, r, on_leaf);
 }
 
 __device__ __forceinline__ void load_tri(const float4* __restrict__ tris, int k, float* a, float* b, float* c,

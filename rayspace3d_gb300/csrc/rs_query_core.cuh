@@ -471,9 +471,9 @@ __device__ __forceinline__ bool segment_fast(const EdgeColumn& col, const Ray& r
 
 // Long path, in the reference loop's order: the crossings in [t_min, len + 1e-6] are
 // walked in (t, triangle id) order with the table's hit rule, kLongChunk at a time.  Each
-// pass traverses once and keeps the kLongChunk smallest crossings beyond the last one
-// walked (the ray's tmax shrinks to the largest kept one once the chunk is full, so the
-// pass visits little beyond it); the walk then takes them, and a full chunk starts the
+// pass traverses once, nearer child first, and keeps the kLongChunk smallest crossings
+// beyond the last one walked (the ray's tmax shrinks to the largest kept one once the
+// chunk is full, so the pass visits little beyond it); the walk then takes them, and a full chunk starts the
 // next pass after its last crossing.  A crossing's t does not depend on tmin or tmax (the
 // node and triangle slab tests only accept or reject), so the passes see exactly the
 // crossings the reference's one-hit-per-trace loop sees, in the same order, while an
@@ -496,7 +496,7 @@ __device__ __forceinline__ void segment_long(Ray r, const int32_t* __restrict__ 
         uint32_t lid[kLongChunk];
         int32_t lobj[kLongChunk];
         int n = 0;
-        const bool ok = traverse<-1, kStack>(nodes, max_steps, r, [&](int first, int cnt) {
+        const bool ok = traverse<-1, kStack, true>(nodes, max_steps, r, [&](int first, int cnt) {
             for (int k = first; k < first + cnt; ++k) {
                 float a[3], b[3], c[3];
                 uint32_t tid;
