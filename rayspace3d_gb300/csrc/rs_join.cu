@@ -36,6 +36,15 @@ constexpr uint64_t kBinMaxEdges = 1ull << 27;
 // cost more than the coherence saves.
 constexpr unsigned int kBinMinLive = 1u << 16;
 
+// Live lists of at most kWarpRayMax edges are traced one warp per edge (k_edge_rays_warp),
+// longer ones one thread per edge (k_edge_rays): with few rays the join waits on the
+// longest chain of dependent node loads, which a warp shortens to the tree's depth plus
+// its node count over 32.
+constexpr unsigned int kWarpRayMax = 4096;
+constexpr int kWarpRayWarps = 8;   // warps per block
+constexpr int kWarpRayStack = 128; // entries of a warp's stack
+constexpr int kWarpRayHits = 16;   // crossings a warp keeps; an edge with more is deferred
+
 // Fast path over the edges order[0..*n_order) of a payload of n_direct edges (or over all
 // of them when order is null); the edges it defers go to deferred[0..*n_def).
 __global__ void __launch_bounds__(kT) k_edge_rays(EdgePayload p, const uint32_t* __restrict__ order,
@@ -47,12 +56,157 @@ __global__ void __launch_bounds__(kT) k_edge_rays(EdgePayload p, const uint32_t*
     __shared__ EdgeSmem<kT, kFastStack> sm;
     const EdgeColumn col = sm.column(threadIdx.x);
     const uint64_t n = live ? (uint64_t)*n_order : n_direct;
+    if (live && n <= kWarpRayMax) return;  // k_edge_rays_warp traces short live lists
     // The cell-ordered list when the job was binned and is long enough, else the live list.
     if (live) order = (order && n >= kBinMinLive) ? order : live;
     for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t e = order ? order[j] : (uint32_t)j;
         if (e >= n_direct) continue;  // never, for a list of this payload's edges
         if (!edge_ray_fast<kFastStack>(col, p, e, nodes, max_steps, tris, swap, table))
+            deferred[atomicAdd(n_def, 1u)] = e;
+    }
+}
+
+// Fast path of one edge by one warp: the lanes pop up to 32 nodes per step from the warp's
+// shared-memory stack, test both children of each, test the triangles of the leaves hit
+// and push the inner children hit; crossings go to a shared-memory list.  Visits the nodes
+// the one-thread traversal visits (the same slab tests over the same [tmin, tmax]), so it
+// finds the same crossings; lane 0 sorts them by (t, id) and walks them with the table's
+// hit rule.  Returns false, having inserted nothing, when there are more than
+// kWarpRayHits crossings or the stack or the step budget runs out.
+__device__ bool edge_ray_warp(int* stack, float* ht, uint32_t* hid, int32_t* hobj, const EdgePayload& p, uint64_t i,
+                              const BNode* __restrict__ nodes, uint32_t max_steps, const float4* __restrict__ tris,
+                              int swap, const PairTable& table) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    Ray r;
+    if (!segment_ray_of(p.starts[3 * i], p.starts[3 * i + 1], p.starts[3 * i + 2], p.ends[3 * i], p.ends[3 * i + 1],
+                        p.ends[3 * i + 2], r))
+        return true;
+    if (lane == 0) stack[0] = 0;
+    __syncwarp();
+    int sp = 1, nh = 0;
+    uint32_t visits = 0;
+    bool ok = true;
+    unsigned int tests = 0;
+    while (sp > 0) {
+        const int take = min(sp, 32);
+        const int node = lane < take ? stack[sp - take + lane] : -1;
+        __syncwarp();
+        sp -= take;
+        visits += (uint32_t)take;
+        if (visits > max_steps) {
+            ok = false;
+            break;
+        }
+        bool h[2] = {false, false};
+        int first[2] = {0, 0}, cnt[2] = {0, 0};
+        if (node >= 0) {
+            const float4 na = __ldg(&nodes[node].a), nb = __ldg(&nodes[node].b), nc = __ldg(&nodes[node].c);
+            const int4 nd = __ldg(&nodes[node].d);
+            const float lo0[3] = {na.x, na.y, na.z}, hi0[3] = {na.w, nb.x, nb.y};
+            const float lo1[3] = {nb.z, nb.w, nc.x}, hi1[3] = {nc.y, nc.z, nc.w};
+            float e, x;
+            h[0] = slab<-1>(r, lo0, hi0, r.tmin, r.tmax, e, x);
+            h[1] = slab<-1>(r, lo1, hi1, r.tmin, r.tmax, e, x);
+            first[0] = nd.x;
+            cnt[0] = nd.y;
+            first[1] = nd.z;
+            cnt[1] = nd.w;
+        }
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const int mine = (h[side] && cnt[side] > 0) ? cnt[side] : 0;
+            tests += (unsigned int)mine;
+            const int rounds = __reduce_max_sync(0xffffffffu, mine);
+            for (int k = 0; k < rounds; ++k) {
+                bool hit = false;
+                float t = 0.0f;
+                uint32_t tid = 0;
+                int32_t obj = 0;
+                if (k < mine) {
+                    float a[3], b[3], c[3];
+                    load_tri(tris, first[side] + k, a, b, c, tid, obj);
+                    hit = hit_triangle<-1>(r, a, b, c, t);
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) {
+                    const int pos = nh + __popc(m & lt);
+                    if (pos < kWarpRayHits) {
+                        ht[pos] = t;
+                        hid[pos] = tid;
+                        hobj[pos] = obj;
+                    }
+                }
+                nh += __popc(m);
+            }
+        }
+        const bool p0 = h[0] && cnt[0] == 0, p1 = h[1] && cnt[1] == 0;
+        const unsigned b0 = __ballot_sync(0xffffffffu, p0), b1 = __ballot_sync(0xffffffffu, p1);
+        const int total = __popc(b0) + __popc(b1);
+        if (sp + total > kWarpRayStack) {
+            ok = false;
+            break;
+        }
+        int pos = sp + __popc(b0 & lt) + __popc(b1 & lt);
+        if (p0) stack[pos++] = first[0];
+        if (p1) stack[pos] = first[1];
+        __syncwarp();
+        sp += total;
+    }
+    add_tests(tests);
+    __syncwarp();
+    if (!ok || nh > kWarpRayHits) return false;
+    if (lane == 0) {
+        // Insertion sort of the crossings by (t, id), then the walk.
+        for (int a = 1; a < nh; ++a) {
+            const float t = ht[a];
+            const uint32_t id = hid[a];
+            const int32_t ob = hobj[a];
+            int b = a;
+            while (b > 0 && hit_less(t, id, ht[b - 1], hid[b - 1])) {
+                ht[b] = ht[b - 1];
+                hid[b] = hid[b - 1];
+                hobj[b] = hobj[b - 1];
+                --b;
+            }
+            ht[b] = t;
+            hid[b] = id;
+            hobj[b] = ob;
+        }
+        EdgeWalk w;
+        int32_t last = INT_MIN;
+        const int32_t* src = p.sources + p.offsets[i];
+        const int nsrc = p.counts[i];
+        for (int a = 0; a < nh; ++a) {
+            if (!w.take(ht[a], table.max_hits, table.next_float)) continue;
+            if (hobj[a] == last) continue;
+            last = hobj[a];
+            insert_sources(table, src, nsrc, last, swap);
+        }
+        count_edge(table, w.n);
+    }
+    __syncwarp();
+    return true;
+}
+
+__global__ void __launch_bounds__(32 * kWarpRayWarps) k_edge_rays_warp(
+    EdgePayload p, const uint32_t* __restrict__ live, const unsigned int* __restrict__ n_live, uint64_t n_direct,
+    const BNode* __restrict__ nodes, uint32_t max_steps, const float4* __restrict__ tris, int swap, PairTable table,
+    uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def) {
+    __shared__ int s_stack[kWarpRayWarps][kWarpRayStack];
+    __shared__ float s_t[kWarpRayWarps][kWarpRayHits];
+    __shared__ uint32_t s_id[kWarpRayWarps][kWarpRayHits];
+    __shared__ int32_t s_obj[kWarpRayWarps][kWarpRayHits];
+    const unsigned int n = *n_live;
+    if (n > kWarpRayMax) return;  // the one-thread kernel traces this list
+    const int wi = threadIdx.x >> 5;
+    const unsigned int nw = gridDim.x * kWarpRayWarps;
+    for (unsigned int j = blockIdx.x * kWarpRayWarps + wi; j < n; j += nw) {  // warp-uniform
+        const uint32_t e = live[j];
+        if (e >= n_direct) continue;
+        if (!edge_ray_warp(s_stack[wi], s_t[wi], s_id[wi], s_obj[wi], p, e, nodes, max_steps, tris, swap, table) &&
+            (threadIdx.x & 31) == 0)
             deferred[atomicAdd(n_def, 1u)] = e;
     }
 }
@@ -196,63 +350,85 @@ __device__ __forceinline__ uint32_t edge_cell(const EdgeJob& j, uint64_t i) {
     return code;
 }
 
-// Broad phase: the edges with at least one candidate source object (k_cull_query) are
-// appended to their job's `live` list; in binned jobs each also takes a rank within its
-// cell (one warp-aggregated atomic per cell and warp).  A light kernel, so the dependent
-// loads of many edges are in flight at once.  Blocks below blocks0 run job j0, the
-// others j1.
+// Whether edge i of job j is live, given its source count ns, its source list sp, and its
+// first source so0 with that object's flag c0 (loaded by the caller).
+__device__ __forceinline__ bool edge_is_live(const EdgeJob& j, uint64_t i, int ns, const int32_t* sp, int32_t so0,
+                                             uint8_t c0) {
+    float qlo[3], qhi[3];
+    bool have_box = false;
+    for (int q = 0; q < ns; ++q) {
+        const int32_t so = q == 0 ? so0 : sp[q];
+        if (so < 0 || (uint64_t)so >= j.n_cull) return true;
+        const uint8_t c = q == 0 ? c0 : j.cull[so];
+        if (c == 0) continue;
+        if (!j.part || c == kCandAll) return true;
+        // The edge is live when its own widened box reaches a partner's widened box.
+        if (!have_box) {
+            edge_query_box(j.p, i, qlo, qhi);
+            have_box = true;
+        }
+        const int32_t* pl = j.part + (uint64_t)so * kPartners;
+        for (int k = 0; k < (int)c; ++k) {
+            const int32_t b = pl[k];
+            if (b < 0 || (uint64_t)b >= j.n_pbox || box_overlaps(j.pbox + 6 * (uint64_t)b, qlo, qhi)) return true;
+        }
+    }
+    return false;
+}
+
+// Broad phase: the edges with at least one candidate source object (k_cull_flag /
+// k_cull_query) are appended to their job's `live` list; in binned jobs each also takes a
+// rank within its cell (one warp-aggregated atomic per cell and warp).  Each thread takes
+// kLiveEdges edges (a block's edges are contiguous, kLiveEdges rounds of blockDim) and
+// issues the dependent loads of all of them together -- count and offset, first source,
+// its flag -- so that a wave of threads keeps several chains in flight.  Blocks below
+// blocks0 run job j0, the others j1.
+constexpr int kLiveEdges = 4;
+
 __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsigned int blocks0) {
     const bool second = blockIdx.x >= blocks0;
     const EdgeJob& j = second ? j1 : j0;
-    const uint64_t i = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x + threadIdx.x;
-    bool any = false;
-    if (i < j.nE) {
-        const int ns = j.p.counts[i];
-        const int32_t* sp = j.p.sources + j.p.offsets[i];
-        float qlo[3], qhi[3];
-        bool have_box = false;
-        for (int q = 0; q < ns && !any; ++q) {
-            const int32_t so = sp[q];
-            if (so < 0 || (uint64_t)so >= j.n_cull) {
-                any = true;
-                break;
-            }
-            const uint8_t c = j.cull[so];
-            if (c == 0) continue;
-            if (!j.part || c == kCandAll) {
-                any = true;
-                break;
-            }
-            // The edge is live when its own widened box reaches a partner's widened box.
-            if (!have_box) {
-                edge_query_box(j.p, i, qlo, qhi);
-                have_box = true;
-            }
-            const int32_t* pl = j.part + (uint64_t)so * kPartners;
-            for (int k = 0; k < (int)c && !any; ++k) {
-                const int32_t b = pl[k];
-                any = b < 0 || (uint64_t)b >= j.n_pbox || box_overlaps(j.pbox + 6 * (uint64_t)b, qlo, qhi);
-            }
-        }
+    const uint64_t base = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * blockDim.x * kLiveEdges + threadIdx.x;
+    int ns[kLiveEdges], off[kLiveEdges];
+    int32_t so0[kLiveEdges];
+    uint8_t c0[kLiveEdges];
+#pragma unroll
+    for (int u = 0; u < kLiveEdges; ++u) {
+        const uint64_t i = base + (uint64_t)u * blockDim.x;
+        const bool valid = i < j.nE;
+        ns[u] = valid ? j.p.counts[i] : 0;
+        off[u] = valid ? j.p.offsets[i] : 0;
     }
-    const unsigned int m = __ballot_sync(0xffffffffu, any);
-    if (!m) return;
-    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+#pragma unroll
+    for (int u = 0; u < kLiveEdges; ++u) so0[u] = ns[u] > 0 ? j.p.sources[off[u]] : -1;
+#pragma unroll
+    for (int u = 0; u < kLiveEdges; ++u)
+        c0[u] = (ns[u] > 0 && so0[u] >= 0 && (uint64_t)so0[u] < j.n_cull) ? j.cull[so0[u]] : (uint8_t)0;
+    const int lane = threadIdx.x & 31;
     const unsigned int below = (1u << lane) - 1u;
-    unsigned int base = 0;
-    if (lane == leader) base = atomicAdd(j.n_live, (unsigned int)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (!any) return;
-    const unsigned int pos = base + __popc(m & below);
-    j.live[pos] = (uint32_t)i;
-    if (j.order) {
-        const uint32_t cell = edge_cell(j, i);
-        const unsigned int peers = __match_any_sync(m, cell);
-        const int first = __ffs(peers) - 1;
-        unsigned int r0 = 0;
-        if (lane == first) r0 = atomicAdd(&j.cells[cell], (unsigned int)__popc(peers));
-        r0 = __shfl_sync(peers, r0, first);
-        j.rank[pos] = r0 + __popc(peers & below);
+#pragma unroll
+    for (int u = 0; u < kLiveEdges; ++u) {
+        const uint64_t i = base + (uint64_t)u * blockDim.x;
+        const bool any = ns[u] > 0 && edge_is_live(j, i, ns[u], j.p.sources + off[u], so0[u], c0[u]);
+        const unsigned int m = __ballot_sync(0xffffffffu, any);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned int pos0 = 0;
+        if (lane == leader) pos0 = atomicAdd(j.n_live, (unsigned int)__popc(m));
+        pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+        const unsigned int pos = pos0 + __popc(m & below);
+        if (any) j.live[pos] = (uint32_t)i;
+        if (j.order) {
+            // Every lane takes part in the match (lanes without a live edge with a cell of
+            // their own, kCells + lane), so that the mask is the full warp.
+            const uint32_t cell = any ? edge_cell(j, i) : (uint32_t)kCells + lane;
+            const unsigned int peers = __match_any_sync(0xffffffffu, cell);
+            const int first = __ffs(peers) - 1;
+            unsigned int r0 = 0;
+            if (any && lane == first) r0 = atomicAdd(&j.cells[cell], (unsigned int)__popc(peers));
+            r0 = __shfl_sync(0xffffffffu, r0, first);
+            if (any) j.rank[pos] = r0 + __popc(peers & below);
+        }
     }
 }
 
@@ -858,7 +1034,7 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
             j.cells = next_cells;
             next_cells += kCells;
         }
-        blocks[d] = (j.nE + 255) / 256;
+        blocks[d] = (j.nE + 256 * kLiveEdges - 1) / (256 * kLiveEdges);
         total_e += j.nE;
     }
     if (e == cudaSuccess && total_e) {
@@ -887,6 +1063,11 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
         for (int d = 0; d < n_jobs; ++d) {
             const EdgeJob& j = jobs[d];
             cudaStream_t st = d == 1 && side ? side : s;
+            launch(k_edge_rays_warp,
+                   (unsigned)std::min<uint64_t>((std::min<uint64_t>(j.nE, kWarpRayMax) + kWarpRayWarps - 1) /
+                                                    kWarpRayWarps, 4ull * sm_count()),
+                   32 * kWarpRayWarps, 0, st, j.p, (const uint32_t*)j.live, (const unsigned int*)j.n_live, j.nE,
+                   j.nodes, j.max_steps, j.tris, j.swap, table, j.rank, j.n_def);
             launch(k_edge_rays, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 8ull * sm_count()), kT, 0, st, j.p,
                    (const uint32_t*)j.order, (const uint32_t*)j.live, (const unsigned int*)j.n_live, j.nE, j.nodes,
                    j.max_steps, j.tris, j.swap, table, j.rank, j.n_def);
