@@ -35,9 +35,17 @@ __device__ __forceinline__ int flt_ord(float f) {
 }
 __device__ __forceinline__ float ord_flt(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
-// bounds[0..2] = min (ordered ints), [3..5] = max; [6..11] same for vertices.
-__global__ void k_init_bounds(int* b) {
-    if (threadIdx.x < 12) b[threadIdx.x] = (threadIdx.x % 6) < 3 ? 0x7fffffff : (int)0x80000000;
+// The build's scratch words, in one launch: bounds[0..2] = min (ordered ints), [3..5] =
+// max, [6..11] the same for vertices, [12] the error flags = 0, [13] the largest object id
+// = -1; the open-subtree count = 0; every cross-block exchange word = -1.
+__global__ void k_build_init(int* __restrict__ b, unsigned int* __restrict__ n_open, int* __restrict__ xchg,
+                             uint64_t n_xchg) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < 12) b[i] = (i % 6) < 3 ? 0x7fffffff : (int)0x80000000;
+    if (i == 12) b[12] = 0;
+    if (i == 13) b[13] = -1;
+    if (i == 14 && n_open) *n_open = 0;
+    for (uint64_t k = i; k < n_xchg; k += (uint64_t)gridDim.x * blockDim.x) xchg[k] = -1;
 }
 
 // Block-wide min/max of the three components (and the largest object id), then one atomic
@@ -642,9 +650,7 @@ int bvh_use(const rs_bvh* h, cudaStream_t s) {
 static void bvh_free(rs_bvh* h) {
     if (h->done) cudaEventSynchronize(h->done);
     pinned_slot_release(h->pending);
-    if (h->nodes) cudaFree(h->nodes);
-    if (h->tris) cudaFree(h->tris);
-    if (h->obox) cudaFree(h->obox);
+    if (h->mem) cudaFree(h->mem);
     for (auto& g : h->cgrid) {
         if (g.start) cudaFree(g.start);
         if (g.list) cudaFree(g.list);
@@ -674,11 +680,6 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     h->leaf_size = leaf_size;
     cudaGetDevice(&h->device);
     const int n = (int)nF;
-    int* bounds = nullptr;  // [6..11] vertex bounds (ordered ints), [12] bad-index flag, [13] max object
-    uint64_t* keys = nullptr;
-    int* xchg = nullptr;
-    OpenTree* open = nullptr;
-    unsigned int* n_open = nullptr;
     cudaError_t e = cudaSuccess;
     int* slot = nullptr;
     const int grid = 4 * sm_count();
@@ -688,38 +689,57 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     const int nG = (n + group - 1) / group;
     h->n_nodes = nG >= 2 ? (uint64_t)nG : 1;  // slot 0 = root, slot p+1 = split p
     h->n_tris = (uint64_t)n;
+    // Object boxes for the broad phase of the joins, for up to min(nF, 2^24) objects
+    // (dense ids: every object has a triangle); more objects, and the joins compute them.
+    h->obox_cap = std::min<uint64_t>(nF, 1ull << 24);
+    auto a256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    // The handle's arrays in one allocation: nodes | tris | obox.
+    const size_t b_nodes = a256(h->n_nodes * sizeof(BNode)), b_tris = a256(3 * (size_t)n * sizeof(float4));
+    const size_t b_obox = a256(6 * h->obox_cap * sizeof(int));
+    // The build's scratch in another: 256 bytes of words (bounds[14], the open count) |
+    // exchange words | keys | open subtrees (at most two per level of the tree -- 64 key
+    // bits -- per block of kTB groups, so nG / 2 + kTB bound them) | the sort's scratch.
+    const size_t n_xchg = (size_t)std::max(nG - 1, 1);
+    const size_t b_xchg = a256(n_xchg * sizeof(int)), b_keys = a256((size_t)n * sizeof(uint64_t));
+    const size_t b_open = a256(((size_t)nG / 2 + kTB) * sizeof(OpenTree));
+    const size_t b_sort = radix_sort_scratch_bytes((size_t)n, 64, 32, false);
+    char* scratch = nullptr;
+    int* bounds = nullptr;  // [6..11] vertex bounds (ordered ints), [12] bad-index flag, [13] max object
+    unsigned int* n_open = nullptr;
+    int* xchg = nullptr;
+    uint64_t* keys = nullptr;
+    OpenTree* open = nullptr;
     const int ptok = prof_begin(P_BVH_BUILD, s);
-    e = alloc(&h->nodes, h->n_nodes, s);
-    if (e == cudaSuccess) e = alloc(&h->tris, 3 * (size_t)n, s);
-    if (e == cudaSuccess) e = alloc(&bounds, 14, s);
+    e = dmalloc(&h->mem, b_nodes + (n ? b_tris + b_obox : 0), s);
+    if (e == cudaSuccess) e = dmalloc((void**)&scratch, 256 + (n ? b_xchg + b_keys + b_open + b_sort : 0), s);
     if (e != cudaSuccess) goto fail;
-    launch(k_init_bounds, 1, 32, 0, s, bounds);
-    cudaMemsetAsync(bounds + 12, 0, sizeof(int), s);
-    cudaMemsetAsync(bounds + 13, 0xff, sizeof(int), s);
+    h->nodes = reinterpret_cast<BNode*>(h->mem);
+    if (n) {
+        h->tris = reinterpret_cast<float4*>(static_cast<char*>(h->mem) + b_nodes);
+        h->obox = reinterpret_cast<int*>(static_cast<char*>(h->mem) + b_nodes + b_tris);
+    } else {
+        h->obox_cap = 0;
+    }
+    bounds = reinterpret_cast<int*>(scratch);
+    n_open = reinterpret_cast<unsigned int*>(scratch + 64);
+    if (n) {
+        xchg = reinterpret_cast<int*>(scratch + 256);
+        keys = reinterpret_cast<uint64_t*>(scratch + 256 + b_xchg);
+        open = reinterpret_cast<OpenTree*>(scratch + 256 + b_xchg + b_keys);
+    }
+    launch(k_build_init, (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n ? n_xchg : 0) / 256 + 1, grid)), 256, 0,
+           s, bounds, n_open, xchg, (uint64_t)(n ? n_xchg : 0));
     if (nV || nF) launch(k_vertex_bounds, grid, kT, 0, s, d_vertices, nV, d_tri2obj, nF, bounds, bounds + 13);
     if (n == 0) {
         launch(k_empty_root, 1, 1, 0, s, h->nodes);
     } else {
         const Groups G{n, group, leaf_size};
-        e = alloc(&keys, n, s);
-        if (e == cudaSuccess) e = alloc(&xchg, std::max(nG - 1, 1), s);
-        // Open subtrees per block: at most two per level of the tree (64 key bits), so
-        // nG / 2 + kT bounds them for blocks of kT groups.
-        if (e == cudaSuccess) e = alloc(&open, (size_t)nG / 2 + kT, s);
-        if (e == cudaSuccess) e = alloc(&n_open, 1, s);
-        if (e != cudaSuccess) goto fail;
-        // Object boxes for the broad phase of the joins, for up to min(nF, 2^24) objects
-        // (dense ids: every object has a triangle); more objects, and the joins compute them.
-        h->obox_cap = std::min<uint64_t>(nF, 1ull << 24);
-        e = alloc(&h->obox, 6 * h->obox_cap, s);
-        if (e != cudaSuccess) goto fail;
         launch(k_obox_init, 2 * sm_count(), kT, 0, s, h->obox, h->obox_cap, (const int*)(bounds + 13));
         launch(k_morton, (n + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, nF, d_tri2obj, (const int*)bounds,
                keys, reinterpret_cast<unsigned int*>(bounds + 12), h->obox, h->obox_cap);
-        e = radix_sort_u64(keys, nullptr, (size_t)n, 64, s, 32, reinterpret_cast<uint32_t*>(bounds + 12), 2u);
+        e = radix_sort_u64_in(keys, nullptr, (size_t)n, 64, s, 32, reinterpret_cast<uint32_t*>(bounds + 12), 2u,
+                              scratch + 256 + b_xchg + b_keys + b_open);
         if (e != cudaSuccess) goto fail;
-        cudaMemsetAsync(xchg, 0xff, (size_t)std::max(nG - 1, 1) * sizeof(int), s);
-        cudaMemsetAsync(n_open, 0, sizeof(unsigned int), s);
         const int utok = prof_begin(P_BUILD_UP, s);
         launch(k_build_tree, (nG + kTB - 1) / kTB, kTB, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys,
                G, nG, h->tris, h->nodes, open, n_open);
@@ -741,15 +761,10 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
 fail:
-    if (keys) cudaFreeAsync(keys, s);
-    if (xchg) cudaFreeAsync(xchg, s);
-    if (open) cudaFreeAsync(open, s);
-    if (n_open) cudaFreeAsync(n_open, s);
-    if (bounds) cudaFreeAsync(bounds, s);
+    if (scratch) cudaFreeAsync(scratch, s);
     if (e != cudaSuccess) {
-        if (h->nodes) cudaFreeAsync(h->nodes, s);
-        if (h->tris) cudaFreeAsync(h->tris, s);
-        if (h->obox) cudaFreeAsync(h->obox, s);
+        if (h->mem) cudaFreeAsync(h->mem, s);
+        h->mem = nullptr;
         h->nodes = nullptr;
         h->tris = nullptr;
         h->obox = nullptr;

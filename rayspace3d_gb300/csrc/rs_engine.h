@@ -41,6 +41,8 @@ struct rs_bvh {
     // pass, for the objects below obox_cap; valid when n_obj <= obox_cap.
     int* obox = nullptr;
     uint64_t obox_cap = 0;
+    // One device allocation holds nodes, tris and obox.
+    void* mem = nullptr;
     int device = 0;
     // Completion of the build, and its device result words until bvh_ready() has read
     // them (asynchronous builds); the fields above that come from them (vmin, vmax,

@@ -493,16 +493,38 @@ __global__ void __launch_bounds__(256) k_edge_order(EdgeJob j0, EdgeJob j1, unsi
 }
 
 // A stream per device for the second direction's rays, forked from and joined back into
-// the join's stream.
-cudaStream_t ray_side_stream() {
-    static cudaStream_t st[64] = {};
-    static std::mutex mu;
+// the join's stream, with its two events, created once.  The caller holds *lock (the
+// device's mutex) from recording the fork event until the join's stream waits on the
+// joined event, so that host threads never record over each other's events.  False when
+// they cannot be had: both directions then run on the join's stream.
+bool ray_side_stream(cudaStream_t* st_out, cudaEvent_t* fork, cudaEvent_t* joined, std::unique_lock<std::mutex>* lock) {
+    struct Side {
+        cudaStream_t st = nullptr;
+        cudaEvent_t fork = nullptr, joined = nullptr;
+        bool ok = false;
+        std::mutex mu;
+    };
+    static Side side[64];
+    static std::mutex create_mu;
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) return nullptr;
-    std::lock_guard<std::mutex> g(mu);
-    if (!st[dev] && cudaStreamCreateWithFlags(&st[dev], cudaStreamNonBlocking) != cudaSuccess) st[dev] = nullptr;
-    return st[dev];
+    if (dev < 0 || dev >= 64) return false;
+    Side& x = side[dev];
+    std::lock_guard<std::mutex> g(create_mu);
+    if (!x.ok) {
+        x.ok = cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking) == cudaSuccess &&
+               cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) == cudaSuccess &&
+               cudaEventCreateWithFlags(&x.joined, cudaEventDisableTiming) == cudaSuccess;
+        if (!x.ok) {
+            cudaGetLastError();
+            return false;
+        }
+    }
+    *st_out = x.st;
+    *fork = x.fork;
+    *joined = x.joined;
+    *lock = std::unique_lock<std::mutex>(x.mu);
+    return true;
 }
 
 __global__ void k_first_tri_init(int32_t* __restrict__ first, uint64_t nObj) {
@@ -1018,19 +1040,30 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
         jobs[d] = job[d];
         if (jobs[d].nE <= kBinMaxEdges) ++n_bin;
     }
+    // One allocation: the zeroed block, then each job's live, rank and (binned jobs) order
+    // lists, each 256-byte aligned; one memset clears the zeroed block.
     const size_t zbytes = (4 + (size_t)n_bin * kCells) * sizeof(uint32_t);
-    cudaError_t e = dmalloc((void**)&zeroed, zbytes, s);
+    auto a256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    size_t total = a256(zbytes);
+    for (int d = 0; d < n_jobs; ++d) {
+        const size_t bytes = a256(std::max<uint64_t>(jobs[d].nE, 1) * sizeof(uint32_t));
+        total += (jobs[d].nE <= kBinMaxEdges ? 3 : 2) * bytes;
+    }
+    cudaError_t e = dmalloc((void**)&zeroed, total, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(zeroed, 0, zbytes, s);
     uint32_t* next_cells = zeroed + 4;
+    char* next = reinterpret_cast<char*>(zeroed) + a256(zbytes);
     for (int d = 0; d < n_jobs && e == cudaSuccess; ++d) {
         EdgeJob& j = jobs[d];
-        const size_t bytes = std::max<uint64_t>(j.nE, 1) * sizeof(uint32_t);
+        const size_t bytes = a256(std::max<uint64_t>(j.nE, 1) * sizeof(uint32_t));
         j.n_live = zeroed + d;
         j.n_def = zeroed + 2 + d;
-        e = dmalloc((void**)&j.live, bytes, s);
-        if (e == cudaSuccess) e = dmalloc((void**)&j.rank, bytes, s);
-        if (e == cudaSuccess && j.nE <= kBinMaxEdges) {
-            e = dmalloc((void**)&j.order, bytes, s);
+        j.live = reinterpret_cast<uint32_t*>(next);
+        j.rank = reinterpret_cast<uint32_t*>(next + bytes);
+        next += 2 * bytes;
+        if (j.nE <= kBinMaxEdges) {
+            j.order = reinterpret_cast<uint32_t*>(next);
+            next += bytes;
             j.cells = next_cells;
             next_cells += kCells;
         }
@@ -1052,11 +1085,11 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
         // list's rays are latency-bound chains when the lists are short, and a full list
         // keeps the GPU busy either way.
         const PairTable table = table_view(ps);
-        cudaStream_t side = n_jobs == 2 ? ray_side_stream() : nullptr;
+        cudaStream_t side = nullptr;
         cudaEvent_t fork = nullptr, joined = nullptr;
-        if (side && (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess ||
-                     cudaEventCreateWithFlags(&joined, cudaEventDisableTiming) != cudaSuccess ||
-                     cudaEventRecord(fork, s) != cudaSuccess || cudaStreamWaitEvent(side, fork, 0) != cudaSuccess)) {
+        std::unique_lock<std::mutex> side_lock;
+        if (n_jobs == 2 && ray_side_stream(&side, &fork, &joined, &side_lock) &&
+            (cudaEventRecord(fork, s) != cudaSuccess || cudaStreamWaitEvent(side, fork, 0) != cudaSuccess)) {
             cudaGetLastError();
             side = nullptr;  // both on s
         }
@@ -1079,15 +1112,8 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
             if (e == cudaSuccess) e = cudaStreamWaitEvent(s, joined, 0);
             if (e != cudaSuccess) cudaStreamSynchronize(side);  // the lists are freed on s below
         }
-        if (fork) cudaEventDestroy(fork);
-        if (joined) cudaEventDestroy(joined);
         prof_end(P_EDGE_JOIN, s, ptok);
         if (e == cudaSuccess) e = cudaGetLastError();
-    }
-    for (int d = 0; d < n_jobs; ++d) {
-        if (jobs[d].live) cudaFreeAsync(jobs[d].live, s);
-        if (jobs[d].rank) cudaFreeAsync(jobs[d].rank, s);
-        if (jobs[d].order) cudaFreeAsync(jobs[d].order, s);
     }
     if (zeroed) cudaFreeAsync(zeroed, s);
     return e;

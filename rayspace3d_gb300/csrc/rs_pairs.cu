@@ -240,8 +240,9 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
     EdgeCull cullA, cullB;
     if (g_overlap_cull && A->n_obj && B->n_obj && A->n_tris && B->n_tris) {
         const uint64_t n_obj = A->n_obj + B->n_obj;
-        cudaError_t e = dmalloc((void**)&cand, n_obj, s);
-        if (e == cudaSuccess) e = dmalloc((void**)&part, n_obj * kPartners * sizeof(int32_t), s);
+        // One allocation: the partner lists, then the flags.
+        cudaError_t e = dmalloc((void**)&part, n_obj * kPartners * sizeof(int32_t) + n_obj, s);
+        if (e == cudaSuccess) cand = reinterpret_cast<uint8_t*>(part + n_obj * kPartners);
         if (e == cudaSuccess)
             e = cull_impl(A, B, a2b ? cand : nullptr, b2a ? cand + A->n_obj : nullptr, part,
                           part + A->n_obj * kPartners, boxes, tmps, s);
@@ -253,7 +254,6 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
         }
     }
     auto release = [&]() {
-        if (cand) cudaFreeAsync(cand, s);
         if (part) cudaFreeAsync(part, s);
         for (int* p : tmps)
             if (p) cudaFreeAsync(p, s);

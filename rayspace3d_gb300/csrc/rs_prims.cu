@@ -511,10 +511,25 @@ uint32_t* sort_error_word() {
     return words[dev];
 }
 
-cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit,
-                           uint32_t* err, uint32_t err_bit) {
+namespace {
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+}  // namespace
+
+size_t radix_sort_scratch_bytes(size_t n, int end_bit, int begin_bit, bool vals) {
+    if (n <= 1 || end_bit <= begin_bit) return 0;
+    const int passes = (end_bit - begin_bit + 7) / 8;
+    const size_t tiles = (n + kOsTile - 1) / kOsTile;
+    return align256(n * sizeof(uint64_t)) + (vals ? align256(n * sizeof(uint32_t)) : 0) +
+           align256((size_t)passes * 256 * sizeof(uint32_t) + passes * sizeof(unsigned int)) +
+           (size_t)passes * tiles * 256 * sizeof(unsigned long long);
+}
+
+// The sort over caller scratch: [k2 | v2 | hist, ctr | status]; the last two regions are
+// zeroed with one memset.
+cudaError_t radix_sort_u64_in(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit,
+                              uint32_t* err, uint32_t err_bit, void* scratch) {
     if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
-    if (n > 0xffffffffull || end_bit > 64 || begin_bit < 0) return cudaErrorInvalidValue;
+    if (n > 0xffffffffull || end_bit > 64 || begin_bit < 0 || !scratch) return cudaErrorInvalidValue;
     if (!err) {
         err = sort_error_word();
         err_bit = 1;
@@ -522,20 +537,21 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit
     }
     const int passes = (end_bit - begin_bit + 7) / 8;
     const size_t tiles = (n + kOsTile - 1) / kOsTile;
-    uint64_t* k2 = nullptr;
+    char* base = static_cast<char*>(scratch);
+    uint64_t* k2 = reinterpret_cast<uint64_t*>(base);
+    base += align256(n * sizeof(uint64_t));
     uint32_t* v2 = nullptr;
-    uint32_t* hist = nullptr;
-    unsigned long long* status = nullptr;
-    unsigned int* ctr = nullptr;
+    if (vals) {
+        v2 = reinterpret_cast<uint32_t*>(base);
+        base += align256(n * sizeof(uint32_t));
+    }
+    char* zero = base;
+    uint32_t* hist = reinterpret_cast<uint32_t*>(base);
+    unsigned int* ctr = reinterpret_cast<unsigned int*>(base + (size_t)passes * 256 * sizeof(uint32_t));
+    base += align256((size_t)passes * 256 * sizeof(uint32_t) + passes * sizeof(unsigned int));
+    unsigned long long* status = reinterpret_cast<unsigned long long*>(base);
     const size_t status_bytes = (size_t)passes * tiles * 256 * sizeof(unsigned long long);
-    cudaError_t e = dmalloc((void**)&k2, n * sizeof(uint64_t), s);
-    if (e == cudaSuccess && vals) e = dmalloc((void**)&v2, n * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = dmalloc((void**)&hist, passes * 256 * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = dmalloc((void**)&status, status_bytes, s);
-    if (e == cudaSuccess) e = dmalloc((void**)&ctr, passes * sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, passes * 256 * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, status_bytes, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, passes * sizeof(unsigned int), s);
+    cudaError_t e = cudaMemsetAsync(zero, 0, (size_t)(base - zero) + status_bytes, s);
     if (e == cudaSuccess) {
         const unsigned hb = (unsigned)std::min<size_t>(tiles, 4 * (size_t)sm_count());
         launch(k_os_hist, hb, kThreads, 0, s, (const uint64_t*)keys, n, begin_bit, end_bit, passes, hist);
@@ -559,8 +575,19 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit
         e = cudaMemcpyAsync(keys, ka, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
         if (e == cudaSuccess && vals) e = cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
     }
-    for (void* q : {(void*)k2, (void*)v2, (void*)hist, (void*)status, (void*)ctr})
-        if (q) cudaFreeAsync(q, s);
+    return e;
+}
+
+cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit,
+                           uint32_t* err, uint32_t err_bit) {
+    const size_t bytes = radix_sort_scratch_bytes(n, end_bit, begin_bit, vals != nullptr);
+    if (bytes == 0) return cudaSuccess;
+    if (n > 0xffffffffull || end_bit > 64 || begin_bit < 0) return cudaErrorInvalidValue;
+    void* scratch = nullptr;
+    cudaError_t e = dmalloc(&scratch, bytes, s);
+    if (e != cudaSuccess) return e;
+    e = radix_sort_u64_in(keys, vals, n, end_bit, s, begin_bit, err, err_bit, scratch);
+    cudaFreeAsync(scratch, s);
     return e;
 }
 

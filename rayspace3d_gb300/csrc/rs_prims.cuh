@@ -15,6 +15,11 @@ namespace rs {
 // result is then invalid.
 cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s,
                            int begin_bit = 0, uint32_t* err = nullptr, uint32_t err_bit = 1);
+// The same sort over caller scratch of radix_sort_scratch_bytes (256-byte aligned): no
+// pool allocation, one memset.
+size_t radix_sort_scratch_bytes(size_t n, int end_bit, int begin_bit, bool vals);
+cudaError_t radix_sort_u64_in(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit,
+                              uint32_t* err, uint32_t err_bit, void* scratch);
 // Queues a copy of the library's sort error word (nonzero after a failed sort) to h_word.
 cudaError_t sort_error_read(uint32_t* h_word, cudaStream_t s);
 cudaError_t sort_error_clear(cudaStream_t s);

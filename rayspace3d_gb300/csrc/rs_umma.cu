@@ -312,7 +312,23 @@ cudaError_t umma_gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, i
     if (!err) return cudaErrorMemoryAllocation;
     const int tiles = (N / UN) * ((M + UM - 1) / UM);
     const int total = K / UK;
-    int split = std::max(1, std::min(total / 4, (sm_count() + tiles - 1) / tiles));
+    // One CTA per SM (the 4-stage ring fills the shared memory).  The split of K is the one
+    // with the least estimated time: waves x k-blocks per CTA at about 0.34 us per k-block
+    // (a second, partial wave costs as much as a full one), plus, for a split, writing and
+    // reading its FP32 slabs (8 bytes per element and split at about 6,800 bytes per ns); at
+    // least 4 k-blocks per CTA, the smaller split on ties.
+    const int sms = sm_count();
+    int split = 1;
+    double best = -1.0;
+    for (int sp = 1; sp <= std::max(1, total / 4); ++sp) {
+        const double waves = (double)(((long long)tiles * sp + sms - 1) / sms);
+        const double cost = waves * (double)((total + sp - 1) / sp) * 340.0 +
+                            (sp > 1 ? (double)sp * M * N * 8.0 / 6800.0 : 0.0);
+        if (best < 0.0 || cost < best) {
+            best = cost;
+            split = sp;
+        }
+    }
     int kps = (total + split - 1) / split;
     split = (total + kps - 1) / kps;
     const dim3 grid(N / UN, (M + UM - 1) / UM, split);
