@@ -67,16 +67,32 @@ __global__ void __launch_bounds__(kT) k_edge_rays(EdgePayload p, const uint32_t*
     }
 }
 
-// Fast path of one edge by one warp: the lanes pop up to 32 nodes per step from the warp's
+// Shared-memory columns of one warp's edge: a stack of STACK node entries, and HITS
+// crossings twice (as found, then sorted).
+template <int STACK, int HITS>
+struct WarpEdgeSmem {
+    int stack[STACK];
+    float t[HITS], t2[HITS];
+    uint32_t id[HITS], id2[HITS];
+    int32_t obj[HITS], obj2[HITS];
+};
+
+// One edge by one warp: the lanes pop up to 32 nodes per step from the warp's
 // shared-memory stack, test both children of each, test the triangles of the leaves hit
 // and push the inner children hit; crossings go to a shared-memory list.  Visits the nodes
 // the one-thread traversal visits (the same slab tests over the same [tmin, tmax]), so it
-// finds the same crossings; lane 0 sorts them by (t, id) and walks them with the table's
-// hit rule.  Returns false, having inserted nothing, when there are more than
-// kWarpRayHits crossings or the stack or the step budget runs out.
-__device__ bool edge_ray_warp(int* stack, float* ht, uint32_t* hid, int32_t* hobj, const EdgePayload& p, uint64_t i,
+// finds the same crossings; the lanes rank them by (t, id) (triangle ids are distinct, so
+// ranks are too) and lane 0 walks them with the table's hit rule.  Returns false, having
+// inserted nothing, when there are more than HITS crossings or the stack or the step
+// budget runs out.
+template <int STACK, int HITS>
+__device__ bool edge_ray_warp(WarpEdgeSmem<STACK, HITS>& w_sm, const EdgePayload& p, uint64_t i,
                               const BNode* __restrict__ nodes, uint32_t max_steps, const float4* __restrict__ tris,
                               int swap, const PairTable& table) {
+    int* stack = w_sm.stack;
+    float* ht = w_sm.t;
+    uint32_t* hid = w_sm.id;
+    int32_t* hobj = w_sm.obj;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Ray r;
@@ -132,7 +148,7 @@ __device__ bool edge_ray_warp(int* stack, float* ht, uint32_t* hid, int32_t* hob
                 const unsigned m = __ballot_sync(0xffffffffu, hit);
                 if (hit) {
                     const int pos = nh + __popc(m & lt);
-                    if (pos < kWarpRayHits) {
+                    if (pos < HITS) {
                         ht[pos] = t;
                         hid[pos] = tid;
                         hobj[pos] = obj;
@@ -144,7 +160,7 @@ __device__ bool edge_ray_warp(int* stack, float* ht, uint32_t* hid, int32_t* hob
         const bool p0 = h[0] && cnt[0] == 0, p1 = h[1] && cnt[1] == 0;
         const unsigned b0 = __ballot_sync(0xffffffffu, p0), b1 = __ballot_sync(0xffffffffu, p1);
         const int total = __popc(b0) + __popc(b1);
-        if (sp + total > kWarpRayStack) {
+        if (sp + total > STACK) {
             ok = false;
             break;
         }
@@ -156,32 +172,26 @@ __device__ bool edge_ray_warp(int* stack, float* ht, uint32_t* hid, int32_t* hob
     }
     add_tests(tests);
     __syncwarp();
-    if (!ok || nh > kWarpRayHits) return false;
+    if (!ok || nh > HITS) return false;
+    for (int a = lane; a < nh; a += 32) {
+        const float t = ht[a];
+        const uint32_t id = hid[a];
+        int rank = 0;
+        for (int b = 0; b < nh; ++b) rank += hit_less(ht[b], hid[b], t, id) ? 1 : 0;
+        w_sm.t2[rank] = t;
+        w_sm.id2[rank] = id;
+        w_sm.obj2[rank] = hobj[a];
+    }
+    __syncwarp();
     if (lane == 0) {
-        // Insertion sort of the crossings by (t, id), then the walk.
-        for (int a = 1; a < nh; ++a) {
-            const float t = ht[a];
-            const uint32_t id = hid[a];
-            const int32_t ob = hobj[a];
-            int b = a;
-            while (b > 0 && hit_less(t, id, ht[b - 1], hid[b - 1])) {
-                ht[b] = ht[b - 1];
-                hid[b] = hid[b - 1];
-                hobj[b] = hobj[b - 1];
-                --b;
-            }
-            ht[b] = t;
-            hid[b] = id;
-            hobj[b] = ob;
-        }
         EdgeWalk w;
         int32_t last = INT_MIN;
         const int32_t* src = p.sources + p.offsets[i];
         const int nsrc = p.counts[i];
-        for (int a = 0; a < nh; ++a) {
-            if (!w.take(ht[a], table.max_hits, table.next_float)) continue;
-            if (hobj[a] == last) continue;
-            last = hobj[a];
+        for (int a = 0; a < nh && !w.done; ++a) {
+            if (!w.take(w_sm.t2[a], table.max_hits, table.next_float)) continue;
+            if (w_sm.obj2[a] == last) continue;
+            last = w_sm.obj2[a];
             insert_sources(table, src, nsrc, last, swap);
         }
         count_edge(table, w.n);
@@ -194,10 +204,7 @@ __global__ void __launch_bounds__(32 * kWarpRayWarps) k_edge_rays_warp(
     EdgePayload p, const uint32_t* __restrict__ live, const unsigned int* __restrict__ n_live, uint64_t n_direct,
     const BNode* __restrict__ nodes, uint32_t max_steps, const float4* __restrict__ tris, int swap, PairTable table,
     uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def) {
-    __shared__ int s_stack[kWarpRayWarps][kWarpRayStack];
-    __shared__ float s_t[kWarpRayWarps][kWarpRayHits];
-    __shared__ uint32_t s_id[kWarpRayWarps][kWarpRayHits];
-    __shared__ int32_t s_obj[kWarpRayWarps][kWarpRayHits];
+    __shared__ WarpEdgeSmem<kWarpRayStack, kWarpRayHits> sm[kWarpRayWarps];
     const unsigned int n = *n_live;
     if (n > kWarpRayMax) return;  // the one-thread kernel traces this list
     const int wi = threadIdx.x >> 5;
@@ -205,21 +212,39 @@ __global__ void __launch_bounds__(32 * kWarpRayWarps) k_edge_rays_warp(
     for (unsigned int j = blockIdx.x * kWarpRayWarps + wi; j < n; j += nw) {  // warp-uniform
         const uint32_t e = live[j];
         if (e >= n_direct) continue;
-        if (!edge_ray_warp(s_stack[wi], s_t[wi], s_id[wi], s_obj[wi], p, e, nodes, max_steps, tris, swap, table) &&
+        if (!edge_ray_warp<kWarpRayStack, kWarpRayHits>(sm[wi], p, e, nodes, max_steps, tris, swap, table) &&
             (threadIdx.x & 31) == 0)
             deferred[atomicAdd(n_def, 1u)] = e;
     }
 }
 
-// Long path over the deferred edges.
-__global__ void __launch_bounds__(kT) k_edge_long(EdgePayload p, const uint32_t* __restrict__ deferred,
-                                                  const unsigned int* __restrict__ n_def,
-                                                  const BNode* __restrict__ nodes, uint32_t max_steps,
-                                                  const float4* __restrict__ tris, int swap, PairTable table) {
+// Long path over the deferred edges, one warp per edge: the warp collects every crossing
+// of the edge in one traversal (up to kLongWarpHits; the reference's walk takes at most
+// --overlap-max-iterations of them) instead of one thread re-traversing per chunk of 16;
+// an edge with more crossings, or a wider traversal than the warp's stack, runs the
+// one-thread chunked loop (segment_long) in lane 0.
+constexpr int kLongWarps = 4;
+constexpr int kLongWarpStack = 256;
+constexpr int kLongWarpHits = 256;
+
+__global__ void __launch_bounds__(32 * kLongWarps) k_edge_long_warp(EdgePayload p, const uint32_t* __restrict__ deferred,
+                                                                    const unsigned int* __restrict__ n_def,
+                                                                    const BNode* __restrict__ nodes, uint32_t max_steps,
+                                                                    const float4* __restrict__ tris, int swap,
+                                                                    PairTable table) {
+    __shared__ WarpEdgeSmem<kLongWarpStack, kLongWarpHits> sm[kLongWarps];
     const unsigned int n = *n_def;
-    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        edge_ray_long(p, deferred[j], nodes, max_steps, tris, swap, table);
+    const int wi = threadIdx.x >> 5;
+    const unsigned int nw = gridDim.x * kLongWarps;
+    for (unsigned int j = blockIdx.x * kLongWarps + wi; j < n; j += nw) {  // warp-uniform
+        const uint32_t e = deferred[j];
+        if (!edge_ray_warp<kLongWarpStack, kLongWarpHits>(sm[wi], p, e, nodes, max_steps, tris, swap, table) &&
+            (threadIdx.x & 31) == 0)
+            edge_ray_long(p, e, nodes, max_steps, tris, swap, table);
+        __syncwarp();
+    }
 }
+
 
 // Legacy per-triangle overlap (mesh_overlap.cu:126-179): record r = 3 t + e is edge e of
 // source triangle t.  Triangles with an index >= nV set *bad and are skipped.  Records the
@@ -994,9 +1019,9 @@ static cudaError_t edge_all_async(const rs_bvh* target, EdgePayload p, uint64_t 
                (const unsigned int*)nullptr, n,
                (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table, deferred,
                n_def);
-        launch(k_edge_long, (unsigned)std::min<uint64_t>((n + kT - 1) / kT, 2ull * sm_count()), kT, 0, s, q,
-               (const uint32_t*)deferred, (const unsigned int*)n_def, (const BNode*)target->nodes, max_steps(target),
-               (const float4*)target->tris, swap, table);
+        launch(k_edge_long_warp, (unsigned)std::min<uint64_t>((n + kLongWarps - 1) / kLongWarps, 4ull * sm_count()),
+               32 * kLongWarps, 0, s, q, (const uint32_t*)deferred, (const unsigned int*)n_def,
+               (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table);
         e = cudaGetLastError();
     }
     prof_end(P_EDGE_JOIN, s, ptok);
@@ -1104,8 +1129,10 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
             launch(k_edge_rays, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 8ull * sm_count()), kT, 0, st, j.p,
                    (const uint32_t*)j.order, (const uint32_t*)j.live, (const unsigned int*)j.n_live, j.nE, j.nodes,
                    j.max_steps, j.tris, j.swap, table, j.rank, j.n_def);
-            launch(k_edge_long, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 2ull * sm_count()), kT, 0, st, j.p,
-                   (const uint32_t*)j.rank, (const unsigned int*)j.n_def, j.nodes, j.max_steps, j.tris, j.swap, table);
+            launch(k_edge_long_warp,
+                   (unsigned)std::min<uint64_t>((j.nE + kLongWarps - 1) / kLongWarps, 4ull * sm_count()),
+                   32 * kLongWarps, 0, st, j.p, (const uint32_t*)j.rank, (const unsigned int*)j.n_def, j.nodes,
+                   j.max_steps, j.tris, j.swap, table);
         }
         if (side) {
             e = cudaEventRecord(joined, side);
