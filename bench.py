@@ -61,6 +61,10 @@ def parse_args():
     ap.add_argument("--no-variants", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--batch-full", action="store_true", help="batched workload at its full size")
     ap.add_argument("--learned-full", action="store_true", help="learned estimator at its full size")
+    ap.add_argument("--learned-pairs", type=str, default=None,
+                    help="TRAIN,HELD_OUT,MAX_OBJECTS dataset pairs of the learned estimator (overrides the default "
+                         "240,60,20000 and --learned-full's 2000,200,200000)")
+    ap.add_argument("--only-learned", action="store_true", help="run the learned-estimator section alone")
     ap.add_argument("--intersection-n", type=int, default=10_000, help="objects per set of the intersection join")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -755,6 +759,8 @@ def run_learned(args, full: bool):
 
     n_train, n_test = (2000, 200) if full else (240, 60)
     n_hi = 200_000 if full else 20_000
+    if getattr(args, "learned_pairs", None):
+        n_train, n_test, n_hi = (int(x) for x in args.learned_pairs.split(","))
     t0 = time.perf_counter()
     samples = [learned.make_sample(10_000 + i, 1000, n_hi) for i in range(n_train + n_test)]
     gen_s = time.perf_counter() - t0
@@ -1004,6 +1010,12 @@ def main():
                 "note": "reference OptiX build unavailable on this box (no OptiX SDK; GB300 has no RT cores); "
                         "CPU port of the same exact tests on all host threads"}
         print(json.dumps(line))
+        return
+    if args.only_learned:
+        # The learned-estimator section alone (a profiling and sizing aid; no headline line).
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"learned": run_learned(args, args.learned_full)}))
         return
     if world > 1:
         import torch.distributed as dist
