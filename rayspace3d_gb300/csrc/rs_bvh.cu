@@ -193,11 +193,19 @@ __global__ void k_obox_init(int* __restrict__ box, uint64_t cap, const int* __re
 // Morton key of each triangle's box centre (and, into obox, the box of each object below
 // obox_cap: triangles of one object are usually stored together, so the lanes of a warp
 // with equal objects reduce first and one of them does the atomics).
-__global__ void k_morton(const float* __restrict__ V, uint64_t nV, const uint32_t* __restrict__ I, uint64_t nF,
-                         const int32_t* __restrict__ T, const int* __restrict__ bounds, uint64_t* __restrict__ keys,
-                         unsigned int* __restrict__ bad_index, int* __restrict__ obox, uint64_t obox_cap) {
-    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (t < nF) {
+// Grid-stride over the triangles; also counts the four 8-bit digits of each Morton code
+// (the sort's histogram, hist[p * 256 + digit p]) in shared memory, added to `hist` once
+// per block, so the sort does not read the keys back for them.
+__global__ void __launch_bounds__(kT) k_morton(const float* __restrict__ V, uint64_t nV,
+                                              const uint32_t* __restrict__ I, uint64_t nF,
+                                              const int32_t* __restrict__ T, const int* __restrict__ bounds,
+                                              uint64_t* __restrict__ keys, unsigned int* __restrict__ bad_index,
+                                              int* __restrict__ obox, uint64_t obox_cap,
+                                              uint32_t* __restrict__ hist) {
+    __shared__ uint32_t s_hist[4 * 256];
+    for (int k = threadIdx.x; k < 4 * 256; k += blockDim.x) s_hist[k] = 0;
+    __syncthreads();
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nF; t += (uint64_t)gridDim.x * blockDim.x) {
         if (I[3 * t] >= nV || I[3 * t + 1] >= nV || I[3 * t + 2] >= nV) atomicOr(bad_index, 1u);
         float lo[3], hi[3];
         tri_box(V, nV, I, t, lo, hi);
@@ -232,7 +240,12 @@ __global__ void k_morton(const float* __restrict__ V, uint64_t nV, const uint32_
         const uint32_t code = ((q[0] >> 10) << 31) | ((q[1] >> 10) << 30) | (spread10(q[0]) << 2) |
                               (spread10(q[1]) << 1) | spread10(q[2]);
         keys[t] = ((uint64_t)code << 32) | (uint32_t)t;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) atomicAdd(&s_hist[p * 256 + ((code >> (8 * p)) & 0xffu)], 1u);
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 4 * 256; k += blockDim.x)
+        if (s_hist[k]) atomicAdd(&hist[k], s_hist[k]);
 }
 
 // Length of the common prefix of the keys of groups g and g+1 (the keys of their first
@@ -761,10 +774,15 @@ static int build_impl(const float* d_vertices, uint64_t nV, const uint32_t* d_in
     } else {
         const Groups G{n, group, leaf_size};
         launch(k_obox_init, 2 * sm_count(), kT, 0, s, h->obox, h->obox_cap, (const int*)(bounds + 13));
-        launch(k_morton, (n + kT - 1) / kT, kT, 0, s, d_vertices, nV, d_indices, nF, d_tri2obj, (const int*)bounds,
-               keys, reinterpret_cast<unsigned int*>(bounds + 12), h->obox, h->obox_cap);
+        char* sort_scratch = scratch + 256 + b_xchg + b_keys + b_open;
+        uint32_t* hist = radix_sort_hist(sort_scratch, (size_t)n, false);
+        e = cudaMemsetAsync(hist, 0, 4 * 256 * sizeof(uint32_t), s);
+        if (e != cudaSuccess) goto fail;
+        launch(k_morton, (unsigned)std::min<uint64_t>(((uint64_t)n + kT - 1) / kT, 8ull * sm_count()), kT, 0, s,
+               d_vertices, nV, d_indices, nF, d_tri2obj, (const int*)bounds, keys,
+               reinterpret_cast<unsigned int*>(bounds + 12), h->obox, h->obox_cap, hist);
         e = radix_sort_u64_in(keys, nullptr, (size_t)n, 64, s, 32, reinterpret_cast<uint32_t*>(bounds + 12), 2u,
-                              scratch + 256 + b_xchg + b_keys + b_open);
+                              sort_scratch, true);
         if (e != cudaSuccess) goto fail;
         const int utok = prof_begin(P_BUILD_UP, s);
         launch(k_build_tree, (nG + kTB - 1) / kTB, kTB, 0, s, d_vertices, nV, d_indices, d_tri2obj, (const uint64_t*)keys,

@@ -524,10 +524,15 @@ size_t radix_sort_scratch_bytes(size_t n, int end_bit, int begin_bit, bool vals)
            (size_t)passes * tiles * 256 * sizeof(unsigned long long);
 }
 
+uint32_t* radix_sort_hist(void* scratch, size_t n, bool vals) {
+    char* base = static_cast<char*>(scratch) + align256(n * sizeof(uint64_t)) + (vals ? align256(n * sizeof(uint32_t)) : 0);
+    return reinterpret_cast<uint32_t*>(base);
+}
+
 // The sort over caller scratch: [k2 | v2 | hist, ctr | status]; the last two regions are
-// zeroed with one memset.
+// zeroed with one memset (without the histogram when the caller has filled it).
 cudaError_t radix_sort_u64_in(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit,
-                              uint32_t* err, uint32_t err_bit, void* scratch) {
+                              uint32_t* err, uint32_t err_bit, void* scratch, bool hist_ready) {
     if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
     if (n > 0xffffffffull || end_bit > 64 || begin_bit < 0 || !scratch) return cudaErrorInvalidValue;
     if (!err) {
@@ -551,10 +556,13 @@ cudaError_t radix_sort_u64_in(uint64_t* keys, uint32_t* vals, size_t n, int end_
     base += align256((size_t)passes * 256 * sizeof(uint32_t) + passes * sizeof(unsigned int));
     unsigned long long* status = reinterpret_cast<unsigned long long*>(base);
     const size_t status_bytes = (size_t)passes * tiles * 256 * sizeof(unsigned long long);
-    cudaError_t e = cudaMemsetAsync(zero, 0, (size_t)(base - zero) + status_bytes, s);
+    char* zero_from = hist_ready ? reinterpret_cast<char*>(ctr) : zero;
+    cudaError_t e = cudaMemsetAsync(zero_from, 0, (size_t)(base - zero_from) + status_bytes, s);
     if (e == cudaSuccess) {
-        const unsigned hb = (unsigned)std::min<size_t>(tiles, 4 * (size_t)sm_count());
-        launch(k_os_hist, hb, kThreads, 0, s, (const uint64_t*)keys, n, begin_bit, end_bit, passes, hist);
+        if (!hist_ready) {
+            const unsigned hb = (unsigned)std::min<size_t>(tiles, 4 * (size_t)sm_count());
+            launch(k_os_hist, hb, kThreads, 0, s, (const uint64_t*)keys, n, begin_bit, end_bit, passes, hist);
+        }
         launch(k_os_offsets, 1, 256, 0, s, hist, passes);
         e = cudaGetLastError();
     }
@@ -586,7 +594,7 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit
     void* scratch = nullptr;
     cudaError_t e = dmalloc(&scratch, bytes, s);
     if (e != cudaSuccess) return e;
-    e = radix_sort_u64_in(keys, vals, n, end_bit, s, begin_bit, err, err_bit, scratch);
+    e = radix_sort_u64_in(keys, vals, n, end_bit, s, begin_bit, err, err_bit, scratch, false);
     cudaFreeAsync(scratch, s);
     return e;
 }

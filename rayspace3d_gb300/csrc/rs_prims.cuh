@@ -16,10 +16,13 @@ namespace rs {
 cudaError_t radix_sort_u64(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s,
                            int begin_bit = 0, uint32_t* err = nullptr, uint32_t err_bit = 1);
 // The same sort over caller scratch of radix_sort_scratch_bytes (256-byte aligned): no
-// pool allocation, one memset.
+// pool allocation, one memset.  With hist_ready the caller has already written, into
+// radix_sort_hist(scratch, ...), the counts of every digit of every pass (hist[p * 256 + d],
+// 8-bit digits from begin_bit), and the sort does not read the keys for them.
 size_t radix_sort_scratch_bytes(size_t n, int end_bit, int begin_bit, bool vals);
+uint32_t* radix_sort_hist(void* scratch, size_t n, bool vals);
 cudaError_t radix_sort_u64_in(uint64_t* keys, uint32_t* vals, size_t n, int end_bit, cudaStream_t s, int begin_bit,
-                              uint32_t* err, uint32_t err_bit, void* scratch);
+                              uint32_t* err, uint32_t err_bit, void* scratch, bool hist_ready);
 // Queues a copy of the library's sort error word (nonzero after a failed sort) to h_word.
 cudaError_t sort_error_read(uint32_t* h_word, cudaStream_t s);
 cudaError_t sort_error_clear(cudaStream_t s);
