@@ -351,11 +351,11 @@ def run_engine(args, rank, world, local):
     if p:
         per_launch = join_bytes(da, db) + join_bytes(db, da) + 8.0 * n_pairs
         achieved = per_launch / (p["avg_ms"] * 1e-3) / 1e9
-        one_dir = profiled_traffic("k_edge_join", args.objects)
-        roof_edges = {"bound": "hbm", "kernel": "k_edge_live + k_edge_join_live (both directions)",
+        roof_edges = {"bound": "hbm",
+                      "kernel": "k_edge_live + k_edge_rays_warp / k_edge_rays + k_edge_long_warp (both directions)",
                       "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5),
                       "algorithmic_bytes_per_launch": int(per_launch), "avg_launch_ms": round(p["avg_ms"], 4),
-                      "traffic": None if one_dir is None else 2 * one_dir}
+                      "traffic": profiled_traffic("edge_rays_w1000", args.objects)}
 
     result = {
         "metric": METRIC, "value": round(dev_ms / 1e3, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -543,7 +543,7 @@ def run_join_variant(args, world_size, steps=5, filtered=False, cpu=False):
         hbm, kind = peaks()
         nbytes = join_bytes(da, db) + join_bytes(db, da) + 8.0 * n_pairs
         ach = nbytes / (p["avg_ms"] * 1e-3) / 1e9
-        out["roofline"] = {"bound": "hbm", "kernel": "edge rays of both directions (k_edge_live .. k_edge_long)",
+        out["roofline"] = {"bound": "hbm", "kernel": "edge rays of both directions (k_edge_live .. k_edge_long_warp)",
                            "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 5),
                            "algorithmic_bytes_per_launch": int(nbytes), "avg_launch_ms": p["avg_ms"],
                            "peak_source": kind + " hbm_gbs", "traffic": None}
