@@ -76,7 +76,15 @@ def far_faces():
     return _bar(0.0, 41.0), B, segments([((0.0, _Y, _Z), (41.0, _Y, _Z), [0])])
 
 
-CASES = {"slab_stack": slab_stack, "shared_face": shared_face, "near_faces": near_faces, "far_faces": far_faces}
+def deep_stack():
+    """slab_stack with 200 slabs: 400 crossings per long edge, more than the 256 one warp
+    of the long path collects in one traversal, so the one-thread loop takes them 16 per
+    traversal (all 400 under the 1000-trace rule)."""
+    return slab_stack(200)
+
+
+CASES = {"slab_stack": slab_stack, "deep_stack": deep_stack, "shared_face": shared_face, "near_faces": near_faces,
+         "far_faces": far_faces}
 RULES = [(100, False), (1000, False), (256, True)]
 
 

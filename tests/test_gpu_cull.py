@@ -68,6 +68,29 @@ def test_cull_with_shared_edges(cuda):
     _check(B, g)
 
 
+@pytest.mark.parametrize("n_small", [3, 8, 9, 40])
+def test_partner_lists_up_to_and_past_eight(cuda, n_small):
+    """A sphere shell crossed by n small spheres on its surface: its query lists n partner
+    objects (up to 8 listed, more marks all its edges live), and each small sphere has the
+    shell as its one partner, so only its edges near the shell's box are traced.  The pairs
+    equal the oracle's with the broad phase on and off."""
+    rng = np.random.default_rng(100 + n_small)
+    v, f = synth.icosphere(3)
+    shell = synth.make_geometry((v * 5.0).astype(np.float32), f, np.zeros(len(f), np.int32))
+    dirs = rng.normal(size=(n_small, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    vs, fs = synth.icosphere(2)
+    Vs, Is, Ts = [], [], []
+    for k in range(n_small):
+        Vs.append((vs * 0.7 + dirs[k] * 5.0).astype(np.float32))
+        Is.append(fs + np.uint32(len(vs) * k))
+        Ts.append(np.full(len(fs), k, np.int32))
+    small = synth.make_geometry(np.concatenate(Vs), np.concatenate(Is), np.concatenate(Ts))
+    want = _check(shell, small)
+    assert len(want) == n_small
+    _check(small, shell)
+
+
 def test_cull_budget_exhausted(cuda):
     """One huge sphere around a cloud of small ones: its query visits more nodes than the
     budget allows, which must switch culling off for the other side, not drop pairs."""

@@ -1,7 +1,8 @@
 """The engine's edge-ray hit rule (rs_pairset_set_edge_rule) and parity iteration cap
 against the oracle, which tests/test_edge_rule_cpu.py pins to the reference's loops run
-literally: an edge crossing 240 faces (the 100-trace cap, and the deferred long path of
-edges with more than 4 crossings), coincident and near-coincident faces of different
+literally: edges crossing 240 and 400 faces (the 100-trace cap, the deferred long path of
+edges with more than 4 crossings, one warp per edge up to 256 crossings and the one-thread
+loop beyond), coincident and near-coincident faces of different
 objects (the 1e-6 and 2e-4 steps), through rs_edge_join, rs_overlap_join (broad phase on
 and off), the batched launch and raytracer_intersection_estimated's
 --overlap-max-iterations.  Pair sets must match bit for bit."""
