@@ -162,6 +162,13 @@ def join_bytes(src, tgt):
     return 32 * len(e.starts) + 4 * len(e.sources) + 12 * tgt.nV + 16 * tgt.nF
 
 
+def live_check_bytes(src):
+    """Bytes of one direction's live-edge check: 8 B per edge (offset, count) and 4 B per
+    source id, plus one flag byte per source object."""
+    e = src.host.edges
+    return 8 * len(e.offsets) + 4 * len(e.sources) + int(src.host.tri2obj.max()) + 1
+
+
 def build_bytes(g):
     """Algorithmic bytes of one BVH build: read vertices/indices/tri2obj, write the
     leaf-ordered triangles (48 B) and the nodes (64 B per internal node)."""
@@ -211,6 +218,9 @@ def run_engine(args, rank, world, local):
             size = api.hash_size_pow2(est)
             key = ("ps", size)
             ps = pairs_out.get(key)
+            if ps is not None and ps.info()[0] != size:
+                ps.close()  # grown by an earlier join: every join starts from the estimate's size
+                ps = None
             if ps is None:
                 ps = api.PairSet(size, pow2=True, stream=stream)
                 pairs_out[key] = ps
@@ -344,12 +354,14 @@ def run_engine(args, rank, world, local):
                 "traffic": profiled_traffic("k_build_tree", args.objects)}
     # The edge rays of one join (the live-edge check of both directions in one launch, then
     # each direction's rays for its live edges, the two directions concurrently; one timed
-    # interval per join), against the bytes they would move if every edge were traced: each
-    # direction's source edge payload and target geometry once, and 8 B per pair-table insert.
+    # interval per join).  Algorithmic bytes: what the interval has to read with the broad
+    # phase's object flags in hand -- each direction's per-edge offset and count (8 B) and
+    # 4 B per source id, one flag byte per object -- and 8 B per pair-table insert; the few
+    # live edges' endpoints and the nodes their rays visit are left out (mostly L2 hits).
     roof_edges = None
     p = prof.get("edge_join")
     if p:
-        per_launch = join_bytes(da, db) + join_bytes(db, da) + 8.0 * n_pairs
+        per_launch = sum(live_check_bytes(g) for g in (da, db)) + 8.0 * n_pairs
         achieved = per_launch / (p["avg_ms"] * 1e-3) / 1e9
         roof_edges = {"bound": "hbm",
                       "kernel": "k_edge_live + k_edge_rays_warp / k_edge_rays + k_edge_long_warp (both directions)",
@@ -493,6 +505,9 @@ def run_join_variant(args, world_size, steps=5, filtered=False, cpu=False):
             est, _ = api.estimate_pairs(da, db, stream=stream)
             size = api.hash_size_pow2(est)
             ps = cache.get(size)
+            if ps is not None and ps.info()[0] != size:
+                ps.close()  # grown by an earlier join: every join starts from the estimate's size
+                ps = None
             if ps is None:
                 ps = cache[size] = api.PairSet(size, pow2=True, stream=stream)
             if filtered:

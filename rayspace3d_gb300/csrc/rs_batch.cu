@@ -193,6 +193,7 @@ struct rs_batch_item {
     const int32_t* sources = nullptr;
     int swap = 0;
     rs_pairset* ps = nullptr;
+    uint64_t gen = 0;  // ps->generation when the batch was committed
 };
 
 struct rs_batch {
@@ -244,7 +245,8 @@ int commit(rs_batch* b, cudaStream_t s) {
     uint64_t chunks = 0;
     bool any_pim = false;
     for (int i = 0; i < nq; ++i) {
-        const rs_batch_item& it = b->items[i];
+        rs_batch_item& it = b->items[i];
+        if (it.ps) it.gen = it.ps->generation;
         const rs_bvh* h = effective(b, it.bvh);
         const int st = bvh_ready(h);
         if (st != RS_OK) return st;
@@ -423,6 +425,8 @@ extern "C" int rs_batch_set_options(rs_batch* b, int chunk, int stack_depth, int
 extern "C" int rs_batch_submit(rs_batch* b, void* stream) {
     if (!b) return RS_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
+    for (const rs_batch_item& it : b->items)
+        if (it.ps && it.ps->generation != it.gen) b->dirty = true;  // its slots were reallocated
     const int st = commit(b, s);
     if (st != RS_OK) return st;
     for (const rs_batch_item& it : b->items) {
@@ -467,7 +471,10 @@ extern "C" int rs_batch_wait(rs_batch* b, int* h_status) {
             if (e != cudaSuccess) return to_status(e);
             bits = (unsigned int)m;
         }
-        const int s = bits & ST_HIT_OVERFLOW ? RS_ERR_OUTPUT_OVERFLOW : status_from_bits(bits);
+        int ts = status_from_bits(bits);
+        if (b->items[i].kind == 1 && (bits & ST_SPILLED) && ts == RS_ERR_TABLE_FULL && !(bits & ST_TABLE_FULL))
+            ts = table_status(b->items[i].ps, b->last_stream, cudaSuccess);  // regrow from the spill list
+        const int s = bits & ST_HIT_OVERFLOW ? RS_ERR_OUTPUT_OVERFLOW : ts;
         if (h_status) h_status[i] = s;
         if (first == RS_OK) first = s;
     }

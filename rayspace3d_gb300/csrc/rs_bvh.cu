@@ -613,7 +613,7 @@ int status_from_bits(uint32_t bits) {
     if (bits & ST_STACK_OVERFLOW) return RS_ERR_ITER_LIMIT;
     if (bits & ST_ITER_LIMIT) return RS_ERR_ITER_LIMIT;
     if (bits & ST_TARGET_OVERFLOW) return RS_ERR_TARGET_OVERFLOW;
-    if (bits & ST_TABLE_FULL) return RS_ERR_TABLE_FULL;
+    if (bits & (ST_TABLE_FULL | ST_SPILLED)) return RS_ERR_TABLE_FULL;  // spilled: not regrown yet
     return RS_OK;
 }
 

@@ -17,6 +17,7 @@
 //  * box tests use the same slab formula, which is monotone in the box bounds,
 //    so BVH culling never changes the hit set.
 #pragma once
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -30,7 +31,9 @@ enum : uint32_t {
     ST_HIT_OVERFLOW = 1u << 1,   // a per-ray hit list overflowed (handled by a fallback pass)
     ST_STACK_OVERFLOW = 1u << 2, // a traversal stack overflowed (result invalid)
     ST_ITER_LIMIT = 1u << 3,     // an iteration budget ran out (result invalid)
-    ST_TARGET_OVERFLOW = 1u << 4 // reserved (containment handles any number of targets in passes)
+    ST_TARGET_OVERFLOW = 1u << 4, // reserved (containment handles any number of targets in passes)
+    ST_SPILLED = 1u << 5         // keys that found no slot went to the spill list (none lost):
+                                 // the table must be regrown from its slots and the list
 };
 
 // ---------------------------------------------------------------------------
@@ -546,12 +549,20 @@ struct PairTable {
     // after t (next_float != 0).
     int max_hits;
     int next_float;
+    // Spill list (nullable): a key that finds no slot within max_probes is appended here
+    // and ST_SPILLED raised; once it is raised, an insert gives up probing after 32 slots
+    // (a full table would make every later insert walk the whole limit).  A key that finds
+    // neither a slot nor room in the list raises ST_TABLE_FULL.
+    unsigned long long* spill;
+    unsigned long long spill_cap;
+    unsigned long long* spill_count;
 };
 
 __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long long key) {
     const unsigned long long h = fmix64(key);
     unsigned long long slot = t.pow2 ? (h & (t.capacity - 1)) : (h % t.capacity);
     for (unsigned int i = 0; i < t.max_probes; ++i) {
+        if ((i & 31u) == 31u && t.spill && (*(volatile unsigned int*)t.status & ST_SPILLED)) break;
         if (t.stats) atomicAdd(&t.stats[0], 1ull);
         unsigned long long cur = t.slots[slot];
         if (cur == key) return;
@@ -566,6 +577,18 @@ __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long l
         if (t.stats) atomicAdd(&t.stats[1], 1ull);
         slot = slot + 1;
         if (slot == t.capacity) slot = 0;
+    }
+    if (t.spill) {
+        // One counter update per group of converged lanes.
+        cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
+        unsigned long long base = 0;
+        if (g.thread_rank() == 0) base = atomicAdd(t.spill_count, (unsigned long long)g.size());
+        base = g.shfl(base, 0) + g.thread_rank();
+        if (base < t.spill_cap) {
+            t.spill[base] = key;
+            if (base == 0) atomicOr(t.status, ST_SPILLED);
+            return;
+        }
     }
     atomicOr(t.status, ST_TABLE_FULL);
 }

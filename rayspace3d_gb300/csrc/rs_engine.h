@@ -58,8 +58,14 @@ struct rs_pairset {
     int pow2 = 1;
     unsigned int max_probes = 4096;
     // Device scratch: [0] status bits (u32 in the low word), [1] distinct-key count,
-    // [2] slot accesses, [3] contended probes, [4..8] query counters (see rs_pairset_counters).
+    // [2] slot accesses, [3] contended probes, [4..8] query counters (see rs_pairset_counters),
+    // [10] finalize gather counter, [11] spill-list count; the spill list follows (kSpillKeys
+    // keys, one allocation with the words).
     unsigned long long* meta = nullptr;
+    unsigned long long* spill = nullptr;
+    // Incremented whenever the slots are reallocated (growth): a captured batch that holds
+    // the old slot pointer recaptures.
+    uint64_t generation = 0;
     int track = 0;  // count slot accesses and contention
     int device = 0;
     // Edge-ray hit rule (rs_pairset_set_edge_rule): the reference's kMaxIterations and
@@ -74,6 +80,15 @@ struct rs_pairset {
 namespace rs {
 constexpr int kMetaWords = 16;
 constexpr int kGatherWord = 10;  // meta word used as the finalize gather counter
+constexpr int kSpillWord = 11;   // meta word counting spill-list appends
+constexpr uint64_t kSpillKeys = 1ull << 20;
+// Waits for the stream and turns the table's status bits into an rs_status.  A table whose
+// inserts spilled (and lost none) is first regrown and rehashed from its slots and spill
+// list, without rerunning the launches that filled it.
+int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e);
+// Queues the regrowth of a spilled table holding `count` keys in its slots and `spilled`
+// appends in its spill list: new slots with room for all of them, the old keys reinserted.
+cudaError_t table_regrow(rs_pairset* ps, uint64_t count, uint64_t spilled, cudaStream_t s);
 // Upper bound on the node visits of one traversal of a valid tree.
 inline uint32_t max_steps(const rs_bvh* b) { return (uint32_t)(2 * b->n_nodes + 8); }
 int to_status(cudaError_t e);

@@ -25,7 +25,6 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources, uint64_t nE,
                             int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull);
 cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cudaStream_t s);
-int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e);
 cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s);
 
 namespace {

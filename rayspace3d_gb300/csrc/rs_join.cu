@@ -985,6 +985,9 @@ PairTable table_view(rs_pairset* ps) {
     t.stats = ps->track ? ps->meta + 2 : nullptr;
     t.max_hits = ps->edge_max_hits;
     t.next_float = ps->edge_next_float;
+    t.spill = ps->spill;
+    t.spill_cap = ps->spill ? kSpillKeys : 0;
+    t.spill_count = ps->meta + kSpillWord;
     return t;
 }
 
@@ -1244,18 +1247,25 @@ cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cu
     return cull_pair_async(src, other, cand, nullptr, s);
 }
 
-// Waits for the stream and turns the table's status bits into an rs_status.
-// The distinct-key count read with it is kept for rs_pairset_finalize/info.
+// The distinct-key count read with the status is kept for rs_pairset_finalize/info.
 int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e) {
-    unsigned long long m[2] = {0, 0};
-    if (e == cudaSuccess) e = cudaMemcpyAsync(m, ps->meta, sizeof(m), cudaMemcpyDeviceToHost, s);
-    cudaError_t e2 = cudaStreamSynchronize(s);
-    prof_collect();
-    if (e == cudaSuccess) e = e2;
-    if (e != cudaSuccess) return to_status(e);
-    const int st = status_from_bits((uint32_t)m[0]);
-    ps->known_count = st == RS_OK ? (long long)m[1] : -1;
-    return st;
+    constexpr uint32_t kHard = ST_TABLE_FULL | ST_STACK_OVERFLOW | ST_ITER_LIMIT | ST_TARGET_OVERFLOW;
+    for (int round = 0;; ++round) {
+        unsigned long long m[kSpillWord + 1] = {};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(m, ps->meta, sizeof(m), cudaMemcpyDeviceToHost, s);
+        cudaError_t e2 = cudaStreamSynchronize(s);
+        prof_collect();
+        if (e == cudaSuccess) e = e2;
+        if (e != cudaSuccess) return to_status(e);
+        const uint32_t bits = (uint32_t)m[0];
+        if ((bits & ST_SPILLED) && !(bits & kHard) && round < 4) {
+            e = table_regrow(ps, m[1], m[kSpillWord], s);
+            continue;
+        }
+        const int st = status_from_bits(bits);
+        ps->known_count = st == RS_OK ? (long long)m[1] : -1;
+        return st;
+    }
 }
 }  // namespace rs
 

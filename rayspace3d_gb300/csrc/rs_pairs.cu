@@ -4,10 +4,12 @@
 // (query/src/applications/raytracer_overlap_estimated_main.cpp:39-112,
 // raytracer_intersection_estimated_main.cpp:77-176), compact_hash_table_pairs and
 // merge_and_deduplicate_pairs_gpu (query/src/cuda/mesh_query_deduplication.cu:56-144).
-// Differences by design: a key that cannot be placed raises RS_ERR_TABLE_FULL
-// (the reference drops it after 5000 / 1000 probes) and the drivers grow the
-// table and rerun; the finalised output is sorted, so it does not depend on
-// slot order or atomic timing.
+// Differences by design: a key that finds no slot within the probe limit (the
+// reference drops it after 5000 / 1000 probes) goes to the table's spill list, and
+// the status read after the launches regrows the table from its slots and the list;
+// only a key that finds no room in the list either raises RS_ERR_TABLE_FULL, after
+// which the drivers grow the table and rerun.  The finalised output is sorted, so it
+// does not depend on slot order or atomic timing.
 #include <algorithm>
 #include <cstring>
 
@@ -28,7 +30,6 @@ cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const fl
                                  const int32_t* countsB, const int32_t* sourcesB, uint64_t nEB, const EdgeCull& cullB,
                                  rs_pairset* ps, cudaStream_t s);
 bool g_overlap_cull = true;
-int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e);
 
 namespace {
 
@@ -57,7 +58,62 @@ cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s) {
     ps->slots = nullptr;
     ps->capacity = capacity;
     ps->max_probes = (unsigned)std::min<uint64_t>(capacity, 8192);
+    ++ps->generation;
     return dmalloc((void**)&ps->slots, capacity * sizeof(unsigned long long), s);
+}
+
+namespace {
+// Reinserts the keys of a spilled table's old slots followed by its spill list (one
+// array: `n` words, empty slots skipped) into the regrown table.
+__global__ void __launch_bounds__(256) k_rehash(PairTable t, const unsigned long long* __restrict__ keys,
+                                                const unsigned long long* __restrict__ spill, uint64_t n_slots,
+                                                uint64_t n_spill) {
+    const uint64_t n = n_slots + n_spill;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = i < n_slots ? keys[i] : spill[i - n_slots];
+        if (k != kEmptyKey) table_insert(t, k);
+    }
+}
+}  // namespace
+
+cudaError_t table_regrow(rs_pairset* ps, uint64_t count, uint64_t spilled, cudaStream_t s) {
+    const uint64_t n_spill = std::min<uint64_t>(spilled, kSpillKeys);
+    // Room for every key at load 1/2 or less (the list may repeat keys, so this is generous),
+    // and at least four times the old slots.
+    const uint64_t need = 2 * (count + n_spill);
+    uint64_t cap = ps->capacity * 4;
+    while (cap < need) cap *= 2;
+    if (!ps->pow2 && cap % 2 == 0) cap += 1;
+    if (cap > (1ull << 34)) return cudaErrorMemoryAllocation;
+    unsigned long long* old = ps->slots;
+    const uint64_t old_cap = ps->capacity;
+    // The spill list is rehashed from a copy: the regrown table spills into the same list.
+    unsigned long long* spill_copy = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (n_spill) {
+        e = dmalloc((void**)&spill_copy, n_spill * sizeof(unsigned long long), s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(spill_copy, ps->spill, n_spill * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToDevice, s);
+    }
+    ps->slots = nullptr;  // the old slots stay allocated until the rehash has read them
+    if (e == cudaSuccess) e = alloc_slots(ps, cap, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ps->slots, 0xff, cap * sizeof(unsigned long long), s);
+    // Status and count start over; the spill count too (word kSpillWord).
+    if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, 2 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta + kSpillWord, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) {
+        PairTable t = table_view(ps);
+        t.stats = nullptr;
+        const uint64_t n = old_cap + n_spill;
+        const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, 4u * sm_count());
+        launch(k_rehash, grid, 256, 0, s, t, (const unsigned long long*)old, (const unsigned long long*)spill_copy,
+               old_cap, n_spill);
+        e = cudaGetLastError();
+    }
+    if (old) cudaFreeAsync(old, s);
+    if (spill_copy) cudaFreeAsync(spill_copy, s);
+    return e;
 }
 }  // namespace rs
 
@@ -94,7 +150,8 @@ extern "C" int rs_pairset_create(uint64_t capacity, int pow2, rs_pairset** out, 
     cudaGetDevice(&ps->device);
     ps->pow2 = pow2 ? 1 : 0;
     if (ps->pow2) capacity = next_pow2(capacity);
-    cudaError_t e = dmalloc((void**)&ps->meta, kMetaWords * sizeof(unsigned long long), s);
+    cudaError_t e = dmalloc((void**)&ps->meta, (kMetaWords + kSpillKeys) * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) ps->spill = ps->meta + kMetaWords;
     if (e == cudaSuccess) e = alloc_slots(ps, capacity, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -159,14 +216,9 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
     if (ps->known_count >= 0) {
         n = (uint64_t)ps->known_count;
     } else {
-        unsigned long long meta[2] = {0, 0};
-        e = cudaMemcpyAsync(meta, ps->meta, sizeof(meta), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return to_status(e);
-        const int st = status_from_bits((uint32_t)meta[0]);
+        const int st = table_status(ps, s, cudaSuccess);  // regrows a spilled table first
         if (st != RS_OK) return st;
-        n = meta[1];
-        ps->known_count = (long long)n;
+        n = (uint64_t)ps->known_count;
     }
     if (n == 0) return RS_OK;
     if (n <= kSmallTableSort && n <= capacity) {
