@@ -467,9 +467,9 @@ constexpr int kStack = 64;
 // child's subtree is then mostly rejected by the shrunken range when it is popped.
 template <int AXIS, int STACK = kStack, bool ORDERED = false, class F>
 __device__ __forceinline__ bool traverse_with(int* stack, int stride, const BNode* __restrict__ nodes,
-                                              uint32_t max_steps, const Ray& r, F&& on_leaf) {
+                                              uint32_t max_steps, const Ray& r, F&& on_leaf, int start = 0) {
     int sp = 0;
-    int node = 0;
+    int node = start;  // the root, or a node known to hold every triangle the ray can hit
     for (uint32_t step = 0;; ++step) {
         if (step > max_steps) return false;
         const float4 na = __ldg(&nodes[node].a);

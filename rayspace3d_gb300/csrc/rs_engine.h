@@ -102,7 +102,9 @@ int ensure_grid(const rs_bvh* h, int axis, cudaStream_t s);
 // have a partner; no culling when cand is null.  With partner lists (part != null):
 // cand[o] = the number of partner objects of the other set (0..kPartners) listed in
 // part[o * kPartners ...], or kCandAll when they were not all collected; pbox holds the
-// other set's object boxes (ordered-int min xyz, max xyz), n_pbox of them.
+// other set's object boxes (ordered-int min xyz, max xyz), n_pbox of them.  entry
+// (nullable, with part): per source object whose flag is set, the node of the other set's
+// BVH under which lie all triangles its edges' rays can hit; they start there.
 constexpr int kPartners = 8;
 constexpr uint8_t kCandAll = 255;
 struct EdgeCull {
@@ -111,6 +113,7 @@ struct EdgeCull {
     const int32_t* part = nullptr;
     const int* pbox = nullptr;
     uint64_t n_pbox = 0;
+    const uint32_t* entry = nullptr;
 };
 
 // Recheck statistics of the translation units that run hit tests (see rs_device.cuh).

@@ -47,23 +47,32 @@ constexpr int kWarpRayHits = 16;   // crossings a warp keeps; an edge with more 
 
 // Fast path over the edges order[0..*n_order) of a payload of n_direct edges (or over all
 // of them when order is null); the edges it defers go to deferred[0..*n_def).
+// entry / order_entry (nullable): the node each listed edge's traversal starts from.
 __global__ void __launch_bounds__(kT) k_edge_rays(EdgePayload p, const uint32_t* __restrict__ order,
                                                   const uint32_t* __restrict__ live,
                                                   const unsigned int* __restrict__ n_order, uint64_t n_direct,
                                                   const BNode* __restrict__ nodes, uint32_t max_steps,
                                                   const float4* __restrict__ tris, int swap, PairTable table,
-                                                  uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def) {
+                                                  uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def,
+                                                  const uint32_t* __restrict__ order_entry,
+                                                  const uint32_t* __restrict__ live_entry) {
     __shared__ EdgeSmem<kT, kFastStack> sm;
     const EdgeColumn col = sm.column(threadIdx.x);
     const uint64_t n = live ? (uint64_t)*n_order : n_direct;
     if (live && n <= kWarpRayMax) return;  // k_edge_rays_warp traces short live lists
     // The cell-ordered list when the job was binned and is long enough, else the live list.
-    if (live) order = (order && n >= kBinMinLive) ? order : live;
+    const uint32_t* entry = nullptr;
+    if (live) {
+        const bool binned = order && n >= kBinMinLive;
+        entry = binned ? order_entry : live_entry;
+        order = binned ? order : live;
+    }
     for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t e = order ? order[j] : (uint32_t)j;
+        const int start = entry ? (int)entry[j] : 0;
         if (e >= n_direct) continue;  // never, for a list of this payload's edges
-        if (!edge_ray_fast<kFastStack>(col, p, e, nodes, max_steps, tris, swap, table))
-            deferred[atomicAdd(n_def, 1u)] = e;
+        if (!edge_ray_fast<kFastStack>(col, p, e, nodes, max_steps, tris, swap, table, start))
+            deferred[atomicAdd(n_def, 1u)] = e;  // the deferred paths start from the root
     }
 }
 
@@ -88,7 +97,7 @@ struct WarpEdgeSmem {
 template <int STACK, int HITS>
 __device__ bool edge_ray_warp(WarpEdgeSmem<STACK, HITS>& w_sm, const EdgePayload& p, uint64_t i,
                               const BNode* __restrict__ nodes, uint32_t max_steps, const float4* __restrict__ tris,
-                              int swap, const PairTable& table) {
+                              int swap, const PairTable& table, int start = 0) {
     int* stack = w_sm.stack;
     float* ht = w_sm.t;
     uint32_t* hid = w_sm.id;
@@ -99,7 +108,7 @@ __device__ bool edge_ray_warp(WarpEdgeSmem<STACK, HITS>& w_sm, const EdgePayload
     if (!segment_ray_of(p.starts[3 * i], p.starts[3 * i + 1], p.starts[3 * i + 2], p.ends[3 * i], p.ends[3 * i + 1],
                         p.ends[3 * i + 2], r))
         return true;
-    if (lane == 0) stack[0] = 0;
+    if (lane == 0) stack[0] = start;
     __syncwarp();
     int sp = 1, nh = 0;
     uint32_t visits = 0;
@@ -203,7 +212,7 @@ __device__ bool edge_ray_warp(WarpEdgeSmem<STACK, HITS>& w_sm, const EdgePayload
 __global__ void __launch_bounds__(32 * kWarpRayWarps) k_edge_rays_warp(
     EdgePayload p, const uint32_t* __restrict__ live, const unsigned int* __restrict__ n_live, uint64_t n_direct,
     const BNode* __restrict__ nodes, uint32_t max_steps, const float4* __restrict__ tris, int swap, PairTable table,
-    uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def) {
+    uint32_t* __restrict__ deferred, unsigned int* __restrict__ n_def, const uint32_t* __restrict__ live_entry) {
     __shared__ WarpEdgeSmem<kWarpRayStack, kWarpRayHits> sm[kWarpRayWarps];
     const unsigned int n = *n_live;
     if (n > kWarpRayMax) return;  // the one-thread kernel traces this list
@@ -211,8 +220,9 @@ __global__ void __launch_bounds__(32 * kWarpRayWarps) k_edge_rays_warp(
     const unsigned int nw = gridDim.x * kWarpRayWarps;
     for (unsigned int j = blockIdx.x * kWarpRayWarps + wi; j < n; j += nw) {  // warp-uniform
         const uint32_t e = live[j];
+        const int start = live_entry ? (int)live_entry[j] : 0;
         if (e >= n_direct) continue;
-        if (!edge_ray_warp<kWarpRayStack, kWarpRayHits>(sm[wi], p, e, nodes, max_steps, tris, swap, table) &&
+        if (!edge_ray_warp<kWarpRayStack, kWarpRayHits>(sm[wi], p, e, nodes, max_steps, tris, swap, table, start) &&
             (threadIdx.x & 31) == 0)
             deferred[atomicAdd(n_def, 1u)] = e;
     }
@@ -342,6 +352,11 @@ struct EdgeJob {
     uint32_t* rank;       // rank of each live edge within its cell; then the deferred edges
     uint32_t* order;      // live edges by cell (binned jobs)
     uint32_t* cells;      // kCells counts, then their exclusive prefix sums (binned jobs)
+    // Entry nodes (nullable, as EdgeCull): per source object, then per edge of live and of
+    // order -- the node an edge's traversal starts from.
+    const uint32_t* entry;
+    uint32_t* live_entry;
+    uint32_t* order_entry;
     unsigned int* n_live;
     unsigned int* n_def;
     const BNode* nodes;
@@ -417,6 +432,7 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
     int ns[kLiveEdges], off[kLiveEdges];
     int32_t so0[kLiveEdges];
     uint8_t c0[kLiveEdges];
+    uint32_t en[kLiveEdges];
 #pragma unroll
     for (int u = 0; u < kLiveEdges; ++u) {
         const uint64_t i = base + (uint64_t)u * blockDim.x;
@@ -427,8 +443,13 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
 #pragma unroll
     for (int u = 0; u < kLiveEdges; ++u) so0[u] = ns[u] > 0 ? j.p.sources[off[u]] : -1;
 #pragma unroll
-    for (int u = 0; u < kLiveEdges; ++u)
-        c0[u] = (ns[u] > 0 && so0[u] >= 0 && (uint64_t)so0[u] < j.n_cull) ? j.cull[so0[u]] : (uint8_t)0;
+    for (int u = 0; u < kLiveEdges; ++u) {
+        const bool in = ns[u] > 0 && so0[u] >= 0 && (uint64_t)so0[u] < j.n_cull;
+        c0[u] = in ? j.cull[so0[u]] : (uint8_t)0;
+        // One source: its entry node (its partner query ran when its flag is set); more
+        // sources: the root.
+        en[u] = (j.entry && in && ns[u] == 1) ? j.entry[so0[u]] : 0u;
+    }
     const int lane = threadIdx.x & 31;
     const unsigned int below = (1u << lane) - 1u;
 #pragma unroll
@@ -443,6 +464,7 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
         pos0 = __shfl_sync(0xffffffffu, pos0, leader);
         const unsigned int pos = pos0 + __popc(m & below);
         if (any) j.live[pos] = (uint32_t)i;
+        if (any && j.live_entry) j.live_entry[pos] = en[u];
         if (j.order) {
             // Every lane takes part in the match (lanes without a live edge with a cell of
             // their own, kCells + lane), so that the mask is the full warp.
@@ -513,7 +535,10 @@ __global__ void __launch_bounds__(256) k_edge_order(EdgeJob j0, EdgeJob j1, unsi
          k += nb * blockDim.x) {
         const uint32_t e = j.live[k];
         const uint32_t pos = j.cells[edge_cell(j, e)] + j.rank[k];
-        if (pos < n) j.order[pos] = e;  // always: the cell is recomputed with the same arithmetic
+        if (pos < n) {  // always: the cell is recomputed with the same arithmetic
+            j.order[pos] = e;
+            if (j.order_entry) j.order_entry[pos] = j.live_entry[k];
+        }
     }
 }
 
@@ -634,7 +659,8 @@ struct CullJob {
     uint32_t max_steps;
     const float4* tris;
     uint8_t* cand;
-    int32_t* part;  // nullable: partner lists (kPartners per object)
+    int32_t* part;    // nullable: partner lists (kPartners per object)
+    uint32_t* entry;  // nullable (partner mode): entry node per object queried
 };
 
 // Flag pass, one thread per object of one set: does its widened box overlap any widened
@@ -729,6 +755,12 @@ __global__ void __launch_bounds__(kT) k_cull_flag(CullJob j0, CullJob j1, unsign
 // list every lane holds.  A query's latency is therefore its depth plus its node count
 // over 32, not its node count.  Blocks below blocks0 run job j0, the others j1 (both
 // directions of a join in one launch).
+//
+// The query also records the object's entry node: the deepest node of the walk's opening
+// chain, where each step holds one node, hits no leaf and hits one inner child.  Every
+// triangle whose widened box overlaps the object's widened box lies under it, so the rays
+// of the object's edges (whose boxes lie inside that box) may start there instead of at
+// the root and still meet every triangle they can hit.
 constexpr int kCullWarps = 4;             // warps (objects) per block
 constexpr int kCullStack = 256;           // entries of a warp's stack
 constexpr uint32_t kPartnerBudget = 8192;  // node visits of a partner query
@@ -766,9 +798,15 @@ __global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, Cull
     __syncwarp();
     int sp = 1;
     uint32_t visits = 0;
+    int entry = 0;      // under it: every triangle the query can find
+    bool chain = true;  // every step so far held one node, hit no leaf and one inner child
     while (sp > 0 && !all) {
         const int take = min(sp, 32);
         const int node = lane < take ? stack[sp - take + lane] : -1;
+        if (chain) {
+            if (take == 1) entry = __shfl_sync(0xffffffffu, node, 0);
+            else chain = false;
+        }
         __syncwarp();
         sp -= take;
         visits += (uint32_t)take;
@@ -788,6 +826,7 @@ __global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, Cull
             first[1] = nd.z;
             cnt[1] = nd.w;
         }
+        if (chain && __any_sync(0xffffffffu, (h[0] && cnt[0] > 0) || (h[1] && cnt[1] > 0))) chain = false;
         // Leaves hit: their triangles, one per lane and round, in warp-uniform rounds.
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
@@ -841,6 +880,7 @@ __global__ void __launch_bounds__(32 * kCullWarps) k_cull_query(CullJob j0, Cull
         sp += total;
     }
     if (lane != 0) return;
+    if (j.entry) j.entry[a] = (uint32_t)entry;
     j.cand[a] = all ? kCandAll : (uint8_t)np;
     if (!all) {
 #pragma unroll
@@ -1021,7 +1061,7 @@ static cudaError_t edge_all_async(const rs_bvh* target, EdgePayload p, uint64_t 
         launch(k_edge_rays, grid, kT, 0, s, q, (const uint32_t*)nullptr, (const uint32_t*)nullptr,
                (const unsigned int*)nullptr, n,
                (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table, deferred,
-               n_def);
+               n_def, (const uint32_t*)nullptr, (const uint32_t*)nullptr);
         launch(k_edge_long_warp, (unsigned)std::min<uint64_t>((n + kLongWarps - 1) / kLongWarps, 4ull * sm_count()),
                32 * kLongWarps, 0, s, q, (const uint32_t*)deferred, (const unsigned int*)n_def,
                (const BNode*)target->nodes, max_steps(target), (const float4*)target->tris, swap, table);
@@ -1047,6 +1087,7 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
     job.part = cull.part;
     job.pbox = cull.pbox;
     job.n_pbox = cull.n_pbox;
+    job.entry = cull.part ? cull.entry : nullptr;
     job.nodes = (const BNode*)target->nodes;
     job.max_steps = max_steps(target);
     job.tris = (const float4*)target->tris;
@@ -1075,7 +1116,8 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
     size_t total = a256(zbytes);
     for (int d = 0; d < n_jobs; ++d) {
         const size_t bytes = a256(std::max<uint64_t>(jobs[d].nE, 1) * sizeof(uint32_t));
-        total += (jobs[d].nE <= kBinMaxEdges ? 3 : 2) * bytes;
+        const bool bin = jobs[d].nE <= kBinMaxEdges;
+        total += ((bin ? 3 : 2) + (jobs[d].entry ? (bin ? 2 : 1) : 0)) * bytes;
     }
     cudaError_t e = dmalloc((void**)&zeroed, total, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(zeroed, 0, zbytes, s);
@@ -1094,6 +1136,14 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
             next += bytes;
             j.cells = next_cells;
             next_cells += kCells;
+        }
+        if (j.entry) {
+            j.live_entry = reinterpret_cast<uint32_t*>(next);
+            next += bytes;
+            if (j.order) {
+                j.order_entry = reinterpret_cast<uint32_t*>(next);
+                next += bytes;
+            }
         }
         blocks[d] = (j.nE + 256 * kLiveEdges - 1) / (256 * kLiveEdges);
         total_e += j.nE;
@@ -1128,10 +1178,11 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
                    (unsigned)std::min<uint64_t>((std::min<uint64_t>(j.nE, kWarpRayMax) + kWarpRayWarps - 1) /
                                                     kWarpRayWarps, 4ull * sm_count()),
                    32 * kWarpRayWarps, 0, st, j.p, (const uint32_t*)j.live, (const unsigned int*)j.n_live, j.nE,
-                   j.nodes, j.max_steps, j.tris, j.swap, table, j.rank, j.n_def);
+                   j.nodes, j.max_steps, j.tris, j.swap, table, j.rank, j.n_def, (const uint32_t*)j.live_entry);
             launch(k_edge_rays, (unsigned)std::min<uint64_t>((j.nE + kT - 1) / kT, 8ull * sm_count()), kT, 0, st, j.p,
                    (const uint32_t*)j.order, (const uint32_t*)j.live, (const unsigned int*)j.n_live, j.nE, j.nodes,
-                   j.max_steps, j.tris, j.swap, table, j.rank, j.n_def);
+                   j.max_steps, j.tris, j.swap, table, j.rank, j.n_def, (const uint32_t*)j.order_entry,
+                   (const uint32_t*)j.live_entry);
             launch(k_edge_long_warp,
                    (unsigned)std::min<uint64_t>((j.nE + kLongWarps - 1) / kLongWarps, 4ull * sm_count()),
                    32 * kLongWarps, 0, st, j.p, (const uint32_t*)j.rank, (const unsigned int*)j.n_def, j.nodes,
@@ -1167,6 +1218,7 @@ cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const fl
         j.part = c.part;
         j.pbox = c.pbox;
         j.n_pbox = c.n_pbox;
+        j.entry = c.part ? c.entry : nullptr;
         j.nodes = (const BNode*)target->nodes;
         j.max_steps = max_steps(target);
         j.tris = (const float4*)target->tris;
@@ -1185,11 +1237,13 @@ cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const fl
 // of the edge rays reads them) and the temporaries go to tmps_out, for the caller to free
 // after those rays; otherwise they are freed here.
 cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, int32_t* partA,
-                      int32_t* partB, const int** boxes_out, int** tmps_out, cudaStream_t s) {
+                      int32_t* partB, uint32_t* entryA, uint32_t* entryB, const int** boxes_out, int** tmps_out,
+                      cudaStream_t s) {
     const rs_bvh* src[2] = {A, B};
     const rs_bvh* other[2] = {B, A};
     uint8_t* cand[2] = {candA, candB};
     int32_t* part[2] = {partA, partB};
+    uint32_t* entry[2] = {entryA, entryB};
     int* tmp[2] = {nullptr, nullptr};
     const int* boxes[2] = {nullptr, nullptr};
     CullJob job[2] = {};
@@ -1214,7 +1268,7 @@ cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t*
         const rs_bvh* h = src[d];
         if (!cand[d] || h->n_obj == 0) continue;
         job[d] = CullJob{boxes[d], h->n_obj, (const BNode*)other[d]->nodes, max_steps(other[d]),
-                         (const float4*)other[d]->tris, cand[d], part[d]};
+                         (const float4*)other[d]->tris, cand[d], part[d], part[d] ? entry[d] : nullptr};
         blocks[d] = (unsigned int)((h->n_obj + kT - 1) / kT);
         if (part[d]) wblocks[d] = (unsigned int)((h->n_obj + kCullWarps - 1) / kCullWarps);
     }
@@ -1239,7 +1293,7 @@ cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t*
 // Broad-phase flags of A's objects against B's BVH into candA and of B's objects against
 // A's BVH into candB (either null: that direction is skipped), both in one launch.
 cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, cudaStream_t s) {
-    return cull_impl(A, B, candA, candB, nullptr, nullptr, nullptr, nullptr, s);
+    return cull_impl(A, B, candA, candB, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, s);
 }
 
 // Broad-phase flags of `src`'s objects against `other`'s BVH.

@@ -23,7 +23,8 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
                             int swap, rs_pairset* ps, cudaStream_t s, const EdgeCull& cull);
 cudaError_t cull_pair_async(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, cudaStream_t s);
 cudaError_t cull_impl(const rs_bvh* A, const rs_bvh* B, uint8_t* candA, uint8_t* candB, int32_t* partA,
-                      int32_t* partB, const int** boxes_out, int** tmps_out, cudaStream_t s);
+                      int32_t* partB, uint32_t* entryA, uint32_t* entryB, const int** boxes_out, int** tmps_out,
+                      cudaStream_t s);
 cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const float* endsA, const int32_t* offsetsA,
                                  const int32_t* countsA, const int32_t* sourcesA, uint64_t nEA, const EdgeCull& cullA,
                                  const rs_bvh* B, const float* startsB, const float* endsB, const int32_t* offsetsB,
@@ -285,22 +286,28 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
     // reuse it): object boxes of each set against the other set's triangle boxes, listing
     // each object's partner objects, so that only edges whose own box reaches a partner's
     // box are traced.
-    uint8_t* cand = nullptr;  // [A objects | B objects]
-    int32_t* part = nullptr;  // kPartners per object, same order
+    uint8_t* cand = nullptr;    // [A objects | B objects]
+    int32_t* part = nullptr;    // kPartners per object, same order
+    uint32_t* entry = nullptr;  // entry node per object, same order
     const int* boxes[2] = {nullptr, nullptr};
     int* tmps[2] = {nullptr, nullptr};
     EdgeCull cullA, cullB;
     if (g_overlap_cull && A->n_obj && B->n_obj && A->n_tris && B->n_tris) {
         const uint64_t n_obj = A->n_obj + B->n_obj;
-        // One allocation: the partner lists, then the flags.
-        cudaError_t e = dmalloc((void**)&part, n_obj * kPartners * sizeof(int32_t) + n_obj, s);
-        if (e == cudaSuccess) cand = reinterpret_cast<uint8_t*>(part + n_obj * kPartners);
+        // One allocation: the partner lists, the entry nodes, then the flags.
+        cudaError_t e = dmalloc((void**)&part, n_obj * (kPartners + 1) * sizeof(int32_t) + n_obj, s);
+        if (e == cudaSuccess) {
+            entry = reinterpret_cast<uint32_t*>(part + n_obj * kPartners);
+            cand = reinterpret_cast<uint8_t*>(entry + n_obj);
+        }
         if (e == cudaSuccess)
             e = cull_impl(A, B, a2b ? cand : nullptr, b2a ? cand + A->n_obj : nullptr, part,
-                          part + A->n_obj * kPartners, boxes, tmps, s);
+                          part + A->n_obj * kPartners, entry, entry + A->n_obj, boxes, tmps, s);
         if (e == cudaSuccess) {
-            if (a2b) cullA = EdgeCull{cand, A->n_obj, part, boxes[1], B->n_obj};
-            if (b2a) cullB = EdgeCull{cand + A->n_obj, B->n_obj, part + A->n_obj * kPartners, boxes[0], A->n_obj};
+            if (a2b) cullA = EdgeCull{cand, A->n_obj, part, boxes[1], B->n_obj, entry};
+            if (b2a)
+                cullB = EdgeCull{cand + A->n_obj, B->n_obj, part + A->n_obj * kPartners, boxes[0], A->n_obj,
+                                 entry + A->n_obj};
         } else {
             cudaGetLastError();  // culling is an optimisation: run without it
         }

@@ -425,7 +425,8 @@ __device__ __forceinline__ void count_edge(const PairTable& table, int taken) {
 template <int STACK>
 __device__ __forceinline__ bool segment_fast(const EdgeColumn& col, const Ray& r, const int32_t* __restrict__ src,
                                              int nsrc, const BNode* __restrict__ nodes, uint32_t max_steps,
-                                             const float4* __restrict__ tris, int swap, const PairTable& table) {
+                                             const float4* __restrict__ tris, int swap, const PairTable& table,
+                                             int start = 0) {
     const int S = col.stride;
     int n = 0;
     unsigned int tests = 0;
@@ -453,7 +454,7 @@ __device__ __forceinline__ bool segment_fast(const EdgeColumn& col, const Ray& r
             }
             ++n;
         }
-    });
+    }, start);
     add_tests(tests);
     if (!ok || n > kEdgeHits) return false;
     EdgeWalk w;
@@ -550,12 +551,14 @@ struct EdgePayload {
 template <int STACK>
 __device__ __forceinline__ bool edge_ray_fast(const EdgeColumn& col, const EdgePayload& p, uint64_t i,
                                               const BNode* __restrict__ nodes, uint32_t max_steps,
-                                              const float4* __restrict__ tris, int swap, const PairTable& table) {
+                                              const float4* __restrict__ tris, int swap, const PairTable& table,
+                                              int start = 0) {
     Ray r;
     if (!segment_ray_of(p.starts[3 * i], p.starts[3 * i + 1], p.starts[3 * i + 2], p.ends[3 * i], p.ends[3 * i + 1],
                         p.ends[3 * i + 2], r))
         return true;
-    return segment_fast<STACK>(col, r, p.sources + p.offsets[i], p.counts[i], nodes, max_steps, tris, swap, table);
+    return segment_fast<STACK>(col, r, p.sources + p.offsets[i], p.counts[i], nodes, max_steps, tris, swap, table,
+                               start);
 }
 
 __device__ __forceinline__ void edge_ray_long(const EdgePayload& p, uint64_t i, const BNode* __restrict__ nodes,
