@@ -472,8 +472,8 @@ extern "C" int rs_batch_wait(rs_batch* b, int* h_status) {
             bits = (unsigned int)m;
         }
         int ts = status_from_bits(bits);
-        if (b->items[i].kind == 1 && (bits & ST_SPILLED) && ts == RS_ERR_TABLE_FULL && !(bits & ST_TABLE_FULL))
-            ts = table_status(b->items[i].ps, b->last_stream, cudaSuccess);  // regrow from the spill list
+        if (b->items[i].kind == 1 && (bits & ST_SPILLED))  // regrow from the overflow table, or empty it
+            ts = table_status(b->items[i].ps, b->last_stream, cudaSuccess);
         const int s = bits & ST_HIT_OVERFLOW ? RS_ERR_OUTPUT_OVERFLOW : ts;
         if (h_status) h_status[i] = s;
         if (first == RS_OK) first = s;

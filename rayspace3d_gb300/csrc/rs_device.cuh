@@ -17,7 +17,6 @@
 //  * box tests use the same slab formula, which is monotone in the box bounds,
 //    so BVH culling never changes the hit set.
 #pragma once
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -32,8 +31,9 @@ enum : uint32_t {
     ST_STACK_OVERFLOW = 1u << 2, // a traversal stack overflowed (result invalid)
     ST_ITER_LIMIT = 1u << 3,     // an iteration budget ran out (result invalid)
     ST_TARGET_OVERFLOW = 1u << 4, // reserved (containment handles any number of targets in passes)
-    ST_SPILLED = 1u << 5         // keys that found no slot went to the spill list (none lost):
-                                 // the table must be regrown from its slots and the list
+    ST_SPILLED = 1u << 5         // the table passed 3/4 load or a key found no slot within the
+                                 // probe limit; later keys may sit in the overflow table (none
+                                 // lost): the table must be regrown from both
 };
 
 // ---------------------------------------------------------------------------
@@ -549,27 +549,57 @@ struct PairTable {
     // after t (next_float != 0).
     int max_hits;
     int next_float;
-    // Spill list (nullable): a key that finds no slot within max_probes is appended here
-    // and ST_SPILLED raised; once it is raised, an insert gives up probing after 32 slots
-    // (a full table would make every later insert walk the whole limit).  A key that finds
-    // neither a slot nor room in the list raises ST_TABLE_FULL.
-    unsigned long long* spill;
-    unsigned long long spill_cap;
-    unsigned long long* spill_count;
+    // Overflow table (nullable): a second open-addressing table of over_mask + 1 slots,
+    // kept empty between joins.  Once the main table passes 3/4 of its slots, or a key
+    // finds no slot within max_probes, ST_SPILLED is raised; from then on an insert that
+    // has not settled after kSpillProbes slots of the main table goes to the overflow
+    // table (a full main table would otherwise make every insert walk its whole probe
+    // limit, each step a dependent load).  A key may then sit in both; the regrowth
+    // merges them.  A key that finds no slot in either raises ST_TABLE_FULL.
+    unsigned long long* over;
+    unsigned long long over_mask;
+    unsigned long long* over_count;
+    unsigned long long spill_at;  // main-table count that raises ST_SPILLED
 };
+
+constexpr unsigned int kSpillProbes = 4;
+constexpr unsigned int kOverProbes = 256;
+
+// Open-addressing insert into slots[0..mask] (a power of two) from hash h; false when no
+// slot was found within `probes`.
+__device__ __forceinline__ bool probe_insert(unsigned long long* slots, unsigned long long mask, unsigned long long h,
+                                             unsigned long long key, unsigned int probes, unsigned long long* count) {
+    unsigned long long slot = h & mask;
+    for (unsigned int i = 0; i < probes; ++i) {
+        const unsigned long long cur = slots[slot];
+        if (cur == key) return true;
+        if (cur == kEmptyKey) {
+            const unsigned long long old = atomicCAS(&slots[slot], kEmptyKey, key);
+            if (old == kEmptyKey) {
+                atomicAdd(count, 1ull);
+                return true;
+            }
+            if (old == key) return true;
+        }
+        slot = (slot + 1) & mask;
+    }
+    return false;
+}
 
 __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long long key) {
     const unsigned long long h = fmix64(key);
     unsigned long long slot = t.pow2 ? (h & (t.capacity - 1)) : (h % t.capacity);
-    for (unsigned int i = 0; i < t.max_probes; ++i) {
-        if ((i & 31u) == 31u && t.spill && (*(volatile unsigned int*)t.status & ST_SPILLED)) break;
+    unsigned int i = 0;
+    for (; i < t.max_probes; ++i) {
+        if (i == kSpillProbes && t.over && (*(volatile unsigned int*)t.status & ST_SPILLED)) break;
         if (t.stats) atomicAdd(&t.stats[0], 1ull);
         unsigned long long cur = t.slots[slot];
         if (cur == key) return;
         if (cur == kEmptyKey) {
             unsigned long long old = atomicCAS(&t.slots[slot], kEmptyKey, key);
             if (old == kEmptyKey) {
-                atomicAdd(t.count, 1ull);
+                const unsigned long long c = atomicAdd(t.count, 1ull);
+                if (t.over && c + 1 == t.spill_at) atomicOr(t.status, ST_SPILLED);
                 return;
             }
             if (old == key) return;
@@ -578,17 +608,10 @@ __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long l
         slot = slot + 1;
         if (slot == t.capacity) slot = 0;
     }
-    if (t.spill) {
-        // One counter update per group of converged lanes.
-        cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
-        unsigned long long base = 0;
-        if (g.thread_rank() == 0) base = atomicAdd(t.spill_count, (unsigned long long)g.size());
-        base = g.shfl(base, 0) + g.thread_rank();
-        if (base < t.spill_cap) {
-            t.spill[base] = key;
-            if (base == 0) atomicOr(t.status, ST_SPILLED);
-            return;
-        }
+    if (t.over) {
+        if (i == t.max_probes) atomicOr(t.status, ST_SPILLED);
+        // The overflow table hashes the other half of the key's hash.
+        if (probe_insert(t.over, t.over_mask, h >> 32 | h << 32, key, kOverProbes, t.over_count)) return;
     }
     atomicOr(t.status, ST_TABLE_FULL);
 }

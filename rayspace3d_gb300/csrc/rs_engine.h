@@ -59,10 +59,11 @@ struct rs_pairset {
     unsigned int max_probes = 4096;
     // Device scratch: [0] status bits (u32 in the low word), [1] distinct-key count,
     // [2] slot accesses, [3] contended probes, [4..8] query counters (see rs_pairset_counters),
-    // [10] finalize gather counter, [11] spill-list count; the spill list follows (kSpillKeys
-    // keys, one allocation with the words).
+    // [10] finalize gather counter, [11] overflow-table key count; the overflow table follows
+    // (kOverSlots slots, one allocation with the words), empty between joins.
     unsigned long long* meta = nullptr;
-    unsigned long long* spill = nullptr;
+    unsigned long long* over = nullptr;
+    bool over_dirty = false;  // a launch may have left keys in the overflow table
     // Incremented whenever the slots are reallocated (growth): a captured batch that holds
     // the old slot pointer recaptures.
     uint64_t generation = 0;
@@ -80,15 +81,18 @@ struct rs_pairset {
 namespace rs {
 constexpr int kMetaWords = 16;
 constexpr int kGatherWord = 10;  // meta word used as the finalize gather counter
-constexpr int kSpillWord = 11;   // meta word counting spill-list appends
-constexpr uint64_t kSpillKeys = 1ull << 20;
-// Waits for the stream and turns the table's status bits into an rs_status.  A table whose
-// inserts spilled (and lost none) is first regrown and rehashed from its slots and spill
-// list, without rerunning the launches that filled it.
+constexpr int kOverWord = 11;    // meta word counting the overflow table's keys
+constexpr uint64_t kOverSlots = 1ull << 20;
+// Waits for the stream and turns the table's status bits into an rs_status.  A table that
+// spilled (and lost no key) is first regrown from its slots and its overflow table, without
+// rerunning the launches that filled it; the overflow table is left empty.
 int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e);
-// Queues the regrowth of a spilled table holding `count` keys in its slots and `spilled`
-// appends in its spill list: new slots with room for all of them, the old keys reinserted.
-cudaError_t table_regrow(rs_pairset* ps, uint64_t count, uint64_t spilled, cudaStream_t s);
+// Queues the regrowth of a spilled table holding `count` keys in its slots and `over` in
+// its overflow table: new slots with room for all of them, both tables' keys reinserted,
+// the overflow table cleared.
+cudaError_t table_regrow(rs_pairset* ps, uint64_t count, uint64_t over, cudaStream_t s);
+// Queues the clearing of the overflow table (and its count) when a launch may have used it.
+cudaError_t over_clear(rs_pairset* ps, cudaStream_t s);
 // Upper bound on the node visits of one traversal of a valid tree.
 inline uint32_t max_steps(const rs_bvh* b) { return (uint32_t)(2 * b->n_nodes + 8); }
 int to_status(cudaError_t e);

@@ -387,6 +387,7 @@ extern "C" int rs_overlap_join_filtered(const float* d_VA, uint64_t nVA, const u
         ps->known_count = -1;
         e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
+        if (e == cudaSuccess) e = over_clear(ps, s);
         if (e == cudaSuccess && a2b && A.cand)
             e = edge_join_async(B.bvh, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, 0, ps, s, cullA);
         if (e == cudaSuccess && b2a && B.cand)

@@ -1025,9 +1025,11 @@ PairTable table_view(rs_pairset* ps) {
     t.stats = ps->track ? ps->meta + 2 : nullptr;
     t.max_hits = ps->edge_max_hits;
     t.next_float = ps->edge_next_float;
-    t.spill = ps->spill;
-    t.spill_cap = ps->spill ? kSpillKeys : 0;
-    t.spill_count = ps->meta + kSpillWord;
+    t.over = ps->over;
+    t.over_mask = kOverSlots - 1;
+    t.over_count = ps->meta + kOverWord;
+    t.spill_at = std::max<unsigned long long>(1, ps->capacity / 4 * 3 + (ps->capacity % 4) * 3 / 4);
+    if (ps->over) ps->over_dirty = true;
     return t;
 }
 
@@ -1305,7 +1307,7 @@ cudaError_t cull_async(const rs_bvh* src, const rs_bvh* other, uint8_t* cand, cu
 int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e) {
     constexpr uint32_t kHard = ST_TABLE_FULL | ST_STACK_OVERFLOW | ST_ITER_LIMIT | ST_TARGET_OVERFLOW;
     for (int round = 0;; ++round) {
-        unsigned long long m[kSpillWord + 1] = {};
+        unsigned long long m[kOverWord + 1] = {};
         if (e == cudaSuccess) e = cudaMemcpyAsync(m, ps->meta, sizeof(m), cudaMemcpyDeviceToHost, s);
         cudaError_t e2 = cudaStreamSynchronize(s);
         prof_collect();
@@ -1313,9 +1315,14 @@ int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e) {
         if (e != cudaSuccess) return to_status(e);
         const uint32_t bits = (uint32_t)m[0];
         if ((bits & ST_SPILLED) && !(bits & kHard) && round < 4) {
-            e = table_regrow(ps, m[1], m[kSpillWord], s);
+            e = table_regrow(ps, m[1], m[kOverWord], s);
             continue;
         }
+        // No spill: nothing went to the overflow table (a key goes there only after
+        // ST_SPILLED is raised).  Otherwise the result is an error: empty it.
+        if (!(bits & ST_SPILLED)) ps->over_dirty = false;
+        else if ((e = over_clear(ps, s)) == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return to_status(e);
         const int st = status_from_bits(bits);
         ps->known_count = st == RS_OK ? (long long)m[1] : -1;
         return st;

@@ -4,12 +4,12 @@
 // (query/src/applications/raytracer_overlap_estimated_main.cpp:39-112,
 // raytracer_intersection_estimated_main.cpp:77-176), compact_hash_table_pairs and
 // merge_and_deduplicate_pairs_gpu (query/src/cuda/mesh_query_deduplication.cu:56-144).
-// Differences by design: a key that finds no slot within the probe limit (the
-// reference drops it after 5000 / 1000 probes) goes to the table's spill list, and
-// the status read after the launches regrows the table from its slots and the list;
-// only a key that finds no room in the list either raises RS_ERR_TABLE_FULL, after
-// which the drivers grow the table and rerun.  The finalised output is sorted, so it
-// does not depend on slot order or atomic timing.
+// Differences by design: no key is dropped (the reference drops one after 5000 / 1000
+// probes).  A table past 3/4 load sends keys that do not settle within a few slots to
+// the pair set's overflow table, and the status read after the launches regrows the
+// table from both; only a key that finds no slot in either raises RS_ERR_TABLE_FULL,
+// after which the drivers grow the table and rerun.  The finalised output is sorted, so
+// it does not depend on slot order or atomic timing.
 #include <algorithm>
 #include <cstring>
 
@@ -64,56 +64,63 @@ cudaError_t alloc_slots(rs_pairset* ps, uint64_t capacity, cudaStream_t s) {
 }
 
 namespace {
-// Reinserts the keys of a spilled table's old slots followed by its spill list (one
-// array: `n` words, empty slots skipped) into the regrown table.
+// Reinserts the keys of a spilled table's old slots (n_slots) and of its overflow table
+// (n_over slots) into the regrown table, skipping empty slots.
 __global__ void __launch_bounds__(256) k_rehash(PairTable t, const unsigned long long* __restrict__ keys,
-                                                const unsigned long long* __restrict__ spill, uint64_t n_slots,
-                                                uint64_t n_spill) {
-    const uint64_t n = n_slots + n_spill;
+                                                const unsigned long long* __restrict__ over, uint64_t n_slots,
+                                                uint64_t n_over) {
+    const uint64_t n = n_slots + n_over;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const unsigned long long k = i < n_slots ? keys[i] : spill[i - n_slots];
+        const unsigned long long k = i < n_slots ? keys[i] : over[i - n_slots];
         if (k != kEmptyKey) table_insert(t, k);
     }
 }
 }  // namespace
 
-cudaError_t table_regrow(rs_pairset* ps, uint64_t count, uint64_t spilled, cudaStream_t s) {
-    const uint64_t n_spill = std::min<uint64_t>(spilled, kSpillKeys);
-    // Room for every key at load 1/2 or less (the list may repeat keys, so this is generous),
-    // and at least four times the old slots.
-    const uint64_t need = 2 * (count + n_spill);
+cudaError_t over_clear(rs_pairset* ps, cudaStream_t s) {
+    if (!ps->over || !ps->over_dirty) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(ps->over, 0xff, kOverSlots * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta + kOverWord, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) ps->over_dirty = false;
+    return e;
+}
+
+cudaError_t table_regrow(rs_pairset* ps, uint64_t count, uint64_t over, cudaStream_t s) {
+    // Room for every key at load 1/2 or less (a key may be in both tables, so this is
+    // generous), and at least four times the old slots.
+    const uint64_t need = 2 * (count + over);
     uint64_t cap = ps->capacity * 4;
     while (cap < need) cap *= 2;
     if (!ps->pow2 && cap % 2 == 0) cap += 1;
     if (cap > (1ull << 34)) return cudaErrorMemoryAllocation;
     unsigned long long* old = ps->slots;
     const uint64_t old_cap = ps->capacity;
-    // The spill list is rehashed from a copy: the regrown table spills into the same list.
-    unsigned long long* spill_copy = nullptr;
+    // The overflow table is rehashed from a copy: the regrown table may overflow into it.
+    unsigned long long* over_copy = nullptr;
     cudaError_t e = cudaSuccess;
-    if (n_spill) {
-        e = dmalloc((void**)&spill_copy, n_spill * sizeof(unsigned long long), s);
+    if (over) {
+        e = dmalloc((void**)&over_copy, kOverSlots * sizeof(unsigned long long), s);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(spill_copy, ps->spill, n_spill * sizeof(unsigned long long),
-                                cudaMemcpyDeviceToDevice, s);
+            e = cudaMemcpyAsync(over_copy, ps->over, kOverSlots * sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                                s);
+        if (e == cudaSuccess) e = over_clear(ps, s);
     }
     ps->slots = nullptr;  // the old slots stay allocated until the rehash has read them
     if (e == cudaSuccess) e = alloc_slots(ps, cap, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ps->slots, 0xff, cap * sizeof(unsigned long long), s);
-    // Status and count start over; the spill count too (word kSpillWord).
+    // Status and count start over.
     if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, 2 * sizeof(unsigned long long), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta + kSpillWord, 0, sizeof(unsigned long long), s);
     if (e == cudaSuccess) {
         PairTable t = table_view(ps);
         t.stats = nullptr;
-        const uint64_t n = old_cap + n_spill;
+        const uint64_t n = old_cap + (over ? kOverSlots : 0);
         const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, 4u * sm_count());
-        launch(k_rehash, grid, 256, 0, s, t, (const unsigned long long*)old, (const unsigned long long*)spill_copy,
-               old_cap, n_spill);
+        launch(k_rehash, grid, 256, 0, s, t, (const unsigned long long*)old, (const unsigned long long*)over_copy,
+               old_cap, over ? kOverSlots : 0);
         e = cudaGetLastError();
     }
     if (old) cudaFreeAsync(old, s);
-    if (spill_copy) cudaFreeAsync(spill_copy, s);
+    if (over_copy) cudaFreeAsync(over_copy, s);
     return e;
 }
 }  // namespace rs
@@ -151,8 +158,12 @@ extern "C" int rs_pairset_create(uint64_t capacity, int pow2, rs_pairset** out, 
     cudaGetDevice(&ps->device);
     ps->pow2 = pow2 ? 1 : 0;
     if (ps->pow2) capacity = next_pow2(capacity);
-    cudaError_t e = dmalloc((void**)&ps->meta, (kMetaWords + kSpillKeys) * sizeof(unsigned long long), s);
-    if (e == cudaSuccess) ps->spill = ps->meta + kMetaWords;
+    cudaError_t e = dmalloc((void**)&ps->meta, (kMetaWords + kOverSlots) * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) {
+        ps->over = ps->meta + kMetaWords;
+        ps->over_dirty = true;  // cleared below
+        e = over_clear(ps, s);
+    }
     if (e == cudaSuccess) e = alloc_slots(ps, capacity, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -171,6 +182,7 @@ extern "C" int rs_pairset_clear(rs_pairset* ps, void* stream) {
     ps->known_count = -1;
     cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = over_clear(ps, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) ps->known_count = 0;
     return to_status(e);
@@ -324,6 +336,7 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
         ps->known_count = -1;
         cudaError_t e = cudaMemsetAsync(ps->slots, 0xff, ps->capacity * sizeof(unsigned long long), s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ps->meta, 0, kMetaWords * sizeof(unsigned long long), s);
+        if (e == cudaSuccess) e = over_clear(ps, s);
         // Both directions with their broad phase and no events: one live-edge launch for both,
         // and the two directions' rays concurrently.  Otherwise each direction reads its
         // source edges only after the caller's event for them.

@@ -1,7 +1,8 @@
-"""Pair-table growth through the spill list: a table far smaller than the join's pair count
-appends the keys that find no slot to its spill list, and the join's status read regrows the
-table from its slots and the list instead of rerunning the rays.  The pair set equals the
-oracle's, and the launch count shows that no ray launch ran twice."""
+"""Pair-table growth through the overflow table: once a table far smaller than the join's pair
+count passes 3/4 load, later keys that do not settle within a few slots go to the pair set's
+overflow table, and the join's status read regrows the table from both instead of rerunning the
+rays.  The pair set equals the oracle's, and the launch count shows that no ray launch ran
+twice."""
 import ctypes
 
 import numpy as np
@@ -26,7 +27,7 @@ def _launches(fn):
 
 
 @pytest.mark.parametrize("containment", [False, True])
-def test_overlap_join_regrows_from_the_spill_list(cuda, containment):
+def test_overlap_join_regrows_from_the_overflow_table(cuda, containment):
     A, B = synth.overlap_workload(n_objects=300, level=2, world=12.0, seed=41)
     want = bind.intersection_join(A, B) if containment else bind.overlap_join(A, B)
     assert len(want) > 256
