@@ -552,9 +552,9 @@ struct PairTable {
     // Overflow table (nullable): a second open-addressing table of over_mask + 1 slots,
     // kept empty between joins.  Once the main table passes 3/4 of its slots, or a key
     // finds no slot within max_probes, ST_SPILLED is raised; from then on an insert that
-    // has not settled after kSpillProbes slots of the main table goes to the overflow
-    // table (a full main table would otherwise make every insert walk its whole probe
-    // limit, each step a dependent load).  A key may then sit in both; the regrowth
+    // does not settle at its first slot of the main table goes to the overflow table (a
+    // full main table would otherwise make every insert walk its whole probe limit, each
+    // step a dependent load).  A key may then sit in both; the regrowth
     // merges them.  A key that finds no slot in either raises ST_TABLE_FULL.
     unsigned long long* over;
     unsigned long long over_mask;
@@ -562,7 +562,6 @@ struct PairTable {
     unsigned long long spill_at;  // main-table count that raises ST_SPILLED
 };
 
-constexpr unsigned int kSpillProbes = 4;
 constexpr unsigned int kOverProbes = 256;
 
 // Open-addressing insert into slots[0..mask] (a power of two) from hash h; false when no
@@ -589,9 +588,16 @@ __device__ __forceinline__ bool probe_insert(unsigned long long* slots, unsigned
 __device__ __forceinline__ void table_insert(const PairTable& t, unsigned long long key) {
     const unsigned long long h = fmix64(key);
     unsigned long long slot = t.pow2 ? (h & (t.capacity - 1)) : (h % t.capacity);
+    // The status word is read with the first probe (the two loads overlap) and again every
+    // 32 probes: once the table has spilled, an insert that does not settle at its first
+    // slot goes to the overflow table.
+    unsigned int st = t.over ? *(volatile unsigned int*)t.status : 0u;
     unsigned int i = 0;
     for (; i < t.max_probes; ++i) {
-        if (i == kSpillProbes && t.over && (*(volatile unsigned int*)t.status & ST_SPILLED)) break;
+        if (i > 0 && t.over) {
+            if ((i & 31u) == 0) st = *(volatile unsigned int*)t.status;
+            if (st & ST_SPILLED) break;
+        }
         if (t.stats) atomicAdd(&t.stats[0], 1ull);
         unsigned long long cur = t.slots[slot];
         if (cur == key) return;

@@ -1,5 +1,5 @@
 """Pair-table growth through the overflow table: once a table far smaller than the join's pair
-count passes 3/4 load, later keys that do not settle within a few slots go to the pair set's
+count passes 3/4 load, later keys that do not settle at their first slot go to the pair set's
 overflow table, and the join's status read regrows the table from both instead of rerunning the
 rays.  The pair set equals the oracle's, and the launch count shows that no ray launch ran
 twice."""
