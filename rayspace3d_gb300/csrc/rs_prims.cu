@@ -128,8 +128,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restr
     const size_t base = (size_t)tile * kOsTile + (size_t)w * kOsWarpSpan;
     uint64_t k[kOsItems];
     uint32_t v[kOsItems];
-    // Item r's stable rank among the warp's keys of its digit (< kOsTile, 16 bits), two per word.
-    uint32_t rank[(kOsItems + 1) / 2] = {};
+    unsigned peers[kOsItems];  // lanes of the warp holding the same digit in item r
 #pragma unroll
     for (int r = 0; r < kOsItems; ++r) {
         const size_t idx = base + (size_t)r * 32 + lane;
@@ -137,18 +136,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restr
         k[r] = valid ? kin[idx] : 0ull;
         if (VALS) v[r] = valid ? vin[idx] : 0u;
     }
-    // Per-warp digit counts and each item's stable rank within its warp and digit: the
-    // warp's earlier keys of the digit (earlier items, then lower lanes of this item).  An
-    // invalid key gets a digit of its own: 256 + lane.
-    const unsigned lt = lanemask_lt();
+    // Per-warp digit counts (an invalid key gets a digit of its own: 256 + lane).
 #pragma unroll
     for (int r = 0; r < kOsItems; ++r) {
         const bool valid = base + (size_t)r * 32 + lane < n;
         const uint32_t dg = valid ? os_digit(k[r], shift, end_bit) : (256u + lane);
-        const unsigned peers = __match_any_sync(0xffffffffu, dg);
-        if (valid) rank[r / 2] |= (s_cnt[w][dg] + __popc(peers & lt)) << (16 * (r & 1));
-        __syncwarp();
-        if (valid && lane == __ffs(peers) - 1) s_cnt[w][dg] += __popc(peers);
+        peers[r] = __match_any_sync(0xffffffffu, dg);
+        if (valid && lane == __ffs(peers[r]) - 1) s_cnt[w][dg] += __popc(peers[r]);
         __syncwarp();
     }
     __syncthreads();
@@ -213,14 +207,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_os_pass(const uint64_t* __restr
     }
     s_gbase[d] = digit_base[d] + (uint32_t)prefix;
     __syncthreads();
-    // Into shared memory, digit-major: the digit's tile start, the warp's offset within the
-    // digit (s_cnt now holds the exclusive sums over warps) and the item's rank.
+    // Stable ranks into shared memory, digit-major.
+    const unsigned lt = lanemask_lt();
 #pragma unroll
     for (int r = 0; r < kOsItems; ++r) {
         const bool valid = base + (size_t)r * 32 + lane < n;
+        const uint32_t dg = os_digit(k[r], shift, end_bit);
+        uint32_t pos = 0;
+        if (valid) pos = s_dstart[dg] + s_cnt[w][dg] + __popc(peers[r] & lt);
+        __syncwarp();
+        if (valid && lane == __ffs(peers[r]) - 1) s_cnt[w][dg] += __popc(peers[r]);
+        __syncwarp();
         if (valid) {
-            const uint32_t dg = os_digit(k[r], shift, end_bit);
-            const uint32_t pos = s_dstart[dg] + s_cnt[w][dg] + ((rank[r / 2] >> (16 * (r & 1))) & 0xffffu);
             s_keys[pos] = k[r];
             if (VALS) s_vals[pos] = v[r];
         }
