@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--intersection-n", type=int, default=10_000, help="objects per set of the intersection join")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--leaf", type=int, default=0, help="BVH leaf size of the joins (0: the engine's default, 2)")
+    ap.add_argument("--endpoints", choices=["host", "device"], default="host",
+                    help="end to end: edge endpoints read in place from pinned host memory (host) or copied (device)")
     return ap.parse_args()
 
 
@@ -271,14 +273,20 @@ def run_engine(args, rank, world, local):
             host[tag] = {"tri": [t.cpu().pin_memory() for t in tri_tensors(g)],
                          "edges": [t.cpu().pin_memory() for t in g.edges],
                          "cells": g.cells.cpu().pin_memory()}
-        h2d = sum(t.numel() * t.element_size() for hs in host.values()
-                  for t in hs["tri"] + hs["edges"] + [hs["cells"]])
+        # With --endpoints host the edge endpoints (starts, ends: 24 B of the 36 B per edge)
+        # stay in pinned host memory and the join reads them in place, only for the edges the
+        # broad phase keeps; everything else is copied.
+        in_place = args.endpoints == "host"
+        copied = {tag: [t for k, t in enumerate(hs["edges"]) if not (in_place and k < 2)] for tag, hs in host.items()}
+        h2d = sum(t.numel() * t.element_size() for tag, hs in host.items()
+                  for t in hs["tri"] + copied[tag] + [hs["cells"]])
         ga2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
         gb2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
-        for dst, src in ((ga2, da), (gb2, db)):
+        for dst, src, tag in ((ga2, da, "A"), (gb2, db, "B")):
             dst.__dict__.update(src.__dict__)
             dst.V, dst.I, dst.T = [torch.empty_like(t) for t in (src.V, src.I, src.T)]
-            dst.edges = tuple(torch.empty_like(t) for t in src.edges)
+            dst.edges = tuple(host[tag]["edges"][k] if (in_place and k < 2) else torch.empty_like(t)
+                              for k, t in enumerate(src.edges))
             dst.cells = torch.empty_like(src.cells)
 
         sc = torch.cuda.Stream(device=dev)
@@ -300,7 +308,8 @@ def run_engine(args, rank, world, local):
                 ev["cells"].record(sc)
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
                     for d, h in zip(dst.edges, host[tag]["edges"]):
-                        d.copy_(h, non_blocking=True)
+                        if d is not h:
+                            d.copy_(h, non_blocking=True)
                     ev["edges" + tag].record(sc)
             sa.wait_event(ev["A"])
             sb.wait_event(ev["B"])
@@ -371,7 +380,9 @@ def run_engine(args, rank, world, local):
                    "edges_per_set": int(da.nE), "triangles_per_set": int(da.nF), "pairs": n_pairs,
                    "l2": "inputs larger than L2 (geometry ~487 MB + grids 64 MB per step)",
                    "bvh_leaf_size": args.leaf or 2, "parallelism": f"independent joins per rank x{world}"},
-        "e2e": {"value": round(e2e_s, 6), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h},
+        "e2e": {"value": round(e2e_s, 6), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
+                "edge_endpoints": ("pinned host memory, read in place by the join for the edges the broad phase "
+                                   "keeps (not copied)") if in_place else "copied with the rest"},
         "gpu_launches": int(launches),
         # The workload's second metric: edge rays of both directions (2 x edges per set) per
         # second of join; the broad phase traces only the live ones.

@@ -216,6 +216,15 @@ int64_t rs_estimate_pairs_from_raw(double raw, const float* h_means4, float cell
 uint64_t rs_hash_size_pow2(int64_t estimated_pairs);
 uint64_t rs_hash_size_odd(int64_t estimated_pairs, float load_factor);
 
+/* The address through which the engine's kernels read the buffer at p (no counterpart in
+ * the reference): device or managed memory as it is; pinned or registered host memory
+ * through its mapped device address, read in place over the host link (only what a kernel
+ * loads crosses it).  RS_ERR_INVALID for pageable host memory, which no kernel may read.
+ * rs_overlap_join and rs_overlap_join_after resolve every edge-payload pointer this way, so
+ * a payload may stay in pinned host memory: the join then reads only the endpoints of the
+ * edges its broad phase keeps (all of them when every object has a partner). */
+int rs_kernel_pointer(const void* p, const void** out);
+
 /* Full joins with automatic table growth on RS_ERR_TABLE_FULL.  The table `ps` is cleared
  * first.  overlap: A-edges into B and B-edges into A (swapped).  intersection: overlap plus
  * containment in both directions.  direction: 0 both, 1 mesh1->mesh2 only, 2 mesh2->mesh1 only

@@ -58,6 +58,7 @@ SIGNATURES = {
     "rs_estimate_grid": (I, [P, P, U64, F, F, F, ctypes.POINTER(ctypes.c_double), P, P]),
     "rs_estimate_grid_cells": (I, [P, P, U64, F, F, F, P, P]),
     "rs_estimate_pairs_from_raw": (I64, [ctypes.c_double, P, F, I]),
+    "rs_kernel_pointer": (I, [P, PP]),
     "rs_hash_size_pow2": (U64, [I64]),
     "rs_hash_size_odd": (U64, [I64, F]),
     "rs_overlap_join": (I, [P, P, P, P, P, P, U64, P, P, P, P, P, P, U64, I, I, P, P]),

@@ -127,6 +127,26 @@ cudaError_t table_regrow(rs_pairset* ps, uint64_t count, uint64_t over, cudaStre
 
 using namespace rs;
 
+extern "C" int rs_kernel_pointer(const void* p, const void** out) {
+    if (!out) return RS_ERR_INVALID;
+    *out = nullptr;
+    if (!p) return RS_OK;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return RS_ERR_INVALID;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+        *out = p;
+        return RS_OK;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+        *out = a.devicePointer;
+        return RS_OK;
+    }
+    return RS_ERR_INVALID;  // pageable host memory: no kernel may read it
+}
+
 extern "C" uint64_t rs_hash_size_pow2(int64_t est) {
     uint64_t size = 16777216ull;
     if (est > 0) {
@@ -277,6 +297,15 @@ extern "C" int rs_pairset_finalize(rs_pairset* ps, int order, uint64_t* d_keys, 
     return n > capacity ? RS_ERR_OUTPUT_OVERFLOW : RS_OK;
 }
 
+// *p replaced by the address kernels read it through (rs_kernel_pointer); false when none.
+template <class T>
+static bool kernel_ptr(const T** p) {
+    const void* q = nullptr;
+    if (rs_kernel_pointer(*p, &q) != RS_OK) return false;
+    *p = static_cast<const T*>(q);
+    return true;
+}
+
 static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
                              const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
                              uint64_t nEA, const rs_bvh* B, const float* d_startsB, const float* d_endsB,
@@ -287,6 +316,11 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
     const bool a2b = direction == 0 || direction == 1;
     const bool b2a = direction == 0 || direction == 2;
     cudaStream_t s = (cudaStream_t)stream;
+    // Payloads in pinned host memory are read in place through their mapped addresses.
+    if (!kernel_ptr(&d_startsA) || !kernel_ptr(&d_endsA) || !kernel_ptr(&d_offsetsA) || !kernel_ptr(&d_countsA) ||
+        !kernel_ptr(&d_sourcesA) || !kernel_ptr(&d_startsB) || !kernel_ptr(&d_endsB) || !kernel_ptr(&d_offsetsB) ||
+        !kernel_ptr(&d_countsB) || !kernel_ptr(&d_sourcesB))
+        return RS_ERR_INVALID;
     {
         int st = bvh_ready(A);  // the broad phase needs the object counts
         if (st == RS_OK) st = bvh_ready(B);

@@ -212,3 +212,34 @@ def test_finalize_orders_and_count(cuda, n_objects, world):
     ps.clear()
     assert ps.info()[1] == 0
     assert ps.finalize().numel() == 0
+
+
+def test_overlap_join_reads_pinned_host_payloads(cuda):
+    """Edge payloads left in pinned host memory (the endpoints only, then all five arrays) are
+    read in place through their mapped addresses: the same pair set as device payloads.
+    rs_kernel_pointer maps pinned memory and refuses pageable memory (checked without a
+    launch: no kernel is ever given a pageable address)."""
+    A, B = synth.overlap_workload(n_objects=300, level=2, world=30.0, seed=9)
+    da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+    ba, bb = api.Bvh(da), api.Bvh(db)
+    ps = api.PairSet(1 << 14)
+    api.overlap_join(ba, bb, ps)
+    want = np.sort(ps.finalize().cpu().numpy())
+    assert len(want) > 0
+    device = [g.edges for g in (da, db)]
+    for k_host in (2, 5):
+        for g, e in zip((da, db), device):
+            g.edges = tuple(t.cpu().pin_memory() if k < k_host else t for k, t in enumerate(e))
+        ps2 = api.PairSet(1 << 14)
+        api.overlap_join(ba, bb, ps2)
+        np.testing.assert_array_equal(np.sort(ps2.finalize().cpu().numpy()), want)
+    L = _lib.load()
+    out = ctypes.c_void_p()
+    pinned = torch.zeros(16, dtype=torch.float32).pin_memory()
+    assert L.rs_kernel_pointer(pinned.data_ptr(), ctypes.byref(out)) == 0 and out.value
+    dev = torch.zeros(16, device="cuda")
+    assert L.rs_kernel_pointer(dev.data_ptr(), ctypes.byref(out)) == 0 and out.value == dev.data_ptr()
+    pageable = np.zeros(16, np.float32)
+    assert L.rs_kernel_pointer(pageable.ctypes.data, ctypes.byref(out)) == _lib.RS_ERR_INVALID
+    ba.close()
+    bb.close()
