@@ -68,8 +68,9 @@ def parse_args():
     ap.add_argument("--intersection-n", type=int, default=10_000, help="objects per set of the intersection join")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--leaf", type=int, default=0, help="BVH leaf size of the joins (0: the engine's default, 2)")
-    ap.add_argument("--endpoints", choices=["host", "device"], default="host",
-                    help="end to end: edge endpoints read in place from pinned host memory (host) or copied (device)")
+    ap.add_argument("--endpoints", choices=["auto", "host", "device"], default="auto",
+                    help="end to end: edge endpoints read in place from pinned host memory (host), copied (device), "
+                         "or chosen per join from its estimate (auto)")
     return ap.parse_args()
 
 
@@ -200,7 +201,7 @@ def run_engine(args, rank, world, local):
         da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
         torch.cuda.synchronize()
 
-        def step(ga, gb, after_copies=False, edges_ready=None):
+        def step(ga, gb, after_copies=False, edges_ready=None, edges_hook=None):
             # The two builds run concurrently on their own streams (after the work already
             # queued on `stream`, or, end to end, after their own geometry copies); the join
             # on `stream` is ordered after both builds by the engine.
@@ -210,6 +211,8 @@ def run_engine(args, rank, world, local):
             ba = api.Bvh(ga, leaf_size=args.leaf, stream=sa, asynchronous=True)
             bb = api.Bvh(gb, leaf_size=args.leaf, stream=sb, asynchronous=True)
             est, _ = api.estimate_pairs(ga, gb, stream=stream)
+            if edges_hook is not None:  # end to end: the edge payloads are queued now
+                edges_ready = edges_hook(est)
             size = api.hash_size_pow2(est)
             key = ("ps", size)
             ps = pairs_out.get(key)
@@ -273,21 +276,28 @@ def run_engine(args, rank, world, local):
             host[tag] = {"tri": [t.cpu().pin_memory() for t in tri_tensors(g)],
                          "edges": [t.cpu().pin_memory() for t in g.edges],
                          "cells": g.cells.cpu().pin_memory()}
-        # With --endpoints host the edge endpoints (starts, ends: 24 B of the 36 B per edge)
-        # stay in pinned host memory and the join reads them in place, only for the edges the
-        # broad phase keeps; everything else is copied.
-        in_place = args.endpoints == "host"
-        copied = {tag: [t for k, t in enumerate(hs["edges"]) if not (in_place and k < 2)] for tag, hs in host.items()}
-        h2d = sum(t.numel() * t.element_size() for tag, hs in host.items()
-                  for t in hs["tri"] + copied[tag] + [hs["cells"]])
+        # The edge endpoints (starts, ends: 24 B of the 36 B per edge) either stay in pinned
+        # host memory, where the join reads them in place for the edges its broad phase
+        # keeps, or are copied with the rest.  In place pays while the kept edges are few:
+        # about two objects per estimated pair have partners, and their edges' endpoints
+        # are read scattered (about three times their 24 B over the link), against 24 B per
+        # edge to copy them all -- in place while est * 2 * (edges per object) * 3 stays
+        # below half the edges, i.e. est < objects / 12 (W = 1000: in place; W = 80.7,
+        # estimate 1,404 for 10k objects: copied).
+        in_place_below = max(1, args.objects // 12)
+        dev_edges = {tag: tuple(torch.empty_like(t) for t in g.edges) for tag, g in (("A", da), ("B", db))}
         ga2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
         gb2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
-        for dst, src, tag in ((ga2, da, "A"), (gb2, db, "B")):
+        for dst, src in ((ga2, da), (gb2, db)):
             dst.__dict__.update(src.__dict__)
             dst.V, dst.I, dst.T = [torch.empty_like(t) for t in (src.V, src.I, src.T)]
-            dst.edges = tuple(host[tag]["edges"][k] if (in_place and k < 2) else torch.empty_like(t)
-                              for k, t in enumerate(src.edges))
             dst.cells = torch.empty_like(src.cells)
+        chosen = []
+
+        def step_h2d(in_place):
+            return sum(t.numel() * t.element_size() for hs in host.values()
+                       for k, t in enumerate(hs["edges"]) if not (in_place and k < 2)) + \
+                   sum(t.numel() * t.element_size() for hs in host.values() for t in hs["tri"] + [hs["cells"]])
 
         sc = torch.cuda.Stream(device=dev)
         ev = {k: torch.cuda.Event() for k in ("A", "B", "cells", "edgesA", "edgesB")}
@@ -296,7 +306,7 @@ def run_engine(args, rank, world, local):
             # All inputs go over one copy stream, in the order the step needs them: each
             # set's triangles (its build starts when they land), the grids (the estimate and
             # the table sizing run while the edge payloads are still in flight), A's edges,
-            # B's edges.
+            # B's edges -- the endpoints only when this join's estimate says to copy them.
             sc.wait_stream(stream)
             with torch.cuda.stream(sc):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
@@ -306,15 +316,24 @@ def run_engine(args, rank, world, local):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
                     dst.cells.copy_(host[tag]["cells"], non_blocking=True)
                 ev["cells"].record(sc)
-                for dst, tag in ((ga2, "A"), (gb2, "B")):
-                    for d, h in zip(dst.edges, host[tag]["edges"]):
-                        if d is not h:
-                            d.copy_(h, non_blocking=True)
-                    ev["edges" + tag].record(sc)
             sa.wait_event(ev["A"])
             sb.wait_event(ev["B"])
             stream.wait_event(ev["cells"])
-            k = step(ga2, gb2, after_copies=True, edges_ready=(ev["edgesA"], ev["edgesB"]))
+
+            def edges_after_estimate(est):
+                in_place = args.endpoints == "host" or (args.endpoints == "auto" and est < in_place_below)
+                chosen.append(in_place)
+                with torch.cuda.stream(sc):
+                    for dst, tag in ((ga2, "A"), (gb2, "B")):
+                        hs = host[tag]["edges"]
+                        dst.edges = tuple(hs[k] if (in_place and k < 2) else dev_edges[tag][k] for k in range(len(hs)))
+                        for d, h in zip(dst.edges, hs):
+                            if d is not h:
+                                d.copy_(h, non_blocking=True)
+                        ev["edges" + tag].record(sc)
+                return ev["edgesA"], ev["edgesB"]
+
+            k = step(ga2, gb2, after_copies=True, edges_hook=edges_after_estimate)
             out = k.cpu()
             return out
 
@@ -330,6 +349,8 @@ def run_engine(args, rank, world, local):
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.steps
         d2h = int(out.numel() * out.element_size())
+        in_place = chosen[-1]
+        h2d = step_h2d(in_place)
         clk.__exit__(None, None, None)
 
     # Parity spot check of this run's output against the previous device-resident result.
@@ -381,8 +402,10 @@ def run_engine(args, rank, world, local):
                    "l2": "inputs larger than L2 (geometry ~487 MB + grids 64 MB per step)",
                    "bvh_leaf_size": args.leaf or 2, "parallelism": f"independent joins per rank x{world}"},
         "e2e": {"value": round(e2e_s, 6), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
-                "edge_endpoints": ("pinned host memory, read in place by the join for the edges the broad phase "
-                                   "keeps (not copied)") if in_place else "copied with the rest"},
+                "edge_endpoints": (("pinned host memory, read in place by the join for the edges the broad phase "
+                                    "keeps (not copied)") if in_place else "copied with the rest") +
+                                  f" (--endpoints {args.endpoints}; auto: in place while the estimate is below "
+                                  f"{in_place_below} pairs)"},
         "gpu_launches": int(launches),
         # The workload's second metric: edge rays of both directions (2 x edges per set) per
         # second of join; the broad phase traces only the live ones.
