@@ -305,8 +305,9 @@ def run_engine(args, rank, world, local):
         def e2e_step():
             # All inputs go over one copy stream, in the order the step needs them: each
             # set's triangles (its build starts when they land), the grids (the estimate and
-            # the table sizing run while the edge payloads are still in flight), A's edges,
-            # B's edges -- the endpoints only when this join's estimate says to copy them.
+            # the table sizing run while the edge payloads are still in flight), the edges'
+            # offsets, counts and sources, then -- only when this join's estimate says to
+            # copy them -- A's and B's endpoints.
             sc.wait_stream(stream)
             with torch.cuda.stream(sc):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
@@ -316,6 +317,9 @@ def run_engine(args, rank, world, local):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
                     dst.cells.copy_(host[tag]["cells"], non_blocking=True)
                 ev["cells"].record(sc)
+                for tag in ("A", "B"):
+                    for k in range(2, len(host[tag]["edges"])):
+                        dev_edges[tag][k].copy_(host[tag]["edges"][k], non_blocking=True)
             sa.wait_event(ev["A"])
             sb.wait_event(ev["B"])
             stream.wait_event(ev["cells"])
@@ -327,9 +331,9 @@ def run_engine(args, rank, world, local):
                     for dst, tag in ((ga2, "A"), (gb2, "B")):
                         hs = host[tag]["edges"]
                         dst.edges = tuple(hs[k] if (in_place and k < 2) else dev_edges[tag][k] for k in range(len(hs)))
-                        for d, h in zip(dst.edges, hs):
-                            if d is not h:
-                                d.copy_(h, non_blocking=True)
+                        if not in_place:
+                            for k in range(2):
+                                dev_edges[tag][k].copy_(hs[k], non_blocking=True)
                         ev["edges" + tag].record(sc)
                 return ev["edgesA"], ev["edgesB"]
 
