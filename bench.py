@@ -69,7 +69,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--leaf", type=int, default=0, help="BVH leaf size of the joins (0: the engine's default, 2)")
     ap.add_argument("--endpoints", choices=["auto", "host", "device"], default="auto",
-                    help="end to end: edge endpoints read in place from pinned host memory (host), copied (device), "
+                    help="end to end: edge payloads read in place from pinned host memory (host), copied (device), "
                          "or chosen per join from its estimate (auto)")
     return ap.parse_args()
 
@@ -211,8 +211,9 @@ def run_engine(args, rank, world, local):
             ba = api.Bvh(ga, leaf_size=args.leaf, stream=sa, asynchronous=True)
             bb = api.Bvh(gb, leaf_size=args.leaf, stream=sb, asynchronous=True)
             est, _ = api.estimate_pairs(ga, gb, stream=stream)
+            indexes = None
             if edges_hook is not None:  # end to end: the edge payloads are queued now
-                edges_ready = edges_hook(est)
+                edges_ready, indexes = edges_hook(est)
             size = api.hash_size_pow2(est)
             key = ("ps", size)
             ps = pairs_out.get(key)
@@ -224,7 +225,7 @@ def run_engine(args, rank, world, local):
                 pairs_out[key] = ps
             # End to end, the broad phase runs while the edge payloads are still in flight
             # and each direction's rays wait for their own payload.
-            api.overlap_join(ba, bb, ps, stream=stream, edges_ready=edges_ready)
+            api.overlap_join(ba, bb, ps, stream=stream, edges_ready=edges_ready, indexes=indexes)
             keys = ps.finalize(order=1, stream=stream)
             ba.close()
             bb.close()
@@ -276,16 +277,21 @@ def run_engine(args, rank, world, local):
             host[tag] = {"tri": [t.cpu().pin_memory() for t in tri_tensors(g)],
                          "edges": [t.cpu().pin_memory() for t in g.edges],
                          "cells": g.cells.cpu().pin_memory()}
-        # The edge endpoints (starts, ends: 24 B of the 36 B per edge) either stay in pinned
-        # host memory, where the join reads them in place for the edges its broad phase
-        # keeps, or are copied with the rest.  In place pays while the kept edges are few:
-        # about two objects per estimated pair have partners, and their edges' endpoints
-        # are read scattered (about three times their 24 B over the link), against 24 B per
-        # edge to copy them all -- in place while est * 2 * (edges per object) * 3 stays
-        # below half the edges, i.e. est < objects / 12 (W = 1000: in place; W = 80.7,
-        # estimate 1,404 for 10k objects: copied).
+        # The edge payloads either stay in pinned host memory, where the join reads in place
+        # only the slabs of 256 edges that can hold an edge of an object with a partner (each
+        # set's slab index, 3 + nE / 256 int64, is built once per dataset like its grid and
+        # copied with the grids), or are copied whole.  In place pays while few objects have
+        # partners: about two per estimated pair, each object's x-slab of the payload holds
+        # roughly edges * (its x extent / the world's), against all edges copied.  It is
+        # chosen per join from the join's own estimate: in place while est < objects / 12
+        # (W = 1000: in place; W = 80.7, estimate 1,404 for 10k objects: copied).
         in_place_below = max(1, args.objects // 12)
+        for tag, g in (("A", da), ("B", db)):
+            idx, ordered = api.edge_index(g)
+            host[tag]["index"] = idx.cpu().pin_memory()
+            host[tag]["ordered"] = ordered
         dev_edges = {tag: tuple(torch.empty_like(t) for t in g.edges) for tag, g in (("A", da), ("B", db))}
+        dev_index = {tag: torch.empty_like(host[tag]["index"], device=dev) for tag in ("A", "B")}
         ga2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
         gb2 = api.DeviceGeometry.__new__(api.DeviceGeometry)
         for dst, src in ((ga2, da), (gb2, db)):
@@ -295,19 +301,18 @@ def run_engine(args, rank, world, local):
         chosen = []
 
         def step_h2d(in_place):
+            edges = sum(t.numel() * t.element_size() for hs in host.values() for t in hs["edges"])
             return sum(t.numel() * t.element_size() for hs in host.values()
-                       for k, t in enumerate(hs["edges"]) if not (in_place and k < 2)) + \
-                   sum(t.numel() * t.element_size() for hs in host.values() for t in hs["tri"] + [hs["cells"]])
+                       for t in hs["tri"] + [hs["cells"], hs["index"]]) + (0 if in_place else edges)
 
         sc = torch.cuda.Stream(device=dev)
         ev = {k: torch.cuda.Event() for k in ("A", "B", "cells", "edgesA", "edgesB")}
 
         def e2e_step():
             # All inputs go over one copy stream, in the order the step needs them: each
-            # set's triangles (its build starts when they land), the grids (the estimate and
-            # the table sizing run while the edge payloads are still in flight), the edges'
-            # offsets, counts and sources, then -- only when this join's estimate says to
-            # copy them -- A's and B's endpoints.
+            # set's triangles (its build starts when they land), the grids and slab indexes
+            # (the estimate and the table sizing run while the rest is in flight), then --
+            # when this join's estimate says to copy them -- A's and B's edge payloads.
             sc.wait_stream(stream)
             with torch.cuda.stream(sc):
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
@@ -316,10 +321,8 @@ def run_engine(args, rank, world, local):
                     ev[tag].record(sc)
                 for dst, tag in ((ga2, "A"), (gb2, "B")):
                     dst.cells.copy_(host[tag]["cells"], non_blocking=True)
+                    dev_index[tag].copy_(host[tag]["index"], non_blocking=True)
                 ev["cells"].record(sc)
-                for tag in ("A", "B"):
-                    for k in range(2, len(host[tag]["edges"])):
-                        dev_edges[tag][k].copy_(host[tag]["edges"][k], non_blocking=True)
             sa.wait_event(ev["A"])
             sb.wait_event(ev["B"])
             stream.wait_event(ev["cells"])
@@ -330,12 +333,12 @@ def run_engine(args, rank, world, local):
                 with torch.cuda.stream(sc):
                     for dst, tag in ((ga2, "A"), (gb2, "B")):
                         hs = host[tag]["edges"]
-                        dst.edges = tuple(hs[k] if (in_place and k < 2) else dev_edges[tag][k] for k in range(len(hs)))
+                        dst.edges = tuple(hs) if in_place else dev_edges[tag]
                         if not in_place:
-                            for k in range(2):
-                                dev_edges[tag][k].copy_(hs[k], non_blocking=True)
+                            for d, h in zip(dev_edges[tag], hs):
+                                d.copy_(h, non_blocking=True)
                         ev["edges" + tag].record(sc)
-                return ev["edgesA"], ev["edgesB"]
+                return (ev["edgesA"], ev["edgesB"]), ((dev_index["A"], dev_index["B"]) if in_place else None)
 
             k = step(ga2, gb2, after_copies=True, edges_hook=edges_after_estimate)
             out = k.cpu()
@@ -406,10 +409,10 @@ def run_engine(args, rank, world, local):
                    "l2": "inputs larger than L2 (geometry ~487 MB + grids 64 MB per step)",
                    "bvh_leaf_size": args.leaf or 2, "parallelism": f"independent joins per rank x{world}"},
         "e2e": {"value": round(e2e_s, 6), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
-                "edge_endpoints": (("pinned host memory, read in place by the join for the edges the broad phase "
-                                    "keeps (not copied)") if in_place else "copied with the rest") +
-                                  f" (--endpoints {args.endpoints}; auto: in place while the estimate is below "
-                                  f"{in_place_below} pairs)"},
+                "edge_payloads": (("pinned host memory, read in place by the join: only the slabs of objects "
+                                   "with partners (slab indexes copied)") if in_place else "copied") +
+                                 f" (--endpoints {args.endpoints}; auto: in place while the estimate is below "
+                                 f"{in_place_below} pairs)"},
         "gpu_launches": int(launches),
         # The workload's second metric: edge rays of both directions (2 x edges per set) per
         # second of join; the broad phase traces only the live ones.

@@ -235,6 +235,30 @@ int rs_overlap_join(const rs_bvh* A, const float* d_startsA, const float* d_ends
                     const int32_t* d_countsB, const int32_t* d_sourcesB, uint64_t nEB,
                     int direction, int with_containment, rs_pairset* ps, void* stream);
 
+/* Slab index of an edge payload (no counterpart in the reference), built once per dataset:
+ * d_index receives 3 + ceil(nE / 256) int64 -- [0] 1 when the payload is in the
+ * reference's order (EdgePreprocessor's std::map over quantised endpoint pairs, so sorted by
+ * the quantised x of each edge's lower endpoint, llround(x * 1e5)) and no source id is
+ * negative, else 0; [1] the largest source id; [2] nE; [3 + b] the key of edge 256 * b.
+ * *h_ordered (nullable) receives [0].  Pointers may be device or pinned host memory. */
+int rs_edge_index(const float* d_starts, const float* d_ends, const int32_t* d_sources, uint64_t nE, uint64_t nS,
+                  int64_t* d_index, int* h_ordered, void* stream);
+
+/* rs_overlap_join_after with each payload's slab index (rs_edge_index; either nullable):
+ * the live-edge check then reads only the slabs of 256 edges that can hold an edge of an
+ * object the broad phase gave a partner -- an index whose [0] is 0, whose [2] is not the
+ * payload's edge count, or whose largest source id is not an object of its set, makes the
+ * check read every edge, as without one.  With
+ * the payloads in pinned host memory a sparse join reads a few of their slabs over the host
+ * link instead of all of them.  Same pair set as rs_overlap_join. */
+int rs_overlap_join_indexed(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
+                            const int32_t* d_offsetsA, const int32_t* d_countsA, const int32_t* d_sourcesA,
+                            uint64_t nEA, const int64_t* d_indexA, const rs_bvh* B, const float* d_startsB,
+                            const float* d_endsB, const int32_t* d_offsetsB, const int32_t* d_countsB,
+                            const int32_t* d_sourcesB, uint64_t nEB, const int64_t* d_indexB, int direction,
+                            int with_containment, rs_pairset* ps, void* edges_a_ready, void* edges_b_ready,
+                            void* stream);
+
 /* rs_overlap_join whose edge payloads may still be in flight (no counterpart in the
  * reference): the broad phase runs at once, each direction's edge rays wait on the stream
  * for the caller's event (cudaEvent_t; nullable) marking its source payload as written --

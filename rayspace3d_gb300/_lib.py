@@ -63,6 +63,8 @@ SIGNATURES = {
     "rs_hash_size_odd": (U64, [I64, F]),
     "rs_overlap_join": (I, [P, P, P, P, P, P, U64, P, P, P, P, P, P, U64, I, I, P, P]),
     "rs_overlap_join_after": (I, [P, P, P, P, P, P, U64, P, P, P, P, P, P, U64, I, I, P, P, P, P]),
+    "rs_edge_index": (I, [P, P, P, U64, U64, P, ctypes.POINTER(I), P]),
+    "rs_overlap_join_indexed": (I, [P, P, P, P, P, P, U64, P, P, P, P, P, P, P, U64, P, I, I, P, P, P, P]),
     "rs_overlap_join_filtered": (I, [P, U64, P, U64, P, P, P, P, P, P, U64, P, U64, P, U64, P, P, P, P, P, P, U64,
                                      I, I, I, P, P]),
     "rs_launch_count": (U64, []),

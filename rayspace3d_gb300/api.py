@@ -44,6 +44,18 @@ def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
     return t.data_ptr()
 
 
+def _kernel_ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    """A device tensor's or a pinned host tensor's address (kernels read pinned memory in
+    place, rs_kernel_pointer)."""
+    if t is None:
+        return None
+    if not (t.is_cuda or t.is_pinned()):
+        raise ValueError("device or pinned host tensor expected")
+    if not t.is_contiguous():
+        raise ValueError("contiguous tensor expected")
+    return t.data_ptr()
+
+
 class DeviceGeometry:
     """One .pre geometry set resident on the GPU (vertices, indices, tri2obj, edges, grid)."""
 
@@ -247,14 +259,38 @@ def triangle_join(target: Bvh, source: DeviceGeometry, ps: PairSet, swap: bool =
                                         _ptr(source.T), int(swap), ps.handle, _stream(stream)), "rs_triangle_join")
 
 
+def edge_index(geom: "DeviceGeometry", out: Optional[torch.Tensor] = None, stream=None):
+    """Slab index of a geometry's edge payload (rs_edge_index): an int64 tensor of
+    3 + ceil(nE / 256) entries (on the GPU, or into `out`, e.g. pinned host memory) and
+    whether the payload is in the reference's key order (else the index only disables
+    itself)."""
+    s, e, _, _, src = geom.edge_ptrs()
+    n = 3 + (int(geom.nE) + 255) // 256
+    if out is None:
+        out = torch.empty(n, dtype=torch.int64, device="cuda")
+    ordered = ctypes.c_int()
+    _check(_lib.load().rs_edge_index(s, e, src, int(geom.nE), int(geom.edges[4].numel()), _kernel_ptr(out),
+                                     ctypes.byref(ordered), _stream(stream)), "rs_edge_index")
+    return out, bool(ordered.value)
+
+
 def overlap_join(A: Bvh, B: Bvh, ps: PairSet, direction: int = 0, with_containment: bool = False,
-                 stream=None, edges_ready=None) -> None:
+                 stream=None, edges_ready=None, indexes=None) -> None:
     """Both edge directions (and containment when asked) into ps, growing it on overflow.
     edges_ready = (event for A's edges, event for B's edges) (torch.cuda.Event, either None):
-    the broad phase runs at once, each direction's rays wait for their event."""
+    the broad phase runs at once, each direction's rays wait for their event.  indexes =
+    (A's slab index, B's) from edge_index (either None): the live-edge check reads only the
+    slabs of objects with partners (rs_overlap_join_indexed)."""
     ea = A.geom.edge_ptrs()
     eb = B.geom.edge_ptrs()
     L = _lib.load()
+    if indexes is not None:
+        evs = [ctypes.c_void_p(e.cuda_event) if e is not None else None for e in (edges_ready or (None, None))]
+        ia, ib = (_kernel_ptr(t) for t in indexes)
+        _check(L.rs_overlap_join_indexed(A.handle, *ea, A.geom.nE, ia, B.handle, *eb, B.geom.nE, ib, int(direction),
+                                         int(with_containment), ps.handle, evs[0], evs[1], _stream(stream)),
+               "rs_overlap_join_indexed")
+        return
     if edges_ready is None:
         _check(L.rs_overlap_join(A.handle, *ea, A.geom.nE, B.handle, *eb, B.geom.nE, int(direction),
                                  int(with_containment), ps.handle, _stream(stream)), "rs_overlap_join")

@@ -118,6 +118,11 @@ struct EdgeCull {
     const int* pbox = nullptr;
     uint64_t n_pbox = 0;
     const uint32_t* entry = nullptr;
+    // Slab index of the source payload (rs_edge_index; nullable) and the source objects' own
+    // boxes (as pbox): with both, only the payload's slabs that can hold an edge of an object
+    // with a partner are checked for live edges.
+    const long long* xindex = nullptr;
+    const int* sbox = nullptr;
 };
 
 // Recheck statistics of the translation units that run hit tests (see rs_device.cuh).

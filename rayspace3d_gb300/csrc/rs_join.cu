@@ -357,6 +357,12 @@ struct EdgeJob {
     const uint32_t* entry;
     uint32_t* live_entry;
     uint32_t* order_entry;
+    // Slab index (nullable, as EdgeCull): the payload's slab keys, the source objects' own
+    // boxes, and one flag per slab (zeroed) for the slabs that may hold a live edge.
+    const long long* xindex;
+    const int* sbox;
+    uint8_t* covered;
+    uint64_t n_slab;
     unsigned int* n_live;
     unsigned int* n_def;
     const BNode* nodes;
@@ -425,6 +431,33 @@ __device__ __forceinline__ bool edge_is_live(const EdgeJob& j, uint64_t i, int n
 // blocks0 run job j0, the others j1.
 constexpr int kLiveEdges = 4;
 
+// Appends edge i to its job's live list when `any` (warp-collective: every lane calls it):
+// one atomic per warp, the entry node beside it, and in binned jobs the edge's rank within
+// its cell.
+__device__ __forceinline__ void live_append(const EdgeJob& j, uint64_t i, bool any, uint32_t en, int lane) {
+    const unsigned int below = (1u << lane) - 1u;
+    const unsigned int m = __ballot_sync(0xffffffffu, any);
+    if (!m) return;
+    const int leader = __ffs(m) - 1;
+    unsigned int pos0 = 0;
+    if (lane == leader) pos0 = atomicAdd(j.n_live, (unsigned int)__popc(m));
+    pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+    const unsigned int pos = pos0 + __popc(m & below);
+    if (any) j.live[pos] = (uint32_t)i;
+    if (any && j.live_entry) j.live_entry[pos] = en;
+    if (j.order) {
+        // Every lane takes part in the match (lanes without a live edge with a cell of
+        // their own, kCells + lane), so that the mask is the full warp.
+        const uint32_t cell = any ? edge_cell(j, i) : (uint32_t)kCells + lane;
+        const unsigned int peers = __match_any_sync(0xffffffffu, cell);
+        const int first = __ffs(peers) - 1;
+        unsigned int r0 = 0;
+        if (any && lane == first) r0 = atomicAdd(&j.cells[cell], (unsigned int)__popc(peers));
+        r0 = __shfl_sync(0xffffffffu, r0, first);
+        if (any) j.rank[pos] = r0 + __popc(peers & below);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsigned int blocks0) {
     const bool second = blockIdx.x >= blocks0;
     const EdgeJob& j = second ? j1 : j0;
@@ -451,32 +484,119 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
         en[u] = (j.entry && in && ns[u] == 1) ? j.entry[so0[u]] : 0u;
     }
     const int lane = threadIdx.x & 31;
-    const unsigned int below = (1u << lane) - 1u;
 #pragma unroll
     for (int u = 0; u < kLiveEdges; ++u) {
         const uint64_t i = base + (uint64_t)u * blockDim.x;
         const bool any = ns[u] > 0 && edge_is_live(j, i, ns[u], j.p.sources + off[u], so0[u], c0[u]);
-        const unsigned int m = __ballot_sync(0xffffffffu, any);
-        if (!m) continue;
-        const int leader = __ffs(m) - 1;
-        unsigned int pos0 = 0;
-        if (lane == leader) pos0 = atomicAdd(j.n_live, (unsigned int)__popc(m));
-        pos0 = __shfl_sync(0xffffffffu, pos0, leader);
-        const unsigned int pos = pos0 + __popc(m & below);
-        if (any) j.live[pos] = (uint32_t)i;
-        if (any && j.live_entry) j.live_entry[pos] = en[u];
-        if (j.order) {
-            // Every lane takes part in the match (lanes without a live edge with a cell of
-            // their own, kCells + lane), so that the mask is the full warp.
-            const uint32_t cell = any ? edge_cell(j, i) : (uint32_t)kCells + lane;
-            const unsigned int peers = __match_any_sync(0xffffffffu, cell);
-            const int first = __ffs(peers) - 1;
-            unsigned int r0 = 0;
-            if (any && lane == first) r0 = atomicAdd(&j.cells[cell], (unsigned int)__popc(peers));
-            r0 = __shfl_sync(0xffffffffu, r0, first);
-            if (any) j.rank[pos] = r0 + __popc(peers & below);
-        }
+        live_append(j, i, any, en[u], lane);
     }
+}
+
+// Slab index of an edge payload (rs_edge_index).  The reference's payload is in std::map
+// order of its edges' quantised endpoint pairs, lower endpoint first
+// (EdgePreprocessor.cpp:41-119: llround(x * 1e5) per coordinate), so it is sorted by the
+// quantised x of each edge's lower endpoint -- the smaller of its two quantised x.  Slab b
+// holds edges [b * kSlab, (b + 1) * kSlab); index[3 + b] is the key of its first edge.
+// index[0] = 1 when the keys never decrease and no source id is negative (else 0), index[1]
+// = the largest source id, index[2] = the edge count it was built for.  The live-edge check then visits only the slabs whose key range
+// meets the quantised x range of an object with a partner: every edge of an object lies
+// between its box's quantised x bounds (llround is monotone), and every live edge has such
+// a source.
+constexpr uint64_t kSlab = 256;
+
+__device__ __forceinline__ long long edge_key_x(const EdgePayload& p, uint64_t e) {
+    return min(llround((double)p.starts[3 * e] * 1e5), llround((double)p.ends[3 * e] * 1e5));
+}
+
+// word[0]: 1 once a key decreases or a source id is negative; word[1]: the largest source id.
+__global__ void __launch_bounds__(256) k_edge_index(EdgePayload p, uint64_t nE, uint64_t nS,
+                                                    long long* __restrict__ index, int* __restrict__ word) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nE; e += stride) {
+        const long long x = edge_key_x(p, e);
+        if (e % kSlab == 0) index[3 + e / kSlab] = x;
+        if (e + 1 < nE && edge_key_x(p, e + 1) < x) bad = true;
+    }
+    int mx = -1;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nS; k += stride) {
+        const int src = p.sources[k];
+        bad |= src < 0;
+        mx = max(mx, src);
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&word[0], 1);
+    if ((threadIdx.x & 31) == 0) atomicMax(&word[1], mx);
+}
+
+__global__ void k_edge_index_head(long long* __restrict__ index, const int* __restrict__ word, uint64_t nE) {
+    index[0] = word[0] ? 0 : 1;
+    index[1] = word[1];
+    index[2] = (long long)nE;
+}
+
+// Slabs of each job that may hold a live edge, one warp per source object: an object with
+// a partner (flag set) covers the slabs whose keys can fall in its box's quantised x range.
+// A payload whose index says it is not in key order, was built for another edge count, or
+// whose source ids reach past the flags, covers every slab (each edge is then checked, as
+// without an index).  Blocks below
+// blocks0 run job j0, the others j1.
+constexpr int kMarkWarps = 8;
+
+__global__ void __launch_bounds__(32 * kMarkWarps) k_slab_mark(EdgeJob j0, EdgeJob j1, unsigned int blocks0) {
+    const bool second = blockIdx.x >= blocks0;
+    const EdgeJob& j = second ? j1 : j0;
+    const int lane = threadIdx.x & 31;
+    const uint64_t o = (uint64_t)(blockIdx.x - (second ? blocks0 : 0u)) * kMarkWarps + (threadIdx.x >> 5);
+    const long long* xq = j.xindex + 3;
+    const bool ordered =
+        j.xindex[0] == 1 && j.xindex[1] < (long long)j.n_cull && j.xindex[2] == (long long)j.nE;
+    if (!ordered) {
+        if (o == 0)
+            for (uint64_t b = lane; b < j.n_slab; b += 32) j.covered[b] = 1;
+        return;
+    }
+    if (o >= j.n_cull || j.cull[o] == 0) return;
+    const float lo = ord2f(j.sbox[6 * o]), hi = ord2f(j.sbox[6 * o + 3]);
+    if (!(lo <= hi)) return;  // no triangles, hence no edges
+    const long long qlo = llround((double)lo * 1e5), qhi = llround((double)hi * 1e5);
+    // first slab whose first key is >= qlo (the one before it may hold keys >= qlo too), and
+    // the last slab whose first key is <= qhi.
+    uint64_t a = 0, b = j.n_slab;
+    while (a < b) {
+        const uint64_t m = (a + b) / 2;
+        if (xq[m] < qlo) a = m + 1;
+        else b = m;
+    }
+    const uint64_t first = a > 0 ? a - 1 : 0;
+    a = 0;
+    b = j.n_slab;
+    while (a < b) {
+        const uint64_t m = (a + b) / 2;
+        if (xq[m] <= qhi) a = m + 1;
+        else b = m;
+    }
+    if (a == 0) return;  // every key is above qhi
+    for (uint64_t s = first + lane; s < a; s += 32) j.covered[s] = 1;
+}
+
+// The live-edge check of k_edge_live over the covered slabs only, one block (kSlab threads)
+// per slab.  Blocks below blocks0 run job j0, the others j1.
+__global__ void __launch_bounds__(kSlab) k_edge_live_slab(EdgeJob j0, EdgeJob j1, unsigned int blocks0) {
+    const bool second = blockIdx.x >= blocks0;
+    const EdgeJob& j = second ? j1 : j0;
+    const uint64_t sl = blockIdx.x - (second ? blocks0 : 0u);
+    if (sl >= j.n_slab || !j.covered[sl]) return;  // block-uniform
+    const uint64_t i = sl * kSlab + threadIdx.x;
+    const bool valid = i < j.nE;
+    const int ns = valid ? j.p.counts[i] : 0;
+    const int off = valid ? j.p.offsets[i] : 0;
+    const int32_t so0 = ns > 0 ? j.p.sources[off] : -1;
+    const bool in = ns > 0 && so0 >= 0 && (uint64_t)so0 < j.n_cull;
+    const uint8_t c0 = in ? j.cull[so0] : (uint8_t)0;
+    const uint32_t en = (j.entry && in && ns == 1) ? j.entry[so0] : 0u;
+    const bool any = ns > 0 && edge_is_live(j, i, ns, j.p.sources + off, so0, c0);
+    live_append(j, i, any, en, threadIdx.x & 31);
 }
 
 // Exclusive prefix sums of the kCells cell counts of each binned job, in place (one block
@@ -1090,6 +1210,8 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
     job.pbox = cull.pbox;
     job.n_pbox = cull.n_pbox;
     job.entry = cull.part ? cull.entry : nullptr;
+    job.xindex = cull.part ? cull.xindex : nullptr;
+    job.sbox = cull.sbox;
     job.nodes = (const BNode*)target->nodes;
     job.max_steps = max_steps(target);
     job.tris = (const float4*)target->tris;
@@ -1102,19 +1224,29 @@ cudaError_t edge_join_async(const rs_bvh* target, const float* d_starts, const f
 // job's on a side stream) and its deferred edges.  Each job's nE < 2^32 and its cull flags
 // set.
 cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream_t s) {
-    // One zeroed block: n_live[2], n_def[2], then the cell counts of the binned jobs.
+    // One zeroed block: n_live[2], n_def[2], the cell counts of the binned jobs, then (slab
+    // mode) each job's slab flags.
     uint32_t* zeroed = nullptr;
     EdgeJob jobs[2] = {};
     uint64_t blocks[2] = {0, 0}, total_e = 0;
     int n_bin = 0;
+    // Slab mode when every job has a slab index (and partner lists): the live-edge check
+    // visits only the slabs of objects with partners.
+    bool slab = n_jobs > 0;
     for (int d = 0; d < n_jobs; ++d) {
         jobs[d] = job[d];
         if (jobs[d].nE <= kBinMaxEdges) ++n_bin;
+        slab = slab && jobs[d].xindex && jobs[d].sbox && jobs[d].part;
+    }
+    auto a256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t cbytes = a256((4 + (size_t)n_bin * kCells) * sizeof(uint32_t));
+    size_t zbytes = cbytes;
+    for (int d = 0; d < n_jobs && slab; ++d) {
+        jobs[d].n_slab = (jobs[d].nE + kSlab - 1) / kSlab;
+        zbytes += a256(std::max<uint64_t>(jobs[d].n_slab, 1));
     }
     // One allocation: the zeroed block, then each job's live, rank and (binned jobs) order
     // lists, each 256-byte aligned; one memset clears the zeroed block.
-    const size_t zbytes = (4 + (size_t)n_bin * kCells) * sizeof(uint32_t);
-    auto a256 = [](size_t b) { return (b + 255) & ~size_t(255); };
     size_t total = a256(zbytes);
     for (int d = 0; d < n_jobs; ++d) {
         const size_t bytes = a256(std::max<uint64_t>(jobs[d].nE, 1) * sizeof(uint32_t));
@@ -1124,6 +1256,7 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
     cudaError_t e = dmalloc((void**)&zeroed, total, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(zeroed, 0, zbytes, s);
     uint32_t* next_cells = zeroed + 4;
+    char* next_flags = reinterpret_cast<char*>(zeroed) + cbytes;
     char* next = reinterpret_cast<char*>(zeroed) + a256(zbytes);
     for (int d = 0; d < n_jobs && e == cudaSuccess; ++d) {
         EdgeJob& j = jobs[d];
@@ -1147,12 +1280,24 @@ cudaError_t edge_jobs_async(EdgeJob* job, int n_jobs, rs_pairset* ps, cudaStream
                 next += bytes;
             }
         }
+        if (slab) {
+            j.covered = reinterpret_cast<uint8_t*>(next_flags);
+            next_flags += a256(std::max<uint64_t>(j.n_slab, 1));
+        }
         blocks[d] = (j.nE + 256 * kLiveEdges - 1) / (256 * kLiveEdges);
         total_e += j.nE;
     }
     if (e == cudaSuccess && total_e) {
         const int ptok = prof_begin(P_EDGE_JOIN, s);
-        launch(k_edge_live, (unsigned)(blocks[0] + blocks[1]), 256, 0, s, jobs[0], jobs[1], (unsigned)blocks[0]);
+        if (slab) {
+            uint64_t mb[2] = {0, 0};
+            for (int d = 0; d < n_jobs; ++d) mb[d] = std::max<uint64_t>((jobs[d].n_cull + kMarkWarps - 1) / kMarkWarps, 1);
+            launch(k_slab_mark, (unsigned)(mb[0] + mb[1]), 32 * kMarkWarps, 0, s, jobs[0], jobs[1], (unsigned)mb[0]);
+            launch(k_edge_live_slab, (unsigned)(jobs[0].n_slab + jobs[1].n_slab), (unsigned)kSlab, 0, s, jobs[0],
+                   jobs[1], (unsigned)jobs[0].n_slab);
+        } else {
+            launch(k_edge_live, (unsigned)(blocks[0] + blocks[1]), 256, 0, s, jobs[0], jobs[1], (unsigned)blocks[0]);
+        }
         if (n_bin) {
             launch(k_cell_scan, 2, 1024, 0, s, jobs[0].cells, n_jobs > 1 ? jobs[1].cells : (uint32_t*)nullptr,
                    (const unsigned int*)jobs[0].n_live,
@@ -1221,6 +1366,8 @@ cudaError_t edge_join_pair_async(const rs_bvh* A, const float* startsA, const fl
         j.pbox = c.pbox;
         j.n_pbox = c.n_pbox;
         j.entry = c.part ? c.entry : nullptr;
+        j.xindex = c.part ? c.xindex : nullptr;
+        j.sbox = c.sbox;
         j.nodes = (const BNode*)target->nodes;
         j.max_steps = max_steps(target);
         j.tris = (const float4*)target->tris;
@@ -1329,6 +1476,37 @@ int table_status(rs_pairset* ps, cudaStream_t s, cudaError_t e) {
     }
 }
 }  // namespace rs
+
+extern "C" int rs_edge_index(const float* d_starts, const float* d_ends, const int32_t* d_sources, uint64_t nE,
+                             uint64_t nS, int64_t* d_index, int* h_ordered, void* stream) {
+    if (!d_index || (nE && (!d_starts || !d_ends)) || (nS && !d_sources)) return RS_ERR_INVALID;
+    const void* q[4] = {d_starts, d_ends, d_sources, d_index};
+    for (const void*& x : q)
+        if (rs_kernel_pointer(x, &x) != RS_OK) return RS_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    int* word = nullptr;
+    cudaError_t e = dmalloc((void**)&word, 2 * sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(word, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(word + 1, 0xff, sizeof(int), s);  // -1
+    long long* index = reinterpret_cast<long long*>(const_cast<void*>(q[3]));
+    if (e == cudaSuccess) {
+        const EdgePayload p{static_cast<const float*>(q[0]), static_cast<const float*>(q[1]), nullptr, nullptr,
+                            static_cast<const int32_t*>(q[2])};
+        const uint64_t n = std::max<uint64_t>(std::max(nE, nS), 1);
+        launch(k_edge_index, (unsigned)std::min<uint64_t>((n + 255) / 256, 4ull * sm_count()), 256, 0, s, p, nE, nS,
+               index, word);
+        launch(k_edge_index_head, 1, 1, 0, s, index, (const int*)word, nE);
+        e = cudaGetLastError();
+    }
+    long long head = 0;
+    if (e == cudaSuccess && h_ordered) {
+        e = cudaMemcpyAsync(&head, index, sizeof(head), cudaMemcpyDefault, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e == cudaSuccess) *h_ordered = head == 1 ? 1 : 0;
+    }
+    if (word) cudaFreeAsync(word, s);
+    return to_status(e);
+}
 
 extern "C" int rs_edge_join(const rs_bvh* target, const float* d_starts, const float* d_ends,
                             const int32_t* d_offsets, const int32_t* d_counts, const int32_t* d_sources,

@@ -311,7 +311,8 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
                              uint64_t nEA, const rs_bvh* B, const float* d_startsB, const float* d_endsB,
                              const int32_t* d_offsetsB, const int32_t* d_countsB, const int32_t* d_sourcesB,
                              uint64_t nEB, int direction, int with_containment, rs_pairset* ps, void* stream,
-                             cudaEvent_t edges_a_ready, cudaEvent_t edges_b_ready) {
+                             cudaEvent_t edges_a_ready, cudaEvent_t edges_b_ready,
+                             const long long* indexA = nullptr, const long long* indexB = nullptr) {
     if (!A || !B || !ps || direction < 0 || direction > 2) return RS_ERR_INVALID;
     const bool a2b = direction == 0 || direction == 1;
     const bool b2a = direction == 0 || direction == 2;
@@ -319,7 +320,7 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
     // Payloads in pinned host memory are read in place through their mapped addresses.
     if (!kernel_ptr(&d_startsA) || !kernel_ptr(&d_endsA) || !kernel_ptr(&d_offsetsA) || !kernel_ptr(&d_countsA) ||
         !kernel_ptr(&d_sourcesA) || !kernel_ptr(&d_startsB) || !kernel_ptr(&d_endsB) || !kernel_ptr(&d_offsetsB) ||
-        !kernel_ptr(&d_countsB) || !kernel_ptr(&d_sourcesB))
+        !kernel_ptr(&d_countsB) || !kernel_ptr(&d_sourcesB) || !kernel_ptr(&indexA) || !kernel_ptr(&indexB))
         return RS_ERR_INVALID;
     {
         int st = bvh_ready(A);  // the broad phase needs the object counts
@@ -350,10 +351,10 @@ static int overlap_join_impl(const rs_bvh* A, const float* d_startsA, const floa
             e = cull_impl(A, B, a2b ? cand : nullptr, b2a ? cand + A->n_obj : nullptr, part,
                           part + A->n_obj * kPartners, entry, entry + A->n_obj, boxes, tmps, s);
         if (e == cudaSuccess) {
-            if (a2b) cullA = EdgeCull{cand, A->n_obj, part, boxes[1], B->n_obj, entry};
+            if (a2b) cullA = EdgeCull{cand, A->n_obj, part, boxes[1], B->n_obj, entry, indexA, boxes[0]};
             if (b2a)
                 cullB = EdgeCull{cand + A->n_obj, B->n_obj, part + A->n_obj * kPartners, boxes[0], A->n_obj,
-                                 entry + A->n_obj};
+                                 entry + A->n_obj, indexB, boxes[1]};
         } else {
             cudaGetLastError();  // culling is an optimisation: run without it
         }
@@ -429,6 +430,21 @@ extern "C" int rs_overlap_join_after(const rs_bvh* A, const float* d_startsA, co
     return overlap_join_impl(A, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, B, d_startsB, d_endsB,
                              d_offsetsB, d_countsB, d_sourcesB, nEB, direction, with_containment, ps, stream,
                              (cudaEvent_t)edges_a_ready, (cudaEvent_t)edges_b_ready);
+}
+
+extern "C" int rs_overlap_join_indexed(const rs_bvh* A, const float* d_startsA, const float* d_endsA,
+                                       const int32_t* d_offsetsA, const int32_t* d_countsA,
+                                       const int32_t* d_sourcesA, uint64_t nEA, const int64_t* d_indexA,
+                                       const rs_bvh* B, const float* d_startsB, const float* d_endsB,
+                                       const int32_t* d_offsetsB, const int32_t* d_countsB,
+                                       const int32_t* d_sourcesB, uint64_t nEB, const int64_t* d_indexB,
+                                       int direction, int with_containment, rs_pairset* ps, void* edges_a_ready,
+                                       void* edges_b_ready, void* stream) {
+    return overlap_join_impl(A, d_startsA, d_endsA, d_offsetsA, d_countsA, d_sourcesA, nEA, B, d_startsB, d_endsB,
+                             d_offsetsB, d_countsB, d_sourcesB, nEB, direction, with_containment, ps, stream,
+                             (cudaEvent_t)edges_a_ready, (cudaEvent_t)edges_b_ready,
+                             reinterpret_cast<const long long*>(d_indexA),
+                             reinterpret_cast<const long long*>(d_indexB));
 }
 
 extern "C" int rs_set_overlap_cull(int on) {

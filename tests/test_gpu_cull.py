@@ -14,13 +14,15 @@ from rayspace3d_gb300 import _lib, api, formats, synth
 pytestmark = pytest.mark.gpu
 
 
-def _join(A, B, cull, containment=False):
+def _join(A, B, cull, containment=False, indexed=False):
     L = _lib.load()
     L.rs_set_overlap_cull(1 if cull else 0)
     try:
-        ba, bb = api.Bvh(api.DeviceGeometry(A)), api.Bvh(api.DeviceGeometry(B))
+        da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+        ba, bb = api.Bvh(da), api.Bvh(db)
         ps = api.PairSet(1 << 12)
-        api.overlap_join(ba, bb, ps, with_containment=containment)
+        indexes = (api.edge_index(da)[0], api.edge_index(db)[0]) if indexed else None
+        api.overlap_join(ba, bb, ps, with_containment=containment, indexes=indexes)
         torch.cuda.synchronize()
         return np.sort(ps.finalize().cpu().numpy().astype(np.uint64))
     finally:
@@ -28,11 +30,15 @@ def _join(A, B, cull, containment=False):
 
 
 def _check(A, B, containment=False):
+    """The oracle's pair set from the join with the broad phase off, on, and on with the
+    payloads' slab indexes."""
     want = bind.intersection_join(A, B) if containment else bind.overlap_join(A, B)
     on = _join(A, B, True, containment)
     off = _join(A, B, False, containment)
+    slabs = _join(A, B, True, containment, indexed=True)
     np.testing.assert_array_equal(off, want)
     np.testing.assert_array_equal(on, want)
+    np.testing.assert_array_equal(slabs, want)
     return want
 
 
@@ -243,3 +249,61 @@ def test_overlap_join_reads_pinned_host_payloads(cuda):
     assert L.rs_kernel_pointer(pageable.ctypes.data, ctypes.byref(out)) == _lib.RS_ERR_INVALID
     ba.close()
     bb.close()
+
+
+def _key_x(v):
+    return np.array([int(np.round(np.float64(x) * 1e5)) if abs(np.float64(x) * 1e5 - np.trunc(np.float64(x) * 1e5)) != 0.5
+                     else int(np.trunc(np.float64(x) * 1e5) + np.sign(x)) for x in v], dtype=np.int64)
+
+
+@pytest.mark.parametrize("world", [6.0, 30.0, 400.0])
+def test_slab_index_and_indexed_join(cuda, world):
+    """rs_edge_index's keys are the quantised x of each slab's first edge's lower endpoint
+    (llround, halves away from zero); the indexed join equals the oracle with the payloads on
+    the device and with payloads and indexes in pinned host memory, in both directions and
+    with one index missing.  A shuffled payload is reported out of order, and the join with
+    its index (which then covers every slab) is still exact."""
+    A, B = synth.overlap_workload(n_objects=300, level=2, world=world, seed=33)
+    want = bind.overlap_join(A, B)
+    da, db = api.DeviceGeometry(A), api.DeviceGeometry(B)
+    ba, bb = api.Bvh(da), api.Bvh(db)
+    ia, oka = api.edge_index(da)
+    ib, okb = api.edge_index(db)
+    assert oka and okb
+    e = A.edges
+    first = np.arange(0, len(e.starts), 256)
+    keys = np.minimum(_key_x(e.starts[first, 0]), _key_x(e.ends[first, 0]))
+    got = ia.cpu().numpy()
+    assert got[0] == 1 and got[1] == int(e.sources.max()) and got[2] == len(e.starts)
+    np.testing.assert_array_equal(got[3:], keys)
+
+    def run(indexes, direction=0):
+        ps = api.PairSet(1 << 12)
+        api.overlap_join(ba, bb, ps, direction=direction, indexes=indexes)
+        return np.sort(ps.finalize().cpu().numpy().astype(np.uint64))
+
+    np.testing.assert_array_equal(run((ia, ib)), want)
+    np.testing.assert_array_equal(run((ia, None)), want)
+    for d in (1, 2):
+        np.testing.assert_array_equal(run((ia, ib), d), run(None, d))
+    # Payloads and indexes in pinned host memory, read in place.
+    device = [g.edges for g in (da, db)]
+    for g, ed in zip((da, db), device):
+        g.edges = tuple(t.cpu().pin_memory() for t in ed)
+    np.testing.assert_array_equal(run((ia.cpu().pin_memory(), ib.cpu().pin_memory())), want)
+    for g, ed in zip((da, db), device):
+        g.edges = ed
+    # A payload out of key order.
+    perm = np.random.default_rng(1).permutation(len(e.starts))
+    shuffled = formats.Edges(e.starts[perm], e.ends[perm], e.offsets[perm], e.counts[perm], e.sources)
+    A2 = synth.make_geometry(A.vertices, A.indices, A.tri2obj, edges=False)
+    A2.edges = shuffled
+    d2 = api.DeviceGeometry(A2)
+    i2, ok2 = api.edge_index(d2)
+    assert not ok2 and int(i2[0]) == 0
+    b2 = api.Bvh(d2)
+    ps = api.PairSet(1 << 12)
+    api.overlap_join(b2, bb, ps, indexes=(i2, ib))
+    np.testing.assert_array_equal(np.sort(ps.finalize().cpu().numpy().astype(np.uint64)), want)
+    for h in (ba, bb, b2):
+        h.close()
