@@ -554,8 +554,8 @@ struct PairTable {
     // finds no slot within max_probes, ST_SPILLED is raised; from then on an insert that
     // does not settle at its first slot of the main table goes to the overflow table (a
     // full main table would otherwise make every insert walk its whole probe limit, each
-    // step a dependent load).  A key may then sit in both; the regrowth
-    // merges them.  A key that finds no slot in either raises ST_TABLE_FULL.
+    // step a dependent load).  A key may then sit in both tables; the regrowth merges
+    // them.  A key that finds no slot in either raises ST_TABLE_FULL.
     unsigned long long* over;
     unsigned long long over_mask;
     unsigned long long* over_count;

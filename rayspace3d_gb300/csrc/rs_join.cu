@@ -497,11 +497,11 @@ __global__ void __launch_bounds__(256) k_edge_live(EdgeJob j0, EdgeJob j1, unsig
 // (EdgePreprocessor.cpp:41-119: llround(x * 1e5) per coordinate), so it is sorted by the
 // quantised x of each edge's lower endpoint -- the smaller of its two quantised x.  Slab b
 // holds edges [b * kSlab, (b + 1) * kSlab); index[3 + b] is the key of its first edge.
-// index[0] = 1 when the keys never decrease and no source id is negative (else 0), index[1]
-// = the largest source id, index[2] = the edge count it was built for.  The live-edge check then visits only the slabs whose key range
-// meets the quantised x range of an object with a partner: every edge of an object lies
-// between its box's quantised x bounds (llround is monotone), and every live edge has such
-// a source.
+// index[0] = 1 when the keys never decrease and no source id is negative (else 0),
+// index[1] = the largest source id, index[2] = the edge count it was built for.  The
+// live-edge check then visits only the slabs whose key range meets the quantised x range
+// of an object with a partner: every edge of an object lies between its box's quantised x
+// bounds (llround is monotone), and every live edge has such a source.
 constexpr uint64_t kSlab = 256;
 
 __device__ __forceinline__ long long edge_key_x(const EdgePayload& p, uint64_t e) {
@@ -539,8 +539,7 @@ __global__ void k_edge_index_head(long long* __restrict__ index, const int* __re
 // a partner (flag set) covers the slabs whose keys can fall in its box's quantised x range.
 // A payload whose index says it is not in key order, was built for another edge count, or
 // whose source ids reach past the flags, covers every slab (each edge is then checked, as
-// without an index).  Blocks below
-// blocks0 run job j0, the others j1.
+// without an index).  Blocks below blocks0 run job j0, the others j1.
 constexpr int kMarkWarps = 8;
 
 __global__ void __launch_bounds__(32 * kMarkWarps) k_slab_mark(EdgeJob j0, EdgeJob j1, unsigned int blocks0) {

@@ -5,7 +5,7 @@
 // raytracer_intersection_estimated_main.cpp:77-176), compact_hash_table_pairs and
 // merge_and_deduplicate_pairs_gpu (query/src/cuda/mesh_query_deduplication.cu:56-144).
 // Differences by design: no key is dropped (the reference drops one after 5000 / 1000
-// probes).  A table past 3/4 load sends keys that do not settle within a few slots to
+// probes).  A table past 3/4 load sends keys that do not settle at their first slot to
 // the pair set's overflow table, and the status read after the launches regrows the
 // table from both; only a key that finds no slot in either raises RS_ERR_TABLE_FULL,
 // after which the drivers grow the table and rerun.  The finalised output is sorted, so
