@@ -257,8 +257,8 @@ def evaluate(m: Mlp, samples: List[Sample]) -> dict:
 def join_seconds(seed: int, estimate: float, n_lo: int = 1000, n_hi: int = 200_000, reps: int = 3) -> float:
     """Device seconds of the exact join of dataset pair `seed` with its pair table sized from
     `estimate` as raytracer_overlap_estimated sizes it (rs_hash_size_pow2): creating and
-    clearing the table, the join (which regrows the table from its spill list when it
-    fills, and reruns only when the list overflows too) and the sorted pair list; the BVHs are built beforehand.  Mean of reps after one warm-up."""
+    clearing the table, the join (which regrows the table from its overflow table when it
+    fills, and reruns only when that fills too) and the sorted pair list; the BVHs are built beforehand.  Mean of reps after one warm-up."""
     A, _, B, _ = dataset_pair(seed, n_lo, n_hi)
     ba, bb = api.Bvh(A), api.Bvh(B)
     size = api.hash_size_pow2(int(round(estimate)))
